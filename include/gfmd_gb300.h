@@ -1,0 +1,136 @@
+/*
+ * gfmd_gb300 — C ABI of the GB300-native GFMD elastic force evaluation.
+ *
+ * This is the boundary a LAMMPS `fix gfmd` solver style (static/gb300,
+ * dynamic/gb300) or any other host code binds to.  Plain C types only; all
+ * pointers are either host memory or CUDA device memory as stated per call.
+ * Every call returns an int status (GFMD_OK = 0) and never aborts, traps or
+ * exits; gfmd_last_error() gives a message for the last failure on the
+ * calling thread.  A handle is not thread-safe: one host thread per handle.
+ *
+ * Grid layout (that of the reference, src/main/fix_gfmd.cpp:763 and
+ * src/solvers/gfmd_solver_fft.cpp:72-80): displacement and force arrays are
+ * [ndof][nx*ny] with the grid index ix*ny + iy (y fastest).
+ *
+ * Transform conventions (reference with LAMMPS >= patch_10Feb2021):
+ * forward exp(-i q.r) unscaled, backward exp(+i q.r) unscaled, Phi(q)
+ * pre-scaled by 1/(nx*ny) (src/main/gfmd_misc.cpp:88-97).
+ */
+#ifndef GFMD_GB300_H
+#define GFMD_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define GFMD_OK 0
+#define GFMD_EINVAL 1        /* bad argument or state */
+#define GFMD_ENOMEM 2        /* device or host allocation failed */
+#define GFMD_ECUDA 3         /* a CUDA runtime call failed */
+#define GFMD_ENONFINITE 4    /* NaN or Inf in the energy or a norm */
+#define GFMD_ETIMEDOUT 5     /* a bounded device wait gave up */
+#define GFMD_ENOTCONVERGED 6 /* iteration cap reached before tolerance */
+#define GFMD_ENOPHI 7        /* no stiffness table uploaded yet */
+
+/* ---- arithmetic of a solver handle -------------------------------------- */
+#define GFMD_PREC_F64 0      /* plain FP64 everywhere (drop-in parity path) */
+#define GFMD_PREC_F32 1      /* FP32 transforms and Phi products with
+                                compensated twiddles; FP64 energy */
+
+/* ---- Phi table layouts accepted by gfmd_set_phi ------------------------- */
+#define GFMD_PHI_FULL 0      /* [nx*ny][ndof][ndof] complex (re,im), index
+                                ix*ny+iy: what fill_phi_buffer produces */
+#define GFMD_PHI_HALF 1      /* [nx][ny/2+1][ndof][ndof] complex (re,im) */
+
+typedef struct gfmd_solver *gfmd_handle_t;
+typedef struct gfmd_kernel *gfmd_kernel_t;
+
+const char *gfmd_last_error(void);
+
+/* Library version string. */
+const char *gfmd_version(void);
+
+/* ---- solver handle ------------------------------------------------------- */
+
+/* Create a solver for an nx x ny grid with ndof = 3*nu degrees of freedom per
+ * grid point (ndof <= 24, nx, ny in [1, 8192]).  Allocates all device scratch
+ * on the current CUDA device.
+ * Replaces: GFMDSolverStatic::GFMDSolverStatic + GFMDSolver::set_grid_size
+ * (src/solvers/gfmd_solver_static.cpp:49-84, src/main/gfmd_solver.cpp:79-136)
+ * for a single process that owns the whole grid. */
+int gfmd_create(int nx, int ny, int ndof, int precision, gfmd_handle_t *out);
+
+/* Release the handle and its device memory. */
+int gfmd_destroy(gfmd_handle_t h);
+
+/* Run all later work of this handle on the given cudaStream_t (NULL = the
+ * legacy default stream). */
+int gfmd_set_stream(gfmd_handle_t h, void *cuda_stream);
+
+/* Upload the stiffness table once (host memory, FP64).  phi is pre-scaled by
+ * 1/(nx*ny) as fill_phi_buffer leaves it; layout is GFMD_PHI_FULL or
+ * GFMD_PHI_HALF; linf holds ndof/3 linear forces per layer (NULL = zeros).
+ * The table is packed on the host into the Hermitian half-spectrum form the
+ * kernels read and copied to the device; the caller keeps ownership of phi.
+ * Replaces: GFMDSolverStatic::set_kernel (src/solvers/gfmd_solver_static.cpp:90-136),
+ * which fills phi via fill_phi_buffer (src/main/gfmd_misc.cpp:32-101). */
+int gfmd_set_phi(gfmd_handle_t h, const double *phi, int layout, const double *linf);
+
+/* One force evaluation on device buffers (FP64, [ndof][nx*ny]); u and f must
+ * not alias.  Writes the elastic energy to *epot (host) and synchronizes the
+ * handle's stream.
+ * Replaces: GFMDSolverStatic::post_force (src/solvers/gfmd_solver_static.cpp:145-249),
+ * the GPU form of which took device double pointers with pitch nxy_loc
+ * (src/cuda/gfmd_solver_cuda.cpp:394-504). */
+int gfmd_post_force(gfmd_handle_t h, const double *d_u, double *d_f, double *epot);
+
+/* The same on host buffers: copies u in and f out inside the call.
+ * Replaces: GFMDSolverStatic::post_force with the CPU double** buffers
+ * allocated by FixGFMD (src/main/fix_gfmd.cpp:613-617). */
+int gfmd_post_force_host(gfmd_handle_t h, const double *u, double *f, double *epot);
+
+/* Asynchronous force evaluation on device-resident state, no host sync.
+ * d_epot (device, one double) receives the energy.  gfmd_force_f64 needs a
+ * GFMD_PREC_F64 handle, gfmd_force_f32 a GFMD_PREC_F32 handle. */
+int gfmd_force_f64(gfmd_handle_t h, const double *d_u, double *d_f, double *d_epot);
+int gfmd_force_f32(gfmd_handle_t h, const float *d_u, float *d_f, double *d_epot);
+
+/* u(q=0) of the last force evaluation, ndof doubles, host.
+ * Replaces: GFMDSolver::get_u0 (src/main/gfmd_solver.h:89-91). */
+int gfmd_get_u0(gfmd_handle_t h, double *u0);
+
+/* Device bytes held by the handle.
+ * Replaces: GFMDSolver::memory_usage (src/main/gfmd_solver.h:97). */
+int gfmd_memory_usage(gfmd_handle_t h, double *bytes);
+
+/* ---- stiffness-kernel tables (host) ------------------------------------- */
+
+/* Parse the stiffness-kernel part of a `fix gfmd` line, e.g.
+ * "ft fcc100 1.0 2 pair-potential 1 1.0 height 64".  Supported here: the
+ * `ft` style on the sc100, fcc100 and fcc111 surfaces with `pair-potential`
+ * force constants.  Other styles are produced by the reference's own
+ * fill_phi_buffer and uploaded with gfmd_set_phi.
+ * Replaces: stiffness_kernel_factory (src/main/surface_stiffness.cpp:440-481). */
+int gfmd_kernel_create(const char *args, gfmd_kernel_t *out);
+int gfmd_kernel_destroy(gfmd_kernel_t k);
+
+/* Kernel dimension ndof (get_dimension) and substrate height (get_height). */
+int gfmd_kernel_info(gfmd_kernel_t k, int *ndof, int *height);
+
+/* Fill a Phi table for an nx x ny grid, scaled by 1/(nx*ny), in
+ * GFMD_PHI_FULL or GFMD_PHI_HALF layout (host memory the caller allocates:
+ * 2*ndof*ndof doubles per stored q), and linf (ndof/3 doubles, may be NULL).
+ * nthreads <= 0 uses every host core.
+ * Replaces: fill_phi_buffer + StiffnessKernel::get_force_at_gamma_point
+ * (src/main/gfmd_misc.cpp:32-101, src/main/surface_stiffness.cpp:430-435). */
+int gfmd_kernel_phi(gfmd_kernel_t k, int nx, int ny, int layout, double *phi,
+                    double *linf, int nthreads);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GFMD_GB300_H */

@@ -1,0 +1,151 @@
+/*
+ * ORACLE harness (project code): a C entry point over the reference's own,
+ * unmodified sources, compiled where they lie by oracle/ref/Makefile into
+ * oracle/_ref/libgfmdref.so.  Used only in the build container, to generate
+ * and check the golden fixtures under tests/golden/ and to pin the oracle
+ * restatement in oracle/gfmd_oracle.c.
+ *
+ * The kernel argument string is the stiffness-kernel part of a `fix gfmd`
+ * line, e.g. "ft fcc100 1.0 2 pair-potential 1 1.0 height 64"; it is handed
+ * to stiffness_kernel_factory the way FixGFMD's constructor does
+ * (src/main/fix_gfmd.cpp:195-197).
+ */
+#include <cstring>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "pointers.h"
+#include "force.h"
+#include "surface_stiffness.h"
+#include "gfmd_misc.h"
+#include "gfmd_solver_static.h"
+
+using namespace LAMMPS_NS;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+struct Env {
+  Error error;
+  Memory memory{&error};
+  Comm comm;
+  Domain domain;
+  Update update;
+  LAMMPS lmp;
+  Env() {
+    lmp.memory = &memory;
+    lmp.error = &error;
+    lmp.comm = &comm;
+    lmp.domain = &domain;
+    lmp.update = &update;
+    lmp.screen = nullptr;
+  }
+};
+
+struct Args {
+  std::vector<std::string> tok;
+  std::vector<char *> argv;
+  explicit Args(const char *s) {
+    std::istringstream is(s);
+    std::string t;
+    while (is >> t) tok.push_back(t);
+    for (auto &x : tok) argv.push_back(&x[0]);
+    argv.push_back(nullptr);
+  }
+  int narg() const { return (int)tok.size(); }
+};
+
+StiffnessKernel *make_kernel(Env &env, Args &a) {
+  if (a.narg() < 1) throw std::runtime_error("empty kernel argument string");
+  int carg = 1;
+  StiffnessKernel *k = stiffness_kernel_factory(a.argv[0], a.narg(), &carg,
+                                                a.argv.data(), &env.domain,
+                                                nullptr, &env.memory,
+                                                &env.error);
+  if (!k) throw std::runtime_error("unknown stiffness kernel '" + a.tok[0] + "'");
+  if (carg != a.narg())
+    throw std::runtime_error("trailing kernel arguments from '" + a.tok[carg] + "'");
+  return k;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *gref_last_error(void) { return g_last_error.c_str(); }
+
+/* Dimension (ndof) and height of a kernel. */
+int gref_kernel_info(const char *args, int *ndof, int *height) {
+  try {
+    Env env;
+    Args a(args);
+    std::unique_ptr<StiffnessKernel> k(make_kernel(env, a));
+    *ndof = k->get_dimension();
+    *height = k->get_height();
+    return 0;
+  } catch (const std::exception &e) {
+    g_last_error = e.what();
+    return -1;
+  }
+}
+
+/* Full-grid Phi(q) table exactly as fill_phi_buffer leaves it
+ * (src/main/gfmd_misc.cpp:32-101): phi[(ix*ny+iy)*ndof*ndof + i*ndof + j]
+ * complex interleaved; linf[ndof/3] from get_force_at_gamma_point. */
+int gref_phi_full(const char *args, int nx, int ny, int normalize,
+                  double *phi, double *linf) {
+  try {
+    Env env;
+    Args a(args);
+    std::unique_ptr<StiffnessKernel> k(make_kernel(env, a));
+    int ndof = k->get_dimension();
+    int nxy = nx * ny;
+    double_complex **buf;
+    env.memory.create(buf, nxy, ndof * ndof, "gref:phi");
+    fill_phi_buffer(ndof, nx, 0, nx - 1, ny, 0, ny - 1, k.get(), buf,
+                    normalize != 0, &env.error);
+    std::memcpy(phi, &buf[0][0], sizeof(double_complex) * (size_t)nxy * ndof * ndof);
+    env.memory.destroy(buf);
+    if (linf) k->get_force_at_gamma_point(linf);
+    return 0;
+  } catch (const std::exception &e) {
+    g_last_error = e.what();
+    return -1;
+  }
+}
+
+/* One call of the reference's GFMDSolverStatic::post_force
+ * (src/solvers/gfmd_solver_static.cpp:145-249) on a single process:
+ * u, f are [ndof][nx*ny]; returns the energy in *epot and u(q=0) in u0. */
+int gref_post_force(const char *args, int nx, int ny, const double *u,
+                    double *f, double *epot, double *u0) {
+  try {
+    Env env;
+    Args a(args);
+    std::unique_ptr<StiffnessKernel> k(make_kernel(env, a));
+    int ndof = k->get_dimension();
+    int nxy = nx * ny;
+    int carg = 0;
+    GFMDSolverStatic solver(&env.lmp, 0, &carg, nullptr);
+    solver.set_grid_size(nx, ny, ndof);
+    solver.set_kernel(k.get(), true);
+    double **ub, **fb;
+    env.memory.create(ub, ndof, nxy, "gref:u");
+    env.memory.create(fb, ndof, nxy, "gref:f");
+    std::memcpy(&ub[0][0], u, sizeof(double) * (size_t)ndof * nxy);
+    *epot = solver.post_force(ub, fb, nullptr);
+    std::memcpy(f, &fb[0][0], sizeof(double) * (size_t)ndof * nxy);
+    if (u0) std::memcpy(u0, solver.get_u0(), sizeof(double) * ndof);
+    env.memory.destroy(ub);
+    env.memory.destroy(fb);
+    return 0;
+  } catch (const std::exception &e) {
+    g_last_error = e.what();
+    return -1;
+  }
+}
+
+}  // extern "C"

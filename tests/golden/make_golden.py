@@ -1,0 +1,88 @@
+"""Generate the golden fixtures of tests/golden/ from the reference itself.
+
+Runs the reference's own, unmodified ``fill_phi_buffer`` and
+``GFMDSolverStatic::post_force`` through oracle/_ref/libgfmdref.so (built
+from the reference sources by oracle/ref/Makefile; needs the reference tree,
+so this script runs only where it is present).  Each fixture stores the
+kernel arguments, the grid, seeded displacements, the reference's forces,
+energy and u(q=0), and — for grids small enough to commit — the reference's
+full Phi table and linear forces.
+
+Usage:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
+REF_LIB = os.path.join(ROOT, "oracle", "_ref", "libgfmdref.so")
+
+# (name, kernel arguments, nx, ny, store phi?)
+CASES = [
+    ("sc100_nnn_h128_16x16", "ft sc100 1 1.0 pair-potential 2 1.0 1.0 height 128", 16, 16, True),
+    ("fcc100x2_h64_12x10", "ft fcc100 1.0 2 pair-potential 1 1.0 height 64", 12, 10, True),
+    ("fcc111_h128_8x6", "ft fcc111 1 1.0 pair-potential 1 1.0 height 128", 8, 6, True),
+    ("fcc100x4_h64_8x8", "ft fcc100 1.0 4 pair-potential 1 1.0 height 64", 8, 8, True),
+    ("fcc100x2_nn2_h10_10x10", "ft fcc100 1.0 2 pair-potential 2 1.0 -0.1 height 10", 10, 10, True),
+    ("sc100_a13_9x7", "ft sc100 1.3 1 pair-potential 2 1.0 1.0 height 128", 9, 7, True),
+    ("fcc100_analytic_linf_8x8", "fcc100 2 1.0 0.0 0.0 height 10 linf 0.05 -0.05", 8, 8, True),
+    ("fcc111_h128_64x37", "ft fcc111 1 1.0 pair-potential 1 1.0 height 128", 64, 37, False),
+    ("sc100_nnn_h128_32x32", "ft sc100 1 1.0 pair-potential 2 1.0 1.0 height 128", 32, 32, False),
+    ("fcc100x2_h64_36x36", "ft fcc100 1.0 2 pair-potential 1 1.0 height 64", 36, 36, False),
+]
+
+SEED = 20261203
+
+
+def load_ref() -> ctypes.CDLL:
+    if not os.path.exists(REF_LIB):
+        subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle", "ref"), "-j8"])
+    L = ctypes.CDLL(REF_LIB)
+    L.gref_last_error.restype = ctypes.c_char_p
+    return L
+
+
+def run_case(L, args: str, nx: int, ny: int, seed: int):
+    nd, ht = ctypes.c_int(), ctypes.c_int()
+    if L.gref_kernel_info(args.encode(), ctypes.byref(nd), ctypes.byref(ht)):
+        raise RuntimeError(L.gref_last_error().decode())
+    d = nd.value
+    phi = np.zeros((nx * ny, d, d), np.complex128)
+    linf = np.zeros(d // 3)
+    if L.gref_phi_full(args.encode(), nx, ny, 1, phi.ctypes.data_as(ctypes.c_void_p),
+                       linf.ctypes.data_as(ctypes.c_void_p)):
+        raise RuntimeError(L.gref_last_error().decode())
+    rng = np.random.default_rng(seed)
+    u = rng.normal(0.0, 0.01, (d, nx * ny))
+    f = np.zeros_like(u)
+    u0 = np.zeros(d)
+    e = ctypes.c_double()
+    if L.gref_post_force(args.encode(), nx, ny, u.ctypes.data_as(ctypes.c_void_p),
+                         f.ctypes.data_as(ctypes.c_void_p), ctypes.byref(e),
+                         u0.ctypes.data_as(ctypes.c_void_p)):
+        raise RuntimeError(L.gref_last_error().decode())
+    return d, ht.value, phi, linf, u, f, e.value, u0
+
+
+def main() -> int:
+    L = load_ref()
+    for i, (name, args, nx, ny, keep_phi) in enumerate(CASES):
+        d, h, phi, linf, u, f, e, u0 = run_case(L, args, nx, ny, SEED + i)
+        out = dict(args=np.array(args), nx=nx, ny=ny, ndof=d, height=h, u=u, f=f,
+                   epot=np.array(e), u0=u0, linf=linf)
+        if keep_phi:
+            out["phi"] = phi
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **out)
+        print(f"{name}: ndof={d} E={e:.16e} -> {os.path.getsize(path)} bytes")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

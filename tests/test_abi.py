@@ -1,0 +1,53 @@
+"""The C-ABI library: loads, exports every declared entry point, rejects bad
+arguments before touching a GPU."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT, gfmd_pkg
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "gfmd_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(gfmd_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = gfmd_pkg().lib()
+    names = _declared()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(L, n), n
+
+
+def test_python_binding_covers_the_header():
+    from importlib import import_module
+
+    sig = import_module("user-gfmd_gb300._lib").SIGNATURES
+    assert sorted(sig) == _declared()
+
+
+def test_argument_errors_return_status_without_gpu():
+    L = gfmd_pkg().lib()
+    h = ctypes.c_void_p()
+    assert L.gfmd_create(0, 8, 3, 0, ctypes.byref(h)) == 1
+    assert L.gfmd_create(8, 8, 4, 0, ctypes.byref(h)) == 1
+    assert L.gfmd_create(8, 8, 27, 0, ctypes.byref(h)) == 1
+    assert L.gfmd_create(8, 8, 3, 7, ctypes.byref(h)) == 1
+    assert L.gfmd_create(8, 8, 3, 0, None) == 1
+    assert L.gfmd_destroy(None) == 1
+    assert L.gfmd_post_force(None, None, None, None) == 1
+    assert L.gfmd_set_phi(None, None, 0, None) == 1
+    assert b"NULL" in L.gfmd_last_error()
+
+
+def test_solver_factory_names():
+    g = gfmd_pkg()
+    assert g.gfmd_solver_factory().get_name() == "static/gb300"
+    assert g.gfmd_solver_factory("static").get_name() == "static/gb300"
+    assert g.gfmd_solver_factory("static/gb300/f32").precision == "f32"
+    with pytest.raises(g.GFMDError):
+        g.gfmd_solver_factory("nosuch")

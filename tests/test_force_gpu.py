@@ -1,0 +1,119 @@
+"""GPU force evaluation against the reference fixtures and the oracle.
+
+FP64 path: relative L2 of forces and relative energy error <= 1e-10 (the
+drop-in parity bar).  FP32 path (compensated twiddles, FP64 energy): the
+errors are reported against the FP64 reference and bounded by FP32_TOL.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import (golden_cases, gfmd_pkg, half_to_full, load_golden, oracle_post_force,
+                      rel_l2)
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+F64_TOL = 1e-10
+FP32_TOL = 5e-6
+
+
+def _phi(c, nx, ny):
+    if "phi" in c:
+        return c["phi"], "full", c["linf"]
+    k = gfmd_pkg().StiffnessKernel(str(c["args"]))
+    phi, linf = k.phi_table(nx, ny, "half")
+    return phi, "half", linf
+
+
+def _solver(nx, ny, d, prec, phi, layout, linf):
+    s = gfmd_pkg().gfmd_solver_factory("static/gb300" if prec == "f64" else "static/gb300/f32")
+    s.set_grid_size(nx, ny, d)
+    s.set_phi(phi, layout, linf)
+    return s
+
+
+@pytest.mark.parametrize("path", golden_cases(), ids=lambda p: os.path.basename(p)[:-4])
+def test_f64_device_matches_reference(path):
+    c = load_golden(path)
+    nx, ny, d = int(c["nx"]), int(c["ny"]), int(c["ndof"])
+    phi, layout, linf = _phi(c, nx, ny)
+    s = _solver(nx, ny, d, "f64", phi, layout, linf)
+    u = torch.from_numpy(c["u"]).cuda()
+    f = torch.empty_like(u)
+    e = s.post_force(u, f)
+    ref_e = float(c["epot"])
+    assert rel_l2(f.cpu().numpy(), c["f"]) <= F64_TOL
+    assert abs(e - ref_e) <= F64_TOL * abs(ref_e)
+    assert np.allclose(s.get_u0(), c["u0"], rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.parametrize("path", golden_cases(), ids=lambda p: os.path.basename(p)[:-4])
+def test_f64_host_buffers_match_reference(path):
+    c = load_golden(path)
+    nx, ny, d = int(c["nx"]), int(c["ny"]), int(c["ndof"])
+    phi, layout, linf = _phi(c, nx, ny)
+    s = _solver(nx, ny, d, "f64", phi, layout, linf)
+    f = np.zeros_like(c["u"])
+    e = s.post_force(c["u"], f)
+    assert rel_l2(f, c["f"]) <= F64_TOL
+    assert abs(e - float(c["epot"])) <= F64_TOL * abs(float(c["epot"]))
+
+
+@pytest.mark.parametrize("path", golden_cases(), ids=lambda p: os.path.basename(p)[:-4])
+def test_f32_matches_reference_within_fp32_tolerance(path):
+    c = load_golden(path)
+    nx, ny, d = int(c["nx"]), int(c["ny"]), int(c["ndof"])
+    phi, layout, linf = _phi(c, nx, ny)
+    s = _solver(nx, ny, d, "f32", phi, layout, linf)
+    f = np.zeros_like(c["u"])
+    e = s.post_force(c["u"], f)
+    assert rel_l2(f, c["f"]) <= FP32_TOL
+    assert abs(e - float(c["epot"])) <= FP32_TOL * abs(float(c["epot"]))
+
+
+@pytest.mark.parametrize(
+    "args,nx,ny",
+    [
+        ("ft sc100 1 1.0 pair-potential 2 1.0 1.0 height 128", 128, 128),
+        ("ft fcc100 1.0 2 pair-potential 1 1.0 height 64", 96, 384),
+        ("ft fcc111 1 1.0 pair-potential 1 1.0 height 128", 64, 37),
+        ("ft fcc100 1.0 4 pair-potential 1 1.0 height 64", 256, 256),
+        ("ft fcc100 1.0 2 pair-potential 1 1.0 height 64", 75, 50),
+        ("ft sc100 1 1.0 pair-potential 2 1.0 1.0 height 128", 1, 64),
+        ("ft sc100 1 1.0 pair-potential 2 1.0 1.0 height 128", 48, 1),
+    ],
+)
+def test_f64_matches_oracle_at_larger_sizes(args, nx, ny):
+    g = gfmd_pkg()
+    k = g.StiffnessKernel(args)
+    d = k.get_dimension()
+    half, linf = k.phi_table(nx, ny, "half")
+    full = half_to_full(half, nx, ny)
+    rng = np.random.default_rng(nx * 7 + ny)
+    u = rng.normal(0.0, 0.01, (d, nx * ny))
+    f_ref, e_ref, u0_ref = oracle_post_force(full, linf, u, nx, ny)
+    for prec, tol in (("f64", F64_TOL), ("f32", FP32_TOL)):
+        s = _solver(nx, ny, d, prec, half, "half", linf)
+        f = np.zeros_like(u)
+        e = s.post_force(u, f)
+        assert rel_l2(f, f_ref) <= tol, prec
+        assert abs(e - e_ref) <= tol * abs(e_ref), prec
+
+
+def test_errors_are_status_codes_on_gpu():
+    g = gfmd_pkg()
+    s = g.gfmd_solver_factory()
+    s.set_grid_size(16, 16, 3)
+    u = torch.zeros(3, 256, dtype=torch.float64, device="cuda")
+    with pytest.raises(g.GFMDError) as ei:
+        s.post_force(u, torch.empty_like(u))
+    assert ei.value.code == 7  # no table yet
+    phi = np.zeros((16, 9, 3, 3), np.complex128)
+    phi[0, 0, 0, 0] = np.nan
+    with pytest.raises(g.GFMDError) as ei:
+        s.set_phi(phi, "half")
+    assert ei.value.code == 4
+    with pytest.raises(g.GFMDError):
+        s.post_force(u, u)

@@ -1,0 +1,70 @@
+"""The oracle restatement, pinned against the reference's own outputs.
+
+The golden fixtures hold forces, energies and u(q=0) of the reference's
+unmodified GFMDSolverStatic::post_force (see tests/golden/make_golden.py).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import (golden_cases, gfmd_pkg, half_to_full, load_golden, oracle,
+                      oracle_post_force, rel_l2)
+
+
+@pytest.mark.parametrize("nx,ny", [(8, 8), (12, 10), (37, 64), (64, 37), (30, 7), (1, 16), (16, 1)])
+def test_oracle_fft_matches_numpy(nx, ny):
+    rng = np.random.default_rng(nx * 1000 + ny)
+    x = rng.normal(size=(nx, ny)) + 1j * rng.normal(size=(nx, ny))
+    a = x.copy()
+    assert oracle().orc_fft2d(a.ctypes.data, nx, ny, 1, 0) == 0
+    b = x.copy()
+    assert oracle().orc_fft2d(b.ctypes.data, nx, ny, -1, 0) == 0
+    assert np.abs(a - np.fft.fft2(x)).max() <= 1e-12 * np.abs(x).sum() ** 0.5 * 10
+    assert np.abs(b - np.fft.ifft2(x) * nx * ny).max() <= 1e-12 * np.abs(x).sum() ** 0.5 * 10
+
+
+def test_oracle_fft_matches_direct_dft():
+    nx, ny = 6, 10
+    rng = np.random.default_rng(3)
+    x = rng.normal(size=(nx, ny)) + 1j * rng.normal(size=(nx, ny))
+    ix = np.arange(nx)[:, None]
+    iy = np.arange(ny)[None, :]
+    direct = np.zeros_like(x)
+    for kx in range(nx):
+        for ky in range(ny):
+            direct[kx, ky] = np.sum(x * np.exp(-2j * np.pi * (kx * ix / nx + ky * iy / ny)))
+    a = x.copy()
+    oracle().orc_fft2d(a.ctypes.data, nx, ny, 1, 1)
+    assert np.abs(a - direct).max() < 1e-12
+
+
+@pytest.mark.parametrize("path", golden_cases(), ids=lambda p: os.path.basename(p)[:-4])
+def test_oracle_matches_reference_fixture(path):
+    c = load_golden(path)
+    nx, ny = int(c["nx"]), int(c["ny"])
+    if "phi" in c:
+        phi = c["phi"]
+    else:
+        k = gfmd_pkg().StiffnessKernel(str(c["args"]))
+        phi, _ = k.phi_table(nx, ny, "full")
+    f, e, u0 = oracle_post_force(phi, c["linf"], c["u"], nx, ny)
+    assert rel_l2(f, c["f"]) <= 1e-12
+    assert abs(e - float(c["epot"])) <= 1e-12 * abs(float(c["epot"]))
+    assert np.allclose(u0, c["u0"], rtol=1e-12, atol=1e-15)
+
+
+def test_energy_identity_without_linf():
+    # E = -1/2 sum u.f when the gamma-point force is zero (observed ~1e-16)
+    c = load_golden(os.path.join(os.path.dirname(__file__), "golden", "fcc100x4_h64_8x8.npz"))
+    e = float(c["epot"])
+    assert abs(e + 0.5 * np.sum(c["u"] * c["f"])) <= 1e-13 * abs(e)
+
+
+def test_half_table_expands_to_reference_table():
+    c = load_golden(os.path.join(os.path.dirname(__file__), "golden", "fcc100x2_h64_12x10.npz"))
+    nx, ny = int(c["nx"]), int(c["ny"])
+    k = gfmd_pkg().StiffnessKernel(str(c["args"]))
+    half, _ = k.phi_table(nx, ny, "half")
+    full = half_to_full(half, nx, ny)
+    assert np.abs(full - c["phi"]).max() <= 1e-13 * np.abs(c["phi"]).max()

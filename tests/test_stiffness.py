@@ -1,0 +1,91 @@
+"""Host-side Phi(q) table producer against the reference's fill_phi_buffer."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import golden_cases, gfmd_pkg, load_golden
+
+
+def _ft_cases():
+    out = []
+    for p in golden_cases():
+        c = load_golden(p)
+        if "phi" in c and str(c["args"]).startswith("ft "):
+            out.append(p)
+    return out
+
+
+@pytest.mark.parametrize("path", _ft_cases(), ids=lambda p: os.path.basename(p)[:-4])
+def test_phi_table_matches_reference(path):
+    c = load_golden(path)
+    nx, ny = int(c["nx"]), int(c["ny"])
+    k = gfmd_pkg().StiffnessKernel(str(c["args"]))
+    assert k.get_dimension() == int(c["ndof"])
+    assert k.get_height() == int(c["height"])
+    phi, linf = k.phi_table(nx, ny, "full")
+    ref = c["phi"]
+    # per wavevector, relative to that wavevector's matrix norm
+    num = np.linalg.norm((phi - ref).reshape(nx * ny, -1), axis=1)
+    den = np.linalg.norm(ref.reshape(nx * ny, -1), axis=1)
+    assert (num / den).max() <= 1e-12
+    assert np.array_equal(linf, c["linf"])
+
+
+def test_phi_half_layout_is_a_slice_of_full():
+    k = gfmd_pkg().StiffnessKernel("ft fcc111 1 1.0 pair-potential 1 1.0 height 16")
+    full, _ = k.phi_table(6, 8, "full")
+    half, _ = k.phi_table(6, 8, "half")
+    assert np.array_equal(full.reshape(6, 8, 6, 6)[:, :5], half)
+
+
+def test_pair_potential_linf_keyword_gives_zero_gamma_force():
+    # FCPairPotential::linear does not override ForceConstants::linear in the
+    # reference, so the gamma-point force of `ft ... pair-potential ... linf`
+    # is zero; the values must still sum to zero.
+    k = gfmd_pkg().StiffnessKernel("ft fcc100 1.0 2 pair-potential 1 1.0 linf 2 0.1 -0.1 height 4")
+    assert np.array_equal(k.get_force_at_gamma_point(), np.zeros(2))
+    g = gfmd_pkg()
+    with pytest.raises(g.GFMDError):
+        g.StiffnessKernel("ft fcc100 1.0 2 pair-potential 1 1.0 linf 2 0.1 0.1 height 4")
+
+
+@pytest.mark.parametrize(
+    "args",
+    [
+        "",
+        "nosuchkernel 1 2",
+        "ft",
+        "ft sc100",
+        "ft nosuchsurface 1.0 1 pair-potential 1 1.0",
+        "ft sc100 1.0 1",
+        "ft sc100 1.0 1 lj/cut 1",
+        "ft sc100 abc 1 pair-potential 1 1.0",
+        "ft sc100 1.0 1 pair-potential 1 1.0 height 8 extra",
+        "ft sc100 1.0 1 pair-potential 4 1 1 1 1",
+    ],
+)
+def test_malformed_kernel_arguments_raise(args):
+    g = gfmd_pkg()
+    with pytest.raises(g.GFMDError) as ei:
+        g.StiffnessKernel(args)
+    assert ei.value.code == 1
+
+
+def test_singular_nn_only_simple_cubic_is_reported():
+    # central nearest-neighbour springs on sc carry no shear: the reference
+    # aborts with "Singular matrix in complex GaussJordan"
+    g = gfmd_pkg()
+    k = g.StiffnessKernel("ft sc100 1.0 1 pair-potential 1 1.0 height 16")
+    with pytest.raises(g.GFMDError):
+        k.phi_table(4, 4, "half")
+
+
+def test_phi_is_hermitian_and_inversion_symmetric():
+    k = gfmd_pkg().StiffnessKernel("ft fcc100 1.0 4 pair-potential 1 1.0 height 8")
+    nx, ny = 6, 10
+    phi, _ = k.phi_table(nx, ny, "full")
+    assert np.abs(phi - np.conj(np.swapaxes(phi, 1, 2))).max() < 1e-15
+    P = phi.reshape(nx, ny, 12, 12)
+    Pm = P[(-np.arange(nx)) % nx][:, (-np.arange(ny)) % ny]
+    assert np.abs(Pm - np.conj(P)).max() < 1e-15

@@ -1,0 +1,94 @@
+"""ctypes binding of the gfmd_gb300 C ABI (include/gfmd_gb300.h).
+
+The native library is required: importing the bindings fails loudly when
+``libgfmd_gb300.so`` has not been built, and there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgfmd_gb300.so")
+
+GFMD_OK = 0
+GFMD_EINVAL = 1
+GFMD_ENOMEM = 2
+GFMD_ECUDA = 3
+GFMD_ENONFINITE = 4
+GFMD_ETIMEDOUT = 5
+GFMD_ENOTCONVERGED = 6
+GFMD_ENOPHI = 7
+
+GFMD_PREC_F64 = 0
+GFMD_PREC_F32 = 1
+GFMD_PHI_FULL = 0
+GFMD_PHI_HALF = 1
+
+_NAMES = {
+    GFMD_EINVAL: "EINVAL",
+    GFMD_ENOMEM: "ENOMEM",
+    GFMD_ECUDA: "ECUDA",
+    GFMD_ENONFINITE: "ENONFINITE",
+    GFMD_ETIMEDOUT: "ETIMEDOUT",
+    GFMD_ENOTCONVERGED: "ENOTCONVERGED",
+    GFMD_ENOPHI: "ENOPHI",
+}
+
+
+class GFMDError(RuntimeError):
+    """A non-zero status from the C ABI, with the library's message."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{_NAMES.get(code, code)}] {msg}")
+        self.code = code
+
+
+_c_int, _c_dbl, _vp = ctypes.c_int, ctypes.c_double, ctypes.c_void_p
+_pi = ctypes.POINTER(ctypes.c_int)
+_pd = ctypes.POINTER(ctypes.c_double)
+
+# (name, argtypes) for every entry point of include/gfmd_gb300.h
+SIGNATURES = {
+    "gfmd_last_error": [],
+    "gfmd_version": [],
+    "gfmd_create": [_c_int, _c_int, _c_int, _c_int, ctypes.POINTER(_vp)],
+    "gfmd_destroy": [_vp],
+    "gfmd_set_stream": [_vp, _vp],
+    "gfmd_set_phi": [_vp, _vp, _c_int, _vp],
+    "gfmd_post_force": [_vp, _vp, _vp, _pd],
+    "gfmd_post_force_host": [_vp, _vp, _vp, _pd],
+    "gfmd_force_f64": [_vp, _vp, _vp, _vp],
+    "gfmd_force_f32": [_vp, _vp, _vp, _vp],
+    "gfmd_get_u0": [_vp, _vp],
+    "gfmd_memory_usage": [_vp, _pd],
+    "gfmd_kernel_create": [ctypes.c_char_p, ctypes.POINTER(_vp)],
+    "gfmd_kernel_destroy": [_vp],
+    "gfmd_kernel_info": [_vp, _pi, _pi],
+    "gfmd_kernel_phi": [_vp, _c_int, _c_int, _c_int, _vp, _vp, _c_int],
+}
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """Load the native library (once)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                f"gfmd_gb300 native library not built: {LIB_PATH} is missing "
+                "(run __graft_entry__.build())"
+            )
+        L = ctypes.CDLL(LIB_PATH)
+        for name, args in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_char_p if name in ("gfmd_last_error", "gfmd_version") else _c_int
+        _lib = L
+    return _lib
+
+
+def check(rc: int) -> None:
+    if rc != GFMD_OK:
+        raise GFMDError(rc, lib().gfmd_last_error().decode(errors="replace"))

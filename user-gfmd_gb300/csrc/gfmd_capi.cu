@@ -1,0 +1,393 @@
+// C ABI of gfmd_gb300 (declared in include/gfmd_gb300.h): solver handles,
+// FFT plans and twiddle tables, stiffness-table packing and upload, and the
+// host-side stiffness-kernel tables.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "gfmd_internal.h"
+#include "stiffness.h"
+
+struct gfmd_kernel {
+  std::unique_ptr<gfmd::StiffnessKernel> k;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg) {
+  g_err = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+  return fail(e == cudaErrorMemoryAllocation ? GFMD_ENOMEM : GFMD_ECUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call, what)                        \
+  do {                                        \
+    cudaError_t e_ = (call);                  \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+constexpr double kPi = 3.14159265358979323846264338327950288;
+
+void release(gfmd_solver *h) {
+  if (!h) return;
+  void *ptrs[] = {h->d_tw_hi, h->d_tw_lo, h->d_W, h->d_phi, h->d_linf, h->d_epart, h->d_scal, h->d_io};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  delete h;
+}
+
+// Runs fn(i0, i1) over [0, n) on all host cores.
+template <typename F> void parallel_for(long n, F fn) {
+  int nt = (int)std::max(1u, std::thread::hardware_concurrency());
+  if (n < 4096) nt = 1;
+  std::vector<std::thread> th;
+  long chunk = (n + nt - 1) / nt;
+  for (int t = 0; t < nt; t++) {
+    long a = t * chunk, b = std::min(n, a + chunk);
+    if (a >= b) break;
+    if (t == nt - 1 || nt == 1) fn(a, b);
+    else th.emplace_back(fn, a, b);
+  }
+  for (auto &t : th) t.join();
+}
+
+}  // namespace
+
+namespace gfmd {
+
+FftPlan make_plan(int n, std::vector<double> &tw) {
+  FftPlan p{};
+  p.n = n;
+  int m = n, k = 0;
+  while (m % 8 == 0) { p.radix[k++] = 8; m /= 8; }
+  if (m % 4 == 0) { p.radix[k++] = 4; m /= 4; }
+  if (m % 2 == 0) { p.radix[k++] = 2; m /= 2; }
+  for (int f = 3; m > 1; f += 2)
+    while (m % f == 0) { p.radix[k++] = f; m /= f; }
+  p.nst = k;
+  int span = 1;
+  for (int s = 0; s < k; s++) {
+    const int R = p.radix[s], L = span * R;
+    p.span[s] = span;
+    p.twoff[s] = (int)(tw.size() / 2);
+    for (int kk = 0; kk < span; kk++)
+      for (int r = 0; r < R; r++) {
+        long e = ((long)r * kk) % L;
+        double a = -2.0 * kPi * (double)e / (double)L;
+        tw.push_back(std::cos(a));
+        tw.push_back(std::sin(a));
+      }
+    p.rootoff[s] = (int)(tw.size() / 2);
+    if (R != 2 && R != 3 && R != 4 && R != 5 && R != 8)
+      for (int mm = 0; mm < R; mm++) {
+        double a = -2.0 * kPi * (double)mm / (double)R;
+        tw.push_back(std::cos(a));
+        tw.push_back(std::sin(a));
+      }
+    span = L;
+  }
+  return p;
+}
+
+}  // namespace gfmd
+
+extern "C" {
+
+const char *gfmd_last_error(void) { return g_err.c_str(); }
+
+const char *gfmd_version(void) { return "gfmd_gb300 0.1 (sm_103a)"; }
+
+int gfmd_create(int nx, int ny, int ndof, int precision, gfmd_handle_t *out) {
+  if (!out) return fail(GFMD_EINVAL, "gfmd_create: out is NULL");
+  *out = nullptr;
+  if (nx < 1 || ny < 1 || nx > 8192 || ny > 8192)
+    return fail(GFMD_EINVAL, "gfmd_create: nx, ny must be in [1, 8192]");
+  if (ndof < 3 || ndof > gfmd::kMaxNdof || ndof % 3 != 0)
+    return fail(GFMD_EINVAL, "gfmd_create: ndof must be 3, 6, ..., 24");
+  if (precision != GFMD_PREC_F64 && precision != GFMD_PREC_F32)
+    return fail(GFMD_EINVAL, "gfmd_create: unknown precision");
+
+  auto *h = new gfmd_solver();
+  h->precision = precision;
+  gfmd::Geom &g = h->g;
+  g.nx = nx;
+  g.ny = ny;
+  g.ndof = ndof;
+  g.nyc = ny / 2 + 1;
+  g.nxp = (nx + 31) / 32 * 32;
+  g.ny_even = (ny % 2 == 0) ? 1 : 0;
+  g.nrow = g.ny_even ? ny / 2 : ny;
+  g.npk = ndof * ndof;
+
+  cudaError_t e = cudaGetDevice(&h->device);
+  if (e != cudaSuccess) { release(h); return cuda_fail(e, "gfmd_create: cudaGetDevice"); }
+  int v = 0;
+  cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, h->device);
+  h->sm_count = v;
+  cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+  h->smem_optin = (size_t)v;
+
+  const size_t cs = precision == GFMD_PREC_F64 ? 16 : 8;
+  if (2 * (size_t)(g.nrow + 1) * cs > h->smem_optin || 2 * (size_t)nx * cs > h->smem_optin) {
+    release(h);
+    return fail(GFMD_EINVAL, "gfmd_create: grid too large for this precision");
+  }
+
+  // plans and twiddles: row plan, column plan, r2c post-twiddles
+  std::vector<double> tw;
+  h->plan_row = gfmd::make_plan(g.nrow, tw);
+  h->plan_col = gfmd::make_plan(nx, tw);
+  g.rpost = (int)(tw.size() / 2);
+  for (int k = 0; k <= ny / 2; k++) {
+    double a = -2.0 * kPi * (double)k / (double)ny;
+    tw.push_back(std::cos(a));
+    tw.push_back(std::sin(a));
+  }
+  const size_t ntw = tw.size() / 2;
+  if (precision == GFMD_PREC_F64) {
+    e = cudaMalloc(&h->d_tw_hi, ntw * sizeof(double2));
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_tw_hi, tw.data(), ntw * sizeof(double2), cudaMemcpyHostToDevice);
+  } else {
+    std::vector<float> hi(2 * ntw), lo(2 * ntw);
+    for (size_t i = 0; i < 2 * ntw; i++) {
+      hi[i] = (float)tw[i];
+      lo[i] = (float)(tw[i] - (double)hi[i]);
+    }
+    e = cudaMalloc(&h->d_tw_hi, ntw * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_tw_lo, ntw * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_tw_hi, hi.data(), ntw * sizeof(float2), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_tw_lo, lo.data(), ntw * sizeof(float2), cudaMemcpyHostToDevice);
+  }
+  if (e != cudaSuccess) { release(h); return cuda_fail(e, "gfmd_create: twiddles"); }
+
+  size_t wb, pb;
+  gfmd::force_layout(g, precision, &wb, &pb, &h->n_epart);
+  e = cudaMalloc(&h->d_W, wb);
+  if (e == cudaSuccess) e = cudaMalloc(&h->d_phi, pb);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_linf, sizeof(double) * (ndof / 3));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_epart, sizeof(double) * h->n_epart);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_scal, sizeof(double) * (1 + gfmd::kMaxNdof));
+  if (e == cudaSuccess) e = cudaMemset(h->d_linf, 0, sizeof(double) * (ndof / 3));
+  if (e == cudaSuccess) e = cudaMemset(h->d_scal, 0, sizeof(double) * (1 + gfmd::kMaxNdof));
+  if (e != cudaSuccess) { release(h); return cuda_fail(e, "gfmd_create: device buffers"); }
+  h->bytes = (double)wb + (double)pb + 8.0 * (h->n_epart + ndof / 3 + 1 + gfmd::kMaxNdof) +
+             (double)ntw * cs * (precision == GFMD_PREC_F64 ? 1 : 2);
+  *out = h;
+  return GFMD_OK;
+}
+
+int gfmd_destroy(gfmd_handle_t h) {
+  if (!h) return fail(GFMD_EINVAL, "gfmd_destroy: NULL handle");
+  release(h);
+  return GFMD_OK;
+}
+
+int gfmd_set_stream(gfmd_handle_t h, void *stream) {
+  if (!h) return fail(GFMD_EINVAL, "gfmd_set_stream: NULL handle");
+  h->stream = reinterpret_cast<cudaStream_t>(stream);
+  return GFMD_OK;
+}
+
+int gfmd_memory_usage(gfmd_handle_t h, double *bytes) {
+  if (!h || !bytes) return fail(GFMD_EINVAL, "gfmd_memory_usage: NULL argument");
+  *bytes = h->bytes;
+  return GFMD_OK;
+}
+
+// Pack the table into [nyc][npk][nxp] reals of the handle's precision:
+// Phi_eff(k) = (Phi(k) + conj Phi(-k)) / 2 on the stored half spectrum, then
+// its Hermitian part H; p < D holds Re H_pp, then (Re H_ij, Im H_ij) for
+// i < j in row-major order.  With Phi_eff the half-spectrum real transforms
+// reproduce the real part of the reference's full complex transforms.
+int gfmd_set_phi(gfmd_handle_t h, const double *phi, int layout, const double *linf) {
+  if (!h || !phi) return fail(GFMD_EINVAL, "gfmd_set_phi: NULL argument");
+  if (layout != GFMD_PHI_FULL && layout != GFMD_PHI_HALF)
+    return fail(GFMD_EINVAL, "gfmd_set_phi: unknown layout");
+  const gfmd::Geom &g = h->g;
+  const int D = g.ndof, D2 = D * D;
+  const size_t nq = (size_t)g.nyc * g.nxp;
+  const bool f64 = h->precision == GFMD_PREC_F64;
+  std::vector<double> packd;
+  std::vector<float> packf;
+  if (f64) packd.assign(nq * D2, 0.0);
+  else packf.assign(nq * D2, 0.0f);
+  bool finite = true;
+
+  auto src = [&](int kx, int ky) -> const double * {
+    if (layout == GFMD_PHI_FULL) return phi + 2 * ((size_t)kx * g.ny + ky) * D2;
+    return phi + 2 * ((size_t)kx * g.nyc + ky) * D2;
+  };
+  parallel_for((long)g.nyc * g.nx, [&](long a, long b) {
+    std::vector<double> eff(2 * D2);
+    bool ok = true;
+    for (long t = a; t < b; t++) {
+      int ky = (int)(t / g.nx), kx = (int)(t % g.nx);
+      int mx = (g.nx - kx) % g.nx, my = (g.ny - ky) % g.ny;
+      const double *pa = src(kx, ky);
+      const double *pb = nullptr;
+      if (layout == GFMD_PHI_FULL) pb = src(mx, my);
+      else if (my == ky) pb = src(mx, ky);  // ky = 0 or ny/2: mirror stored
+      for (int e = 0; e < D2; e++) {
+        if (pb) {
+          eff[2 * e] = 0.5 * (pa[2 * e] + pb[2 * e]);
+          eff[2 * e + 1] = 0.5 * (pa[2 * e + 1] - pb[2 * e + 1]);
+        } else {
+          eff[2 * e] = pa[2 * e];
+          eff[2 * e + 1] = pa[2 * e + 1];
+        }
+      }
+      size_t base = (size_t)ky * D2 * g.nxp + kx;
+      auto put = [&](int p, double v) {
+        if (!std::isfinite(v)) ok = false;
+        if (f64) packd[base + (size_t)p * g.nxp] = v;
+        else packf[base + (size_t)p * g.nxp] = (float)v;
+      };
+      for (int i = 0; i < D; i++) put(i, eff[2 * (i * D + i)]);
+      int p = D;
+      for (int i = 0; i < D; i++)
+        for (int j = i + 1; j < D; j++) {
+          double re = 0.5 * (eff[2 * (i * D + j)] + eff[2 * (j * D + i)]);
+          double im = 0.5 * (eff[2 * (i * D + j) + 1] - eff[2 * (j * D + i) + 1]);
+          put(p++, re);
+          put(p++, im);
+        }
+    }
+    if (!ok) finite = false;
+  });
+  if (!finite) return fail(GFMD_ENONFINITE, "gfmd_set_phi: table holds NaN or Inf");
+  const void *hp = f64 ? (const void *)packd.data() : (const void *)packf.data();
+  size_t bytes = nq * D2 * (f64 ? 8 : 4);
+  CK(cudaMemcpy(h->d_phi, hp, bytes, cudaMemcpyHostToDevice), "gfmd_set_phi: upload");
+  std::vector<double> lf(D / 3, 0.0);
+  if (linf)
+    for (int i = 0; i < D / 3; i++) lf[i] = linf[i];
+  CK(cudaMemcpy(h->d_linf, lf.data(), sizeof(double) * lf.size(), cudaMemcpyHostToDevice),
+     "gfmd_set_phi: linf");
+  h->have_phi = true;
+  return GFMD_OK;
+}
+
+static int force_common(gfmd_handle_t h, const void *d_u, int in_t, void *d_f, int out_t,
+                        double *d_epot, const char *who) {
+  if (!h || !d_u || !d_f) return fail(GFMD_EINVAL, std::string(who) + ": NULL argument");
+  if (d_u == d_f) return fail(GFMD_EINVAL, std::string(who) + ": u and f must not alias");
+  if (!h->have_phi) return fail(GFMD_ENOPHI, std::string(who) + ": no stiffness table uploaded");
+  cudaError_t e = gfmd::enqueue_force(h, d_u, in_t, d_f, out_t, d_epot ? d_epot : h->d_scal);
+  if (e != cudaSuccess) return cuda_fail(e, who);
+  return GFMD_OK;
+}
+
+int gfmd_force_f64(gfmd_handle_t h, const double *d_u, double *d_f, double *d_epot) {
+  if (h && h->precision != GFMD_PREC_F64)
+    return fail(GFMD_EINVAL, "gfmd_force_f64: handle is not FP64");
+  return force_common(h, d_u, 0, d_f, 0, d_epot, "gfmd_force_f64");
+}
+
+int gfmd_force_f32(gfmd_handle_t h, const float *d_u, float *d_f, double *d_epot) {
+  if (h && h->precision != GFMD_PREC_F32)
+    return fail(GFMD_EINVAL, "gfmd_force_f32: handle is not FP32");
+  return force_common(h, d_u, 1, d_f, 1, d_epot, "gfmd_force_f32");
+}
+
+int gfmd_post_force(gfmd_handle_t h, const double *d_u, double *d_f, double *epot) {
+  int rc = force_common(h, d_u, 0, d_f, 0, h ? h->d_scal : nullptr, "gfmd_post_force");
+  if (rc) return rc;
+  double e = 0.0;
+  CK(cudaMemcpyAsync(&e, h->d_scal, sizeof(double), cudaMemcpyDeviceToHost, h->stream),
+     "gfmd_post_force: energy");
+  CK(cudaStreamSynchronize(h->stream), "gfmd_post_force");
+  if (!std::isfinite(e)) return fail(GFMD_ENONFINITE, "gfmd_post_force: energy is not finite");
+  if (epot) *epot = e;
+  return GFMD_OK;
+}
+
+int gfmd_post_force_host(gfmd_handle_t h, const double *u, double *f, double *epot) {
+  if (!h || !u || !f) return fail(GFMD_EINVAL, "gfmd_post_force_host: NULL argument");
+  const size_t n = (size_t)h->g.ndof * h->g.nx * h->g.ny;
+  if (!h->d_io) CK(cudaMalloc(&h->d_io, 2 * n * sizeof(double)), "gfmd_post_force_host: staging");
+  double *du = reinterpret_cast<double *>(h->d_io), *df = du + n;
+  CK(cudaMemcpyAsync(du, u, n * sizeof(double), cudaMemcpyHostToDevice, h->stream),
+     "gfmd_post_force_host: copy in");
+  int rc = force_common(h, du, 0, df, 0, h->d_scal, "gfmd_post_force_host");
+  if (rc) return rc;
+  double e = 0.0;
+  CK(cudaMemcpyAsync(f, df, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream),
+     "gfmd_post_force_host: copy out");
+  CK(cudaMemcpyAsync(&e, h->d_scal, sizeof(double), cudaMemcpyDeviceToHost, h->stream),
+     "gfmd_post_force_host: energy");
+  CK(cudaStreamSynchronize(h->stream), "gfmd_post_force_host");
+  if (!std::isfinite(e)) return fail(GFMD_ENONFINITE, "gfmd_post_force_host: energy is not finite");
+  if (epot) *epot = e;
+  return GFMD_OK;
+}
+
+int gfmd_get_u0(gfmd_handle_t h, double *u0) {
+  if (!h || !u0) return fail(GFMD_EINVAL, "gfmd_get_u0: NULL argument");
+  CK(cudaMemcpyAsync(u0, h->d_scal + 1, sizeof(double) * h->g.ndof, cudaMemcpyDeviceToHost,
+                     h->stream),
+     "gfmd_get_u0");
+  CK(cudaStreamSynchronize(h->stream), "gfmd_get_u0");
+  return GFMD_OK;
+}
+
+// ---- stiffness-kernel tables ----------------------------------------------
+
+int gfmd_kernel_create(const char *args, gfmd_kernel_t *out) {
+  if (!args || !out) return fail(GFMD_EINVAL, "gfmd_kernel_create: NULL argument");
+  *out = nullptr;
+  std::istringstream is(args);
+  std::vector<std::string> tok;
+  std::string t;
+  while (is >> t) tok.push_back(t);
+  try {
+    size_t pos = 0;
+    std::unique_ptr<gfmd::StiffnessKernel> k(gfmd::StiffnessKernel::create(tok, pos));
+    if (pos != tok.size())
+      return fail(GFMD_EINVAL, "gfmd_kernel_create: unexpected argument '" + tok[pos] + "'");
+    *out = new gfmd_kernel{std::move(k)};
+  } catch (const std::exception &ex) {
+    return fail(GFMD_EINVAL, std::string("gfmd_kernel_create: ") + ex.what());
+  }
+  return GFMD_OK;
+}
+
+int gfmd_kernel_destroy(gfmd_kernel_t k) {
+  if (!k) return fail(GFMD_EINVAL, "gfmd_kernel_destroy: NULL kernel");
+  delete k;
+  return GFMD_OK;
+}
+
+int gfmd_kernel_info(gfmd_kernel_t k, int *ndof, int *height) {
+  if (!k) return fail(GFMD_EINVAL, "gfmd_kernel_info: NULL kernel");
+  if (ndof) *ndof = k->k->ndof();
+  if (height) *height = k->k->height();
+  return GFMD_OK;
+}
+
+int gfmd_kernel_phi(gfmd_kernel_t k, int nx, int ny, int layout, double *phi, double *linf,
+                    int nthreads) {
+  if (!k || !phi) return fail(GFMD_EINVAL, "gfmd_kernel_phi: NULL argument");
+  std::string err = gfmd::fill_phi_table(*k->k, nx, ny, layout, phi, nthreads);
+  if (!err.empty()) return fail(GFMD_EINVAL, "gfmd_kernel_phi: " + err);
+  if (linf) {
+    std::vector<double> l = k->k->linf();
+    for (size_t i = 0; i < l.size(); i++) linf[i] = l[i];
+  }
+  return GFMD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,80 @@
+// Internal declarations shared by the CUDA translation units of gfmd_gb300.
+#ifndef GFMD_GB300_INTERNAL_H
+#define GFMD_GB300_INTERNAL_H
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/gfmd_gb300.h"
+
+namespace gfmd {
+
+constexpr int kMaxStages = 24;
+constexpr int kMaxNdof = 24;
+
+// Mixed-radix Stockham plan of a length-n complex transform.  Stage s has
+// radix radix[s] and span (product of earlier radices) span[s]; its forward
+// twiddles exp(-2 pi i r k / (span*radix)) sit at twoff[s] + k*radix + r of
+// the handle's twiddle table, and for radices without a hand-written
+// butterfly the roots exp(-2 pi i m / radix) sit at rootoff[s] + m.
+struct FftPlan {
+  int n;
+  int nst;
+  int radix[kMaxStages];
+  int span[kMaxStages];
+  int twoff[kMaxStages];
+  int rootoff[kMaxStages];
+};
+
+// Builds the plan and appends its twiddles (FP64) to `tw`.
+FftPlan make_plan(int n, std::vector<double> &tw);
+
+// Geometry of one solver handle.
+struct Geom {
+  int nx, ny, ndof;
+  int nyc;      // ny/2 + 1 stored wavevectors along y
+  int nxp;      // padded row pitch (elements) of the spectrum and Phi arrays
+  int ny_even;  // ny even: real rows go through a half-length complex FFT
+  int nrow;     // length of the complex row transform (ny/2 or ny)
+  int rpost;    // table offset of exp(-2 pi i k/ny), k = 0..ny/2
+  int npk;      // packed Phi reals per wavevector (= ndof*ndof)
+};
+
+struct Launch;  // per-precision launch parameters (force_kernels.cu)
+
+}  // namespace gfmd
+
+struct gfmd_solver {
+  gfmd::Geom g;
+  int precision;
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  int sm_count = 0;
+  size_t smem_optin = 0;
+
+  gfmd::FftPlan plan_row{}, plan_col{};
+  void *d_tw_hi = nullptr;   // double2 (FP64) or float2 (FP32) twiddles
+  void *d_tw_lo = nullptr;   // float2 residuals (FP32 only)
+  void *d_W = nullptr;       // spectrum [nyc][ndof][nxp] complex
+  void *d_phi = nullptr;     // packed Phi [nyc][npk][nxp] real
+  double *d_linf = nullptr;  // [ndof/3]
+  double *d_epart = nullptr; // per-block energy partials
+  double *d_scal = nullptr;  // [0] energy, [1..ndof] u(q=0)
+  void *d_io = nullptr;      // staging for host-buffer calls: u then f, FP64
+  int n_epart = 0;
+  bool have_phi = false;
+  double bytes = 0.0;
+};
+
+namespace gfmd {
+// Enqueue one force evaluation.  u/f are [ndof][nx*ny] of type in_t/out_t
+// (0 = double, 1 = float); energy -> d_epot (device double).
+cudaError_t enqueue_force(gfmd_solver *h, const void *d_u, int in_t, void *d_f, int out_t,
+                          double *d_epot);
+// Device bytes of the spectrum/Phi arrays and the number of energy partials.
+void force_layout(const Geom &g, int precision, size_t *w_bytes, size_t *phi_bytes, int *n_epart);
+}  // namespace gfmd
+
+#endif

@@ -1,0 +1,504 @@
+// Host-side Phi(q) table producer; see stiffness.h for the reference
+// functions each part restates.
+#include "stiffness.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <stdexcept>
+#include <thread>
+
+namespace gfmd {
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846264338327950288;
+
+void inv3(const double *m, double *r) {
+  double det = m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) +
+               m[2] * (m[3] * m[7] - m[4] * m[6]);
+  if (det == 0.0) throw std::runtime_error("singular surface cell");
+  double id = 1.0 / det;
+  r[0] = (m[4] * m[8] - m[5] * m[7]) * id;
+  r[1] = (m[2] * m[7] - m[1] * m[8]) * id;
+  r[2] = (m[1] * m[5] - m[2] * m[4]) * id;
+  r[3] = (m[5] * m[6] - m[3] * m[8]) * id;
+  r[4] = (m[0] * m[8] - m[2] * m[6]) * id;
+  r[5] = (m[2] * m[3] - m[0] * m[5]) * id;
+  r[6] = (m[3] * m[7] - m[4] * m[6]) * id;
+  r[7] = (m[1] * m[6] - m[0] * m[7]) * id;
+  r[8] = (m[0] * m[4] - m[1] * m[3]) * id;
+}
+
+void matvec3(const double *m, const double *v, double *r) {
+  for (int i = 0; i < 3; i++) r[i] = m[3 * i] * v[0] + m[3 * i + 1] * v[1] + m[3 * i + 2] * v[2];
+}
+
+double parse_double(const std::vector<std::string> &tok, size_t &pos, const char *what,
+                    double lo, double hi) {
+  if (pos >= tok.size()) throw std::runtime_error(std::string("missing ") + what);
+  const char *s = tok[pos].c_str();
+  char *end;
+  double v = std::strtod(s, &end);
+  if (end == s) throw std::runtime_error(std::string("cannot convert ") + what + " '" + tok[pos] + "'");
+  if (lo != hi && (v < lo || v > hi))
+    throw std::runtime_error(std::string(what) + " out of range: '" + tok[pos] + "'");
+  pos++;
+  return v;
+}
+
+long parse_int(const std::vector<std::string> &tok, size_t &pos, const char *what, long lo,
+               long hi) {
+  if (pos >= tok.size()) throw std::runtime_error(std::string("missing ") + what);
+  const char *s = tok[pos].c_str();
+  char *end;
+  long v = std::strtol(s, &end, 10);
+  if (end == s) throw std::runtime_error(std::string("cannot convert ") + what + " '" + tok[pos] + "'");
+  if (lo != hi && (v < lo || v > hi))
+    throw std::runtime_error(std::string(what) + " out of range: '" + tok[pos] + "'");
+  pos++;
+  return v;
+}
+
+// ---- small dense complex matrices (row-major) ------------------------------
+
+inline cplx cmul(cplx a, cplx b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+
+// C = A*B
+void matmul(int n, const cplx *A, const cplx *B, cplx *C) {
+  for (int i = 0; i < n; i++) {
+    double cr[32], ci[32];
+    for (int j = 0; j < n; j++) cr[j] = ci[j] = 0.0;
+    for (int k = 0; k < n; k++) {
+      double ar = A[i * n + k].re, ai = A[i * n + k].im;
+      const cplx *b = B + k * n;
+      for (int j = 0; j < n; j++) {
+        cr[j] += ar * b[j].re - ai * b[j].im;
+        ci[j] += ar * b[j].im + ai * b[j].re;
+      }
+    }
+    for (int j = 0; j < n; j++) C[i * n + j] = {cr[j], ci[j]};
+  }
+}
+
+// In-place inverse by Gauss-Jordan elimination with partial (row) pivoting.
+bool invert(int n, cplx *A) {
+  int perm[32];
+  for (int c = 0; c < n; c++) {
+    int p = c;
+    double best = -1.0;
+    for (int r = c; r < n; r++) {
+      double m = A[r * n + c].re * A[r * n + c].re + A[r * n + c].im * A[r * n + c].im;
+      if (m > best) { best = m; p = r; }
+    }
+    if (!(best > 0.0)) return false;
+    perm[c] = p;
+    if (p != c)
+      for (int j = 0; j < n; j++) std::swap(A[c * n + j], A[p * n + j]);
+    cplx piv = A[c * n + c];
+    double d = 1.0 / (piv.re * piv.re + piv.im * piv.im);
+    cplx pinv = {piv.re * d, -piv.im * d};
+    A[c * n + c] = {1.0, 0.0};
+    for (int j = 0; j < n; j++) A[c * n + j] = cmul(A[c * n + j], pinv);
+    for (int r = 0; r < n; r++) {
+      if (r == c) continue;
+      cplx f = A[r * n + c];
+      if (f.re == 0.0 && f.im == 0.0) continue;
+      A[r * n + c] = {0.0, 0.0};
+      for (int j = 0; j < n; j++) {
+        cplx t = cmul(f, A[c * n + j]);
+        A[r * n + j].re -= t.re;
+        A[r * n + j].im -= t.im;
+      }
+    }
+  }
+  // undo the row interchanges as column interchanges, in reverse order
+  for (int c = n - 1; c >= 0; c--) {
+    int p = perm[c];
+    if (p != c)
+      for (int i = 0; i < n; i++) std::swap(A[i * n + c], A[i * n + p]);
+  }
+  return true;
+}
+
+}  // namespace
+
+// ---- crystal surfaces -------------------------------------------------------
+
+void CrystalSurface::set_cell(const double *c) {
+  if (c[1] != 0.0 || c[3] != 0.0 || c[6] != 0.0 || c[7] != 0.0)
+    throw std::runtime_error("cell must be aligned along x- and y-axis");
+  std::memcpy(cell, c, sizeof(cell));
+  inv3(cell, invcell);
+}
+
+// CrystalSurface::supercell(1, 1, nz) (src/main/crystal_surface.cpp:428-548),
+// before any neighbour list exists.
+void CrystalSurface::supercell_z(int nz) {
+  double old_cell[9];
+  std::memcpy(old_cell, cell, sizeof(cell));
+  double nc[9];
+  std::memcpy(nc, cell, sizeof(nc));
+  nc[2] *= nz;
+  nc[5] *= nz;
+  nc[8] *= nz;
+  nc[2] -= std::floor(nc[2] / nc[0]) * nc[0];
+  nc[5] -= std::floor(nc[5] / nc[4]) * nc[4];
+  set_cell(nc);
+  std::vector<double> np(3 * nat * nz);
+  for (int z = 0; z < nz; z++) {
+    for (int i = 0; i < nat; i++) {
+      int k = i + nat * z;
+      double c[3] = {0.0, 0.0, (double)z}, d[3], p[3], s[3];
+      matvec3(old_cell, c, d);
+      for (int a = 0; a < 3; a++) p[a] = pos[3 * i + a] + d[a];
+      matvec3(invcell, p, s);
+      for (int a = 0; a < 3; a++) s[a] -= std::floor(s[a]);
+      matvec3(cell, s, &np[3 * k]);
+    }
+  }
+  nat *= nz;
+  pos.swap(np);
+}
+
+void CrystalSurface::reverse_indices() {
+  std::vector<double> np(pos.size());
+  for (int i = 0; i < nat; i++)
+    for (int a = 0; a < 3; a++) np[3 * i + a] = pos[3 * (nat - 1 - i) + a];
+  pos.swap(np);
+}
+
+// set_cell_and_scale_atoms(a*cell): positions keep their scaled coordinates.
+void CrystalSurface::scale_cell(double a) {
+  double nc[9];
+  for (int i = 0; i < 9; i++) nc[i] = a * cell[i];
+  for (int i = 0; i < nat; i++) {
+    double s[3];
+    matvec3(invcell, &pos[3 * i], s);
+    std::memcpy(&pos[3 * i], s, sizeof(s));
+  }
+  set_cell(nc);
+  for (int i = 0; i < nat; i++) {
+    double r[3];
+    matvec3(cell, &pos[3 * i], r);
+    std::memcpy(&pos[3 * i], r, sizeof(r));
+  }
+}
+
+// compute_neighbor_list + identify_neighbor_shells
+// (src/main/crystal_surface.cpp:166-258).  The search range uses the squared
+// lattice-vector lengths exactly as the reference does.
+void CrystalSurface::compute_neighbor_list(double rcut) {
+  double lx = cell[0] * cell[0] + cell[3] * cell[3] + cell[6] * cell[6];
+  double ly = cell[1] * cell[1] + cell[4] * cell[4] + cell[7] * cell[7];
+  double lz = cell[2] * cell[2] + cell[5] * cell[5] + cell[8] * cell[8];
+  int nx = (int)std::lrint(std::floor(rcut / lx)) + 1;
+  int ny = (int)std::lrint(std::floor(rcut / ly)) + 1;
+  int nz = (int)std::lrint(std::floor(rcut / lz)) + 1;
+  neigh.clear();
+  for (int i = 0; i < nat; i++) {
+    for (int j = 0; j < nat; j++) {
+      for (int x = -nx; x <= nx; x++) {
+        for (int y = -ny; y <= ny; y++) {
+          for (int z = -nz; z <= nz; z++) {
+            if (i == j && x == 0 && y == 0 && z == 0) continue;
+            double d[3] = {(double)x, (double)y, (double)z}, cd[3];
+            matvec3(cell, d, cd);
+            LatticeNeighbor n;
+            for (int a = 0; a < 3; a++) n.r[a] = pos[3 * i + a] - pos[3 * j + a] - cd[a];
+            n.rnorm = std::sqrt(n.r[0] * n.r[0] + n.r[1] * n.r[1] + n.r[2] * n.r[2]);
+            if (n.rnorm < rcut) {
+              n.i = i;
+              n.j = j;
+              n.x = x;
+              n.y = y;
+              n.ab = z;
+              n.shell = -1;
+              neigh.push_back(n);
+            }
+          }
+        }
+      }
+    }
+  }
+  std::vector<double> shells;
+  for (auto &n : neigh) {
+    bool found = false;
+    for (double r : shells)
+      if (std::abs(n.rnorm - r) < 0.01) { found = true; break; }
+    if (!found) shells.push_back(n.rnorm);
+  }
+  std::sort(shells.begin(), shells.end());
+  for (auto &n : neigh)
+    for (size_t k = 0; k < shells.size(); k++)
+      if (std::abs(n.rnorm - shells[k]) < 0.01) { n.shell = (int)k; break; }
+}
+
+// ---- the ft kernel with pair-potential force constants ---------------------
+
+StiffnessKernel *StiffnessKernel::create(const std::vector<std::string> &tok, size_t &pos) {
+  if (pos >= tok.size()) throw std::runtime_error("missing stiffness kernel keyword");
+  const std::string kw = tok[pos++];
+  if (kw != "ft")
+    throw std::runtime_error("stiffness kernel '" + kw +
+                             "' has no table producer here; pass its table to gfmd_set_phi");
+  StiffnessKernel *k = new StiffnessKernel();
+  try {
+    k->name_ = "ft";
+    // crystal surface (crystal_surface_factory, src/main/crystal_surface.cpp:696-725)
+    if (pos >= tok.size()) throw std::runtime_error("missing crystal surface");
+    const std::string sname = tok[pos++];
+    CrystalSurface &s = k->surf_;
+    s.name = sname;
+    const double r2 = std::sqrt(2.0), r3 = std::sqrt(3.0);
+    if (sname == "sc100") {
+      const double c[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+      s.set_cell(c);
+      s.nat = 1;
+      s.pos = {0, 0, 0};
+    } else if (sname == "fcc100") {
+      const double c[9] = {1, 0, 0.5, 0, 1, 0.5, 0, 0, 1.0 / r2};
+      s.set_cell(c);
+      s.nat = 1;
+      s.pos = {0, 0, 0};
+    } else if (sname == "fcc111") {
+      const double c[9] = {1, 0, 0.5, 0, r3, 1.0 / (2.0 * r3), 0, 0, std::sqrt(2.0 / 3.0)};
+      s.set_cell(c);
+      s.nat = 2;
+      s.pos.assign(6, 0.0);
+      const double sp[3] = {0.5, 0.5, 0.0};
+      matvec3(s.cell, sp, &s.pos[3]);
+    } else {
+      throw std::runtime_error("could not find crystal surface '" + sname + "'");
+    }
+    double a = parse_double(tok, pos, "lattice constant", 0, 100);
+    int nu = (int)parse_int(tok, pos, "number of lattice cells", 1, 100);
+    if (nu > 1) {
+      s.supercell_z(nu);
+      s.reverse_indices();
+    }
+    s.scale_cell(a);
+
+    // force constants (force_constants_factory, src/main/force_constants.cpp:113-164)
+    if (pos >= tok.size()) throw std::runtime_error("missing interaction model");
+    const std::string fc = tok[pos++];
+    if (fc != "pair-potential")
+      throw std::runtime_error("interaction model '" + fc + "' is not available here");
+    s.compute_neighbor_list(2.01 * std::max(s.cell[0], s.cell[4]));
+    if (pos >= tok.size()) throw std::runtime_error("missing number of interacting neighbors");
+    std::string nks = tok[pos];
+    bool x = !nks.empty() && nks.back() == 'x';
+    if (x) nks.pop_back();
+    {
+      char *end;
+      long nk = std::strtol(nks.c_str(), &end, 10);
+      if (end == nks.c_str()) throw std::runtime_error("cannot convert neighbor shell count");
+      if (nk < 0 || nk > 3) throw std::runtime_error("at most 3 neighbor shells are supported");
+      pos++;
+      for (long i = 0; i < nk; i++) {
+        k->k_[i] = parse_double(tok, pos, "spring constant", 0, 0);
+        if (x) k->kappa_[i] = parse_double(tok, pos, "spring constant", 0, 0);
+      }
+    }
+    // optional keywords: `linf` (fc_pair_potential.cpp:99-132), `height` (ft_stiffness.cpp:85-99)
+    k->linf_.assign(s.nat, 0.0);
+    bool found = true;
+    while (pos + 1 < tok.size() && found) {
+      found = false;
+      if (tok[pos] == "linf") {
+        pos++;
+        int nl = (int)parse_int(tok, pos, "number of layers", 0, 0);
+        if (nl != s.nat) throw std::runtime_error("linf: number of layers must match the surface cell");
+        double sum = 0.0;
+        for (int i = 0; i < nl; i++) {
+          k->linf_[i] = parse_double(tok, pos, "linf", 0, 0);
+          sum += k->linf_[i];
+        }
+        if (std::abs(sum) > 1e-12) throw std::runtime_error("linear force contributions must sum to zero");
+        found = true;
+      } else if (tok[pos] == "height") {
+        pos++;
+        k->height_ = (int)parse_int(tok, pos, "height", 0, 0);
+        found = true;
+      }
+    }
+    k->dim_ = 3 * s.nat;
+    k->pre_compute();
+  } catch (...) {
+    delete k;
+    throw;
+  }
+  return k;
+}
+
+// FCPairPotential::offsite: D = -k e(x)e - kappa (1 - e(x)e).
+void StiffnessKernel::offsite(const LatticeNeighbor &n, double *D) const {
+  double e[3] = {n.r[0] / n.rnorm, n.r[1] / n.rnorm, n.r[2] / n.rnorm};
+  double k = 0.0, kap = 0.0;
+  if (n.shell < 3) {
+    k = k_[n.shell];
+    kap = kappa_[n.shell];
+  }
+  for (int a = 0; a < 3; a++)
+    for (int b = 0; b < 3; b++) {
+      double para = e[a] * e[b];
+      double perp = (a == b ? 1.0 : 0.0) - para;
+      D[3 * a + b] = -k * para - kap * perp;
+    }
+}
+
+// ForceConstants::onsite: D_ii = -sum_{neighbours with ab <= layer} D_ij.
+void StiffnessKernel::onsite(int i, int ab, double *D) const {
+  for (int a = 0; a < 9; a++) D[a] = 0.0;
+  for (const auto &n : surf_.neigh) {
+    if (n.i != i || n.ab > ab) continue;
+    double t[9];
+    offsite(n, t);
+    for (int a = 0; a < 9; a++) D[a] -= t[a];
+  }
+}
+
+// FTStiffnessKernel::pre_compute (src/stiffness_kernels/ft_stiffness.cpp:138-208).
+void StiffnessKernel::pre_compute() {
+  const int nn = (int)surf_.neigh.size();
+  Dij_.assign(9 * (size_t)nn, 0.0);
+  for (int n = 0; n < nn; n++) offsite(surf_.neigh[n], &Dij_[9 * (size_t)n]);
+  D0ii_.assign(9 * (size_t)surf_.nat, 0.0);
+  D1ii_.assign(9 * (size_t)surf_.nat, 0.0);
+  for (int i = 0; i < surf_.nat; i++) {
+    onsite(i, 0, &D0ii_[9 * (size_t)i]);
+    onsite(i, 1, &D1ii_[9 * (size_t)i]);
+  }
+}
+
+void StiffnessKernel::dynamical_matrices(double qx, double qy, cplx *U0, cplx *U, cplx *V) const {
+  const int d = dim_;
+  for (int i = 0; i < d * d; i++) U0[i] = U[i] = V[i] = {0.0, 0.0};
+  const int nn = (int)surf_.neigh.size();
+  for (int n = 0; n < nn; n++) {
+    const LatticeNeighbor &nb = surf_.neigh[n];
+    if (nb.ab < -1 || nb.ab > 0) continue;  // ab = +1 is the conjugate partner; |ab| > 1 ignored
+    double ph = nb.x * qx + nb.y * qy;
+    cplx phase = {std::cos(ph), std::sin(ph)};
+    const double *Y = &Dij_[9 * (size_t)n];
+    cplx *M = nb.ab == 0 ? U : V;
+    for (int a = 0; a < 3; a++)
+      for (int b = 0; b < 3; b++) {
+        size_t idx = (size_t)(3 * nb.i + a) * d + 3 * nb.j + b;
+        double y = Y[3 * a + b];
+        M[idx].re += phase.re * y;
+        M[idx].im += phase.im * y;
+        if (nb.ab == 0) {
+          U0[idx].re += phase.re * y;
+          U0[idx].im += phase.im * y;
+        }
+      }
+  }
+  for (int i = 0; i < surf_.nat; i++)
+    for (int a = 0; a < 3; a++)
+      for (int b = 0; b < 3; b++) {
+        size_t idx = (size_t)(3 * i + a) * d + 3 * i + b;
+        U0[idx].re += D0ii_[9 * (size_t)i + 3 * a + b];
+        U[idx].re += D1ii_[9 * (size_t)i + 3 * a + b];
+      }
+}
+
+// greens_function_transfer_matrix_stiffness with iterate_Gnn run exactly
+// height-1 times (src/main/surface_stiffness.cpp:811-873, 493-548):
+//   X = -V U^-1 V^+;  repeat: X = -V (U + X)^-1 V^+;  Phi = U0 + X.
+bool StiffnessKernel::stiffness(double qx, double qy, cplx *phi, cplx *work) const {
+  const int d = dim_, d2 = d * d;
+  cplx *U0 = work, *U = work + d2, *V = work + 2 * d2, *Vd = work + 3 * d2, *X = work + 4 * d2,
+       *T = work + 5 * d2;
+  dynamical_matrices(qx, qy, U0, U, V);
+  if (height_ == 0) {
+    std::memcpy(phi, U0, sizeof(cplx) * d2);
+    return true;
+  }
+  for (int i = 0; i < d; i++)
+    for (int j = 0; j < d; j++) Vd[i * d + j] = {-V[j * d + i].re, V[j * d + i].im};
+  std::memcpy(X, U, sizeof(cplx) * d2);
+  if (!invert(d, X)) return false;
+  matmul(d, X, Vd, T);
+  matmul(d, V, T, X);
+  if (height_ > 0) {
+    for (int it = 0; it < height_ - 1; it++) {
+      for (int i = 0; i < d2; i++) { X[i].re += U[i].re; X[i].im += U[i].im; }
+      if (!invert(d, X)) return false;
+      matmul(d, X, Vd, T);
+      matmul(d, V, T, X);
+    }
+  } else {
+    // semi-infinite substrate: iterate to a fixed point (eps 1e-8, :836)
+    cplx *L = phi;  // scratch until the end
+    for (int it = 0; it < 100000; it++) {
+      std::memcpy(L, X, sizeof(cplx) * d2);
+      for (int i = 0; i < d2; i++) { X[i].re += U[i].re; X[i].im += U[i].im; }
+      if (!invert(d, X)) return false;
+      matmul(d, X, Vd, T);
+      matmul(d, V, T, X);
+      double dn = 0.0;
+      for (int i = 0; i < d2; i++) {
+        double a = X[i].re - L[i].re, b = X[i].im - L[i].im;
+        dn += a * a + b * b;
+      }
+      if (dn <= 1e-16) break;
+      if (it == 99999) return false;
+    }
+  }
+  for (int i = 0; i < d2; i++) phi[i] = {U0[i].re + X[i].re, U0[i].im + X[i].im};
+  return true;
+}
+
+std::string fill_phi_table(const StiffnessKernel &k, int nx, int ny, int layout, double *phi,
+                           int nthreads) {
+  if (nx < 1 || ny < 1) return "grid dimensions must be positive";
+  if (layout != 0 && layout != 1) return "unknown table layout";
+  const int d = k.ndof(), d2 = d * d;
+  const int nyc = layout == 0 ? ny : ny / 2 + 1;
+  const double inv = 1.0 / ((double)nx * (double)ny);
+  if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
+  std::atomic<int> next(0);
+  std::atomic<int> bad_ix(-1), bad_herm(-1);
+  auto worker = [&]() {
+    std::vector<cplx> work(6 * (size_t)d2), p((size_t)d2);
+    for (;;) {
+      int ix = next.fetch_add(1);
+      if (ix >= nx) break;
+      // wavevector folding of fill_phi_buffer (src/main/gfmd_misc.cpp:43-48)
+      double qx = (ix <= nx / 2) ? 2.0 * kPi * ix / nx : 2.0 * kPi * (ix - nx) / nx;
+      for (int iy = 0; iy < nyc; iy++) {
+        double qy = (iy <= ny / 2) ? 2.0 * kPi * iy / ny : 2.0 * kPi * (iy - ny) / ny;
+        if (!k.stiffness(qx, qy, p.data(), work.data())) {
+          bad_ix.store(ix);
+          return;
+        }
+        // Hermitian check with the reference's tolerance (gfmd_misc.cpp:55-76)
+        double tr = 0.0, tri = 0.0;
+        for (int i = 0; i < d; i++) { tr += p[i * d + i].re; tri += p[i * d + i].im; }
+        double trabs = std::sqrt(tr * tr + tri * tri);
+        for (int i = 0; i < d; i++)
+          for (int j = 0; j < d; j++) {
+            double a = p[i * d + j].re - p[j * d + i].re, b = p[i * d + j].im + p[j * d + i].im;
+            if (std::sqrt(a * a + b * b) > 1e-6 * trabs) bad_herm.store(ix);
+          }
+        double *out = phi + 2 * ((size_t)ix * nyc + iy) * d2;
+        for (int e = 0; e < d2; e++) {
+          out[2 * e] = p[e].re * inv;
+          out[2 * e + 1] = p[e].im * inv;
+        }
+      }
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < nthreads; t++) th.emplace_back(worker);
+  worker();
+  for (auto &t : th) t.join();
+  if (bad_ix.load() >= 0) return "singular matrix while computing the stiffness kernel";
+  if (bad_herm.load() >= 0) return "kernel is not Hermitian";
+  return std::string();
+}
+
+}  // namespace gfmd

@@ -1,0 +1,226 @@
+"""Host-side mirror of the reference's solver and stiffness-kernel interface.
+
+Names, argument meaning and error behaviour follow the USER-GFMD classes they
+stand in for, so a caller of the reference's API finds the same calls:
+
+* ``StiffnessKernel`` / ``stiffness_kernel_factory`` —
+  ``StiffnessKernel`` (src/main/surface_stiffness.h:36-180) and
+  ``stiffness_kernel_factory`` (src/main/surface_stiffness.cpp:440-481);
+* ``GFMDSolverGB300`` / ``gfmd_solver_factory`` —
+  ``GFMDSolver`` (src/main/gfmd_solver.h:34-123), ``GFMDSolverStatic``
+  (src/solvers/gfmd_solver_static.cpp) and ``gfmd_solver_factory``
+  (src/main/gfmd_solver.cpp:209-256).
+
+Everything runs through the C ABI of ``libgfmd_gb300.so``; errors surface as
+``GFMDError`` carrying the C status code.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import GFMDError, check, lib
+
+
+def _ptr(a) -> int:
+    """Device or host address of a torch tensor or numpy array."""
+    if hasattr(a, "data_ptr"):
+        return int(a.data_ptr())
+    if isinstance(a, np.ndarray):
+        return int(a.ctypes.data)
+    if hasattr(a, "__cuda_array_interface__"):
+        return int(a.__cuda_array_interface__["data"][0])
+    raise TypeError(f"cannot take the address of {type(a)!r}")
+
+
+def _is_device(a) -> bool:
+    if hasattr(a, "is_cuda"):
+        return bool(a.is_cuda)
+    return hasattr(a, "__cuda_array_interface__")
+
+
+class StiffnessKernel:
+    """A stiffness kernel parsed from the kernel part of a ``fix gfmd`` line,
+    e.g. ``"ft fcc100 1.0 2 pair-potential 1 1.0 height 64"``."""
+
+    def __init__(self, args: str):
+        h = ctypes.c_void_p()
+        check(lib().gfmd_kernel_create(args.encode(), ctypes.byref(h)))
+        self._h = h
+        self.args = args
+        nd, ht = ctypes.c_int(), ctypes.c_int()
+        check(lib().gfmd_kernel_info(self._h, ctypes.byref(nd), ctypes.byref(ht)))
+        self._ndof, self._height = nd.value, ht.value
+        self._name = args.split()[0]
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value:
+            lib().gfmd_kernel_destroy(h)
+            self._h = ctypes.c_void_p()
+
+    def get_dimension(self) -> int:
+        return self._ndof
+
+    def get_number_of_atoms(self) -> int:
+        return self._ndof // 3
+
+    def get_height(self) -> int:
+        return self._height
+
+    def get_name(self) -> str:
+        return self._name
+
+    def phi_table(self, nx: int, ny: int, layout: str = "half", nthreads: int = 0):
+        """Phi(q) / (nx*ny) on the grid; returns (phi, linf).  ``layout``
+        "full" gives [nx*ny, ndof, ndof] (fill_phi_buffer's output), "half"
+        gives [nx, ny//2+1, ndof, ndof]."""
+        d = self._ndof
+        if layout == "full":
+            phi = np.empty((nx * ny, d, d), dtype=np.complex128)
+            lay = _lib.GFMD_PHI_FULL
+        elif layout == "half":
+            phi = np.empty((nx, ny // 2 + 1, d, d), dtype=np.complex128)
+            lay = _lib.GFMD_PHI_HALF
+        else:
+            raise ValueError(f"unknown layout {layout!r}")
+        linf = np.zeros(d // 3)
+        check(lib().gfmd_kernel_phi(self._h, nx, ny, lay, _ptr(phi), _ptr(linf), nthreads))
+        return phi, linf
+
+    def get_force_at_gamma_point(self) -> np.ndarray:
+        _, linf = self.phi_table(1, 1, "full")
+        return linf
+
+
+def stiffness_kernel_factory(keyword: str, *args: str) -> StiffnessKernel:
+    """``stiffness_kernel_factory(keyword, narg, carg, arg, ...)`` for string
+    arguments: ``stiffness_kernel_factory("ft", "sc100", "1.0", "1", ...)``."""
+    return StiffnessKernel(" ".join((keyword,) + tuple(args)))
+
+
+class GFMDSolverGB300:
+    """GB300 force evaluation behind the ``GFMDSolver`` interface.
+
+    ``post_force(u, f)`` takes [ndof, nx*ny] arrays: numpy (host, copied in
+    and out inside the call) or CUDA tensors (device, no host copies), and
+    returns the elastic energy like ``GFMDSolverStatic::post_force``.
+    """
+
+    def __init__(self, precision: str = "f64", name: str = "static/gb300"):
+        if precision not in ("f64", "f32"):
+            raise ValueError("precision must be 'f64' or 'f32'")
+        self.precision = precision
+        self.name = name
+        self._h = ctypes.c_void_p()
+        self.nx = self.ny = self.ndof = 0
+        self.u0 = None
+
+    # -- GFMDSolver API ------------------------------------------------------
+    def get_name(self) -> str:
+        return self.name
+
+    def set_grid_size(self, nx: int, ny: int, ndof: int) -> None:
+        self._free()
+        prec = _lib.GFMD_PREC_F64 if self.precision == "f64" else _lib.GFMD_PREC_F32
+        check(lib().gfmd_create(nx, ny, ndof, prec, ctypes.byref(self._h)))
+        self.nx, self.ny, self.ndof = nx, ny, ndof
+
+    def set_kernel(self, kernel: StiffnessKernel, normalize: bool = True) -> None:
+        if kernel.get_dimension() != self.ndof:
+            raise GFMDError(_lib.GFMD_EINVAL, "kernel dimension does not match ndof")
+        phi, linf = kernel.phi_table(self.nx, self.ny, "half")
+        if not normalize:
+            phi = phi * float(self.nx * self.ny)
+        self.set_phi(phi, "half", linf)
+
+    def set_phi(self, phi: np.ndarray, layout: str = "full", linf=None) -> None:
+        """Upload a table already scaled by 1/(nx*ny)."""
+        phi = np.ascontiguousarray(phi, dtype=np.complex128)
+        lay = _lib.GFMD_PHI_FULL if layout == "full" else _lib.GFMD_PHI_HALF
+        lf = None if linf is None else np.ascontiguousarray(linf, dtype=np.float64)
+        check(lib().gfmd_set_phi(self._handle(), _ptr(phi), lay, None if lf is None else _ptr(lf)))
+
+    def set_stream(self, stream) -> None:
+        addr = stream if isinstance(stream, int) else int(getattr(stream, "cuda_stream", 0))
+        check(lib().gfmd_set_stream(self._handle(), addr))
+
+    def post_force(self, u, f, dump_prefix=None) -> float:
+        if dump_prefix is not None:
+            raise GFMDError(_lib.GFMD_EINVAL, "q-space dumps are not supported by this solver")
+        e = ctypes.c_double()
+        if _is_device(u) and _is_device(f):
+            check(lib().gfmd_post_force(self._handle(), _ptr(u), _ptr(f), ctypes.byref(e)))
+        elif not _is_device(u) and not _is_device(f):
+            uh = np.ascontiguousarray(u, dtype=np.float64)
+            if not (isinstance(f, np.ndarray) and f.dtype == np.float64 and f.flags.c_contiguous):
+                raise TypeError("f must be a C-contiguous float64 numpy array")
+            check(lib().gfmd_post_force_host(self._handle(), _ptr(uh), _ptr(f), ctypes.byref(e)))
+        else:
+            raise TypeError("u and f must both be host arrays or both be device tensors")
+        return e.value
+
+    def force_async(self, u, f, epot) -> None:
+        """Device-resident evaluation without a host sync; epot is a device
+        float64 scalar tensor."""
+        fn = lib().gfmd_force_f64 if self.precision == "f64" else lib().gfmd_force_f32
+        check(fn(self._handle(), _ptr(u), _ptr(f), _ptr(epot)))
+
+    def get_u0(self) -> np.ndarray:
+        u0 = np.zeros(self.ndof)
+        check(lib().gfmd_get_u0(self._handle(), _ptr(u0)))
+        return u0
+
+    def memory_usage(self) -> float:
+        b = ctypes.c_double()
+        check(lib().gfmd_memory_usage(self._handle(), ctypes.byref(b)))
+        return b.value
+
+    def get_nxy_loc(self) -> int:
+        return self.nx * self.ny
+
+    def get_xlo_loc(self) -> int:
+        return 0
+
+    def get_xhi_loc(self) -> int:
+        return self.nx - 1
+
+    def get_ylo_loc(self) -> int:
+        return 0
+
+    def get_yhi_loc(self) -> int:
+        return self.ny - 1
+
+    # -- internals -----------------------------------------------------------
+    def _handle(self) -> ctypes.c_void_p:
+        if not self._h.value:
+            raise GFMDError(_lib.GFMD_EINVAL, "set_grid_size has not been called")
+        return self._h
+
+    def _free(self) -> None:
+        if self._h.value:
+            lib().gfmd_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self._free()
+        except Exception:
+            pass
+
+
+_SOLVERS = {"static": "f64", "static/gb300": "f64", "static/gb300/f32": "f32"}
+
+
+def gfmd_solver_factory(keyword: str | None = None, suffix: str | None = "gb300") -> GFMDSolverGB300:
+    """Solver by name.  Like the reference, ``<name>/<suffix>`` is looked up
+    when a suffix is active (src/main/gfmd_solver.cpp:215-221); the default
+    style is ``static``."""
+    name = keyword or "static"
+    if suffix and not name.endswith("/" + suffix) and "/" not in name:
+        name = f"{name}/{suffix}"
+    if name not in _SOLVERS:
+        raise GFMDError(_lib.GFMD_EINVAL, f"Unknown solver name encountered: '{name}'")
+    return GFMDSolverGB300(precision=_SOLVERS[name], name=name)
