@@ -1,0 +1,380 @@
+"""Benchmark: GFMD force evaluations per second at 2048^2.
+
+Workload (default): `fix gfmd` kernel `ft fcc100 1.0 4 pair-potential 1 1.0
+height 64` (fcc(100), four layers per surface cell, ndof = 12, 12x12
+Hermitian Phi per wavevector) on a 2048 x 2048 periodic grid; displacements
+seeded Gaussian, sigma = 0.01 lattice constants.  One step = one force
+evaluation u(r) -> f(r), E through the FP32 path (compensated twiddles, FP64
+energy), inputs resident in HBM (u 201 MB, Phi 1.21 GB: all larger than L2).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference's algorithm on the host cores: the
+oracle port of GFMDSolverStatic::post_force (per-DOF full complex 2-D FFTs,
+full-grid Phi table), on the same workload, all host threads.
+
+Prints one JSON line (rank 0).  Multi-GPU: the single-surface evaluation does
+not shard (every evaluation is a global 2-D FFT), so N GPUs run N independent
+replicas (weak scaling, no data-path collective).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "GFMD force evals/s at 2048²; static solve time to 1e-6 vs plain FP64 GPU"
+KERNEL = "ft fcc100 1.0 4 pair-potential 1 1.0 height 64"
+SEED = 20261203
+PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "force_eval_2048x2048_fcc100x4.md")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nx", type=int, default=2048)
+    ap.add_argument("--ny", type=int, default=2048)
+    ap.add_argument("--kernel", default=KERNEL)
+    ap.add_argument("--precision", default="f32", choices=["f32", "f64"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-f64", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def algorithmic_bytes(nx, ny, d, s):
+    """Bytes of one force evaluation: read u, write f, read the
+    Hermitian-packed half-spectrum Phi (ndof^2 reals per stored wavevector)."""
+    return 2 * nx * ny * d * s + nx * (ny // 2 + 1) * d * d * s
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            m = json.load(fh)
+        return float(m["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per force evaluation from the committed ncu summary."""
+    if not os.path.exists(PROFILE_SUMMARY):
+        return None
+    for line in open(PROFILE_SUMMARY):
+        if line.startswith("traffic_bytes_per_eval:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU reference (oracle port of GFMDSolverStatic::post_force)
+# ---------------------------------------------------------------------------
+
+def _oracle():
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle")])
+    L = ctypes.CDLL(os.path.join(ROOT, "oracle", "liboracle.so"))
+    L.orc_post_force.restype = ctypes.c_double
+    L.orc_post_force.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p] * 5 + [ctypes.c_int]
+    L.orc_phi_half_to_full.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p] * 2 + [ctypes.c_int]
+    L.orc_max_threads.restype = ctypes.c_int
+    return L
+
+
+def cpu_reference(args, half, linf, u, steps, warmup):
+    """Times the oracle port on all host threads; returns (evals/s, cores, seconds)."""
+    nx, ny, d = args.nx, args.ny, u.shape[0]
+    L = _oracle()
+    cores = L.orc_max_threads()
+    full = np.empty((nx * ny, d, d), np.complex128)
+    L.orc_phi_half_to_full(nx, ny, d, half.ctypes.data, full.ctypes.data, 0)
+    f = np.empty_like(u)
+    for _ in range(warmup):
+        L.orc_post_force(nx, ny, d, full.ctypes.data, linf.ctypes.data, u.ctypes.data,
+                         f.ctypes.data, None, 0)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        L.orc_post_force(nx, ny, d, full.ctypes.data, linf.ctypes.data, u.ctypes.data,
+                         f.ctypes.data, None, 0)
+    dt = time.perf_counter() - t0
+    del full
+    return steps / dt, cores, dt
+
+
+def workload_config(args, d):
+    return {
+        "workload": f"force evaluation, {args.kernel}, {args.nx}x{args.ny} periodic grid, ndof {d}",
+        "nx": args.nx, "ny": args.ny, "ndof": d, "kernel": args.kernel,
+        "u": f"seeded Gaussian sigma 0.01 a (seed {SEED})",
+        "l2": "inputs larger than L2 (u, f, Phi > 129 MB); no flush",
+        "parallelism": "replicas",
+    }
+
+
+def make_inputs(g, args):
+    k = g.StiffnessKernel(args.kernel)
+    d = k.get_dimension()
+    t = time.perf_counter()
+    half, linf = k.phi_table(args.nx, args.ny, "half")
+    t_phi = time.perf_counter() - t
+    rng = np.random.default_rng(SEED)
+    u = rng.normal(0.0, 0.01, (d, args.nx * args.ny))
+    return d, half, linf, u, t_phi
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    g = importlib.import_module("user-gfmd_gb300")
+    d, half, linf, u, _ = make_inputs(g, args)
+    steps = max(1, min(args.steps, 5))
+    warm = 1
+    v, cores, dt = cpu_reference(args, half, linf, u, steps, warm)
+    line = {
+        "metric": METRIC, "value": v, "unit": "evals/s", "n_gpus": args.gpus, "steps": steps,
+        "warmup": warm, "ms_per_step": 1000.0 * dt / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "impl": "reference", "config": workload_config(args, d),
+        "cpu_baseline": {"value": v, "unit": "evals/s", "cores": cores, "kind": "port",
+                         "sample": f"{steps} full force evaluations ({args.nx}x{args.ny}, ndof {d}) "
+                                   "after 1 warm-up; oracle restatement of "
+                                   "GFMDSolverStatic::post_force with its own FFT"},
+        "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GB300 arm
+# ---------------------------------------------------------------------------
+
+def time_device(torch, s, u, f, ep, steps, warmup, stream):
+    for _ in range(warmup):
+        s.force_async(u, f, ep)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        s.force_async(u, f, ep)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def run_gb300(args):
+    import torch
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    g = importlib.import_module("user-gfmd_gb300")
+    d, half, linf, u_h, t_phi = make_inputs(g, args)
+    nx, ny = args.nx, args.ny
+    stream = torch.cuda.current_stream(dev)
+
+    def solver(prec):
+        s = g.gfmd_solver_factory("static/gb300" if prec == "f64" else "static/gb300/f32")
+        s.set_grid_size(nx, ny, d)
+        s.set_phi(half, "half", linf)
+        s.set_stream(stream.cuda_stream)
+        return s
+
+    s = solver(args.precision)
+    tdt = torch.float32 if args.precision == "f32" else torch.float64
+    u = torch.from_numpy(u_h).to(dev, tdt)
+    f = torch.empty_like(u)
+    ep = torch.zeros(1, dtype=torch.float64, device=dev)
+
+    # warm-up, then the timed region bracketed by barrier + synchronize
+    for _ in range(args.warmup):
+        s.force_async(u, f, ep)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    clk = ClockSampler(local)
+    clk.start()
+    time.sleep(0.3)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        s.force_async(u, f, ep)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    if ws > 1:
+        torch.distributed.barrier()
+    clocks = clk.stop()
+    if ws > 1:
+        t = torch.tensor([ms], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * 1000.0 / ms
+
+    # accuracy of this path against the FP64 path on the same input
+    extra = {}
+    if not args.no_f64:
+        s64 = solver("f64")
+        u64 = torch.from_numpy(u_h).to(dev)
+        f64 = torch.empty_like(u64)
+        ep64 = torch.zeros(1, dtype=torch.float64, device=dev)
+        ms64 = time_device(torch, s64, u64, f64, ep64, max(3, args.steps // 10), 2, stream)
+        s.force_async(u, f, ep)
+        torch.cuda.synchronize()
+        rel = float(torch.linalg.norm(f.double() - f64) / torch.linalg.norm(f64))
+        rele = float(abs(ep - ep64) / abs(ep64))
+        extra["f64_path"] = {"value": 1000.0 / ms64, "unit": "evals/s", "ms_per_step": ms64,
+                             "dtype": "f64"}
+        extra["error_vs_f64"] = {"rel_l2_force": rel, "rel_energy": rele}
+        del s64, u64, f64
+
+    # end to end through the reference-facing call on host buffers
+    e2e = None
+    if not args.no_e2e:
+        uh = torch.from_numpy(u_h).pin_memory()
+        fh = torch.empty_like(uh).pin_memory()
+        uh_np, fh_np = uh.numpy(), fh.numpy()
+        for _ in range(2):
+            s.post_force(uh_np, fh_np)
+        n_e2e = max(3, min(args.steps, 20))
+        t0 = time.perf_counter()
+        for _ in range(n_e2e):
+            s.post_force(uh_np, fh_np)
+        dt = (time.perf_counter() - t0) / n_e2e
+        nb = u_h.size * 8
+        e2e = {"value": ws / dt, "unit": "evals/s", "h2d_bytes_per_step": nb,
+               "d2h_bytes_per_step": nb + 8,
+               "call": "gfmd_post_force_host (FP64 host buffers, pinned)"}
+
+    peak, peak_kind = measured_peaks()
+    sz = 4 if args.precision == "f32" else 8
+    bts = algorithmic_bytes(nx, ny, d, sz)
+    achieved = bts / (ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": profile_traffic(),
+                "kernel": "one force evaluation (all launches of the evaluation)",
+                "algorithmic_bytes": bts, "peak_kind": peak_kind}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        v, cores, dt = cpu_reference(args, half, linf, u_h, 1, 1)
+        cpu = {"value": v, "unit": "evals/s", "cores": cores, "kind": "port",
+               "sample": f"1 full force evaluation ({nx}x{ny}, ndof {d}) after 1 warm-up; oracle "
+                         "restatement of GFMDSolverStatic::post_force, per-DOF complex FFTs"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": args.precision, "data": "synthetic",
+            "config": workload_config(args, d), "roofline": roofline, "cpu_baseline": cpu,
+            "e2e": e2e, "gpu_launches": args.steps * LAUNCHES_PER_EVAL,
+            "clocks": clocks, "phi_table_seconds": t_phi, **extra,
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+# kernel launches one force evaluation makes (row_fwd, col_fft, phi_apply,
+# reduce, col_fft, row_inv)
+LAUNCHES_PER_EVAL = 6
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -284,3 +284,27 @@ double orc_post_force(int nx, int ny, int ndof, const double *phi,
     free(q);
     return epot;
 }
+
+void orc_phi_half_to_full(int nx, int ny, int ndof, const double *half, double *full,
+                          int nthreads)
+{
+    const int nyc = ny / 2 + 1;
+    const size_t d2 = (size_t)ndof * ndof;
+    if (nthreads <= 0) nthreads = orc_max_threads();
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+    for (int ix = 0; ix < nx; ix++) {
+        for (int iy = 0; iy < ny; iy++) {
+            double *dst = full + 2 * ((size_t)ix * ny + iy) * d2;
+            if (iy < nyc) {
+                memcpy(dst, half + 2 * ((size_t)ix * nyc + iy) * d2, sizeof(double) * 2 * d2);
+            } else {
+                int mx = (nx - ix) % nx, my = ny - iy;
+                const double *src = half + 2 * ((size_t)mx * nyc + my) * d2;
+                for (size_t e = 0; e < d2; e++) {
+                    dst[2 * e] = src[2 * e];
+                    dst[2 * e + 1] = -src[2 * e + 1];
+                }
+            }
+        }
+    }
+}

@@ -54,6 +54,12 @@ double orc_post_force(int nx, int ny, int ndof, const double *phi,
                       const double *linf, const double *u, double *f,
                       double *u0, int nthreads);
 
+/* Expand a half-spectrum table [nx][ny/2+1][ndof][ndof] to the full grid
+ * [nx*ny][ndof][ndof] using Phi(-q) = conj Phi(q) (test and baseline input
+ * preparation; the reference itself computes every grid point). */
+void orc_phi_half_to_full(int nx, int ny, int ndof, const double *half, double *full,
+                          int nthreads);
+
 /* Number of threads the oracle uses when nthreads <= 0. */
 int orc_max_threads(void);
 
