@@ -106,6 +106,28 @@ int gfmd_get_u0(gfmd_handle_t h, double *u0);
  * Replaces: GFMDSolver::memory_usage (src/main/gfmd_solver.h:97). */
 int gfmd_memory_usage(gfmd_handle_t h, double *bytes);
 
+/* ---- allocation-free force evaluation ------------------------------------- */
+
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * (a host whose pooling allocator owns the device memory, or a time-critical
+ * loop where an allocation's implicit synchronization is not acceptable):
+ * the FP64 force evaluation of gfmd_post_force without a handle and without
+ * allocating.  Inputs and outputs are the caller's device memory:
+ *   d_phi_half  [nx][ny/2+1][ndof][ndof] complex (re,im), GFMD_PHI_HALF layout,
+ *               scaled by 1/(nx*ny), Phi(-q) = conj Phi(q) assumed off the
+ *               ky = 0 and ky = ny/2 columns;
+ *   d_linf      ndof/3 linear forces, or NULL;
+ *   d_u, d_f    [ndof][nx*ny], must not alias;  d_epot: one double.
+ * Scratch (twiddles, spectrum, energy partials) lives in one fixed 16 MiB
+ * device array inside the library, held on every GPU that loads it until the
+ * process exits; grids that need more (e.g. beyond 512 x 512 at ndof 6) are
+ * rejected with GFMD_EINVAL.  Calls share that array: calls that overlap on
+ * the GPU race.  The first call on each device looks up the array's address;
+ * make it before any stream capture.  Asynchronous on cuda_stream. */
+int gfmd_post_force_noalloc(int nx, int ny, int ndof, const double *d_phi_half,
+                            const double *d_linf, const double *d_u, double *d_f,
+                            double *d_epot, void *cuda_stream);
+
 /* ---- stiffness-kernel tables (host) ------------------------------------- */
 
 /* Parse the stiffness-kernel part of a `fix gfmd` line, e.g.

@@ -69,6 +69,8 @@ template <typename F> void parallel_for(long n, F fn) {
 
 namespace gfmd {
 
+int set_error(int code, const std::string &msg) { return fail(code, msg); }
+
 FftPlan make_plan(int n, std::vector<double> &tw) {
   FftPlan p{};
   p.n = n;

@@ -73,6 +73,8 @@ namespace gfmd {
 // (0 = double, 1 = float); energy -> d_epot (device double).
 cudaError_t enqueue_force(gfmd_solver *h, const void *d_u, int in_t, void *d_f, int out_t,
                           double *d_epot);
+// Records msg as the calling thread's gfmd_last_error() and returns code.
+int set_error(int code, const std::string &msg);
 // Device bytes of the spectrum/Phi arrays and the number of energy partials.
 void force_layout(const Geom &g, int precision, size_t *w_bytes, size_t *phi_bytes, int *n_epart);
 }  // namespace gfmd
