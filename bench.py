@@ -355,18 +355,13 @@ def run_gb300(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": args.precision, "data": "synthetic",
             "config": workload_config(args, d), "roofline": roofline, "cpu_baseline": cpu,
-            "e2e": e2e, "gpu_launches": args.steps * LAUNCHES_PER_EVAL,
+            "e2e": e2e, "gpu_launches": args.steps * s.info()["launches_per_eval"],
             "clocks": clocks, "phi_table_seconds": t_phi, **extra,
         }
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
     return 0
-
-
-# kernel launches one force evaluation makes (row_fwd, col_fft, phi_apply,
-# reduce, col_fft, row_inv)
-LAUNCHES_PER_EVAL = 6
 
 
 def main():

@@ -106,6 +106,11 @@ int gfmd_get_u0(gfmd_handle_t h, double *u0);
  * Replaces: GFMDSolver::memory_usage (src/main/gfmd_solver.h:97). */
 int gfmd_memory_usage(gfmd_handle_t h, double *bytes);
 
+/* Kernel launches one force evaluation of this handle makes, and whether it
+ * runs the fused power-of-two path (1) or the general-size path (0).  No
+ * counterpart in the reference (introspection for benchmarks and tests). */
+int gfmd_solver_info(gfmd_handle_t h, int *launches_per_eval, int *fused);
+
 /* ---- allocation-free force evaluation ------------------------------------- */
 
 /* No counterpart in the reference.  For callers that cannot call cudaMalloc

@@ -117,3 +117,62 @@ def test_errors_are_status_codes_on_gpu():
     assert ei.value.code == 4
     with pytest.raises(g.GFMDError):
         s.post_force(u, u)
+
+
+@pytest.mark.parametrize(
+    "args,nx,ny",
+    [
+        ("ft fcc100 1.0 2 pair-potential 1 1.0 height 64", 64, 64),
+        ("ft fcc100 1.0 4 pair-potential 1 1.0 height 64", 512, 512),
+        ("ft sc100 1 1.0 pair-potential 2 1.0 1.0 height 128", 256, 1024),
+        ("ft fcc111 1 1.0 pair-potential 1 1.0 height 128", 1024, 64),
+        ("ft fcc100 1.0 4 pair-potential 1 1.0 height 64", 2048, 32),
+        ("ft sc100 1 1.0 pair-potential 2 1.0 1.0 height 128", 32, 4096),
+    ],
+)
+def test_fused_path_matches_oracle_and_plain_path(args, nx, ny, monkeypatch):
+    g = gfmd_pkg()
+    k = g.StiffnessKernel(args)
+    d = k.get_dimension()
+    half, linf = k.phi_table(nx, ny, "half")
+    full = half_to_full(half, nx, ny)
+    rng = np.random.default_rng(nx + 3 * ny)
+    u = rng.normal(0.0, 0.01, (d, nx * ny))
+    f_ref, e_ref, u0_ref = oracle_post_force(full, linf, u, nx, ny)
+    for prec, tol in (("f64", F64_TOL), ("f32", FP32_TOL)):
+        s = _solver(nx, ny, d, prec, half, "half", linf)
+        fused = s.info()["fused"]
+        f = np.zeros_like(u)
+        e = s.post_force(u, f)
+        assert rel_l2(f, f_ref) <= tol, prec
+        assert abs(e - e_ref) <= tol * abs(e_ref), prec
+        # u(q=0) is a sum over the grid: FP32 error scales with sum |u|
+        atol = (FP32_TOL if prec == "f32" else 1e-13) * np.abs(u).sum(axis=1).max()
+        assert np.allclose(s.get_u0(), u0_ref, rtol=0, atol=atol)
+        if prec == "f32":
+            assert fused, "power-of-two FP32 grid should take the fused path"
+        # the general-size path on the same input
+        monkeypatch.setenv("GFMD_PLAIN_PATH", "1")
+        sp = _solver(nx, ny, d, prec, half, "half", linf)
+        monkeypatch.delenv("GFMD_PLAIN_PATH")
+        assert not sp.info()["fused"]
+        fp = np.zeros_like(u)
+        ep = sp.post_force(u, fp)
+        assert rel_l2(fp, f_ref) <= tol, prec
+        assert abs(ep - e_ref) <= tol * abs(e_ref), prec
+
+
+def test_fused_energy_is_deterministic_over_repeats():
+    g = gfmd_pkg()
+    nx = ny = 256
+    k = g.StiffnessKernel("ft fcc100 1.0 2 pair-potential 1 1.0 height 64")
+    half, linf = k.phi_table(nx, ny, "half")
+    s = _solver(nx, ny, 6, "f32", half, "half", linf)
+    u = torch.from_numpy(np.random.default_rng(5).normal(0, 0.01, (6, nx * ny))).float().cuda()
+    f = torch.empty_like(u)
+    ep = torch.zeros(1, dtype=torch.float64, device="cuda")
+    vals = set()
+    for _ in range(20):
+        s.force_async(u, f, ep)
+        vals.add(float(ep.item()))
+    assert len(vals) == 1

@@ -62,6 +62,7 @@ SIGNATURES = {
     "gfmd_force_f32": [_vp, _vp, _vp, _vp],
     "gfmd_get_u0": [_vp, _vp],
     "gfmd_memory_usage": [_vp, _pd],
+    "gfmd_solver_info": [_vp, _pi, _pi],
     "gfmd_post_force_noalloc": [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp],
     "gfmd_kernel_create": [ctypes.c_char_p, ctypes.POINTER(_vp)],
     "gfmd_kernel_destroy": [_vp],

@@ -5,6 +5,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <sstream>
@@ -44,7 +45,9 @@ constexpr double kPi = 3.14159265358979323846264338327950288;
 
 void release(gfmd_solver *h) {
   if (!h) return;
-  void *ptrs[] = {h->d_tw_hi, h->d_tw_lo, h->d_W, h->d_phi, h->d_linf, h->d_epart, h->d_scal, h->d_io};
+  void *ptrs[] = {h->d_tw_hi, h->d_tw_lo,  h->d_W,     h->d_phi,     h->d_linf,
+                  h->d_epart, h->d_scal,   h->d_io,    h->d_ftw,
+                  h->d_counter};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   delete h;
@@ -63,6 +66,112 @@ template <typename F> void parallel_for(long n, F fn) {
     else th.emplace_back(fn, a, b);
   }
   for (auto &t : th) t.join();
+}
+
+bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+// Position of frequency k after the in-place DIF stages of plan p.
+int p2_digit_rev(const gfmd::P2Plan &p, int k) {
+  int pos = 0, lgS = p.lgn;
+  for (int s = 0; s < p.nst; s++) {
+    lgS -= p.lg[s];
+    pos += (k & ((1 << p.lg[s]) - 1)) << lgS;
+    k >>= p.lg[s];
+  }
+  return pos;
+}
+
+gfmd::P2Plan make_p2(int n) {
+  gfmd::P2Plan p{};
+  p.n = n;
+  while ((1 << p.lgn) < n) p.lgn++;
+  int m = n;
+  while (m % 16 == 0) { p.radix[p.nst] = 16; p.lg[p.nst++] = 4; m /= 16; }
+  if (m > 1) {
+    p.radix[p.nst] = m;
+    p.lg[p.nst++] = m == 8 ? 3 : (m == 4 ? 2 : 1);
+  }
+  return p;
+}
+
+// Appends the per-stage twiddle tables of plan p (entry [m][j] =
+// exp(-2 pi i j m / L_s), so consecutive j sit in consecutive entries) as (c, s) doubles to d and (c_hi, s_hi, c_lo, s_lo)
+// floats to f, setting p.toff relative to the start of this plan's table.
+void push_stage_tables(gfmd::P2Plan &p, std::vector<double> &d, std::vector<float> &f) {
+  auto push = [&](double c, double sn) {
+    d.push_back(c);
+    d.push_back(sn);
+    float ch = (float)c, sh = (float)sn;
+    f.push_back(ch);
+    f.push_back(sh);
+    f.push_back((float)(c - (double)ch));
+    f.push_back((float)(sn - (double)sh));
+  };
+  const size_t base = d.size() / 2;
+  int L = p.n;
+  for (int s = 0; s < p.nst; s++) {
+    const int R = p.radix[s], S = L / R;
+    p.toff[s] = (int)(d.size() / 2 - base);
+    for (int m = 0; m < R; m++)
+      for (int j = 0; j < S; j++) {
+        long e = ((long)j * m) % L;
+        double a = -2.0 * kPi * (double)e / (double)L;
+        push(std::cos(a), std::sin(a));
+      }
+    L = S;
+  }
+  p.tsize = (int)(d.size() / 2 - base);
+}
+
+// Sets up the fused power-of-two path when the grid allows it.
+cudaError_t setup_fast(gfmd_solver *h) {
+  const gfmd::Geom &g = h->g;
+  const size_t cs = h->precision == GFMD_PREC_F64 ? 16 : 8;
+  if (!is_pow2(g.nx) || g.nx < 16 || !g.ny_even || !is_pow2(g.nrow) || g.nrow < 16) return cudaSuccess;
+  if (g.nx > 8192 || g.nrow > 8192) return cudaSuccess;
+  gfmd::P2Plan pr = make_p2(g.nrow), pc = make_p2(g.nx);
+  std::vector<double> d;
+  std::vector<float> f;
+  push_stage_tables(pr, d, f);
+  pr.tpost = pr.tsize;
+  for (int k = 0; k <= g.ny / 2; k++) {
+    double a = -2.0 * kPi * (double)k / (double)g.ny;
+    double c = std::cos(a), sn = std::sin(a);
+    d.push_back(c);
+    d.push_back(sn);
+    float ch = (float)c, sh = (float)sn;
+    f.push_back(ch);
+    f.push_back(sh);
+    f.push_back((float)(c - (double)ch));
+    f.push_back((float)(sn - (double)sh));
+  }
+  pr.tsize += g.ny / 2 + 1;
+  const int col_off = pr.tsize;
+  push_stage_tables(pc, d, f);
+  // shared-memory budgets (static shared memory of the kernels < 256 bytes)
+  const size_t slack = 256;
+  if ((size_t)pc.tsize * 16 + (size_t)g.ndof * g.nx * cs + slack > h->smem_optin) return cudaSuccess;
+  const size_t row_bytes = (size_t)(g.nrow + 1) * cs;
+  const size_t row_fixed = (size_t)pr.tsize * 16 + ((size_t)g.nrow * 2 + 15) / 16 * 16;
+  int rb = 16;
+  while (rb > 1 && (rb > g.nx || row_fixed + rb * row_bytes > 72 * 1024)) rb /= 2;
+  if (row_fixed + rb * row_bytes + slack > h->smem_optin) return cudaSuccess;
+  const size_t nent = (size_t)col_off + pc.tsize;
+  cudaError_t e = cudaMalloc(&h->d_ftw, nent * 16);
+  if (e == cudaSuccess) {
+    const void *src = h->precision == GFMD_PREC_F64 ? (const void *)d.data() : (const void *)f.data();
+    e = cudaMemcpy(h->d_ftw, src, nent * 16, cudaMemcpyHostToDevice);
+  }
+  if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_counter, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMemset(h->d_counter, 0, sizeof(unsigned));
+  if (e != cudaSuccess) return e;
+  h->p2_row = pr;
+  h->p2_col = pc;
+  h->ftw_col_off = col_off;
+  h->fast_rb = rb;
+  h->bytes += (double)nent * 16 + sizeof(unsigned);
+  h->fast = true;
+  return cudaSuccess;
 }
 
 }  // namespace
@@ -188,6 +297,10 @@ int gfmd_create(int nx, int ny, int ndof, int precision, gfmd_handle_t *out) {
   if (e != cudaSuccess) { release(h); return cuda_fail(e, "gfmd_create: device buffers"); }
   h->bytes = (double)wb + (double)pb + 8.0 * (h->n_epart + ndof / 3 + 1 + gfmd::kMaxNdof) +
              (double)ntw * cs * (precision == GFMD_PREC_F64 ? 1 : 2);
+  if (getenv("GFMD_PLAIN_PATH") == nullptr || getenv("GFMD_PLAIN_PATH")[0] == '0') {
+    e = setup_fast(h);
+    if (e != cudaSuccess) { release(h); return cuda_fail(e, "gfmd_create: fused-path tables"); }
+  }
   *out = h;
   return GFMD_OK;
 }
@@ -201,6 +314,13 @@ int gfmd_destroy(gfmd_handle_t h) {
 int gfmd_set_stream(gfmd_handle_t h, void *stream) {
   if (!h) return fail(GFMD_EINVAL, "gfmd_set_stream: NULL handle");
   h->stream = reinterpret_cast<cudaStream_t>(stream);
+  return GFMD_OK;
+}
+
+int gfmd_solver_info(gfmd_handle_t h, int *launches_per_eval, int *fused) {
+  if (!h) return fail(GFMD_EINVAL, "gfmd_solver_info: NULL handle");
+  if (launches_per_eval) *launches_per_eval = gfmd::force_launches(h);
+  if (fused) *fused = h->fast ? 1 : 0;
   return GFMD_OK;
 }
 
@@ -223,6 +343,7 @@ int gfmd_set_phi(gfmd_handle_t h, const double *phi, int layout, const double *l
   const int D = g.ndof, D2 = D * D;
   const size_t nq = (size_t)g.nyc * g.nxp;
   const bool f64 = h->precision == GFMD_PREC_F64;
+  const bool fused = h->fast;
   std::vector<double> packd;
   std::vector<float> packf;
   if (f64) packd.assign(nq * D2, 0.0);
@@ -252,11 +373,16 @@ int gfmd_set_phi(gfmd_handle_t h, const double *phi, int layout, const double *l
           eff[2 * e + 1] = pa[2 * e + 1];
         }
       }
-      size_t base = (size_t)ky * D2 * g.nxp + kx;
+      // plain path: [ky][p][nxp]; fused path: [ky][nxp/32][p][32] over the
+      // digit-reversed position of kx (the order the fused forward FFT leaves)
+      const int xs = fused ? p2_digit_rev(h->p2_col, kx) : kx;
+      const size_t base = fused ? ((size_t)ky * (g.nxp / 32) + xs / 32) * D2 * 32 + (xs % 32)
+                                : (size_t)ky * D2 * g.nxp + kx;
+      const size_t pstride = fused ? 32 : (size_t)g.nxp;
       auto put = [&](int p, double v) {
         if (!std::isfinite(v)) ok = false;
-        if (f64) packd[base + (size_t)p * g.nxp] = v;
-        else packf[base + (size_t)p * g.nxp] = (float)v;
+        if (f64) packd[base + (size_t)p * pstride] = v;
+        else packf[base + (size_t)p * pstride] = (float)v;
       };
       for (int i = 0; i < D; i++) put(i, eff[2 * (i * D + i)]);
       int p = D;

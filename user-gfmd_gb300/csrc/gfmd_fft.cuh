@@ -6,6 +6,8 @@
 
 #include <cuda_runtime.h>
 
+#include <utility>
+
 #include "gfmd_internal.h"
 
 namespace gfmd {
@@ -145,6 +147,81 @@ template <typename T> struct Dft<T, 5> {
     v[4] = csub<T>(a1, b1);
     v[2] = cadd<T>(a2, b2);
     v[3] = csub<T>(a2, b2);
+  }
+};
+
+// Radix 16 as 4 x 4: X[k1 + 4 k2] = sum_n2 w4^{n2 k2} w16^{n2 k1} sum_n1 x[4 n1 + n2] w4^{n1 k1}.
+template <typename T> struct Dft<T, 16> {
+  static __device__ __forceinline__ C<T> w16(int e, int s) {
+    // exp(s 2 pi i e / 16), e in [0, 9]
+    const T c1 = (T)0.92387953251128675612818318939678829;
+    const T s1 = (T)0.38268343236508977172845998403039887;
+    const T h = (T)0.70710678118654752440084436210484904;
+    T cr, ci;
+    switch (e) {
+      case 0: cr = 1; ci = 0; break;
+      case 1: cr = c1; ci = s1; break;
+      case 2: cr = h; ci = h; break;
+      case 3: cr = s1; ci = c1; break;
+      case 4: cr = 0; ci = 1; break;
+      case 6: cr = -h; ci = h; break;
+      default: cr = -c1; ci = -s1; break;  // e = 9
+    }
+    return mk<T>(cr, s > 0 ? ci : -ci);
+  }
+  static __device__ __forceinline__ void run(C<T> *v, int s) {
+    C<T> y[16];
+#pragma unroll
+    for (int n2 = 0; n2 < 4; n2++) {
+      C<T> a[4];
+#pragma unroll
+      for (int n1 = 0; n1 < 4; n1++) a[n1] = v[4 * n1 + n2];
+      Dft<T, 4>::run(a, s);
+#pragma unroll
+      for (int k1 = 0; k1 < 4; k1++)
+        y[n2 * 4 + k1] = (n2 * k1 == 0) ? a[k1] : cmul<T>(a[k1], w16(n2 * k1, s));
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < 4; k1++) {
+      C<T> b[4];
+#pragma unroll
+      for (int n2 = 0; n2 < 4; n2++) b[n2] = y[n2 * 4 + k1];
+      Dft<T, 4>::run(b, s);
+#pragma unroll
+      for (int k2 = 0; k2 < 4; k2++) v[k1 + 4 * k2] = b[k2];
+    }
+  }
+};
+
+// F += H u for the off-diagonal part of a packed Hermitian D x D matrix
+// (pair (I, J), I < J, at packed index D + 2 (I D - I (I+1)/2 + J - I - 1)
+// holding (Re H_IJ, Im H_IJ)), fully unrolled at compile time so that u and F
+// stay in registers.  ph points at element 0 of this wavevector; elements
+// are ps apart.
+template <typename T, int D> struct HermPairs {
+  template <int I, int J>
+  static __device__ __forceinline__ void pair(const T *__restrict__ ph, size_t ps, const C<T> *uq,
+                                              C<T> *F) {
+    constexpr int P = D + 2 * (I * D - I * (I + 1) / 2 + (J - I - 1));
+    const T hr = ph[P * ps], hi = ph[(P + 1) * ps];
+    F[I].x += hr * uq[J].x - hi * uq[J].y;
+    F[I].y += hr * uq[J].y + hi * uq[J].x;
+    F[J].x += hr * uq[I].x + hi * uq[I].y;
+    F[J].y += hr * uq[I].y - hi * uq[I].x;
+  }
+  template <int I, int... Js>
+  static __device__ __forceinline__ void row(const T *__restrict__ ph, size_t ps, const C<T> *uq,
+                                             C<T> *F, std::integer_sequence<int, Js...>) {
+    (pair<I, I + 1 + Js>(ph, ps, uq, F), ...);
+  }
+  template <int... Is>
+  static __device__ __forceinline__ void rows(const T *__restrict__ ph, size_t ps, const C<T> *uq,
+                                              C<T> *F, std::integer_sequence<int, Is...>) {
+    (row<Is>(ph, ps, uq, F, std::make_integer_sequence<int, D - 1 - Is>{}), ...);
+  }
+  static __device__ __forceinline__ void run(const T *__restrict__ ph, size_t ps, const C<T> *uq,
+                                             C<T> *F) {
+    rows(ph, ps, uq, F, std::make_integer_sequence<int, D - 1>{});
   }
 };
 

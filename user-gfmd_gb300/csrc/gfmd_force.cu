@@ -21,6 +21,7 @@
 
 #include "gfmd_fft.cuh"
 #include "gfmd_internal.h"
+#include "gfmd_fast_kernels.cuh"
 #include "gfmd_plain_kernels.cuh"
 
 namespace gfmd {
@@ -51,9 +52,66 @@ void launch_phi(gfmd_solver *h, dim3 grid, double *d_epot_unused) {
       h->d_epart, h->d_scal);
 }
 
+template <typename T, int D>
+void launch_col_fast(gfmd_solver *h, C<T> *W, size_t sm, double *d_epot) {
+  using E = typename TwE<T>::type;
+  auto kf = k_col_phi_fast<T, D>;
+  cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  kf<<<h->g.nyc, ColThreads<T, D>::value, sm, h->stream>>>(
+      W, reinterpret_cast<const T *>(h->d_phi), h->g, h->p2_col,
+      reinterpret_cast<const E *>(h->d_ftw) + h->ftw_col_off, h->d_linf, h->d_epart, h->d_scal,
+      h->d_counter, d_epot);
+}
+
+// Fused power-of-two path: three launches.
+template <typename T>
+cudaError_t enqueue_fast(gfmd_solver *h, const void *d_u, int in_t, void *d_f, int out_t,
+                         double *d_epot) {
+  using E = typename TwE<T>::type;
+  const Geom &g = h->g;
+  const E *tab_row = reinterpret_cast<const E *>(h->d_ftw);
+  C<T> *W = reinterpret_cast<C<T> *>(h->d_W);
+  const int rb = h->fast_rb;
+  const size_t smr = (size_t)h->p2_row.tsize * sizeof(E) + srev_bytes(g.nrow) +
+                     (size_t)rb * (g.nrow + 1) * sizeof(C<T>);
+  dim3 gridr((g.nx + rb - 1) / rb, g.ndof);
+  if (in_t == 0) {
+    auto kf = k_row_fwd_fast<T, double>;
+    cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr);
+    kf<<<gridr, kRowThreads, smr, h->stream>>>(reinterpret_cast<const double *>(d_u), W, g, h->p2_row, tab_row, rb);
+  } else {
+    auto kf = k_row_fwd_fast<T, float>;
+    cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr);
+    kf<<<gridr, kRowThreads, smr, h->stream>>>(reinterpret_cast<const float *>(d_u), W, g, h->p2_row, tab_row, rb);
+  }
+  const size_t smc = (size_t)h->p2_col.tsize * sizeof(E) + (size_t)g.ndof * g.nx * sizeof(C<T>);
+  switch (g.ndof) {
+    case 3: launch_col_fast<T, 3>(h, W, smc, d_epot); break;
+    case 6: launch_col_fast<T, 6>(h, W, smc, d_epot); break;
+    case 9: launch_col_fast<T, 9>(h, W, smc, d_epot); break;
+    case 12: launch_col_fast<T, 12>(h, W, smc, d_epot); break;
+    case 15: launch_col_fast<T, 15>(h, W, smc, d_epot); break;
+    case 18: launch_col_fast<T, 18>(h, W, smc, d_epot); break;
+    case 21: launch_col_fast<T, 21>(h, W, smc, d_epot); break;
+    case 24: launch_col_fast<T, 24>(h, W, smc, d_epot); break;
+    default: return cudaErrorInvalidValue;
+  }
+  if (out_t == 0) {
+    auto kf = k_row_inv_fast<T, double>;
+    cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr);
+    kf<<<gridr, kRowThreads, smr, h->stream>>>(W, reinterpret_cast<double *>(d_f), g, h->p2_row, tab_row, rb);
+  } else {
+    auto kf = k_row_inv_fast<T, float>;
+    cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr);
+    kf<<<gridr, kRowThreads, smr, h->stream>>>(W, reinterpret_cast<float *>(d_f), g, h->p2_row, tab_row, rb);
+  }
+  return cudaGetLastError();
+}
+
 template <typename T>
 cudaError_t enqueue_t(gfmd_solver *h, const void *d_u, int in_t, void *d_f, int out_t,
                       double *d_epot) {
+  if (h->fast) return enqueue_fast<T>(h, d_u, in_t, d_f, out_t, d_epot);
   const Geom &g = h->g;
   Tw<T> tw;
   tw.hi = reinterpret_cast<decltype(tw.hi)>(h->d_tw_hi);
@@ -123,8 +181,10 @@ void force_layout(const Geom &g, int precision, size_t *w_bytes, size_t *phi_byt
   size_t s = precision == GFMD_PREC_F64 ? 8 : 4;
   *w_bytes = (size_t)g.nyc * g.ndof * g.nxp * 2 * s;
   *phi_bytes = (size_t)g.nyc * g.npk * g.nxp * s;
-  *n_epart = ((g.nx + kPhiThreads - 1) / kPhiThreads) * g.nyc;
+  *n_epart = ((g.nx + kPhiThreads - 1) / kPhiThreads) * g.nyc;  // >= nyc (fused path)
 }
+
+int force_launches(const gfmd_solver *h) { return h->fast ? 3 : 6; }
 
 cudaError_t enqueue_force(gfmd_solver *h, const void *d_u, int in_t, void *d_f, int out_t,
                           double *d_epot) {

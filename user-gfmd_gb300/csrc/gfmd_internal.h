@@ -31,6 +31,19 @@ struct FftPlan {
 // Builds the plan and appends its twiddles (FP64) to `tw`.
 FftPlan make_plan(int n, std::vector<double> &tw);
 
+// Power-of-two plan of the fused kernels: in-place decimation-in-frequency
+// stages with radices radix[0..nst) (16s, then one 8, 4 or 2); twiddles
+// w_n^k, k = 0..n-1, at table offset twoff.
+struct P2Plan {
+  int n, lgn;
+  int nst;
+  int radix[4];
+  int lg[4];     // log2 radix
+  int toff[4];   // table entry offset of each stage's [j][m] twiddles
+  int tpost;     // entry offset of the real-to-complex post-twiddles (rows)
+  int tsize;     // table entries (16 bytes each)
+};
+
 // Geometry of one solver handle.
 struct Geom {
   int nx, ny, ndof;
@@ -65,6 +78,15 @@ struct gfmd_solver {
   void *d_io = nullptr;      // staging for host-buffer calls: u then f, FP64
   int n_epart = 0;
   bool have_phi = false;
+
+  // fused power-of-two path (see gfmd_fast_kernels.cuh)
+  bool fast = false;
+  gfmd::P2Plan p2_row{}, p2_col{};
+  int fast_rb = 8;           // rows per block of the row kernels
+  void *d_ftw = nullptr;     // octant tables of w_ny and w_nx (see gfmd_fast_kernels.cuh)
+  int ftw_col_off = 0;       // entry offset of the w_nx table
+  unsigned *d_counter = nullptr;  // blocks finished in the column kernel
+  int fast_rpost = 0;
   double bytes = 0.0;
 };
 
@@ -75,6 +97,8 @@ cudaError_t enqueue_force(gfmd_solver *h, const void *d_u, int in_t, void *d_f, 
                           double *d_epot);
 // Records msg as the calling thread's gfmd_last_error() and returns code.
 int set_error(int code, const std::string &msg);
+// Kernel launches one force evaluation makes.
+int force_launches(const gfmd_solver *h);
 // Device bytes of the spectrum/Phi arrays and the number of energy partials.
 void force_layout(const Geom &g, int precision, size_t *w_bytes, size_t *phi_bytes, int *n_epart);
 }  // namespace gfmd

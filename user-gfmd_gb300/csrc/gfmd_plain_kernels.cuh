@@ -193,31 +193,20 @@ __global__ void __launch_bounds__(kPhiThreads) k_phi_apply(C<T> *__restrict__ W,
       F[i].x += h * uq[i].x;
       F[i].y += h * uq[i].y;
     }
-    int pidx = D;
-#pragma unroll
-    for (int i = 0; i < D; i++) {
-#pragma unroll
-      for (int j = i + 1; j < D; j++) {
-        T hr = ph[pidx * cs], hi = ph[(pidx + 1) * cs];
-        pidx += 2;
-        // F_i += H_ij u_j ; F_j += conj(H_ij) u_i
-        F[i].x += hr * uq[j].x - hi * uq[j].y;
-        F[i].y += hr * uq[j].y + hi * uq[j].x;
-        F[j].x += hr * uq[i].x + hi * uq[i].y;
-        F[j].y += hr * uq[i].y - hi * uq[i].x;
-      }
-    }
+    // F_i += H_ij u_j ; F_j += conj(H_ij) u_i
+    HermPairs<T, D>::run(ph, cs, uq, F);
     const bool mirror_self = (ky == 0) || (g.ny_even && ky == g.ny / 2);
     const double w = mirror_self ? 1.0 : 2.0;
-    double es = 0.0;
+    T es = 0;
 #pragma unroll
-    for (int i = 0; i < D; i++) es += to_d(F[i].x) * to_d(uq[i].x) + to_d(F[i].y) * to_d(uq[i].y);
-    e = w * es;
+    for (int i = 0; i < D; i++) es = fma(F[i].x, uq[i].x, fma(F[i].y, uq[i].y, es));
+    e = w * (double)es;
     if (ky == 0 && x == 0) {
       // u(q=0) (gfmd_solver_static.cpp:169-177); gamma-point energy (:193-197)
       // and linear force (:228-231)
 #pragma unroll
       for (int j = 0; j < D; j++) scal[1 + j] = to_d(uq[j].x);
+#pragma unroll
       for (int l = 0; l < D / 3; l++) {
         e -= 2.0 * linf[l] * to_d(uq[3 * l + 2].x);
         F[3 * l + 2].x -= (T)linf[l];

@@ -178,6 +178,12 @@ class GFMDSolverGB300:
         check(lib().gfmd_memory_usage(self._handle(), ctypes.byref(b)))
         return b.value
 
+    def info(self) -> dict:
+        """Launches per force evaluation and whether the fused path runs."""
+        n, f = ctypes.c_int(), ctypes.c_int()
+        check(lib().gfmd_solver_info(self._handle(), ctypes.byref(n), ctypes.byref(f)))
+        return {"launches_per_eval": n.value, "fused": bool(f.value)}
+
     def get_nxy_loc(self) -> int:
         return self.nx * self.ny
 
