@@ -111,6 +111,81 @@ int gfmd_memory_usage(gfmd_handle_t h, double *bytes);
  * counterpart in the reference (introspection for benchmarks and tests). */
 int gfmd_solver_info(gfmd_handle_t h, int *launches_per_eval, int *fused);
 
+/* ---- solver loops ----------------------------------------------------- */
+
+/* Obstacles acting on every atom of the grid.  The position of the atom of
+ * layer l at grid site (ix, iy) is (ix*lattice[0], iy*lattice[1], 0) +
+ * layer_offset[l] + u.  No counterpart as one struct in the reference: it
+ * carries the parameters of the obstacle fixes listed per kind. */
+#define GFMD_OBST_NONE 0
+#define GFMD_OBST_SPHERE_EXP 1 /* e = eps exp(-g/sigma) on the gap g = |r-c| - R
+                                  (exponential wall of FixWallMap::eval_exp,
+                                  src/extras/fix_wall_map.cpp:575-582, on a sphere) */
+#define GFMD_OBST_SPHERE_LJ 2  /* LJ 12-6 on the gap, shifted at cutoff
+                                  (FixContactSphere, src/extras/fix_contact_sphere.cpp:207-264) */
+#define GFMD_OBST_MAP_EXP 3    /* exponential wall on dz = norm (z - (map + map_z0)),
+                                  normal force only (FixWallMap::pre_force,
+                                  src/extras/fix_wall_map.cpp:686-817) */
+
+typedef struct {
+  int kind;
+  double center[3];     /* sphere centre */
+  double radius;        /* sphere radius */
+  double epsilon;       /* energy scale */
+  double sigma;         /* length scale (decay length of the exponential) */
+  double cutoff;        /* on the gap; <= 0: none */
+  const double *d_map;  /* MAP_EXP: rigid surface heights [nx*ny], device */
+  double map_z0;        /* MAP_EXP: offset added to the map */
+  int norm;             /* MAP_EXP: +1 wall below the atoms, -1 above (0 = +1) */
+  double lattice[2];    /* grid spacing along x and y (<= 0: 1) */
+  int nlayer;           /* layers (from l = 0) that feel the obstacle (<= 0: all) */
+  double layer_offset[8][3];
+} gfmd_obstacle_t;
+
+#define GFMD_MIN_CG 0   /* Polak-Ribiere CG, Newton line search (LAMMPS min_style cg
+                           as used on fix gfmd by tests/TEST_Hertz_x/lammps.in) */
+#define GFMD_MIN_FIRE 1 /* FIRE (FixFIRE, src/cuda/fix_fire.cpp:117-297) */
+
+typedef struct {
+  int method;           /* GFMD_MIN_CG or GFMD_MIN_FIRE */
+  double ftol;          /* converged when max |f_i| <= ftol (per component) */
+  int maxiter;          /* <= 0: 100000 */
+  int recompute;        /* CG: recompute F_el(u) from scratch every n iterations (<= 0: 50) */
+  gfmd_handle_t refine; /* optional FP64 handle (same grid and table): when the
+                           loop converges, forces are recomputed with it and the
+                           loop continues until it also converges */
+  /* FIRE parameters (<= 0: the defaults of FixFIRE, src/cuda/fix_fire.cpp:63-69) */
+  int fire_minsteps;
+  double fire_incfac, fire_decfac, fire_mix, fire_mixdec, fire_dtmax, fire_dt, fire_xlimit;
+} gfmd_min_params_t;
+
+typedef struct {
+  int status;           /* GFMD_OK or the failure code */
+  int iterations;
+  int force_evals;      /* FFT force evaluations */
+  double energy;        /* elastic + obstacle energy at the end */
+  double fmax;          /* max |f_i| at the end (from freshly computed forces) */
+  double fnorm;         /* |f|_2 at the end (LAMMPS' fnorm) */
+  double seconds;       /* wall time of the call */
+} gfmd_min_report_t;
+
+/* Static minimization of elastic + obstacle energy from the displacements in
+ * d_u (device, [ndof][nx*ny], FP64; updated in place).  Replaces LAMMPS'
+ * minimize driving fix gfmd through min_pre_force/min_post_force
+ * (src/main/fix_gfmd.cpp:1078-1088) and FixFIRE. */
+int gfmd_minimize(gfmd_handle_t h, const gfmd_obstacle_t *obst, const gfmd_min_params_t *params,
+                  double *d_u, gfmd_min_report_t *report);
+
+/* Damped velocity Verlet (unit masses): v_h = v + dt/2 (f - gamma v),
+ * u += dt v_h, v = (v_h + dt/2 f) / (1 + dt gamma/2); gamma = 0 is fix nve.
+ * d_u, d_v device FP64 [ndof][nx*ny] updated in place; energies (host,
+ * nsteps+1 doubles, may be NULL) receives the total energy before the first
+ * and after every step.  Replaces the fix nve + fix gfmd loop of the
+ * reference's dynamics runs (tests/TEST_energy_conservation_x/lammps.in). */
+int gfmd_run_dynamics(gfmd_handle_t h, const gfmd_obstacle_t *obst, double dt, double gamma,
+                      int nsteps, double *d_u, double *d_v, double *energies,
+                      gfmd_min_report_t *report);
+
 /* ---- allocation-free force evaluation ------------------------------------- */
 
 /* No counterpart in the reference.  For callers that cannot call cudaMalloc

@@ -1,0 +1,237 @@
+"""ORACLE — test infrastructure, not product code.
+
+FP64 numpy restatement of the solver loops and obstacles the GPU library runs
+(user-gfmd_gb300/csrc/gfmd_solvers.cu), with elastic forces from the C
+oracle's restatement of GFMDSolverStatic::post_force (oracle/gfmd_oracle.c).
+Only tests/ import this module.
+
+Reference behaviour restated:
+  obstacles  exponential wall e = eps exp(-g/sigma) - offset
+             (FixWallMap::eval_exp, src/extras/fix_wall_map.cpp:575-582) on a
+             sphere gap g = |r - c| - R; Lennard-Jones 12-6 sphere
+             (FixContactSphere::post_force, src/extras/fix_contact_sphere.cpp:207-264);
+             exponential map wall, normal force (FixWallMap::pre_force,
+             src/extras/fix_wall_map.cpp:686-817);
+  FIRE       FixFIRE::initial_integrate / final_integrate
+             (src/cuda/fix_fire.cpp:117-297);
+  CG         Polak-Ribiere conjugate gradients (LAMMPS min_style cg, which
+             the reference's Hertz tests run on fix gfmd) with a Newton line
+             search along the direction;
+  dynamics   velocity Verlet (fix nve) with linear damping.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+SPHERE_EXP, SPHERE_LJ, MAP_EXP = 1, 2, 3
+
+
+class ObstacleSpec:
+    def __init__(self, kind, center=(0, 0, 0), radius=0.0, epsilon=1.0, sigma=1.0, cutoff=0.0,
+                 lattice=(1.0, 1.0), layer_offsets=(), nlayer=0, zmap=None, map_z0=0.0, norm=1):
+        self.kind, self.c, self.R = kind, np.asarray(center, float), radius
+        self.eps, self.sigma, self.cutoff = epsilon, sigma, cutoff
+        self.ax, self.ay = lattice
+        self.offsets = list(layer_offsets)
+        self.nlayer = nlayer
+        self.zmap, self.map_z0, self.norm = zmap, map_z0, norm
+        if kind == SPHERE_LJ:
+            self.c1 = 48.0 * epsilon * sigma ** 12
+            self.c2 = 24.0 * epsilon * sigma ** 6
+            self.c3 = 4.0 * epsilon * sigma ** 12
+            self.c4 = 4.0 * epsilon * sigma ** 6
+            r6 = cutoff ** -6 if cutoff > 0 else 0.0
+            self.offset = r6 * (self.c3 * r6 - self.c4) if cutoff > 0 else 0.0
+        else:
+            self.offset = epsilon * np.exp(-cutoff / sigma) if cutoff > 0 else 0.0
+
+
+def wall(ob: ObstacleSpec | None, u, nx, ny, direction=None, a=0.0):
+    """Obstacle energy E, force f [ndof, N], and along `direction`:
+    sum f.dir and sum dir^T H dir at u + a*dir."""
+    ndof = u.shape[0]
+    f = np.zeros_like(u)
+    if ob is None:
+        return 0.0, f, 0.0, 0.0
+    nl = ndof // 3
+    nlo = min(nl, ob.nlayer if ob.nlayer > 0 else nl)
+    ix, iy = np.divmod(np.arange(nx * ny), ny)
+    E = fdir = curv = 0.0
+    for l in range(nlo):
+        off = ob.offsets[l] if l < len(ob.offsets) else (0.0, 0.0, 0.0)
+        d = direction[3 * l:3 * l + 3] if direction is not None else np.zeros((3, nx * ny))
+        r = u[3 * l:3 * l + 3] + a * d
+        r = r + np.asarray(off, float)[:, None]
+        r[0] += ix * ob.ax
+        r[1] += iy * ob.ay
+        if ob.kind in (SPHERE_EXP, SPHERE_LJ):
+            dv = r - ob.c[:, None]
+            lx, ly = ob.ax * nx, ob.ay * ny
+            dv[0] -= lx * np.rint(dv[0] / lx)
+            dv[1] -= ly * np.rint(dv[1] / ly)
+            rho = np.sqrt((dv ** 2).sum(0))
+            g = rho - ob.R
+            m = np.ones_like(g, bool) if ob.cutoff <= 0 else g < ob.cutoff
+            if ob.kind == SPHERE_EXP:
+                ex = ob.eps * np.exp(-g / ob.sigma)
+                e = ex - ob.offset
+                F = ex / ob.sigma
+                E2 = F / ob.sigma
+            else:
+                gi = 1.0 / g
+                g6 = gi ** 6
+                e = g6 * (ob.c3 * g6 - ob.c4) - ob.offset
+                F = g6 * (ob.c1 * g6 - ob.c2) * gi
+                E2 = g6 * gi * gi * (13.0 * ob.c1 * g6 - 7.0 * ob.c2)
+            n = dv / rho
+            fl = F * n
+            dn = (d * n).sum(0)
+            dd = (d * d).sum(0)
+            cv = E2 * dn * dn - F / rho * (dd - dn * dn)
+            f[3 * l:3 * l + 3] = np.where(m, fl, 0.0)
+            E += np.where(m, e, 0.0).sum()
+            fdir += np.where(m, (fl * d).sum(0), 0.0).sum()
+            curv += np.where(m, cv, 0.0).sum()
+        elif ob.kind == MAP_EXP:
+            dz = ob.norm * (r[2] - (ob.zmap + ob.map_z0))
+            m = np.ones_like(dz, bool) if ob.cutoff <= 0 else dz < ob.cutoff
+            ex = ob.eps * np.exp(-dz / ob.sigma)
+            fz = ob.norm * ex / ob.sigma
+            f[3 * l + 2] = np.where(m, fz, 0.0)
+            E += np.where(m, ex - ob.offset, 0.0).sum()
+            fdir += np.where(m, fz * d[2], 0.0).sum()
+            curv += np.where(m, ex / ob.sigma ** 2 * d[2] ** 2, 0.0).sum()
+    return E, f, fdir, curv
+
+
+def cg(elastic, ob, u, nx, ny, ftol=1e-6, maxiter=100000, recompute=50):
+    """Polak-Ribiere CG with a Newton line search; elastic(v, with_linf)
+    returns (force, energy).  Returns (u, report)."""
+    u = u.copy()
+    it = evals = 0
+
+    def restart():
+        nonlocal evals
+        fel, _ = elastic(u, True)
+        evals += 1
+        _, fw, _, _ = wall(ob, u, nx, ny)
+        g = fel + fw
+        return fel, g, g.copy()
+
+    fel, g, h = restart()
+    since = 0
+    while True:
+        fmax = np.abs(g).max()
+        if fmax <= ftol or it >= maxiter:
+            break
+        fKh, _ = elastic(h, False)
+        evals += 1
+        Kh = -fKh
+        hKh = (h * Kh).sum()
+        felh = (fel * h).sum()
+        a, lo, hi = 0.0, 0.0, -1.0
+        for _ in range(30):
+            fwh = cw = 0.0
+            if ob is not None:
+                _, _, fwh, cw = wall(ob, u, nx, ny, h, a)
+            gdir = felh - a * hKh + fwh
+            curv = hKh + cw
+            if gdir > 0:
+                lo = a
+            else:
+                hi = a
+            an = a + gdir / curv if curv > 0 else -1.0
+            if hi >= 0 and (an <= lo or an >= hi or an < 0):
+                an = 0.5 * (lo + hi)
+            elif an < 0:
+                an = 2 * lo if lo > 0 else 1e-3
+            step = abs(an - a)
+            a = an
+            if step <= 1e-12 * max(1.0, abs(a)) or ob is None:
+                break
+        u += a * h
+        fel -= a * Kh
+        _, fw, _, _ = wall(ob, u, nx, ny)
+        gn = fel + fw
+        it += 1
+        since += 1
+        if since >= recompute:
+            fel, g, h = restart()
+            since = 0
+            continue
+        beta = max(0.0, ((gn * gn).sum() - (gn * g).sum()) / (g * g).sum())
+        h = gn + beta * h
+        if (h * gn).sum() <= 0:
+            h = gn.copy()
+        g = gn
+    fel, E_el = elastic(u, True)
+    E_w, fw, _, _ = wall(ob, u, nx, ny)
+    f = fel + fw
+    return u, {"iterations": it, "force_evals": evals + 1, "energy": E_el + E_w,
+               "fmax": np.abs(f).max(), "fnorm": np.sqrt((f * f).sum())}
+
+
+def fire(elastic, ob, u, nx, ny, ftol=1e-6, maxiter=100000, minsteps=10, incfac=1.2,
+         decfac=0.5, mix_in=0.1, mixdec=0.99, dtmax=0.001, dt=None, xlimit=0.0):
+    """FixFIRE (src/cuda/fix_fire.cpp:117-297) with unit masses."""
+    u = u.copy()
+    v = np.zeros_like(u)
+    dt = dtmax if dt is None else dt
+    nl = u.shape[0] // 3
+
+    def total():
+        fel, E = elastic(u, True)
+        Ew, fw, _, _ = wall(ob, u, nx, ny)
+        return fel + fw, E + Ew
+
+    def limit(vv, vlimsq):
+        if vlimsq <= 0:
+            return vv
+        vv = vv.reshape(nl, 3, -1)
+        vsq = (vv ** 2).sum(1, keepdims=True)
+        sc = np.where(vsq > vlimsq, np.sqrt(vlimsq / np.maximum(vsq, 1e-300)), 1.0)
+        return (vv * sc).reshape(3 * nl, -1)
+
+    f, E = total()
+    evals, it, cut, mix = 1, 0, minsteps, mix_in
+    while np.abs(f).max() > ftol and it < maxiter:
+        dtf = 0.5 * dt
+        vlimsq = (xlimit / dt) ** 2 if xlimit > 0 else 0.0
+        v = limit(v + dtf * f, vlimsq)
+        u += dt * v
+        f, E = total()
+        evals += 1
+        v = limit(v + dtf * f, vlimsq)
+        vf, vv, ff = (v * f).sum(), (v * v).sum(), (f * f).sum()
+        help_ = mix * np.sqrt(vv / ff) if ff > 0 else 0.0
+        if vf < 0:
+            v[:] = 0.0
+            cut, dt, mix = minsteps, dt * decfac, mix_in
+        else:
+            v = (1 - mix) * v + help_ * f
+            if cut < 0:
+                dt, mix = min(dt * incfac, dtmax), mix * mixdec
+            else:
+                cut -= 1
+        it += 1
+    return u, {"iterations": it, "force_evals": evals, "energy": E, "fmax": np.abs(f).max()}
+
+
+def verlet(elastic, ob, u, v, nx, ny, dt, gamma, nsteps):
+    """Damped velocity Verlet; returns (u, v, energies[nsteps+1])."""
+    u, v = u.copy(), v.copy()
+
+    def total():
+        fel, E = elastic(u, True)
+        Ew, fw, _, _ = wall(ob, u, nx, ny)
+        return fel + fw, E + Ew
+
+    f, E = total()
+    out = [E + 0.5 * (v * v).sum()]
+    for _ in range(nsteps):
+        v = v + 0.5 * dt * (f - gamma * v)
+        u += dt * v
+        f, E = total()
+        v = (v + 0.5 * dt * f) / (1.0 + 0.5 * dt * gamma)
+        out.append(E + 0.5 * (v * v).sum())
+    return u, v, np.array(out)

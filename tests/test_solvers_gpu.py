@@ -1,0 +1,157 @@
+"""GPU solver loops against the oracle's restatement (FP64)."""
+import numpy as np
+import pytest
+
+from conftest import gfmd_pkg, rel_l2
+from solver_cases import (KERNEL_FCC2, KERNEL_SC, gpu_obstacle, oracle_elastic, osv,
+                          sphere_spec, tables)
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def _solver(nx, ny, d, half, linf, prec="f64"):
+    s = gfmd_pkg().gfmd_solver_factory("static/gb300" if prec == "f64" else "static/gb300/f32")
+    s.set_grid_size(nx, ny, d)
+    s.set_phi(half, "half", linf)
+    return s
+
+
+def _problem(kind=osv.SPHERE_EXP, nx=32, ny=32):
+    d, half, full, linf = tables(KERNEL_SC, nx, ny)
+    if kind == osv.SPHERE_LJ:
+        ob = sphere_spec(nx, ny, R=6.0, pen=-0.9, eps=0.02, sigma=0.5, kind=kind, cutoff=2.5)
+    elif kind == osv.MAP_EXP:
+        rng = np.random.default_rng(4)
+        zq = np.fft.rfft2(rng.normal(0, 1, (nx, ny)))
+        kx = np.fft.fftfreq(nx)[:, None]
+        ky = np.fft.rfftfreq(ny)[None, :]
+        zq *= np.exp(-((kx ** 2 + ky ** 2) * 200.0))
+        zmap = np.fft.irfft2(zq, (nx, ny)).ravel()
+        zmap = 0.3 * zmap / np.abs(zmap).max()
+        ob = osv.ObstacleSpec(kind, epsilon=0.05, sigma=0.5, cutoff=4.0, zmap=zmap,
+                              map_z0=-0.2, norm=-1)
+    else:
+        ob = sphere_spec(nx, ny, R=6.0, pen=0.3, cutoff=4.0)
+    return d, half, full, linf, ob
+
+
+def _gpu_obst(ob):
+    o = gpu_obstacle(ob)
+    keep = None
+    if ob.kind == osv.MAP_EXP:
+        keep = torch.from_numpy(ob.zmap).cuda()
+        o.d_map = keep.data_ptr()
+    return o, keep
+
+
+@pytest.mark.parametrize("kind", [osv.SPHERE_EXP, osv.SPHERE_LJ, osv.MAP_EXP])
+def test_cg_matches_oracle(kind):
+    nx = ny = 32
+    d, half, full, linf, ob = _problem(kind)
+    el = oracle_elastic(full, linf, nx, ny)
+    u0 = np.zeros((d, nx * ny))
+    u_ref, r_ref = osv.cg(el, ob, u0, nx, ny, ftol=1e-8)
+    s = _solver(nx, ny, d, half, linf)
+    o, keep = _gpu_obst(ob)
+    u = torch.zeros(d, nx * ny, dtype=torch.float64, device="cuda")
+    rep = s.minimize(u, o, "cg", ftol=1e-8)
+    assert rep["fmax"] <= 1e-8
+    assert rel_l2(u.cpu().numpy(), u_ref) <= 1e-6
+    assert abs(rep["energy"] - r_ref["energy"]) <= 1e-9 * abs(r_ref["energy"])
+
+
+def test_fire_matches_oracle_minimum():
+    nx = ny = 32
+    d, half, full, linf, ob = _problem()
+    el = oracle_elastic(full, linf, nx, ny)
+    u_ref, r_ref = osv.cg(el, ob, np.zeros((d, nx * ny)), nx, ny, ftol=1e-8)
+    s = _solver(nx, ny, d, half, linf)
+    o, _ = _gpu_obst(ob)
+    u = torch.zeros(d, nx * ny, dtype=torch.float64, device="cuda")
+    rep = s.minimize(u, o, "fire", ftol=1e-8, maxiter=20000, dtmax=0.2, dt=0.05)
+    assert rep["fmax"] <= 1e-8
+    assert rel_l2(u.cpu().numpy(), u_ref) <= 1e-6
+
+
+def test_fire_trajectory_matches_oracle():
+    nx = ny = 32
+    d, half, full, linf, ob = _problem()
+    el = oracle_elastic(full, linf, nx, ny)
+    u_ref, r_ref = osv.fire(el, ob, np.zeros((d, nx * ny)), nx, ny, ftol=0.0, maxiter=60,
+                            dtmax=0.2, dt=0.05)
+    s = _solver(nx, ny, d, half, linf)
+    o, _ = _gpu_obst(ob)
+    u = torch.zeros(d, nx * ny, dtype=torch.float64, device="cuda")
+    g = gfmd_pkg()
+    with pytest.raises(g.GFMDError) as ei:
+        s.minimize(u, o, "fire", ftol=0.0, maxiter=60, dtmax=0.2, dt=0.05)
+    assert ei.value.code == 6  # iteration cap: ENOTCONVERGED, state still updated
+    assert rel_l2(u.cpu().numpy(), u_ref) <= 1e-10
+
+
+def test_mixed_precision_cg_with_fp64_refinement():
+    nx = ny = 64
+    d, half, full, linf, ob = _problem(nx=nx, ny=ny)
+    s64 = _solver(nx, ny, d, half, linf, "f64")
+    s32 = _solver(nx, ny, d, half, linf, "f32")
+    o, _ = _gpu_obst(ob)
+    u64 = torch.zeros(d, nx * ny, dtype=torch.float64, device="cuda")
+    r64 = s64.minimize(u64, o, "cg", ftol=1e-8)
+    um = torch.zeros_like(u64)
+    rm = s32.minimize(um, o, "cg", ftol=1e-8, refine=s64)
+    assert rm["fmax"] <= 1e-8  # checked with FP64 forces
+    assert rel_l2(um.cpu().numpy(), u64.cpu().numpy()) <= 1e-6
+    assert abs(rm["energy"] - r64["energy"]) <= 1e-9 * abs(r64["energy"])
+
+
+def test_damped_verlet_matches_oracle():
+    nx = ny = 16
+    d, half, full, linf = tables(KERNEL_FCC2, nx, ny)
+    el = oracle_elastic(full, linf, nx, ny)
+    rng = np.random.default_rng(9)
+    u0 = rng.normal(0, 0.05, (d, nx * ny))
+    v0 = rng.normal(0, 0.01, (d, nx * ny))
+    ob = osv.ObstacleSpec(osv.SPHERE_EXP, center=(8.0, 8.0, 6.2), radius=6.0, epsilon=0.05,
+                          sigma=0.5, cutoff=3.0, layer_offsets=[(0, 0, 0), (0.5, 0.5, -0.7071)])
+    u_ref, v_ref, e_ref = osv.verlet(el, ob, u0, v0, nx, ny, 0.01, 0.1, 100)
+    s = _solver(nx, ny, d, half, linf)
+    o, _ = _gpu_obst(ob)
+    u = torch.from_numpy(u0).cuda()
+    v = torch.from_numpy(v0).cuda()
+    e, rep = s.run_dynamics(u, v, 0.01, 0.1, 100, o)
+    assert np.abs(e - e_ref).max() <= 1e-10 * np.abs(e_ref).max()
+    assert rel_l2(u.cpu().numpy(), u_ref) <= 1e-10
+    assert rel_l2(v.cpu().numpy(), v_ref) <= 1e-9
+    assert e[-1] < e[0]  # damped
+
+
+def test_nve_energy_conservation_like_the_reference_test():
+    # tests/TEST_energy_conservation_fcc100_pair_potential of the reference:
+    # ft fcc100 1.0 2 pair-potential 2 1.0 -0.1 height 10 on 10 x 10, random
+    # displacements of 0.1, dt = 0.01, |E - <E>| / <E> < 1e-4
+    nx = ny = 10
+    d, half, full, linf = tables(KERNEL_FCC2, nx, ny)
+    s = _solver(nx, ny, d, half, linf)
+    rng = np.random.default_rng(12472634)
+    u = torch.from_numpy(rng.uniform(-0.1, 0.1, (d, nx * ny))).cuda()
+    v = torch.zeros_like(u)
+    e, _ = s.run_dynamics(u, v, 0.01, 0.0, 20000)
+    assert np.abs(e - e.mean()).max() / abs(e.mean()) < 1e-4
+
+
+def test_solver_status_codes():
+    g = gfmd_pkg()
+    nx = ny = 16
+    d, half, full, linf = tables(KERNEL_SC, nx, ny)
+    s = _solver(nx, ny, d, half, linf)
+    u = torch.zeros(d, nx * ny, dtype=torch.float64, device="cuda")
+    o = g.Obstacle()
+    o.kind = 3  # map without a map
+    with pytest.raises(g.GFMDError) as ei:
+        s.minimize(u, o, "cg")
+    assert ei.value.code == 1
+    bad = torch.full_like(u, float("nan"))
+    with pytest.raises(g.GFMDError) as ei:
+        s.minimize(bad, None, "cg", maxiter=5)
+    assert ei.value.code == 4

@@ -25,6 +25,70 @@ GFMD_PREC_F32 = 1
 GFMD_PHI_FULL = 0
 GFMD_PHI_HALF = 1
 
+GFMD_OBST_NONE = 0
+GFMD_OBST_SPHERE_EXP = 1
+GFMD_OBST_SPHERE_LJ = 2
+GFMD_OBST_MAP_EXP = 3
+GFMD_MIN_CG = 0
+GFMD_MIN_FIRE = 1
+
+
+class Obstacle(ctypes.Structure):
+    """gfmd_obstacle_t"""
+
+    _fields_ = [
+        ("kind", ctypes.c_int),
+        ("center", ctypes.c_double * 3),
+        ("radius", ctypes.c_double),
+        ("epsilon", ctypes.c_double),
+        ("sigma", ctypes.c_double),
+        ("cutoff", ctypes.c_double),
+        ("d_map", ctypes.c_void_p),
+        ("map_z0", ctypes.c_double),
+        ("norm", ctypes.c_int),
+        ("lattice", ctypes.c_double * 2),
+        ("nlayer", ctypes.c_int),
+        ("layer_offset", (ctypes.c_double * 3) * 8),
+    ]
+
+
+class MinParams(ctypes.Structure):
+    """gfmd_min_params_t"""
+
+    _fields_ = [
+        ("method", ctypes.c_int),
+        ("ftol", ctypes.c_double),
+        ("maxiter", ctypes.c_int),
+        ("recompute", ctypes.c_int),
+        ("refine", ctypes.c_void_p),
+        ("fire_minsteps", ctypes.c_int),
+        ("fire_incfac", ctypes.c_double),
+        ("fire_decfac", ctypes.c_double),
+        ("fire_mix", ctypes.c_double),
+        ("fire_mixdec", ctypes.c_double),
+        ("fire_dtmax", ctypes.c_double),
+        ("fire_dt", ctypes.c_double),
+        ("fire_xlimit", ctypes.c_double),
+    ]
+
+
+class MinReport(ctypes.Structure):
+    """gfmd_min_report_t"""
+
+    _fields_ = [
+        ("status", ctypes.c_int),
+        ("iterations", ctypes.c_int),
+        ("force_evals", ctypes.c_int),
+        ("energy", ctypes.c_double),
+        ("fmax", ctypes.c_double),
+        ("fnorm", ctypes.c_double),
+        ("seconds", ctypes.c_double),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 _NAMES = {
     GFMD_EINVAL: "EINVAL",
     GFMD_ENOMEM: "ENOMEM",
@@ -63,6 +127,10 @@ SIGNATURES = {
     "gfmd_get_u0": [_vp, _vp],
     "gfmd_memory_usage": [_vp, _pd],
     "gfmd_solver_info": [_vp, _pi, _pi],
+    "gfmd_minimize": [_vp, ctypes.POINTER(Obstacle), ctypes.POINTER(MinParams), _vp,
+                      ctypes.POINTER(MinReport)],
+    "gfmd_run_dynamics": [_vp, ctypes.POINTER(Obstacle), _c_dbl, _c_dbl, _c_int, _vp, _vp, _vp,
+                          ctypes.POINTER(MinReport)],
     "gfmd_post_force_noalloc": [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp],
     "gfmd_kernel_create": [ctypes.c_char_p, ctypes.POINTER(_vp)],
     "gfmd_kernel_destroy": [_vp],

@@ -45,7 +45,7 @@ constexpr double kPi = 3.14159265358979323846264338327950288;
 
 void release(gfmd_solver *h) {
   if (!h) return;
-  void *ptrs[] = {h->d_tw_hi, h->d_tw_lo,  h->d_W,     h->d_phi,     h->d_linf,
+  void *ptrs[] = {h->d_zero,  h->d_tw_hi, h->d_tw_lo,  h->d_W,     h->d_phi,     h->d_linf,
                   h->d_epart, h->d_scal,   h->d_io,    h->d_ftw,
                   h->d_counter};
   for (void *p : ptrs)
@@ -292,6 +292,8 @@ int gfmd_create(int nx, int ny, int ndof, int precision, gfmd_handle_t *out) {
   if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_linf, sizeof(double) * (ndof / 3));
   if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_epart, sizeof(double) * h->n_epart);
   if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_scal, sizeof(double) * (1 + gfmd::kMaxNdof));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_zero, sizeof(double) * gfmd::kMaxNdof);
+  if (e == cudaSuccess) e = cudaMemset(h->d_zero, 0, sizeof(double) * gfmd::kMaxNdof);
   if (e == cudaSuccess) e = cudaMemset(h->d_linf, 0, sizeof(double) * (ndof / 3));
   if (e == cudaSuccess) e = cudaMemset(h->d_scal, 0, sizeof(double) * (1 + gfmd::kMaxNdof));
   if (e != cudaSuccess) { release(h); return cuda_fail(e, "gfmd_create: device buffers"); }

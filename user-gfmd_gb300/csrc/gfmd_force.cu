@@ -192,4 +192,13 @@ cudaError_t enqueue_force(gfmd_solver *h, const void *d_u, int in_t, void *d_f, 
   return enqueue_t<float>(h, d_u, in_t, d_f, out_t, d_epot);
 }
 
+cudaError_t enqueue_force_opts(gfmd_solver *h, const void *d_u, int in_t, void *d_f, int out_t,
+                               double *d_epot, bool with_linf) {
+  double *keep = h->d_linf;
+  if (!with_linf) h->d_linf = h->d_zero;
+  cudaError_t e = enqueue_force(h, d_u, in_t, d_f, out_t, d_epot);
+  h->d_linf = keep;
+  return e;
+}
+
 }  // namespace gfmd

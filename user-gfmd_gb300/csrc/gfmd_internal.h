@@ -73,6 +73,7 @@ struct gfmd_solver {
   void *d_W = nullptr;       // spectrum [nyc][ndof][nxp] complex
   void *d_phi = nullptr;     // packed Phi [nyc][npk][nxp] real
   double *d_linf = nullptr;  // [ndof/3]
+  double *d_zero = nullptr;  // [kMaxNdof] zeros (linf switched off)
   double *d_epart = nullptr; // per-block energy partials
   double *d_scal = nullptr;  // [0] energy, [1..ndof] u(q=0)
   void *d_io = nullptr;      // staging for host-buffer calls: u then f, FP64
@@ -95,6 +96,10 @@ namespace gfmd {
 // (0 = double, 1 = float); energy -> d_epot (device double).
 cudaError_t enqueue_force(gfmd_solver *h, const void *d_u, int in_t, void *d_f, int out_t,
                           double *d_epot);
+// The same with the gamma-point linear force switched off (with_linf = false),
+// for the force of a search direction.
+cudaError_t enqueue_force_opts(gfmd_solver *h, const void *d_u, int in_t, void *d_f, int out_t,
+                               double *d_epot, bool with_linf);
 // Records msg as the calling thread's gfmd_last_error() and returns code.
 int set_error(int code, const std::string &msg);
 // Kernel launches one force evaluation makes.

@@ -168,6 +168,37 @@ class GFMDSolverGB300:
         fn = lib().gfmd_force_f64 if self.precision == "f64" else lib().gfmd_force_f32
         check(fn(self._handle(), _ptr(u), _ptr(f), _ptr(epot)))
 
+    def minimize(self, u, obstacle=None, method: str = "cg", ftol: float = 1e-6,
+                 maxiter: int = 0, refine: "GFMDSolverGB300 | None" = None, **fire) -> dict:
+        """Static minimization from the displacements in u (CUDA float64
+        tensor [ndof, nx*ny], updated in place); returns the report.  Raises
+        GFMDError on failure (e.g. ENOTCONVERGED)."""
+        p = _lib.MinParams()
+        p.method = _lib.GFMD_MIN_CG if method == "cg" else _lib.GFMD_MIN_FIRE
+        p.ftol = ftol
+        p.maxiter = maxiter
+        p.refine = refine._handle().value if refine is not None else None
+        for k, v in fire.items():
+            setattr(p, "fire_" + k, v)
+        rep = _lib.MinReport()
+        ob = ctypes.byref(obstacle) if obstacle is not None else None
+        rc = lib().gfmd_minimize(self._handle(), ob, ctypes.byref(p), _ptr(u), ctypes.byref(rep))
+        if rc != _lib.GFMD_OK:
+            err = GFMDError(rc, lib().gfmd_last_error().decode(errors="replace"))
+            err.report = rep.as_dict()
+            raise err
+        return rep.as_dict()
+
+    def run_dynamics(self, u, v, dt: float, gamma: float, nsteps: int, obstacle=None):
+        """Damped velocity Verlet on CUDA float64 tensors u, v (in place);
+        returns (energies[nsteps+1], report)."""
+        e = np.zeros(nsteps + 1)
+        rep = _lib.MinReport()
+        ob = ctypes.byref(obstacle) if obstacle is not None else None
+        check(lib().gfmd_run_dynamics(self._handle(), ob, dt, gamma, nsteps, _ptr(u), _ptr(v),
+                                      _ptr(e), ctypes.byref(rep)))
+        return e, rep.as_dict()
+
     def get_u0(self) -> np.ndarray:
         u0 = np.zeros(self.ndof)
         check(lib().gfmd_get_u0(self._handle(), _ptr(u0)))
