@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-f64", action="store_true")
+    ap.add_argument("--no-static", action="store_true")
+    ap.add_argument("--static-n", type=int, default=2048)
     return ap.parse_args()
 
 
@@ -225,6 +227,58 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------------------
+# Static solve: time to max|f| <= 1e-6, plain FP64 CG vs FP32 CG + FP64 refinement
+
+STATIC_KERNEL = "ft fcc100 1.0 1 pair-potential 1 1.0 height 128"
+
+
+def static_solve(g, torch, dev, stream, n):
+    """Hertz-like indentation of a 2048^2 fcc(100) surface (E* = 1.39 kernel
+    of the reference's tests/TEST_Hertz_fcc100_128x128): rigid sphere
+    R = 100 a centred on the grid, exponential wall e = exp(-g / 0.5 a) on
+    the gap, 1.0 a penetration, CG to max|f_i| <= 1e-6."""
+    k = g.StiffnessKernel(STATIC_KERNEL)
+    d = k.get_dimension()
+    half, linf = k.phi_table(n, n, "half")
+    R, pen = 100.0, 1.0
+    ob = g.sphere_obstacle((n / 2.0, n / 2.0, R - pen), R, 1.0, 0.5)
+
+    def solver(prec):
+        s = g.gfmd_solver_factory("static/gb300" if prec == "f64" else "static/gb300/f32")
+        s.set_grid_size(n, n, d)
+        s.set_phi(half, "half", linf)
+        s.set_stream(stream.cuda_stream)
+        return s
+
+    s64, s32 = solver("f64"), solver("f32")
+    out = {"config": f"{STATIC_KERNEL}, {n}x{n}, sphere R=100 a, exp wall range 0.5 a, "
+                     "penetration 1.0 a, CG to max|f| <= 1e-6 (ftol)"}
+    u64 = torch.zeros(d, n * n, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r64 = s64.minimize(u64, ob, "cg", ftol=1e-6, maxiter=50000)
+    torch.cuda.synchronize()
+    t64 = time.perf_counter() - t0
+    um = torch.zeros_like(u64)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rm = s32.minimize(um, ob, "cg", ftol=1e-6, maxiter=50000, refine=s64)
+    torch.cuda.synchronize()
+    tm = time.perf_counter() - t0
+    err = float(torch.linalg.norm(um - u64) / torch.linalg.norm(u64))
+    out["plain_fp64"] = {"seconds": t64, "iterations": r64["iterations"],
+                         "force_evals": r64["force_evals"], "fmax": r64["fmax"],
+                         "energy": r64["energy"]}
+    out["mixed_fp32_fp64_refine"] = {"seconds": tm, "iterations": rm["iterations"],
+                                     "force_evals": rm["force_evals"], "fmax": rm["fmax"],
+                                     "energy": rm["energy"],
+                                     "rel_displacement_error_vs_fp64": err}
+    out["speedup"] = t64 / tm
+    out["unit"] = "s"
+    return out
+
+
+# ---------------------------------------------------------------------------
 # GB300 arm
 # ---------------------------------------------------------------------------
 
@@ -340,6 +394,9 @@ def run_gb300(args):
                 "frac": achieved / peak, "traffic": profile_traffic(),
                 "kernel": "one force evaluation (all launches of the evaluation)",
                 "algorithmic_bytes": bts, "peak_kind": peak_kind}
+
+    if not args.no_static:
+        extra["static_solve"] = static_solve(g, torch, dev, stream, args.static_n)
 
     cpu = None
     if rank == 0 and not args.no_cpu:

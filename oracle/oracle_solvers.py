@@ -130,7 +130,7 @@ def cg(elastic, ob, u, nx, ny, ftol=1e-6, maxiter=100000, recompute=50):
         hKh = (h * Kh).sum()
         felh = (fel * h).sum()
         a, lo, hi = 0.0, 0.0, -1.0
-        for _ in range(30):
+        for _ in range(16):
             fwh = cw = 0.0
             if ob is not None:
                 _, _, fwh, cw = wall(ob, u, nx, ny, h, a)
@@ -147,7 +147,7 @@ def cg(elastic, ob, u, nx, ny, ftol=1e-6, maxiter=100000, recompute=50):
                 an = 2 * lo if lo > 0 else 1e-3
             step = abs(an - a)
             a = an
-            if step <= 1e-12 * max(1.0, abs(a)) or ob is None:
+            if step <= 1e-6 * abs(a) or ob is None:
                 break
         u += a * h
         fel -= a * Kh

@@ -50,6 +50,8 @@ struct Obst {
   double ax, ay, lx, ly;  // lattice spacing, box
   int nlayer;
   double off[8][3];
+  double gcut;     // effective cutoff on the gap (exp walls without one: 40 sigma)
+  double margin;   // extra distance kept in the active-site list
 };
 
 struct WallOut {
@@ -69,7 +71,7 @@ __device__ __forceinline__ WallOut wall_eval(const Obst &o, int s_ix, int s_iy, 
     d[1] -= o.ly * rint(d[1] / o.ly);
     const double rho = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
     const double g = rho - o.R;
-    if (o.cutoff > 0.0 && g >= o.cutoff) return w;
+    if (g >= o.gcut) return w;
     double e, F, E2;  // E(g), F = -dE/dg, d2E/dg2
     if (o.kind == GFMD_OBST_SPHERE_EXP) {
       const double ex = o.eps * exp(-g / o.sigma);
@@ -95,13 +97,26 @@ __device__ __forceinline__ WallOut wall_eval(const Obst &o, int s_ix, int s_iy, 
   } else if (o.kind == GFMD_OBST_MAP_EXP) {
     const double zm = o.map[site] + o.map_z0;
     const double dz = o.norm * (r[2] - zm);
-    if (o.cutoff > 0.0 && dz >= o.cutoff) return w;
+    if (dz >= o.gcut) return w;
     const double ex = o.eps * exp(-dz / o.sigma);
     w.e = ex - o.offset;
     w.f[2] = o.norm * ex / o.sigma;
     w.curv = ex / (o.sigma * o.sigma) * dir[2] * dir[2];
   }
   return w;
+}
+
+// Cheap FP32 estimate of the gap of an atom (no minimum image subtleties
+// beyond what the margin covers); used to skip the FP64 evaluation far away.
+__device__ __forceinline__ float gap_estimate(const Obst &o, size_t site, const double r[3]) {
+  if (o.kind == GFMD_OBST_MAP_EXP) {
+    return (float)o.norm * ((float)r[2] - (float)(o.map[site] + o.map_z0));
+  }
+  float dx = (float)(r[0] - o.cx), dy = (float)(r[1] - o.cy), dz = (float)(r[2] - o.cz);
+  const float lx = (float)o.lx, ly = (float)o.ly;
+  dx -= lx * rintf(dx / lx);
+  dy -= ly * rintf(dy / ly);
+  return sqrtf(dx * dx + dy * dy + dz * dz) - (float)o.R;
 }
 
 // Per-thread accumulators -> block partials part[blockIdx.x * kMaxRed + k]
@@ -156,13 +171,16 @@ __device__ __forceinline__ void site_pos(const Obst &o, const Geom &g, size_t s,
   r[1] += iy * o.ay;
 }
 
-// Line-search probe at u + a h: sums of (F_w . h), (h^T H_w h), E_w.
+// Line-search probe at u + a h over the sites flagged near the obstacle (in
+// grid order, so the sums are reproducible): sums of (F_w . h), (h^T H_w h), E_w.
 __global__ void __launch_bounds__(kRedThreads) k_wall_line(Obst o, Geom g, const double *__restrict__ x,
                                                            const double *__restrict__ h, double a,
-                                                           double *__restrict__ part) {
+                                                           double *__restrict__ part,
+                                                           const unsigned char *__restrict__ active) {
   const size_t N = (size_t)g.nx * g.ny;
   double acc[3] = {0.0, 0.0, 0.0};
   for (size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x; s < N; s += (size_t)gridDim.x * blockDim.x) {
+    if (!active[s]) continue;
     for (int l = 0; l < o.nlayer; l++) {
       double r[3], dir[3];
       site_pos(o, g, s, l, x, N, a, h, r, dir);
@@ -180,17 +198,23 @@ __global__ void __launch_bounds__(kRedThreads) k_wall_line(Obst o, Geom g, const
 __global__ void __launch_bounds__(kRedThreads) k_total_force(Obst o, Geom g, const double *__restrict__ x,
                                                              const double *__restrict__ fel,
                                                              double *__restrict__ ftot,
-                                                             double *__restrict__ part) {
+                                                             double *__restrict__ part,
+                                                             unsigned char *__restrict__ active) {
   const size_t N = (size_t)g.nx * g.ny;
   const int nl = g.ndof / 3;
   double acc[3] = {0.0, 0.0, 0.0};
   for (size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x; s < N; s += (size_t)gridDim.x * blockDim.x) {
+    bool near = false;
     for (int l = 0; l < nl; l++) {
       double fw[3] = {0.0, 0.0, 0.0};
       if (l < o.nlayer && o.kind != GFMD_OBST_NONE) {
         double r[3], dir[3];
         site_pos(o, g, s, l, x, N, 0.0, nullptr, r, dir);
-        WallOut w = wall_eval(o, (int)(s / g.ny), (int)(s % g.ny), s, r, dir);
+        const float ge = gap_estimate(o, s, r);
+        if (ge < (float)(o.gcut + o.margin)) near = true;
+        WallOut w{0.0, {0.0, 0.0, 0.0}, 0.0};
+        if (ge < (float)o.gcut + 0.01f * (float)o.gcut + 1e-3f)
+          w = wall_eval(o, (int)(s / g.ny), (int)(s % g.ny), s, r, dir);
         fw[0] = w.f[0];
         fw[1] = w.f[1];
         fw[2] = w.f[2];
@@ -204,6 +228,7 @@ __global__ void __launch_bounds__(kRedThreads) k_total_force(Obst o, Geom g, con
         acc[2] = fmax(acc[2], fabs(f));
       }
     }
+    if (active) active[s] = near ? 1 : 0;
   }
   block_reduce(acc, 2, true, part);
 }
@@ -216,11 +241,13 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_update(Obst o, Geom g, doubl
                                                            const double *__restrict__ Kh,
                                                            double *__restrict__ fel,
                                                            double *__restrict__ gprev, double a,
-                                                           double *__restrict__ part) {
+                                                           double *__restrict__ part,
+                                                           unsigned char *__restrict__ active) {
   const size_t N = (size_t)g.nx * g.ny;
   const int nl = g.ndof / 3;
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
   for (size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x; s < N; s += (size_t)gridDim.x * blockDim.x) {
+    bool near = false;
     for (int l = 0; l < nl; l++) {
       for (int c = 0; c < 3; c++) {
         const size_t idx = (size_t)(3 * l + c) * N + s;
@@ -231,7 +258,11 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_update(Obst o, Geom g, doubl
       if (l < o.nlayer && o.kind != GFMD_OBST_NONE) {
         double r[3], dir[3];
         site_pos(o, g, s, l, x, N, 0.0, nullptr, r, dir);
-        WallOut w = wall_eval(o, (int)(s / g.ny), (int)(s % g.ny), s, r, dir);
+        const float ge = gap_estimate(o, s, r);
+        if (ge < (float)(o.gcut + o.margin)) near = true;
+        WallOut w{0.0, {0.0, 0.0, 0.0}, 0.0};
+        if (ge < (float)o.gcut + 0.01f * (float)o.gcut + 1e-3f)
+          w = wall_eval(o, (int)(s / g.ny), (int)(s % g.ny), s, r, dir);
         fw[0] = w.f[0];
         fw[1] = w.f[1];
         fw[2] = w.f[2];
@@ -246,6 +277,7 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_update(Obst o, Geom g, doubl
         gprev[idx] = gv;
       }
     }
+    if (active) active[s] = near ? 1 : 0;
   }
   block_reduce(acc, 3, true, part);
 }
@@ -274,9 +306,19 @@ __global__ void __launch_bounds__(kRedThreads) k_dot(size_t n, const double *__r
   block_reduce(acc, 1, false, part);
 }
 
-__global__ void k_negate(size_t n, double *__restrict__ a) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    a[i] = -a[i];
+// Kh = -fKh in place; sums: h.Kh, fel.h
+__global__ void __launch_bounds__(kRedThreads) k_cg_dirforce(size_t n, double *__restrict__ Kh,
+                                                             const double *__restrict__ h,
+                                                             const double *__restrict__ fel,
+                                                             double *__restrict__ part) {
+  double acc[2] = {0.0, 0.0};
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const double k = -Kh[i], hv = h[i];
+    Kh[i] = k;
+    acc[0] += hv * k;
+    acc[1] += fel[i] * hv;
+  }
+  block_reduce(acc, 2, false, part);
 }
 
 // FIRE, first half (FixFIRE::initial_integrate): v += dtf f, |v| per atom
@@ -375,6 +417,7 @@ struct Work {
   double *res = nullptr;   // kMaxRed (device)
   double *hres = nullptr;  // pinned host copy
   double *d_e = nullptr;   // energy of a force evaluation
+  unsigned char *active = nullptr;  // per site: near the obstacle (line search)
   double *bufs[6] = {};
   size_t n = 0;
   ~Work() {
@@ -382,6 +425,7 @@ struct Work {
     if (res) cudaFree(res);
     if (hres) cudaFreeHost(hres);
     if (d_e) cudaFree(d_e);
+    if (active) cudaFree(active);
     for (double *b : bufs)
       if (b) cudaFree(b);
   }
@@ -396,6 +440,7 @@ cudaError_t work_init(Work &w, gfmd_solver *h, int nbuf) {
   if (e == cudaSuccess) e = cudaMalloc((void **)&w.res, sizeof(double) * kMaxRed);
   if (e == cudaSuccess) e = cudaMallocHost((void **)&w.hres, sizeof(double) * kMaxRed);
   if (e == cudaSuccess) e = cudaMalloc((void **)&w.d_e, sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&w.active, (size_t)h->g.nx * h->g.ny);
   for (int i = 0; i < nbuf && e == cudaSuccess; i++) e = cudaMalloc((void **)&w.bufs[i], sizeof(double) * w.n);
   return e;
 }
@@ -457,6 +502,10 @@ Obst make_obst(const gfmd_obstacle_t *ob, const Geom &g) {
   } else if (o.cutoff > 0.0) {
     o.offset = o.eps * std::exp(-o.cutoff / o.sigma);
   }
+  // exponential walls without a cutoff: beyond 40 sigma the force is below
+  // 4e-18 eps/sigma, far under any force tolerance
+  o.gcut = o.cutoff > 0.0 ? o.cutoff : (o.kind == GFMD_OBST_SPHERE_LJ ? 1e30 : 40.0 * o.sigma);
+  o.margin = 10.0 * o.sigma + 1.0;
   return o;
 }
 
@@ -471,7 +520,7 @@ cudaError_t total_force(Work &w, gfmd_solver *hh, const Obst &o, const double *u
                         double *ftot, double *E, double *fmax, double *f2) {
   double eel = 0.0;
   RT(elastic(w, hh, u, fel, true, &eel));
-  k_total_force<<<w.nblk, kRedThreads, 0, w.st>>>(o, hh->g, u, fel, ftot, w.part);
+  k_total_force<<<w.nblk, kRedThreads, 0, w.st>>>(o, hh->g, u, fel, ftot, w.part, w.active);
   RT(fetch(w, 2, true));
   if (E) *E = eel + w.hres[0];
   if (f2) *f2 = w.hres[1];
@@ -498,7 +547,7 @@ int cg_solve(gfmd_solver *hp, const gfmd_obstacle_t *ob, const gfmd_min_params_t
     // fel = F_el(u); gprev = g = fel + F_w; h = g
     RT(elastic(w, hh, u, fel, true, nullptr));
     evals++;
-    k_total_force<<<w.nblk, kRedThreads, 0, w.st>>>(o, hh->g, u, fel, gp, w.part);
+    k_total_force<<<w.nblk, kRedThreads, 0, w.st>>>(o, hh->g, u, fel, gp, w.part, w.active);
     RT(fetch(w, 2, true));
     f2 = w.hres[1];
     fmax = w.hres[2];
@@ -529,19 +578,16 @@ int cg_solve(gfmd_solver *hp, const gfmd_obstacle_t *ob, const gfmd_min_params_t
     ce = elastic(w, hh, h, Kh, false, nullptr);
     if (ce != cudaSuccess) break;
     evals++;
-    k_negate<<<w.nblk, kRedThreads, 0, w.st>>>(w.n, Kh);
-    k_dot<<<w.nblk, kRedThreads, 0, w.st>>>(w.n, h, Kh, w.part);
-    if ((ce = fetch(w, 1, false)) != cudaSuccess) break;
+    k_cg_dirforce<<<w.nblk, kRedThreads, 0, w.st>>>(w.n, Kh, h, fel, w.part);
+    if ((ce = fetch(w, 2, false)) != cudaSuccess) break;
     const double hKh = w.hres[0];
-    k_dot<<<w.nblk, kRedThreads, 0, w.st>>>(w.n, fel, h, w.part);
-    if ((ce = fetch(w, 1, false)) != cudaSuccess) break;
-    const double felh = w.hres[0];
+    const double felh = w.hres[1];
     // Newton line search on phi'(a) = -(fel.h - a hKh + F_w(u + a h).h)
     double a = 0.0, lo = 0.0, hi = -1.0;
-    for (int ls = 0; ls < 30; ls++) {
+    for (int ls = 0; ls < 16; ls++) {
       double fwh = 0.0, cw = 0.0;
       if (o.kind != GFMD_OBST_NONE) {
-        k_wall_line<<<w.nblk, kRedThreads, 0, w.st>>>(o, hh->g, u, h, a, w.part);
+        k_wall_line<<<w.nblk, kRedThreads, 0, w.st>>>(o, hh->g, u, h, a, w.part, w.active);
         if ((ce = fetch(w, 3, false)) != cudaSuccess) break;
         fwh = w.hres[0];
         cw = w.hres[1];
@@ -554,12 +600,14 @@ int cg_solve(gfmd_solver *hp, const gfmd_obstacle_t *ob, const gfmd_min_params_t
       else if (an < 0.0) an = lo > 0.0 ? 2.0 * lo : 1e-3;
       const double step = std::fabs(an - a);
       a = an;
-      if (step <= 1e-12 * std::max(1.0, std::fabs(a))) break;
+      // an exact line minimum is not needed: Polak-Ribiere with restarts
+      // converges from a step within 1e-6 of it
+      if (step <= 1e-6 * std::fabs(a)) break;
       if (o.kind == GFMD_OBST_NONE) break;  // quadratic: one Newton step is exact
     }
     if (ce != cudaSuccess) break;
     // update
-    k_cg_update<<<w.nblk, kRedThreads, 0, w.st>>>(o, hh->g, u, h, Kh, fel, gp, a, w.part);
+    k_cg_update<<<w.nblk, kRedThreads, 0, w.st>>>(o, hh->g, u, h, Kh, fel, gp, a, w.part, w.active);
     // gp held g_old; kernel computed g.g and g.g_old before overwriting
     const double gg_old = f2;
     if ((ce = fetch(w, 3, true)) != cudaSuccess) break;
