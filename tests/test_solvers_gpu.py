@@ -105,6 +105,47 @@ def test_mixed_precision_cg_with_fp64_refinement():
     assert abs(rm["energy"] - r64["energy"]) <= 1e-9 * abs(r64["energy"])
 
 
+def test_cg_is_reproducible():
+    nx = ny = 32
+    d, half, full, linf, ob = _problem()
+    s = _solver(nx, ny, d, half, linf)
+    o, _ = _gpu_obst(ob)
+    runs = []
+    for _ in range(2):
+        u = torch.zeros(d, nx * ny, dtype=torch.float64, device="cuda")
+        rep = s.minimize(u, o, "cg", ftol=1e-8)
+        runs.append((u, rep))
+    assert torch.equal(runs[0][0], runs[1][0])
+    assert runs[0][1]["iterations"] == runs[1][1]["iterations"]
+    assert runs[0][1]["energy"] == runs[1][1]["energy"]
+
+
+def test_cg_iteration_count_close_to_oracle():
+    nx = ny = 32
+    d, half, full, linf, ob = _problem()
+    el = oracle_elastic(full, linf, nx, ny)
+    _, r_ref = osv.cg(el, ob, np.zeros((d, nx * ny)), nx, ny, ftol=1e-8)
+    s = _solver(nx, ny, d, half, linf)
+    o, _ = _gpu_obst(ob)
+    u = torch.zeros(d, nx * ny, dtype=torch.float64, device="cuda")
+    rep = s.minimize(u, o, "cg", ftol=1e-8)
+    assert rep["iterations"] <= 1.5 * r_ref["iterations"] + 5
+
+
+def test_fp32_cg_without_refinement():
+    nx = ny = 64
+    d, half, full, linf, ob = _problem(nx=nx, ny=ny)
+    s64 = _solver(nx, ny, d, half, linf, "f64")
+    s32 = _solver(nx, ny, d, half, linf, "f32")
+    o, _ = _gpu_obst(ob)
+    u64 = torch.zeros(d, nx * ny, dtype=torch.float64, device="cuda")
+    s64.minimize(u64, o, "cg", ftol=1e-8)
+    u32 = torch.zeros_like(u64)
+    rep = s32.minimize(u32, o, "cg", ftol=1e-5)
+    assert rep["fmax"] <= 1e-5  # FP32 forces
+    assert rel_l2(u32.cpu().numpy(), u64.cpu().numpy()) <= 1e-3
+
+
 def test_damped_verlet_matches_oracle():
     nx = ny = 16
     d, half, full, linf = tables(KERNEL_FCC2, nx, ny)

@@ -1,0 +1,687 @@
+// Polak-Ribiere conjugate gradients with a Newton line search, resident on
+// the GPU with its scalar control on the device.
+//
+// The minimizer LAMMPS runs on fix gfmd through `minimize` (the reference's
+// Hertz tests, tests/TEST_Hertz_*/lammps.in, use min_style cg), restated for
+// a grid of displacements u[ndof][nx*ny] with the elastic force from the
+// handle's force evaluation and an obstacle force (gfmd_obstacle.cuh).
+//
+// Layout of one CG iteration (all on one stream, no host round trip):
+//   fKh = F_el(h)                  force evaluation of the direction (no
+//                                  gamma-point term); F_el is linear, so
+//                                  F_el(u + a h) = F_el(u) + a fKh exactly
+//   k_dirforce                     h.K.h, g.h, wall curvature along h at a = 0,
+//                                  first Newton step
+//   k_probe x kLsMax               Newton steps on the line derivative,
+//                                  each a no-op once the step has converged
+//   k_update                       u += a h, f_el += a fKh, g = f_el + F_w(u),
+//                                  Polak-Ribiere beta with the descent check,
+//                                  convergence test, loop condition
+//   k_dir                          h = g + beta h
+// The iteration is the body of a CUDA graph WHILE node; the loop condition is
+// set by the last block of k_update, which counts the iterations, so every
+// launch of the graph runs at most `recompute` iterations.  Each launch
+// starts from a fresh evaluation of F_el(u) (the drift of the incremental
+// update is reset) and steepest descent.
+//
+// Precision: the state is held in two types, Tx for u and f_el (the
+// quantities that accumulate) and Tv for g, h and fKh.  Plain FP64 runs
+// <double, double>; the mixed solve runs an FP32 phase <float, float> with
+// FP32 force evaluations and then an FP64 refinement <double, float> whose
+// restarts use the FP64 force evaluation while the direction forces stay
+// FP32 (their error is relative to |h|, which shrinks as the solve
+// converges).  Dot products are FP64 (plain) or compensated FP32
+// (TwoProd/TwoSum error-free transformations, Ogita, Rump and Oishi 2005),
+// which carries about 48 significant bits on the FP32 pipes: on this GPU the
+// FP64 ALU rate is below the rate at which HBM streams operands, so FP64
+// arithmetic per element would bound these kernels.  Per-block partials are
+// combined in FP64 in a fixed order by the last block, so results are
+// bit-reproducible.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <string>
+
+#include "gfmd_internal.h"
+#include "gfmd_obstacle.cuh"
+
+namespace gfmd {
+
+namespace {
+
+constexpr int kT = 256;     // threads per block
+constexpr int kQ = 8;       // partial slots per block
+constexpr int kLsMax = 8;   // Newton probes per line search
+
+#define RT_CHECK(call)                \
+  do {                                \
+    cudaError_t e_ = (call);          \
+    if (e_ != cudaSuccess) return e_; \
+  } while (0)
+
+struct CgCtl {
+  double a, lo, hi;         // line search: step and bracket
+  double gh, hKh;           // g.h and h.K.h at the start of the line search
+  double gg;                // g.g of the current gradient
+  double fmax;              // max |g_i|
+  double ew;                // obstacle energy at the last update
+  double beta;              // next direction: h = g + beta h
+  double ftol;              // tolerance of the running phase
+  double ftol_req;          // requested tolerance
+  double fmax_restart;      // max |g_i| at the last restart
+  int bulk;                 // FP32 phase: tolerance floored at the FP32 noise level
+  int it, since, maxit, recompute;
+  int ls_it, ls_done;
+  int done;                 // 0 running, 1 converged, 2 iteration cap, 3 non-finite
+  int obst;
+  unsigned int counter;     // last-block detection
+};
+
+// ---- per-thread accumulation ------------------------------------------------
+template <typename T> struct Dot;
+template <> struct Dot<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double a, double b) { s = fma(a, b, s); }
+  __device__ __forceinline__ double get() const { return s; }
+};
+// Compensated FP32 dot product: TwoProd via fmaf, TwoSum on the running sum.
+template <> struct Dot<float> {
+  float hi = 0.0f, lo = 0.0f;
+  __device__ __forceinline__ void add(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float pe = fmaf(a, b, -p);
+    const float s = __fadd_rn(hi, p);
+    const float bb = __fsub_rn(s, hi);
+    const float se = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(se, pe));
+  }
+  __device__ __forceinline__ double get() const { return (double)hi + (double)lo; }
+};
+
+// Block partials of NS sums followed by NM maxima -> part; the block that
+// finishes last combines all partials in a fixed order into res[] and
+// returns true (all its threads).
+template <int NS, int NM>
+__device__ bool reduce_last(const double *acc, double *part, unsigned int *counter, double *res) {
+  constexpr int NQ = NS + NM;
+  static_assert(NQ <= kQ, "too many reduced scalars");
+  __shared__ double sh[kT / 32][NQ];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NQ; k++) {
+    double v = acc[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double t = __shfl_down_sync(0xffffffffu, v, o);
+      v = (k >= NS) ? fmax(v, t) : v + t;
+    }
+    if (lane == 0) sh[warp][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < NQ) {
+    const int k = threadIdx.x;
+    double v = sh[0][k];
+    for (int w = 1; w < kT / 32; w++) v = (k >= NS) ? fmax(v, sh[w][k]) : v + sh[w][k];
+    part[blockIdx.x * kQ + k] = v;
+    __threadfence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicInc(counter, gridDim.x - 1) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return false;
+#pragma unroll
+  for (int k = 0; k < NQ; k++) {
+    double v = 0.0;  // sums start at 0; maxima are of |.| >= 0
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += kT) {
+      const double t = __ldcg(part + (size_t)b * kQ + k);
+      v = (k >= NS) ? fmax(v, t) : v + t;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double t = __shfl_down_sync(0xffffffffu, v, o);
+      v = (k >= NS) ? fmax(v, t) : v + t;
+    }
+    if (lane == 0) sh[warp][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < NQ) {
+    const int k = threadIdx.x;
+    double v = sh[0][k];
+    for (int w = 1; w < kT / 32; w++) v = (k >= NS) ? fmax(v, sh[w][k]) : v + sh[w][k];
+    res[k] = v;
+  }
+  __syncthreads();
+  return true;
+}
+
+// Position of atom (site s, layer l) at x + a h, in FP64 and FP32.
+template <typename Tx, typename Tv>
+__device__ __forceinline__ void atom_pos(const Obst &o, int ix, int iy, int l, const Tx *x, const Tv *h,
+                                         size_t N, size_t s, double a, double r[3], double d[3]) {
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const size_t idx = (size_t)(3 * l + c) * N + s;
+    const double hv = h ? (double)h[idx] : 0.0;
+    d[c] = hv;
+    r[c] = (double)x[idx] + a * hv + o.off[l][c];
+  }
+  r[0] += ix * o.ax;
+  r[1] += iy * o.ay;
+}
+
+template <typename Tx>
+__device__ __forceinline__ float gap_of(const Obst &o, int ix, int iy, int l, const Tx *x, size_t N, size_t s) {
+  float r[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) r[c] = (float)x[(size_t)(3 * l + c) * N + s] + (float)o.off[l][c];
+  r[0] += (float)ix * (float)o.ax;
+  r[1] += (float)iy * (float)o.ay;
+  return gap_estimate_f(o, s, r);
+}
+
+__device__ __forceinline__ bool wall_near(const Obst &o, float ge) {
+  return ge < (float)o.gcut + 0.01f * (float)o.gcut + 1e-3f;
+}
+
+__device__ __forceinline__ void set_loop(cudaGraphConditionalHandle hc, int use, unsigned int v) {
+  if (use) cudaGraphSetConditional(hc, v);
+}
+
+// ---- restart: g = f_el + F_w(u), h = g; arms the loop ---------------------
+template <typename Tx, typename Tv>
+__global__ void __launch_bounds__(kT) k_restart(Obst o, Geom gm, const Tx *__restrict__ x,
+                                                 const Tx *__restrict__ fel, Tv *__restrict__ g,
+                                                 Tv *__restrict__ h, unsigned char *__restrict__ active,
+                                                 double *__restrict__ part, CgCtl *ctl,
+                                                 cudaGraphConditionalHandle hc, int use_hc) {
+  const int N = gm.nx * gm.ny;
+  const int nl = gm.ndof / 3;
+  Dot<Tv> gg;
+  double ew = 0.0;
+  float fmx = 0.0f, femx = 0.0f;
+  double fmx_d = 0.0;
+  for (int s = blockIdx.x * kT + threadIdx.x; s < N; s += gridDim.x * kT) {
+    const int ix = s / gm.ny, iy = s - ix * gm.ny;
+    bool nearflag = false;
+    for (int l = 0; l < nl; l++) {
+#pragma unroll
+      for (int c = 0; c < 3; c++) femx = fmaxf(femx, fabsf((float)fel[(size_t)(3 * l + c) * N + s]));
+      double fw[3] = {0.0, 0.0, 0.0};
+      if (l < o.nlayer && o.kind != GFMD_OBST_NONE) {
+        const float ge = gap_of(o, ix, iy, l, x, N, s);
+        if (ge < (float)(o.gcut + o.margin)) nearflag = true;
+        if (wall_near(o, ge)) {
+          double r[3], d[3];
+          atom_pos<Tx, Tv>(o, ix, iy, l, x, nullptr, N, s, 0.0, r, d);
+          const WallOut w = wall_eval(o, ix, iy, s, r, d);
+          fw[0] = w.f[0];
+          fw[1] = w.f[1];
+          fw[2] = w.f[2];
+          ew += w.e;
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const size_t idx = (size_t)(3 * l + c) * N + s;
+        Tv gv;
+        if (fw[c] != 0.0) gv = (Tv)((double)fel[idx] + fw[c]);
+        else gv = (Tv)fel[idx];
+        g[idx] = gv;
+        h[idx] = gv;
+        gg.add(gv, gv);
+        if constexpr (sizeof(Tv) == 4) fmx = fmaxf(fmx, fabsf(gv));
+        else fmx_d = fmax(fmx_d, fabs(gv));
+      }
+    }
+    active[s] = nearflag ? 1 : 0;
+  }
+  const double acc[4] = {gg.get(), ew, sizeof(Tv) == 4 ? (double)fmx : fmx_d, (double)femx};
+  __shared__ double res[4];
+  if (!reduce_last<2, 2>(acc, part, &ctl->counter, res)) return;
+  if (threadIdx.x == 0) {
+    ctl->gg = res[0];
+    ctl->ew = res[1];
+    ctl->fmax = res[2];
+    ctl->fmax_restart = res[2];
+    ctl->since = 0;
+    ctl->beta = 0.0;
+    // FP32 state resolves g = f_el + F_w to about eps32 |f_el|: the FP32
+    // phase stops at 64 eps32 max|f_el| if that is above the request
+    ctl->ftol = ctl->bulk ? fmax(ctl->ftol_req, 64.0 * 5.960464477539063e-8 * res[3]) : ctl->ftol_req;
+    if (!isfinite(res[0])) ctl->done = 3;
+    else if (res[2] <= ctl->ftol) ctl->done = 1;
+    else if (ctl->it >= ctl->maxit) ctl->done = 2;
+    else ctl->done = 0;
+    set_loop(hc, use_hc, ctl->done == 0 ? 1u : 0u);
+  }
+}
+
+// ---- along the direction: h.K.h, g.h, wall curvature, first Newton step ----
+template <typename Tx, typename Tv>
+__global__ void __launch_bounds__(kT) k_dirforce(Obst o, Geom gm, const Tx *__restrict__ x,
+                                                  const Tv *__restrict__ fKh, const Tv *__restrict__ h,
+                                                  const Tv *__restrict__ g,
+                                                  const unsigned char *__restrict__ active,
+                                                  double *__restrict__ part, CgCtl *ctl) {
+  const int N = gm.nx * gm.ny;
+  const int nl = gm.ndof / 3;
+  Dot<Tv> hkh, gh;
+  double cw = 0.0;
+  for (int s = blockIdx.x * kT + threadIdx.x; s < N; s += gridDim.x * kT) {
+    for (int l = 0; l < nl; l++) {
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const size_t idx = (size_t)(3 * l + c) * N + s;
+        const Tv hv = h[idx];
+        hkh.add(hv, fKh[idx]);
+        gh.add(g[idx], hv);
+      }
+    }
+    if (o.kind != GFMD_OBST_NONE && active[s]) {
+      const int ix = s / gm.ny, iy = s - ix * gm.ny;
+      for (int l = 0; l < o.nlayer; l++) {
+        double r[3], d[3];
+        atom_pos<Tx, Tv>(o, ix, iy, l, x, h, N, s, 0.0, r, d);
+        cw += wall_eval(o, ix, iy, s, r, d).curv;
+      }
+    }
+  }
+  const double acc[3] = {-hkh.get(), gh.get(), cw};
+  __shared__ double res[3];
+  if (!reduce_last<3, 0>(acc, part, &ctl->counter, res)) return;
+  if (threadIdx.x == 0) {
+    const double hKh = res[0], ghv = res[1], curv = res[0] + res[2];
+    ctl->hKh = hKh;
+    ctl->gh = ghv;
+    ctl->lo = 0.0;
+    ctl->hi = -1.0;
+    ctl->ls_it = 0;
+    // Newton step from a = 0 on phi'(a) = -(g.h - a hKh + dF_w(a).h)
+    double a;
+    if (curv > 0.0 && ghv > 0.0) a = ghv / curv;
+    else a = ghv > 0.0 ? 1e-3 : 0.0;
+    ctl->a = a;
+    ctl->ls_done = (o.kind == GFMD_OBST_NONE || ghv <= 0.0) ? 1 : 0;
+  }
+}
+
+// ---- one Newton probe of the line search at u + a h ------------------------
+// gdir(a) = g.h - a hKh + sum (F_w(u + a h) - F_w(u)).h   (= -phi'(a))
+// curv(a) = hKh + sum h^T H_w(u + a h) h                   (=  phi''(a))
+template <typename Tx, typename Tv>
+__global__ void __launch_bounds__(kT) k_probe(Obst o, Geom gm, const Tx *__restrict__ x,
+                                               const Tv *__restrict__ h,
+                                               const unsigned char *__restrict__ active,
+                                               double *__restrict__ part, CgCtl *ctl) {
+  if (ctl->ls_done) return;  // uniform over the grid
+  const double a = ctl->a;
+  const int N = gm.nx * gm.ny;
+  double dfh = 0.0, cw = 0.0;
+  for (int s = blockIdx.x * kT + threadIdx.x; s < N; s += gridDim.x * kT) {
+    if (!active[s]) continue;
+    const int ix = s / gm.ny, iy = s - ix * gm.ny;
+    for (int l = 0; l < o.nlayer; l++) {
+      double r[3], d[3];
+      atom_pos<Tx, Tv>(o, ix, iy, l, x, h, N, s, a, r, d);
+      const WallOut w1 = wall_eval(o, ix, iy, s, r, d);
+      atom_pos<Tx, Tv>(o, ix, iy, l, x, h, N, s, 0.0, r, d);
+      const WallOut w0 = wall_eval(o, ix, iy, s, r, d);
+      dfh += (w1.f[0] - w0.f[0]) * d[0] + (w1.f[1] - w0.f[1]) * d[1] + (w1.f[2] - w0.f[2]) * d[2];
+      cw += w1.curv;
+    }
+  }
+  const double acc[2] = {dfh, cw};
+  __shared__ double res[2];
+  if (!reduce_last<2, 0>(acc, part, &ctl->counter, res)) return;
+  if (threadIdx.x == 0) {
+    const double gdir = ctl->gh - a * ctl->hKh + res[0];
+    const double curv = ctl->hKh + res[1];
+    double lo = ctl->lo, hi = ctl->hi;
+    if (gdir > 0.0) lo = a;
+    else hi = a;
+    double an = (curv > 0.0) ? a + gdir / curv : -1.0;
+    if (hi >= 0.0 && (an <= lo || an >= hi || an < 0.0)) an = 0.5 * (lo + hi);
+    else if (an < 0.0) an = lo > 0.0 ? 2.0 * lo : 1e-3;
+    const double step = fabs(an - a);
+    ctl->lo = lo;
+    ctl->hi = hi;
+    ctl->a = an;
+    ctl->ls_it += 1;
+    // an exact line minimum is not needed: Polak-Ribiere with restarts
+    // converges from a step within 1e-6 of it
+    if (step <= 1e-6 * fabs(an) || ctl->ls_it >= kLsMax || !isfinite(an)) ctl->ls_done = 1;
+    if (!isfinite(an)) ctl->a = 0.0;
+  }
+}
+
+// ---- update after the line search ------------------------------------------
+template <typename Tx, typename Tv>
+__global__ void __launch_bounds__(kT) k_update(Obst o, Geom gm, Tx *__restrict__ x,
+                                                const Tv *__restrict__ h, const Tv *__restrict__ fKh,
+                                                Tx *__restrict__ fel, Tv *__restrict__ g,
+                                                unsigned char *__restrict__ active,
+                                                double *__restrict__ part, CgCtl *ctl,
+                                                cudaGraphConditionalHandle hc, int use_hc) {
+  const double ad = ctl->a;
+  const Tx a = (Tx)ad;
+  const int N = gm.nx * gm.ny;
+  const int nl = gm.ndof / 3;
+  Dot<Tv> gg, ggo, hg;
+  double ew = 0.0;
+  float fmx = 0.0f;
+  double fmx_d = 0.0;
+  for (int s = blockIdx.x * kT + threadIdx.x; s < N; s += gridDim.x * kT) {
+    const int ix = s / gm.ny, iy = s - ix * gm.ny;
+    bool nearflag = false;
+    for (int l = 0; l < nl; l++) {
+      Tx fe[3];
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const size_t idx = (size_t)(3 * l + c) * N + s;
+        const Tx hv = (Tx)h[idx];
+        x[idx] = x[idx] + a * hv;
+        fe[c] = fel[idx] + a * (Tx)fKh[idx];
+        fel[idx] = fe[c];
+      }
+      double fw[3] = {0.0, 0.0, 0.0};
+      if (l < o.nlayer && o.kind != GFMD_OBST_NONE) {
+        const float ge = gap_of(o, ix, iy, l, x, N, s);
+        if (ge < (float)(o.gcut + o.margin)) nearflag = true;
+        if (wall_near(o, ge)) {
+          double r[3], d[3];
+          atom_pos<Tx, Tv>(o, ix, iy, l, x, nullptr, N, s, 0.0, r, d);
+          const WallOut w = wall_eval(o, ix, iy, s, r, d);
+          fw[0] = w.f[0];
+          fw[1] = w.f[1];
+          fw[2] = w.f[2];
+          ew += w.e;
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const size_t idx = (size_t)(3 * l + c) * N + s;
+        Tv gv;
+        if (fw[c] != 0.0) gv = (Tv)((double)fe[c] + fw[c]);
+        else gv = (Tv)fe[c];
+        const Tv go = g[idx];
+        gg.add(gv, gv);
+        ggo.add(gv, go);
+        hg.add(h[idx], gv);
+        if constexpr (sizeof(Tv) == 4) fmx = fmaxf(fmx, fabsf(gv));
+        else fmx_d = fmax(fmx_d, fabs(gv));
+        g[idx] = gv;
+      }
+    }
+    active[s] = nearflag ? 1 : 0;
+  }
+  const double acc[5] = {gg.get(), ggo.get(), hg.get(), ew, sizeof(Tv) == 4 ? (double)fmx : fmx_d};
+  __shared__ double res[5];
+  if (!reduce_last<4, 1>(acc, part, &ctl->counter, res)) return;
+  if (threadIdx.x == 0) {
+    const double gg_new = res[0], g_gold = res[1], h_g = res[2];
+    const double gg_old = ctl->gg;
+    double beta = gg_old > 0.0 ? (gg_new - g_gold) / gg_old : 0.0;  // Polak-Ribiere
+    if (beta < 0.0) beta = 0.0;
+    // new direction h' = g + beta h must descend: h'.g = gg_new + beta h.g > 0
+    if (!(gg_new + beta * h_g > 0.0)) beta = 0.0;
+    ctl->beta = beta;
+    ctl->gg = gg_new;
+    ctl->ew = res[3];
+    ctl->fmax = res[4];
+    ctl->it += 1;
+    ctl->since += 1;
+    if (!isfinite(gg_new)) ctl->done = 3;
+    else if (res[4] <= ctl->ftol) ctl->done = 1;
+    else if (ctl->it >= ctl->maxit) ctl->done = 2;
+    const bool go_on = ctl->done == 0 && ctl->since < ctl->recompute;
+    set_loop(hc, use_hc, go_on ? 1u : 0u);
+  }
+}
+
+// h = g + beta h
+template <typename Tv>
+__global__ void __launch_bounds__(kT) k_dir(size_t n, Tv *__restrict__ h, const Tv *__restrict__ g,
+                                             const CgCtl *ctl) {
+  const Tv beta = (Tv)ctl->beta;
+  for (size_t i = blockIdx.x * (size_t)kT + threadIdx.x; i < n; i += (size_t)gridDim.x * kT)
+    h[i] = g[i] + beta * h[i];
+}
+
+__global__ void k_f2d(size_t n, const float *__restrict__ a, double *__restrict__ b) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    b[i] = (double)a[i];
+}
+__global__ void k_d2f(size_t n, const double *__restrict__ a, float *__restrict__ b) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+// ---- host side ---------------------------------------------------------------
+
+template <typename T> constexpr int io_type() { return sizeof(T) == 8 ? 0 : 1; }
+
+struct CgBufs {
+  cudaStream_t cs = nullptr;
+  int nblk = 0;
+  size_t n = 0;
+  void *fel = nullptr;      // n doubles (holds float or double)
+  void *g = nullptr, *h = nullptr, *fKh = nullptr;  // n doubles each (Tv)
+  float *u32 = nullptr;
+  unsigned char *active = nullptr;
+  double *part = nullptr;
+  double *d_e = nullptr;
+  CgCtl *ctl = nullptr;
+  CgCtl *hctl = nullptr;  // pinned
+  cudaEvent_t ev = nullptr;
+  ~CgBufs() {
+    for (void *p : {fel, g, h, fKh, (void *)u32, (void *)active, (void *)part, (void *)d_e, (void *)ctl})
+      if (p) cudaFree(p);
+    if (hctl) cudaFreeHost(hctl);
+    if (ev) cudaEventDestroy(ev);
+    if (cs) cudaStreamDestroy(cs);
+  }
+};
+
+cudaError_t bufs_init(CgBufs &b, gfmd_solver *h, bool mixed) {
+  const Geom &g = h->g;
+  b.n = (size_t)g.ndof * g.nx * g.ny;
+  const size_t nsite = (size_t)g.nx * g.ny;
+  b.nblk = (int)std::max<size_t>(1, std::min<size_t>((size_t)h->sm_count * 4, (nsite + kT - 1) / kT));
+  cudaError_t e = cudaStreamCreateWithFlags(&b.cs, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b.ev, cudaEventDisableTiming);
+  const size_t vb = sizeof(double) * b.n;
+  if (e == cudaSuccess) e = cudaMalloc(&b.fel, vb);
+  if (e == cudaSuccess) e = cudaMalloc(&b.g, vb);
+  if (e == cudaSuccess) e = cudaMalloc(&b.h, vb);
+  if (e == cudaSuccess) e = cudaMalloc(&b.fKh, vb);
+  if (e == cudaSuccess && mixed) e = cudaMalloc((void **)&b.u32, sizeof(float) * b.n);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b.active, nsite);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b.part, sizeof(double) * kQ * b.nblk);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b.d_e, sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b.ctl, sizeof(CgCtl));
+  if (e == cudaSuccess) e = cudaMallocHost((void **)&b.hctl, sizeof(CgCtl));
+  if (e == cudaSuccess) e = cudaMemsetAsync(b.active, 0, nsite, b.cs);
+  return e;
+}
+
+// Force evaluation on stream st with handle hh.
+cudaError_t eval_on(gfmd_solver *hh, cudaStream_t st, const void *in, int in_t, void *out, int out_t,
+                    double *d_e, bool with_linf) {
+  cudaStream_t keep = hh->stream;
+  hh->stream = st;
+  cudaError_t e = enqueue_force_opts(hh, in, in_t, out, out_t, d_e, with_linf);
+  hh->stream = keep;
+  return e;
+}
+
+// One phase as a graph: restart (fresh F_el(u), g, h = g) then
+// WHILE(condition) { CG iteration }.  hr evaluates the restart force in Tx,
+// hd the direction force in Tv.
+template <typename Tx, typename Tv>
+cudaError_t build_phase(CgBufs &b, gfmd_solver *hr, gfmd_solver *hd, const Obst &o, Tx *x,
+                        cudaGraph_t *graph_out, cudaGraphExec_t *exec_out) {
+  const Geom &gm = hr->g;
+  Tx *fel = reinterpret_cast<Tx *>(b.fel);
+  Tv *g = reinterpret_cast<Tv *>(b.g), *h = reinterpret_cast<Tv *>(b.h), *fKh = reinterpret_cast<Tv *>(b.fKh);
+  cudaGraph_t top = nullptr;
+  RT_CHECK(cudaGraphCreate(&top, 0));
+  *graph_out = top;
+  cudaGraphConditionalHandle hc;
+  RT_CHECK(cudaGraphConditionalHandleCreate(&hc, top, 0, cudaGraphCondAssignDefault));
+  RT_CHECK(cudaStreamBeginCaptureToGraph(b.cs, top, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  cudaError_t e = cudaMemsetAsync(&b.ctl->counter, 0, sizeof(unsigned int), b.cs);
+  if (e == cudaSuccess) e = eval_on(hr, b.cs, x, io_type<Tx>(), fel, io_type<Tx>(), b.d_e, true);
+  if (e == cudaSuccess) {
+    k_restart<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(o, gm, x, fel, g, h, b.active, b.part, b.ctl, hc, 1);
+    e = cudaGetLastError();
+  }
+  cudaGraphNodeParams cp = {};
+  cudaGraphNode_t cnode = nullptr;
+  if (e == cudaSuccess) {
+    cudaStreamCaptureStatus st;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t nd = 0;
+    e = cudaStreamGetCaptureInfo(b.cs, &st, nullptr, nullptr, &deps, nullptr, &nd);
+    if (e == cudaSuccess) {
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = hc;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      e = cudaGraphAddNode(&cnode, top, deps, nullptr, nd, &cp);
+    }
+    if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(b.cs, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies);
+  }
+  cudaGraph_t got = nullptr;
+  cudaError_t e2 = cudaStreamEndCapture(b.cs, &got);
+  if (e == cudaSuccess) e = e2;
+  if (e != cudaSuccess) return e;
+  // loop body
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  RT_CHECK(cudaStreamBeginCaptureToGraph(b.cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  e = eval_on(hd, b.cs, h, io_type<Tv>(), fKh, io_type<Tv>(), b.d_e, false);
+  if (e == cudaSuccess) {
+    k_dirforce<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(o, gm, x, fKh, h, g, b.active, b.part, b.ctl);
+    if (o.kind != GFMD_OBST_NONE)
+      for (int p = 0; p < kLsMax; p++)
+        k_probe<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(o, gm, x, h, b.active, b.part, b.ctl);
+    k_update<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(o, gm, x, h, fKh, fel, g, b.active, b.part, b.ctl, hc, 1);
+    k_dir<Tv><<<b.nblk * 4, kT, 0, b.cs>>>(b.n, h, g, b.ctl);
+    e = cudaGetLastError();
+  }
+  e2 = cudaStreamEndCapture(b.cs, &got);
+  if (e == cudaSuccess) e = e2;
+  if (e != cudaSuccess) return e;
+  return cudaGraphInstantiate(exec_out, top, 0);
+}
+
+struct GraphHolder {
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t x = nullptr;
+  ~GraphHolder() {
+    if (x) cudaGraphExecDestroy(x);
+    if (g) cudaGraphDestroy(g);
+  }
+};
+
+// Runs one phase until it converges, fails or reaches the iteration cap.
+// Returns the phase's done code (1, 2, 3) or -1 on a CUDA error.
+// The FP32 phase also ends when a whole restart chunk has not halved max|g|
+// (it has reached what FP32 state resolves).
+template <typename Tx, typename Tv>
+int run_phase(CgBufs &b, gfmd_solver *hr, gfmd_solver *hd, const Obst &o, Tx *x, int *evals,
+              cudaError_t *err) {
+  GraphHolder gh;
+  cudaError_t e = build_phase<Tx, Tv>(b, hr, hd, o, x, &gh.g, &gh.x);
+  if (e != cudaSuccess) { *err = e; return -1; }
+  for (;;) {
+    const int it0 = b.hctl->it;
+    e = cudaGraphLaunch(gh.x, b.cs);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b.hctl, b.ctl, sizeof(CgCtl), cudaMemcpyDeviceToHost, b.cs);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b.cs);
+    if (e != cudaSuccess) { *err = e; return -1; }
+    *evals += 1 + (b.hctl->it - it0);
+    if (b.hctl->done != 0) return b.hctl->done;
+    if (b.hctl->it == it0) {  // an armed loop always iterates
+      *err = cudaErrorUnknown;
+      return -1;
+    }
+    if (b.hctl->bulk && b.hctl->since >= b.hctl->recompute && !(b.hctl->fmax < 0.5 * b.hctl->fmax_restart))
+      return 1;
+  }
+}
+
+}  // namespace
+
+int cg_minimize(gfmd_solver *hp, const gfmd_obstacle_t *ob, const gfmd_min_params_t *prm, double *u,
+                gfmd_min_report_t *rep, std::string &err) {
+  const bool mixed = hp->precision == GFMD_PREC_F32;
+  gfmd_solver *hr64 = prm->refine ? prm->refine : nullptr;
+  CgBufs b;
+  cudaError_t ce = bufs_init(b, hp, mixed);
+  if (ce != cudaSuccess) {
+    err = cudaGetErrorString(ce);
+    return ce == cudaErrorMemoryAllocation ? GFMD_ENOMEM : GFMD_ECUDA;
+  }
+  // order the solve after the caller's stream
+  if ((ce = cudaEventRecord(b.ev, hp->stream)) == cudaSuccess) ce = cudaStreamWaitEvent(b.cs, b.ev, 0);
+  const Obst o = make_obst(ob, hp->g);
+  CgCtl c{};
+  c.ftol = prm->ftol;
+  c.ftol_req = prm->ftol;
+  c.bulk = mixed ? 1 : 0;
+  c.maxit = prm->maxiter > 0 ? prm->maxiter : 100000;
+  c.recompute = std::min(10000, prm->recompute > 0 ? prm->recompute : 50);
+  c.obst = o.kind != GFMD_OBST_NONE;
+  *b.hctl = c;
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(b.ctl, b.hctl, sizeof(CgCtl), cudaMemcpyHostToDevice, b.cs);
+  int evals = 0, done = -1;
+  const int eb = 4 * hp->sm_count;
+  if (ce == cudaSuccess) {
+    if (!mixed) {
+      done = run_phase<double, double>(b, hp, hp, o, u, &evals, &ce);
+    } else {
+      k_d2f<<<eb, 256, 0, b.cs>>>(b.n, u, b.u32);
+      done = run_phase<float, float>(b, hp, hp, o, b.u32, &evals, &ce);
+      if (done >= 0) {
+        k_f2d<<<eb, 256, 0, b.cs>>>(b.n, b.u32, u);
+        if (done == 1 && hr64) {
+          // FP64 refinement: FP64 restarts, FP32 direction forces
+          b.hctl->done = 0;
+          b.hctl->bulk = 0;
+          ce = cudaMemcpyAsync(b.ctl, b.hctl, sizeof(CgCtl), cudaMemcpyHostToDevice, b.cs);
+          if (ce == cudaSuccess) done = run_phase<double, float>(b, hr64, hp, o, u, &evals, &ce);
+        }
+      }
+    }
+  }
+  if (done < 0 || ce != cudaSuccess) {
+    err = cudaGetErrorString(ce);
+    cudaStreamSynchronize(b.cs);
+    return GFMD_ECUDA;
+  }
+  // report from a fresh evaluation with the most accurate handle
+  double E = 0.0, fm = 0.0, ff2 = 0.0;
+  ce = report_total_force(hr64 ? hr64 : hp, b.cs, o, u, &E, &fm, &ff2);
+  if (ce == cudaSuccess) ce = cudaEventRecord(b.ev, b.cs);
+  if (ce == cudaSuccess) ce = cudaStreamWaitEvent(hp->stream, b.ev, 0);
+  if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return GFMD_ECUDA; }
+  evals++;
+  if (rep) {
+    rep->iterations = b.hctl->it;
+    rep->force_evals = evals;
+    rep->energy = E;
+    rep->fmax = fm;
+    rep->fnorm = std::sqrt(ff2);
+  }
+  int status = done == 1 ? GFMD_OK : (done == 3 ? GFMD_ENONFINITE : GFMD_ENOTCONVERGED);
+  if (status == GFMD_OK && !(fm <= prm->ftol * 1.0000001)) status = GFMD_ENOTCONVERGED;
+  if (status == GFMD_ENOTCONVERGED) err = "CG did not reach max|f| <= ftol";
+  if (status == GFMD_ENONFINITE) err = "non-finite force during CG";
+  return status;
+}
+
+}  // namespace gfmd

@@ -100,6 +100,9 @@ cudaError_t enqueue_force(gfmd_solver *h, const void *d_u, int in_t, void *d_f, 
 // for the force of a search direction.
 cudaError_t enqueue_force_opts(gfmd_solver *h, const void *d_u, int in_t, void *d_f, int out_t,
                                double *d_epot, bool with_linf);
+// Polak-Ribiere CG with device-side control (gfmd_cg.cu).
+int cg_minimize(gfmd_solver *hp, const gfmd_obstacle_t *ob, const gfmd_min_params_t *prm, double *u,
+                gfmd_min_report_t *rep, std::string &err);
 // Records msg as the calling thread's gfmd_last_error() and returns code.
 int set_error(int code, const std::string &msg);
 // Kernel launches one force evaluation makes.

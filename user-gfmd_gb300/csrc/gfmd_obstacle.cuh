@@ -1,0 +1,153 @@
+// Rigid obstacles acting on the atoms of the grid, shared by the solver loops.
+//   sphere, exponential wall   e = eps exp(-g/sigma) on the gap g = |r-c| - R
+//                              (FixWallMap::eval_exp, src/extras/fix_wall_map.cpp:575-582,
+//                              applied to a sphere);
+//   sphere, Lennard-Jones 12-6 on the gap, shifted at the cutoff
+//                              (FixContactSphere::post_force, src/extras/fix_contact_sphere.cpp:207-264);
+//   rigid map, exponential wall on dz = r_z - z_map (normal force only;
+//                              FixWallMap::pre_force, src/extras/fix_wall_map.cpp:686-817).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "gfmd_internal.h"
+
+namespace gfmd {
+
+struct Obst {
+  int kind;
+  double cx, cy, cz, R, eps, sigma, cutoff, offset;
+  double c1, c2, c3, c4;  // LJ coefficients
+  const double *map;
+  double map_z0;
+  int norm;
+  double ax, ay, lx, ly;  // lattice spacing, box
+  int nlayer;
+  double off[8][3];
+  double gcut;     // effective cutoff on the gap (exp walls without one: 40 sigma)
+  double margin;   // extra distance kept in the active-site list
+};
+
+struct WallOut {
+  double e;        // energy
+  double f[3];     // force on the atom
+  double curv;     // h^T (d2E/dr2) h for the given direction
+};
+
+// Obstacle energy, force and curvature along dir at position r.
+__device__ __forceinline__ WallOut wall_eval(const Obst &o, int s_ix, int s_iy, size_t site,
+                                             const double r[3], const double dir[3]) {
+  WallOut w{0.0, {0.0, 0.0, 0.0}, 0.0};
+  if (o.kind == GFMD_OBST_SPHERE_EXP || o.kind == GFMD_OBST_SPHERE_LJ) {
+    double d[3] = {r[0] - o.cx, r[1] - o.cy, r[2] - o.cz};
+    // minimum image in x and y (periodic grid)
+    d[0] -= o.lx * rint(d[0] / o.lx);
+    d[1] -= o.ly * rint(d[1] / o.ly);
+    const double rho = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    const double g = rho - o.R;
+    if (g >= o.gcut) return w;
+    double e, F, E2;  // E(g), F = -dE/dg, d2E/dg2
+    if (o.kind == GFMD_OBST_SPHERE_EXP) {
+      const double ex = o.eps * exp(-g / o.sigma);
+      e = ex - o.offset;
+      F = ex / o.sigma;
+      E2 = F / o.sigma;
+    } else {
+      const double ginv = 1.0 / g, g2 = ginv * ginv, g6 = g2 * g2 * g2;
+      e = g6 * (o.c3 * g6 - o.c4) - o.offset;
+      F = g6 * (o.c1 * g6 - o.c2) * ginv;
+      E2 = g6 * g2 * (13.0 * o.c1 * g6 - 7.0 * o.c2);
+    }
+    const double ir = 1.0 / rho;
+    const double n[3] = {d[0] * ir, d[1] * ir, d[2] * ir};
+    w.e = e;
+    w.f[0] = F * n[0];
+    w.f[1] = F * n[1];
+    w.f[2] = F * n[2];
+    const double dn = dir[0] * n[0] + dir[1] * n[1] + dir[2] * n[2];
+    const double dd = dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2];
+    // Hessian of E(|r-c|): E'' n n^T + (E'/rho)(1 - n n^T), E' = -F
+    w.curv = E2 * dn * dn - F * ir * (dd - dn * dn);
+  } else if (o.kind == GFMD_OBST_MAP_EXP) {
+    const double zm = o.map[site] + o.map_z0;
+    const double dz = o.norm * (r[2] - zm);
+    if (dz >= o.gcut) return w;
+    const double ex = o.eps * exp(-dz / o.sigma);
+    w.e = ex - o.offset;
+    w.f[2] = o.norm * ex / o.sigma;
+    w.curv = ex / (o.sigma * o.sigma) * dir[2] * dir[2];
+  }
+  return w;
+}
+
+// Cheap FP32 estimate of the gap of an atom (no minimum image subtleties
+// beyond what the margin covers); used to skip the FP64 evaluation far away.
+__device__ __forceinline__ float gap_estimate(const Obst &o, size_t site, const double r[3]) {
+  if (o.kind == GFMD_OBST_MAP_EXP) {
+    return (float)o.norm * ((float)r[2] - (float)(o.map[site] + o.map_z0));
+  }
+  float dx = (float)(r[0] - o.cx), dy = (float)(r[1] - o.cy), dz = (float)(r[2] - o.cz);
+  const float lx = (float)o.lx, ly = (float)o.ly;
+  dx -= lx * rintf(dx / lx);
+  dy -= ly * rintf(dy / ly);
+  return sqrtf(dx * dx + dy * dy + dz * dz) - (float)o.R;
+}
+
+// FP32 gap estimate from an FP32 position (gating only).
+__device__ __forceinline__ float gap_estimate_f(const Obst &o, size_t site, const float r[3]) {
+  if (o.kind == GFMD_OBST_MAP_EXP) return (float)o.norm * (r[2] - (float)(o.map[site] + o.map_z0));
+  float dx = r[0] - (float)o.cx, dy = r[1] - (float)o.cy, dz = r[2] - (float)o.cz;
+  const float lx = (float)o.lx, ly = (float)o.ly;
+  dx -= lx * rintf(dx / lx);
+  dy -= ly * rintf(dy / ly);
+  return sqrtf(dx * dx + dy * dy + dz * dz) - (float)o.R;
+}
+
+inline Obst make_obst(const gfmd_obstacle_t *ob, const Geom &g) {
+  Obst o{};
+  o.kind = ob ? ob->kind : GFMD_OBST_NONE;
+  if (!ob) return o;
+  o.cx = ob->center[0];
+  o.cy = ob->center[1];
+  o.cz = ob->center[2];
+  o.R = ob->radius;
+  o.eps = ob->epsilon;
+  o.sigma = ob->sigma;
+  o.cutoff = ob->cutoff;
+  o.map = ob->d_map;
+  o.map_z0 = ob->map_z0;
+  o.norm = ob->norm == 0 ? 1 : ob->norm;
+  o.ax = ob->lattice[0] > 0 ? ob->lattice[0] : 1.0;
+  o.ay = ob->lattice[1] > 0 ? ob->lattice[1] : 1.0;
+  o.lx = o.ax * g.nx;
+  o.ly = o.ay * g.ny;
+  o.nlayer = std::min(g.ndof / 3, ob->nlayer > 0 ? ob->nlayer : g.ndof / 3);
+  for (int l = 0; l < 8; l++)
+    for (int c = 0; c < 3; c++) o.off[l][c] = ob->layer_offset[l][c];
+  if (o.kind == GFMD_OBST_SPHERE_LJ) {
+    o.c1 = 48.0 * o.eps * std::pow(o.sigma, 12.0);
+    o.c2 = 24.0 * o.eps * std::pow(o.sigma, 6.0);
+    o.c3 = 4.0 * o.eps * std::pow(o.sigma, 12.0);
+    o.c4 = 4.0 * o.eps * std::pow(o.sigma, 6.0);
+    if (o.cutoff > 0.0) {
+      const double r2 = 1.0 / (o.cutoff * o.cutoff), r6 = r2 * r2 * r2;
+      o.offset = r6 * (o.c3 * r6 - o.c4);
+    }
+  } else if (o.cutoff > 0.0) {
+    o.offset = o.eps * std::exp(-o.cutoff / o.sigma);
+  }
+  // exponential walls without a cutoff: beyond 40 sigma the force is below
+  // 4e-18 eps/sigma, far under any force tolerance
+  o.gcut = o.cutoff > 0.0 ? o.cutoff : (o.kind == GFMD_OBST_SPHERE_LJ ? 1e30 : 40.0 * o.sigma);
+  o.margin = 10.0 * o.sigma + 1.0;
+  return o;
+}
+
+// Total force F_el(u) + F_w(u) of FP64 displacements with handle hh on
+// stream st: energy, max |f_i| and |f|^2 (synchronizes st).
+cudaError_t report_total_force(gfmd_solver *hh, cudaStream_t st, const Obst &o, const double *u,
+                               double *E, double *fmax, double *f2);
+
+}  // namespace gfmd

@@ -1,28 +1,13 @@
 // Solver loops around the force evaluation, resident on the GPU:
-//   static  - Polak-Ribiere conjugate gradients with a Newton line search
-//             (the minimizer LAMMPS runs on fix gfmd through `minimize`,
-//             tests/TEST_Hertz_*/lammps.in: min_style cg), or FIRE
-//             (FixFIRE, src/cuda/fix_fire.cpp:117-297);
+//   static  - FIRE (FixFIRE, src/cuda/fix_fire.cpp:117-297); conjugate
+//             gradients live in gfmd_cg.cu;
 //   dynamic - damped velocity Verlet (fix nve plus linear damping).
-// Obstacles, acting on every atom of the grid:
-//   sphere, exponential wall   e = eps exp(-g/sigma) on the gap g = |r-c| - R
-//                              (FixWallMap::eval_exp, src/extras/fix_wall_map.cpp:575-582,
-//                              applied to a sphere);
-//   sphere, Lennard-Jones 12-6 on the gap, shifted at the cutoff
-//                              (FixContactSphere::post_force, src/extras/fix_contact_sphere.cpp:207-264);
-//   rigid map, exponential wall on dz = r_z - z_map (normal force only;
-//                              FixWallMap::pre_force, src/extras/fix_wall_map.cpp:686-817).
+// Obstacles (gfmd_obstacle.cuh) act on every atom of the grid.
 //
-// All state vectors are FP64 [ndof][nx*ny]; the elastic forces come from the
+// State vectors here are FP64 [ndof][nx*ny]; the elastic forces come from the
 // handle's force evaluation (FP64 or FP32 arithmetic).  Scalars (dot
 // products, maxima, energies) are reduced in FP64 in a fixed order: per-block
 // partials, then one block, so runs are bit-reproducible.
-//
-// CG uses that the elastic force is linear in u: with Kh = -F_el(h) from one
-// force evaluation per iteration, F_el(u + a h) = F_el(u) - a Kh exactly, so
-// the line search only re-evaluates the (local, cheap) obstacle term.
-// F_el(u) is recomputed from scratch every `recompute` iterations and at the
-// end to keep the incremental update from drifting.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -32,6 +17,7 @@
 #include <vector>
 
 #include "gfmd_internal.h"
+#include "gfmd_obstacle.cuh"
 
 namespace gfmd {
 
@@ -39,85 +25,6 @@ namespace {
 
 constexpr int kRedThreads = 256;
 constexpr int kMaxRed = 8;  // scalars per reduction
-
-struct Obst {
-  int kind;
-  double cx, cy, cz, R, eps, sigma, cutoff, offset;
-  double c1, c2, c3, c4;  // LJ coefficients
-  const double *map;
-  double map_z0;
-  int norm;
-  double ax, ay, lx, ly;  // lattice spacing, box
-  int nlayer;
-  double off[8][3];
-  double gcut;     // effective cutoff on the gap (exp walls without one: 40 sigma)
-  double margin;   // extra distance kept in the active-site list
-};
-
-struct WallOut {
-  double e;        // energy
-  double f[3];     // force on the atom
-  double curv;     // h^T (d2E/dr2) h for the given direction
-};
-
-// Obstacle energy, force and curvature along dir at position r.
-__device__ __forceinline__ WallOut wall_eval(const Obst &o, int s_ix, int s_iy, size_t site,
-                                             const double r[3], const double dir[3]) {
-  WallOut w{0.0, {0.0, 0.0, 0.0}, 0.0};
-  if (o.kind == GFMD_OBST_SPHERE_EXP || o.kind == GFMD_OBST_SPHERE_LJ) {
-    double d[3] = {r[0] - o.cx, r[1] - o.cy, r[2] - o.cz};
-    // minimum image in x and y (periodic grid)
-    d[0] -= o.lx * rint(d[0] / o.lx);
-    d[1] -= o.ly * rint(d[1] / o.ly);
-    const double rho = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-    const double g = rho - o.R;
-    if (g >= o.gcut) return w;
-    double e, F, E2;  // E(g), F = -dE/dg, d2E/dg2
-    if (o.kind == GFMD_OBST_SPHERE_EXP) {
-      const double ex = o.eps * exp(-g / o.sigma);
-      e = ex - o.offset;
-      F = ex / o.sigma;
-      E2 = F / o.sigma;
-    } else {
-      const double ginv = 1.0 / g, g2 = ginv * ginv, g6 = g2 * g2 * g2;
-      e = g6 * (o.c3 * g6 - o.c4) - o.offset;
-      F = g6 * (o.c1 * g6 - o.c2) * ginv;
-      E2 = g6 * g2 * (13.0 * o.c1 * g6 - 7.0 * o.c2);
-    }
-    const double ir = 1.0 / rho;
-    const double n[3] = {d[0] * ir, d[1] * ir, d[2] * ir};
-    w.e = e;
-    w.f[0] = F * n[0];
-    w.f[1] = F * n[1];
-    w.f[2] = F * n[2];
-    const double dn = dir[0] * n[0] + dir[1] * n[1] + dir[2] * n[2];
-    const double dd = dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2];
-    // Hessian of E(|r-c|): E'' n n^T + (E'/rho)(1 - n n^T), E' = -F
-    w.curv = E2 * dn * dn - F * ir * (dd - dn * dn);
-  } else if (o.kind == GFMD_OBST_MAP_EXP) {
-    const double zm = o.map[site] + o.map_z0;
-    const double dz = o.norm * (r[2] - zm);
-    if (dz >= o.gcut) return w;
-    const double ex = o.eps * exp(-dz / o.sigma);
-    w.e = ex - o.offset;
-    w.f[2] = o.norm * ex / o.sigma;
-    w.curv = ex / (o.sigma * o.sigma) * dir[2] * dir[2];
-  }
-  return w;
-}
-
-// Cheap FP32 estimate of the gap of an atom (no minimum image subtleties
-// beyond what the margin covers); used to skip the FP64 evaluation far away.
-__device__ __forceinline__ float gap_estimate(const Obst &o, size_t site, const double r[3]) {
-  if (o.kind == GFMD_OBST_MAP_EXP) {
-    return (float)o.norm * ((float)r[2] - (float)(o.map[site] + o.map_z0));
-  }
-  float dx = (float)(r[0] - o.cx), dy = (float)(r[1] - o.cy), dz = (float)(r[2] - o.cz);
-  const float lx = (float)o.lx, ly = (float)o.ly;
-  dx -= lx * rintf(dx / lx);
-  dy -= ly * rintf(dy / ly);
-  return sqrtf(dx * dx + dy * dy + dz * dz) - (float)o.R;
-}
 
 // Per-thread accumulators -> block partials part[blockIdx.x * kMaxRed + k]
 // (sums for k < nsum, maximum at k = nsum).
@@ -143,18 +50,34 @@ __device__ __forceinline__ void block_reduce(double *acc, int nsum, bool with_ma
   }
 }
 
-// Fixed-order combination of nblk partials into out[0..nq).
-__global__ void k_finish(const double *__restrict__ part, int nblk, int nsum, int with_max,
-                         double *__restrict__ out) {
-  const int k = threadIdx.x;
+// Fixed-order combination of nblk partials into out[0..nq): thread t takes
+// partials t, t+256, ... in order, then a fixed shuffle tree.
+__global__ void __launch_bounds__(kRedThreads) k_finish(const double *__restrict__ part, int nblk, int nsum,
+                                                        int with_max, double *__restrict__ out) {
+  __shared__ double sh[kRedThreads / 32][kMaxRed];
   const int nq = nsum + with_max;
-  if (k >= nq) return;
-  double v = part[k];
-  for (int b = 1; b < nblk; b++) {
-    const double t = part[b * kMaxRed + k];
-    v = (with_max && k == nsum) ? fmax(v, t) : v + t;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int k = 0; k < nq; k++) {
+    const bool mx = with_max && k == nsum;
+    double v = 0.0;
+    for (int b = threadIdx.x; b < nblk; b += kRedThreads) {
+      const double t = part[b * kMaxRed + k];
+      v = mx ? fmax(v, t) : v + t;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const double t = __shfl_down_sync(0xffffffffu, v, o);
+      v = mx ? fmax(v, t) : v + t;
+    }
+    if (lane == 0) sh[warp][k] = v;
   }
-  out[k] = v;
+  __syncthreads();
+  if (threadIdx.x < nq) {
+    const int k = threadIdx.x;
+    const bool mx = with_max && k == nsum;
+    double v = sh[0][k];
+    for (int w = 1; w < kRedThreads / 32; w++) v = mx ? fmax(v, sh[w][k]) : v + sh[w][k];
+    out[k] = v;
+  }
 }
 
 __device__ __forceinline__ void site_pos(const Obst &o, const Geom &g, size_t s, int l,
@@ -169,28 +92,6 @@ __device__ __forceinline__ void site_pos(const Obst &o, const Geom &g, size_t s,
   }
   r[0] += ix * o.ax;
   r[1] += iy * o.ay;
-}
-
-// Line-search probe at u + a h over the sites flagged near the obstacle (in
-// grid order, so the sums are reproducible): sums of (F_w . h), (h^T H_w h), E_w.
-__global__ void __launch_bounds__(kRedThreads) k_wall_line(Obst o, Geom g, const double *__restrict__ x,
-                                                           const double *__restrict__ h, double a,
-                                                           double *__restrict__ part,
-                                                           const unsigned char *__restrict__ active) {
-  const size_t N = (size_t)g.nx * g.ny;
-  double acc[3] = {0.0, 0.0, 0.0};
-  for (size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x; s < N; s += (size_t)gridDim.x * blockDim.x) {
-    if (!active[s]) continue;
-    for (int l = 0; l < o.nlayer; l++) {
-      double r[3], dir[3];
-      site_pos(o, g, s, l, x, N, a, h, r, dir);
-      WallOut w = wall_eval(o, (int)(s / g.ny), (int)(s % g.ny), s, r, dir);
-      acc[0] += w.f[0] * dir[0] + w.f[1] * dir[1] + w.f[2] * dir[2];
-      acc[1] += w.curv;
-      acc[2] += w.e;
-    }
-  }
-  block_reduce(acc, 3, false, part);
 }
 
 // f_total = f_el + F_w(u); optionally stores it; sums: E_w, |f|^2, and the
@@ -233,69 +134,6 @@ __global__ void __launch_bounds__(kRedThreads) k_total_force(Obst o, Geom g, con
   block_reduce(acc, 2, true, part);
 }
 
-// CG update after the line search (step a along h):
-//   u += a h; f_el -= a Kh; g = f_el + F_w(u);
-//   sums: g.g, g.gprev, E_w; max |g|; then gprev <- g.
-__global__ void __launch_bounds__(kRedThreads) k_cg_update(Obst o, Geom g, double *__restrict__ x,
-                                                           const double *__restrict__ h,
-                                                           const double *__restrict__ Kh,
-                                                           double *__restrict__ fel,
-                                                           double *__restrict__ gprev, double a,
-                                                           double *__restrict__ part,
-                                                           unsigned char *__restrict__ active) {
-  const size_t N = (size_t)g.nx * g.ny;
-  const int nl = g.ndof / 3;
-  double acc[4] = {0.0, 0.0, 0.0, 0.0};
-  for (size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x; s < N; s += (size_t)gridDim.x * blockDim.x) {
-    bool near = false;
-    for (int l = 0; l < nl; l++) {
-      for (int c = 0; c < 3; c++) {
-        const size_t idx = (size_t)(3 * l + c) * N + s;
-        x[idx] += a * h[idx];
-        fel[idx] -= a * Kh[idx];
-      }
-      double fw[3] = {0.0, 0.0, 0.0};
-      if (l < o.nlayer && o.kind != GFMD_OBST_NONE) {
-        double r[3], dir[3];
-        site_pos(o, g, s, l, x, N, 0.0, nullptr, r, dir);
-        const float ge = gap_estimate(o, s, r);
-        if (ge < (float)(o.gcut + o.margin)) near = true;
-        WallOut w{0.0, {0.0, 0.0, 0.0}, 0.0};
-        if (ge < (float)o.gcut + 0.01f * (float)o.gcut + 1e-3f)
-          w = wall_eval(o, (int)(s / g.ny), (int)(s % g.ny), s, r, dir);
-        fw[0] = w.f[0];
-        fw[1] = w.f[1];
-        fw[2] = w.f[2];
-        acc[2] += w.e;
-      }
-      for (int c = 0; c < 3; c++) {
-        const size_t idx = (size_t)(3 * l + c) * N + s;
-        const double gv = fel[idx] + fw[c];
-        acc[0] += gv * gv;
-        acc[1] += gv * gprev[idx];
-        acc[3] = fmax(acc[3], fabs(gv));
-        gprev[idx] = gv;
-      }
-    }
-    if (active) active[s] = near ? 1 : 0;
-  }
-  block_reduce(acc, 3, true, part);
-}
-
-// h = g + beta h (beta < 0: h = g); sums: h.g
-__global__ void __launch_bounds__(kRedThreads) k_cg_dir(Geom g, double *__restrict__ h,
-                                                        const double *__restrict__ gv, double beta,
-                                                        double *__restrict__ part) {
-  const size_t n = (size_t)g.nx * g.ny * g.ndof;
-  double acc[1] = {0.0};
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const double hv = beta < 0.0 ? gv[i] : gv[i] + beta * h[i];
-    h[i] = hv;
-    acc[0] += hv * gv[i];
-  }
-  block_reduce(acc, 1, false, part);
-}
-
 // sums: a.b
 __global__ void __launch_bounds__(kRedThreads) k_dot(size_t n, const double *__restrict__ a,
                                                      const double *__restrict__ b,
@@ -304,21 +142,6 @@ __global__ void __launch_bounds__(kRedThreads) k_dot(size_t n, const double *__r
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     acc[0] += a[i] * b[i];
   block_reduce(acc, 1, false, part);
-}
-
-// Kh = -fKh in place; sums: h.Kh, fel.h
-__global__ void __launch_bounds__(kRedThreads) k_cg_dirforce(size_t n, double *__restrict__ Kh,
-                                                             const double *__restrict__ h,
-                                                             const double *__restrict__ fel,
-                                                             double *__restrict__ part) {
-  double acc[2] = {0.0, 0.0};
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const double k = -Kh[i], hv = h[i];
-    Kh[i] = k;
-    acc[0] += hv * k;
-    acc[1] += fel[i] * hv;
-  }
-  block_reduce(acc, 2, false, part);
 }
 
 // FIRE, first half (FixFIRE::initial_integrate): v += dtf f, |v| per atom
@@ -431,9 +254,9 @@ struct Work {
   }
 };
 
-cudaError_t work_init(Work &w, gfmd_solver *h, int nbuf) {
+cudaError_t work_init(Work &w, gfmd_solver *h, int nbuf, cudaStream_t st = nullptr, bool use_st = false) {
   w.h = h;
-  w.st = h->stream;
+  w.st = use_st ? st : h->stream;
   w.n = (size_t)h->g.ndof * h->g.nx * h->g.ny;
   w.nblk = std::max(1, std::min(h->sm_count * 4, (int)((w.n / 3 + kRedThreads - 1) / kRedThreads)));
   cudaError_t e = cudaMalloc((void **)&w.part, sizeof(double) * w.nblk * kMaxRed);
@@ -447,7 +270,7 @@ cudaError_t work_init(Work &w, gfmd_solver *h, int nbuf) {
 
 // Reduce the partials and copy nq scalars to w.hres (synchronizes).
 cudaError_t fetch(Work &w, int nsum, bool with_max) {
-  k_finish<<<1, 32, 0, w.st>>>(w.part, w.nblk, nsum, with_max ? 1 : 0, w.res);
+  k_finish<<<1, kRedThreads, 0, w.st>>>(w.part, w.nblk, nsum, with_max ? 1 : 0, w.res);
   cudaError_t e = cudaMemcpyAsync(w.hres, w.res, sizeof(double) * (nsum + (with_max ? 1 : 0)),
                                   cudaMemcpyDeviceToHost, w.st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(w.st);
@@ -469,46 +292,6 @@ cudaError_t elastic(Work &w, gfmd_solver *hh, const double *u, double *f, bool w
   return e;
 }
 
-Obst make_obst(const gfmd_obstacle_t *ob, const Geom &g) {
-  Obst o{};
-  o.kind = ob ? ob->kind : GFMD_OBST_NONE;
-  if (!ob) return o;
-  o.cx = ob->center[0];
-  o.cy = ob->center[1];
-  o.cz = ob->center[2];
-  o.R = ob->radius;
-  o.eps = ob->epsilon;
-  o.sigma = ob->sigma;
-  o.cutoff = ob->cutoff;
-  o.map = ob->d_map;
-  o.map_z0 = ob->map_z0;
-  o.norm = ob->norm == 0 ? 1 : ob->norm;
-  o.ax = ob->lattice[0] > 0 ? ob->lattice[0] : 1.0;
-  o.ay = ob->lattice[1] > 0 ? ob->lattice[1] : 1.0;
-  o.lx = o.ax * g.nx;
-  o.ly = o.ay * g.ny;
-  o.nlayer = std::min(g.ndof / 3, ob->nlayer > 0 ? ob->nlayer : g.ndof / 3);
-  for (int l = 0; l < 8; l++)
-    for (int c = 0; c < 3; c++) o.off[l][c] = ob->layer_offset[l][c];
-  if (o.kind == GFMD_OBST_SPHERE_LJ) {
-    o.c1 = 48.0 * o.eps * std::pow(o.sigma, 12.0);
-    o.c2 = 24.0 * o.eps * std::pow(o.sigma, 6.0);
-    o.c3 = 4.0 * o.eps * std::pow(o.sigma, 12.0);
-    o.c4 = 4.0 * o.eps * std::pow(o.sigma, 6.0);
-    if (o.cutoff > 0.0) {
-      const double r2 = 1.0 / (o.cutoff * o.cutoff), r6 = r2 * r2 * r2;
-      o.offset = r6 * (o.c3 * r6 - o.c4);
-    }
-  } else if (o.cutoff > 0.0) {
-    o.offset = o.eps * std::exp(-o.cutoff / o.sigma);
-  }
-  // exponential walls without a cutoff: beyond 40 sigma the force is below
-  // 4e-18 eps/sigma, far under any force tolerance
-  o.gcut = o.cutoff > 0.0 ? o.cutoff : (o.kind == GFMD_OBST_SPHERE_LJ ? 1e30 : 40.0 * o.sigma);
-  o.margin = 10.0 * o.sigma + 1.0;
-  return o;
-}
-
 #define RT(call)                              \
   do {                                        \
     cudaError_t e_ = (call);                  \
@@ -526,127 +309,6 @@ cudaError_t total_force(Work &w, gfmd_solver *hh, const Obst &o, const double *u
   if (f2) *f2 = w.hres[1];
   if (fmax) *fmax = w.hres[2];
   return cudaSuccess;
-}
-
-// ---- static: conjugate gradients ------------------------------------------
-int cg_solve(gfmd_solver *hp, const gfmd_obstacle_t *ob, const gfmd_min_params_t *prm,
-             double *u, gfmd_min_report_t *rep, std::string &err) {
-  Work w;
-  // bufs: fel, h, Kh, gprev
-  cudaError_t ce = work_init(w, hp, 4);
-  if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return ce == cudaErrorMemoryAllocation ? GFMD_ENOMEM : GFMD_ECUDA; }
-  double *fel = w.bufs[0], *h = w.bufs[1], *Kh = w.bufs[2], *gp = w.bufs[3];
-  const Obst o = make_obst(ob, hp->g);
-  const int maxit = prm->maxiter > 0 ? prm->maxiter : 100000;
-  const int recompute = prm->recompute > 0 ? prm->recompute : 50;
-  gfmd_solver *hh = hp;  // current force handle
-  bool refining = false;
-  int it = 0, evals = 0;
-  double fmax = 0.0, f2 = 0.0, E = 0.0;
-  auto restart = [&](void) -> cudaError_t {
-    // fel = F_el(u); gprev = g = fel + F_w; h = g
-    RT(elastic(w, hh, u, fel, true, nullptr));
-    evals++;
-    k_total_force<<<w.nblk, kRedThreads, 0, w.st>>>(o, hh->g, u, fel, gp, w.part, w.active);
-    RT(fetch(w, 2, true));
-    f2 = w.hres[1];
-    fmax = w.hres[2];
-    RT(cudaMemcpyAsync(h, gp, sizeof(double) * w.n, cudaMemcpyDeviceToDevice, w.st));
-    return cudaSuccess;
-  };
-  ce = restart();
-  int status = GFMD_ENOTCONVERGED;
-  int since = 0;
-  while (ce == cudaSuccess) {
-    if (!std::isfinite(fmax) || !std::isfinite(f2)) { status = GFMD_ENONFINITE; break; }
-    if (fmax <= prm->ftol) {
-      if (prm->refine && !refining) {
-        // switch to the refinement handle and re-check from exact forces
-        refining = true;
-        hh = prm->refine;
-        ce = restart();
-        since = 0;
-        if (ce != cudaSuccess) break;
-        if (fmax <= prm->ftol) { status = GFMD_OK; break; }
-        continue;
-      }
-      status = GFMD_OK;
-      break;
-    }
-    if (it >= maxit) break;
-    // Kh = -F_el(h) (no linear term)
-    ce = elastic(w, hh, h, Kh, false, nullptr);
-    if (ce != cudaSuccess) break;
-    evals++;
-    k_cg_dirforce<<<w.nblk, kRedThreads, 0, w.st>>>(w.n, Kh, h, fel, w.part);
-    if ((ce = fetch(w, 2, false)) != cudaSuccess) break;
-    const double hKh = w.hres[0];
-    const double felh = w.hres[1];
-    // Newton line search on phi'(a) = -(fel.h - a hKh + F_w(u + a h).h)
-    double a = 0.0, lo = 0.0, hi = -1.0;
-    for (int ls = 0; ls < 16; ls++) {
-      double fwh = 0.0, cw = 0.0;
-      if (o.kind != GFMD_OBST_NONE) {
-        k_wall_line<<<w.nblk, kRedThreads, 0, w.st>>>(o, hh->g, u, h, a, w.part, w.active);
-        if ((ce = fetch(w, 3, false)) != cudaSuccess) break;
-        fwh = w.hres[0];
-        cw = w.hres[1];
-      }
-      const double gdir = felh - a * hKh + fwh;  // = -phi'(a)
-      const double curv = hKh + cw;              // = phi''(a)
-      if (gdir > 0.0) lo = a; else hi = a;
-      double an = (curv > 0.0) ? a + gdir / curv : -1.0;
-      if (hi >= 0.0 && (an <= lo || an >= hi || an < 0.0)) an = 0.5 * (lo + hi);
-      else if (an < 0.0) an = lo > 0.0 ? 2.0 * lo : 1e-3;
-      const double step = std::fabs(an - a);
-      a = an;
-      // an exact line minimum is not needed: Polak-Ribiere with restarts
-      // converges from a step within 1e-6 of it
-      if (step <= 1e-6 * std::fabs(a)) break;
-      if (o.kind == GFMD_OBST_NONE) break;  // quadratic: one Newton step is exact
-    }
-    if (ce != cudaSuccess) break;
-    // update
-    k_cg_update<<<w.nblk, kRedThreads, 0, w.st>>>(o, hh->g, u, h, Kh, fel, gp, a, w.part, w.active);
-    // gp held g_old; kernel computed g.g and g.g_old before overwriting
-    const double gg_old = f2;
-    if ((ce = fetch(w, 3, true)) != cudaSuccess) break;
-    f2 = w.hres[0];
-    const double g_gold = w.hres[1];
-    fmax = w.hres[3];
-    it++;
-    since++;
-    if (since >= recompute) {
-      ce = restart();
-      since = 0;
-      continue;
-    }
-    double beta = gg_old > 0.0 ? (f2 - g_gold) / gg_old : 0.0;  // Polak-Ribiere
-    if (beta < 0.0) beta = 0.0;
-    k_cg_dir<<<w.nblk, kRedThreads, 0, w.st>>>(hh->g, h, gp, beta, w.part);
-    if ((ce = fetch(w, 1, false)) != cudaSuccess) break;
-    if (w.hres[0] <= 0.0) {
-      k_cg_dir<<<w.nblk, kRedThreads, 0, w.st>>>(hh->g, h, gp, -1.0, w.part);
-      if ((ce = fetch(w, 1, false)) != cudaSuccess) break;
-    }
-  }
-  if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return GFMD_ECUDA; }
-  // final energy and forces from scratch
-  double fm = 0.0, ff2 = 0.0;
-  ce = total_force(w, hh, o, u, fel, nullptr, &E, &fm, &ff2);
-  if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return GFMD_ECUDA; }
-  evals++;
-  if (rep) {
-    rep->iterations = it;
-    rep->force_evals = evals;
-    rep->energy = E;
-    rep->fmax = fm;
-    rep->fnorm = std::sqrt(ff2);
-  }
-  if (status == GFMD_OK && !(fm <= prm->ftol * 1.0000001 + 0.0)) status = GFMD_ENOTCONVERGED;
-  if (status == GFMD_ENOTCONVERGED) err = "CG reached the iteration cap before max|f| <= ftol";
-  if (status == GFMD_ENONFINITE) err = "non-finite force during CG";
-  return status;
 }
 
 // ---- static: FIRE -----------------------------------------------------------
@@ -729,6 +391,13 @@ int fire_solve(gfmd_solver *hp, const gfmd_obstacle_t *ob, const gfmd_min_params
 
 }  // namespace
 
+cudaError_t report_total_force(gfmd_solver *hh, cudaStream_t st, const Obst &o, const double *u,
+                               double *E, double *fmax, double *f2) {
+  Work w;
+  RT(work_init(w, hh, 1, st, true));
+  return total_force(w, hh, o, u, w.bufs[0], nullptr, E, fmax, f2);
+}
+
 }  // namespace gfmd
 
 extern "C" {
@@ -749,7 +418,7 @@ int gfmd_minimize(gfmd_handle_t h, const gfmd_obstacle_t *obst, const gfmd_min_p
   std::string err;
   auto t0 = std::chrono::steady_clock::now();
   int rc;
-  if (prm->method == GFMD_MIN_CG) rc = gfmd::cg_solve(h, obst, prm, d_u, rep, err);
+  if (prm->method == GFMD_MIN_CG) rc = gfmd::cg_minimize(h, obst, prm, d_u, rep, err);
   else if (prm->method == GFMD_MIN_FIRE) rc = gfmd::fire_solve(h, obst, prm, d_u, rep, err);
   else return gfmd::set_error(GFMD_EINVAL, "gfmd_minimize: unknown method");
   if (rep) {
