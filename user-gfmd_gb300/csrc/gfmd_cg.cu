@@ -14,7 +14,7 @@
 //                                  first Newton step
 //   k_probe x kLsMax               Newton steps on the line derivative,
 //                                  each a no-op once the step has converged
-//   k_update                       u += a h, f_el += a fKh, g = f_el + F_w(u),
+//   k_update                       u += a h, g += a fKh + F_w(u_new) - F_w(u_old),
 //                                  Polak-Ribiere beta with the descent check,
 //                                  convergence test, loop condition
 //   k_dir                          h = g + beta h
@@ -24,8 +24,8 @@
 // starts from a fresh evaluation of F_el(u) (the drift of the incremental
 // update is reset) and steepest descent.
 //
-// Precision: the state is held in two types, Tx for u and f_el (the
-// quantities that accumulate) and Tv for g, h and fKh.  Plain FP64 runs
+// Precision: the state is held in two types, Tx for u (the quantity that
+// accumulates) and Tv for g, h and fKh.  Plain FP64 runs
 // <double, double>; the mixed solve runs an FP32 phase <float, float> with
 // FP32 force evaluations and then an FP64 refinement <double, float> whose
 // restarts use the FP64 force evaluation while the direction forces stay
@@ -64,6 +64,7 @@ constexpr int kLsMax = 8;   // Newton probes per line search
 struct CgCtl {
   double a, lo, hi;         // line search: step and bracket
   double gh, hKh;           // g.h and h.K.h at the start of the line search
+  double fw0h;              // F_w(u).h over the line-search set
   double gg;                // g.g of the current gradient
   double fmax;              // max |g_i|
   double ew;                // obstacle energy at the last update
@@ -177,15 +178,13 @@ template <typename Tx>
 __device__ __forceinline__ float gap_of(const Obst &o, int ix, int iy, int l, const Tx *x, size_t N, size_t s) {
   float r[3];
 #pragma unroll
-  for (int c = 0; c < 3; c++) r[c] = (float)x[(size_t)(3 * l + c) * N + s] + (float)o.off[l][c];
-  r[0] += (float)ix * (float)o.ax;
-  r[1] += (float)iy * (float)o.ay;
+  for (int c = 0; c < 3; c++) r[c] = (float)x[(size_t)(3 * l + c) * N + s] + o.foff[l][c];
+  r[0] += (float)ix * o.fax;
+  r[1] += (float)iy * o.fay;
   return gap_estimate_f(o, s, r);
 }
 
-__device__ __forceinline__ bool wall_near(const Obst &o, float ge) {
-  return ge < (float)o.gcut + 0.01f * (float)o.gcut + 1e-3f;
-}
+__device__ __forceinline__ bool wall_near(const Obst &o, float ge) { return ge < o.fgate_wall; }
 
 __device__ __forceinline__ void set_loop(cudaGraphConditionalHandle hc, int use, unsigned int v) {
   if (use) cudaGraphSetConditional(hc, v);
@@ -193,7 +192,7 @@ __device__ __forceinline__ void set_loop(cudaGraphConditionalHandle hc, int use,
 
 // ---- restart: g = f_el + F_w(u), h = g; arms the loop ---------------------
 template <typename Tx, typename Tv>
-__global__ void __launch_bounds__(kT) k_restart(Obst o, Geom gm, const Tx *__restrict__ x,
+__global__ void __launch_bounds__(kT, 4) k_restart(Obst o, Geom gm, const Tx *__restrict__ x,
                                                  const Tx *__restrict__ fel, Tv *__restrict__ g,
                                                  Tv *__restrict__ h, unsigned char *__restrict__ active,
                                                  double *__restrict__ part, CgCtl *ctl,
@@ -210,10 +209,11 @@ __global__ void __launch_bounds__(kT) k_restart(Obst o, Geom gm, const Tx *__res
     for (int l = 0; l < nl; l++) {
 #pragma unroll
       for (int c = 0; c < 3; c++) femx = fmaxf(femx, fabsf((float)fel[(size_t)(3 * l + c) * N + s]));
-      double fw[3] = {0.0, 0.0, 0.0};
+      double fw[3];
+      bool hit = false;
       if (l < o.nlayer && o.kind != GFMD_OBST_NONE) {
         const float ge = gap_of(o, ix, iy, l, x, N, s);
-        if (ge < (float)(o.gcut + o.margin)) nearflag = true;
+        if (ge < o.fgate_active) nearflag = true;
         if (wall_near(o, ge)) {
           double r[3], d[3];
           atom_pos<Tx, Tv>(o, ix, iy, l, x, nullptr, N, s, 0.0, r, d);
@@ -222,13 +222,14 @@ __global__ void __launch_bounds__(kT) k_restart(Obst o, Geom gm, const Tx *__res
           fw[1] = w.f[1];
           fw[2] = w.f[2];
           ew += w.e;
+          hit = true;
         }
       }
 #pragma unroll
       for (int c = 0; c < 3; c++) {
         const size_t idx = (size_t)(3 * l + c) * N + s;
         Tv gv;
-        if (fw[c] != 0.0) gv = (Tv)((double)fel[idx] + fw[c]);
+        if (hit) gv = (Tv)((double)fel[idx] + fw[c]);
         else gv = (Tv)fel[idx];
         g[idx] = gv;
         h[idx] = gv;
@@ -270,7 +271,8 @@ __global__ void __launch_bounds__(kT) k_dirforce(Obst o, Geom gm, const Tx *__re
   const int N = gm.nx * gm.ny;
   const int nl = gm.ndof / 3;
   Dot<Tv> hkh, gh;
-  double cw = 0.0;
+  double cw = 0.0, fw0h = 0.0;
+#pragma unroll 2
   for (int s = blockIdx.x * kT + threadIdx.x; s < N; s += gridDim.x * kT) {
     for (int l = 0; l < nl; l++) {
 #pragma unroll
@@ -286,17 +288,20 @@ __global__ void __launch_bounds__(kT) k_dirforce(Obst o, Geom gm, const Tx *__re
       for (int l = 0; l < o.nlayer; l++) {
         double r[3], d[3];
         atom_pos<Tx, Tv>(o, ix, iy, l, x, h, N, s, 0.0, r, d);
-        cw += wall_eval(o, ix, iy, s, r, d).curv;
+        const WallOut w = wall_eval(o, ix, iy, s, r, d);
+        cw += w.curv;
+        fw0h += w.f[0] * d[0] + w.f[1] * d[1] + w.f[2] * d[2];
       }
     }
   }
-  const double acc[3] = {-hkh.get(), gh.get(), cw};
-  __shared__ double res[3];
-  if (!reduce_last<3, 0>(acc, part, &ctl->counter, res)) return;
+  const double acc[4] = {-hkh.get(), gh.get(), cw, fw0h};
+  __shared__ double res[4];
+  if (!reduce_last<4, 0>(acc, part, &ctl->counter, res)) return;
   if (threadIdx.x == 0) {
     const double hKh = res[0], ghv = res[1], curv = res[0] + res[2];
     ctl->hKh = hKh;
     ctl->gh = ghv;
+    ctl->fw0h = res[3];
     ctl->lo = 0.0;
     ctl->hi = -1.0;
     ctl->ls_it = 0;
@@ -310,7 +315,7 @@ __global__ void __launch_bounds__(kT) k_dirforce(Obst o, Geom gm, const Tx *__re
 }
 
 // ---- one Newton probe of the line search at u + a h ------------------------
-// gdir(a) = g.h - a hKh + sum (F_w(u + a h) - F_w(u)).h   (= -phi'(a))
+// gdir(a) = g.h - a hKh + sum F_w(u + a h).h - F_w(u).h   (= -phi'(a))
 // curv(a) = hKh + sum h^T H_w(u + a h) h                   (=  phi''(a))
 template <typename Tx, typename Tv>
 __global__ void __launch_bounds__(kT) k_probe(Obst o, Geom gm, const Tx *__restrict__ x,
@@ -328,9 +333,7 @@ __global__ void __launch_bounds__(kT) k_probe(Obst o, Geom gm, const Tx *__restr
       double r[3], d[3];
       atom_pos<Tx, Tv>(o, ix, iy, l, x, h, N, s, a, r, d);
       const WallOut w1 = wall_eval(o, ix, iy, s, r, d);
-      atom_pos<Tx, Tv>(o, ix, iy, l, x, h, N, s, 0.0, r, d);
-      const WallOut w0 = wall_eval(o, ix, iy, s, r, d);
-      dfh += (w1.f[0] - w0.f[0]) * d[0] + (w1.f[1] - w0.f[1]) * d[1] + (w1.f[2] - w0.f[2]) * d[2];
+      dfh += w1.f[0] * d[0] + w1.f[1] * d[1] + w1.f[2] * d[2];
       cw += w1.curv;
     }
   }
@@ -338,7 +341,7 @@ __global__ void __launch_bounds__(kT) k_probe(Obst o, Geom gm, const Tx *__restr
   __shared__ double res[2];
   if (!reduce_last<2, 0>(acc, part, &ctl->counter, res)) return;
   if (threadIdx.x == 0) {
-    const double gdir = ctl->gh - a * ctl->hKh + res[0];
+    const double gdir = ctl->gh - a * ctl->hKh + (res[0] - ctl->fw0h);
     const double curv = ctl->hKh + res[1];
     double lo = ctl->lo, hi = ctl->hi;
     if (gdir > 0.0) lo = a;
@@ -359,17 +362,62 @@ __global__ void __launch_bounds__(kT) k_probe(Obst o, Geom gm, const Tx *__restr
 }
 
 // ---- update after the line search ------------------------------------------
+// u += a h; g += a fKh + F_w(u_new) - F_w(u_old).  The elastic part of g is
+// updated through the linearity of F_el, so f_el itself is not stored, and
+// the rounding of the FP32 state is relative to the (small) gradient rather
+// than to the elastic force.
 template <typename Tx, typename Tv>
-__global__ void __launch_bounds__(kT) k_update(Obst o, Geom gm, Tx *__restrict__ x,
-                                                const Tv *__restrict__ h, const Tv *__restrict__ fKh,
-                                                Tx *__restrict__ fel, Tv *__restrict__ g,
-                                                unsigned char *__restrict__ active,
-                                                double *__restrict__ part, CgCtl *ctl,
-                                                cudaGraphConditionalHandle hc, int use_hc) {
+__device__ __forceinline__ void wall_at(const Obst &o, int ix, int iy, int l, size_t s, const Tx xv[3],
+                                        WallOut &w) {
+  const double zero[3] = {0.0, 0.0, 0.0};
+  double r[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) r[c] = (double)xv[c] + o.off[l][c];
+  r[0] += ix * o.ax;
+  r[1] += iy * o.ay;
+  w = wall_eval(o, ix, iy, s, r, zero);
+}
+
+// Near the obstacle: g_new = g_old + a fKh + F_w(x_new) - F_w(x_old) in FP64,
+// with E_w(x_new).  Kept out of line (arguments by value, so the caller's
+// arrays stay in registers) so the far-field loop stays small.
+template <typename T> struct V3 { T v[3]; };
+template <typename Tv> struct WallDelta { double e; Tv g[3]; };
+
+template <typename Tx, typename Tv>
+__device__ __forceinline__ WallDelta<Tv> wall_delta(const Obst &o, int ix, int iy, int l, int s, V3<Tx> xv,
+                                                 V3<Tx> xn, V3<Tv> go, V3<Tv> fk, double a) {
+  WallOut w1, w0;
+  wall_at<Tx, Tv>(o, ix, iy, l, s, xn.v, w1);
+  wall_at<Tx, Tv>(o, ix, iy, l, s, xv.v, w0);
+  WallDelta<Tv> r;
+  r.e = w1.e;
+  for (int c = 0; c < 3; c++) r.g[c] = (Tv)((double)go.v[c] + a * (double)fk.v[c] + (w1.f[c] - w0.f[c]));
+  return r;
+}
+
+template <typename Tx>
+__device__ __forceinline__ float gap_reg(const Obst &o, int ix, int iy, int l, size_t s, const Tx xv[3]) {
+  float r[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) r[c] = (float)xv[c] + o.foff[l][c];
+  r[0] += (float)ix * o.fax;
+  r[1] += (float)iy * o.fay;
+  return gap_estimate_f(o, s, r);
+}
+
+template <typename Tx, typename Tv>
+__global__ void __launch_bounds__(kT, 4) k_update(Obst o, Geom gm, Tx *__restrict__ x,
+                                                   const Tv *__restrict__ h, const Tv *__restrict__ fKh,
+                                                   Tv *__restrict__ g, unsigned char *__restrict__ active,
+                                                   double *__restrict__ part, CgCtl *ctl,
+                                                   cudaGraphConditionalHandle hc, int use_hc) {
   const double ad = ctl->a;
   const Tx a = (Tx)ad;
+  const Tv av = (Tv)ad;
   const int N = gm.nx * gm.ny;
   const int nl = gm.ndof / 3;
+  const bool obst = o.kind != GFMD_OBST_NONE;
   Dot<Tv> gg, ggo, hg;
   double ew = 0.0;
   float fmx = 0.0f;
@@ -378,42 +426,48 @@ __global__ void __launch_bounds__(kT) k_update(Obst o, Geom gm, Tx *__restrict__
     const int ix = s / gm.ny, iy = s - ix * gm.ny;
     bool nearflag = false;
     for (int l = 0; l < nl; l++) {
-      Tx fe[3];
+      Tx xv[3];
+      Tv hv[3], fk[3], go[3];
 #pragma unroll
       for (int c = 0; c < 3; c++) {
         const size_t idx = (size_t)(3 * l + c) * N + s;
-        const Tx hv = (Tx)h[idx];
-        x[idx] = x[idx] + a * hv;
-        fe[c] = fel[idx] + a * (Tx)fKh[idx];
-        fel[idx] = fe[c];
+        xv[c] = x[idx];
+        hv[c] = h[idx];
+        fk[c] = fKh[idx];
+        go[c] = g[idx];
       }
-      double fw[3] = {0.0, 0.0, 0.0};
-      if (l < o.nlayer && o.kind != GFMD_OBST_NONE) {
-        const float ge = gap_of(o, ix, iy, l, x, N, s);
-        if (ge < (float)(o.gcut + o.margin)) nearflag = true;
-        if (wall_near(o, ge)) {
-          double r[3], d[3];
-          atom_pos<Tx, Tv>(o, ix, iy, l, x, nullptr, N, s, 0.0, r, d);
-          const WallOut w = wall_eval(o, ix, iy, s, r, d);
-          fw[0] = w.f[0];
-          fw[1] = w.f[1];
-          fw[2] = w.f[2];
-          ew += w.e;
+      Tx xn[3];
+      Tv gn[3];
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        xn[c] = xv[c] + a * (Tx)hv[c];
+        gn[c] = go[c] + av * fk[c];
+      }
+      if (obst && l < o.nlayer) {
+        const float ge_new = gap_reg(o, ix, iy, l, s, xn);
+        const float ge_old = gap_reg(o, ix, iy, l, s, xv);
+        if (ge_new < o.fgate_active) nearflag = true;
+        if (ge_new < o.fgate_wall || ge_old < o.fgate_wall) {
+          const WallDelta<Tv> wd = wall_delta<Tx, Tv>(o, ix, iy, l, s, V3<Tx>{{xv[0], xv[1], xv[2]}},
+                                                      V3<Tx>{{xn[0], xn[1], xn[2]}},
+                                                      V3<Tv>{{go[0], go[1], go[2]}},
+                                                      V3<Tv>{{fk[0], fk[1], fk[2]}}, ad);
+          ew += wd.e;
+          gn[0] = wd.g[0];
+          gn[1] = wd.g[1];
+          gn[2] = wd.g[2];
         }
       }
 #pragma unroll
       for (int c = 0; c < 3; c++) {
         const size_t idx = (size_t)(3 * l + c) * N + s;
-        Tv gv;
-        if (fw[c] != 0.0) gv = (Tv)((double)fe[c] + fw[c]);
-        else gv = (Tv)fe[c];
-        const Tv go = g[idx];
-        gg.add(gv, gv);
-        ggo.add(gv, go);
-        hg.add(h[idx], gv);
-        if constexpr (sizeof(Tv) == 4) fmx = fmaxf(fmx, fabsf(gv));
-        else fmx_d = fmax(fmx_d, fabs(gv));
-        g[idx] = gv;
+        gg.add(gn[c], gn[c]);
+        ggo.add(gn[c], go[c]);
+        hg.add(hv[c], gn[c]);
+        if constexpr (sizeof(Tv) == 4) fmx = fmaxf(fmx, fabsf(gn[c]));
+        else fmx_d = fmax(fmx_d, fabs(gn[c]));
+        x[idx] = xn[c];
+        g[idx] = gn[c];
       }
     }
     active[s] = nearflag ? 1 : 0;
@@ -471,6 +525,7 @@ struct CgBufs {
   void *fel = nullptr;      // n doubles (holds float or double)
   void *g = nullptr, *h = nullptr, *fKh = nullptr;  // n doubles each (Tv)
   float *u32 = nullptr;
+  float *mapf = nullptr;    // FP32 copy of a map obstacle (gating)
   unsigned char *active = nullptr;
   double *part = nullptr;
   double *d_e = nullptr;
@@ -478,7 +533,8 @@ struct CgBufs {
   CgCtl *hctl = nullptr;  // pinned
   cudaEvent_t ev = nullptr;
   ~CgBufs() {
-    for (void *p : {fel, g, h, fKh, (void *)u32, (void *)active, (void *)part, (void *)d_e, (void *)ctl})
+    for (void *p : {fel, g, h, fKh, (void *)u32, (void *)mapf, (void *)active, (void *)part, (void *)d_e,
+                    (void *)ctl})
       if (p) cudaFree(p);
     if (hctl) cudaFreeHost(hctl);
     if (ev) cudaEventDestroy(ev);
@@ -568,7 +624,7 @@ cudaError_t build_phase(CgBufs &b, gfmd_solver *hr, gfmd_solver *hd, const Obst 
     if (o.kind != GFMD_OBST_NONE)
       for (int p = 0; p < kLsMax; p++)
         k_probe<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(o, gm, x, h, b.active, b.part, b.ctl);
-    k_update<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(o, gm, x, h, fKh, fel, g, b.active, b.part, b.ctl, hc, 1);
+    k_update<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(o, gm, x, h, fKh, g, b.active, b.part, b.ctl, hc, 1);
     k_dir<Tv><<<b.nblk * 4, kT, 0, b.cs>>>(b.n, h, g, b.ctl);
     e = cudaGetLastError();
   }
@@ -628,7 +684,15 @@ int cg_minimize(gfmd_solver *hp, const gfmd_obstacle_t *ob, const gfmd_min_param
   }
   // order the solve after the caller's stream
   if ((ce = cudaEventRecord(b.ev, hp->stream)) == cudaSuccess) ce = cudaStreamWaitEvent(b.cs, b.ev, 0);
-  const Obst o = make_obst(ob, hp->g);
+  Obst o = make_obst(ob, hp->g);
+  if (ce == cudaSuccess && o.kind == GFMD_OBST_MAP_EXP) {
+    const size_t nsite = (size_t)hp->g.nx * hp->g.ny;
+    ce = cudaMalloc((void **)&b.mapf, sizeof(float) * nsite);
+    if (ce == cudaSuccess) {
+      k_d2f<<<4 * hp->sm_count, 256, 0, b.cs>>>(nsite, o.map, b.mapf);
+      o.mapf = b.mapf;
+    }
+  }
   CgCtl c{};
   c.ftol = prm->ftol;
   c.ftol_req = prm->ftol;

@@ -28,6 +28,13 @@ struct Obst {
   double off[8][3];
   double gcut;     // effective cutoff on the gap (exp walls without one: 40 sigma)
   double margin;   // extra distance kept in the active-site list
+  // FP32 copies for the per-site gating, so sites far from the obstacle cost
+  // no FP64 instruction
+  float fcx, fcy, fcz, fR, flx, fly, fax, fay, fz0, fnorm;
+  float fgate_wall;    // evaluate the wall below this gap estimate
+  float fgate_active;  // keep the site in the line-search set below this
+  float foff[8][3];
+  const float *mapf;   // FP32 copy of the map (may be NULL: then map is read)
 };
 
 struct WallOut {
@@ -97,12 +104,14 @@ __device__ __forceinline__ float gap_estimate(const Obst &o, size_t site, const 
 
 // FP32 gap estimate from an FP32 position (gating only).
 __device__ __forceinline__ float gap_estimate_f(const Obst &o, size_t site, const float r[3]) {
-  if (o.kind == GFMD_OBST_MAP_EXP) return (float)o.norm * (r[2] - (float)(o.map[site] + o.map_z0));
-  float dx = r[0] - (float)o.cx, dy = r[1] - (float)o.cy, dz = r[2] - (float)o.cz;
-  const float lx = (float)o.lx, ly = (float)o.ly;
-  dx -= lx * rintf(dx / lx);
-  dy -= ly * rintf(dy / ly);
-  return sqrtf(dx * dx + dy * dy + dz * dz) - (float)o.R;
+  if (o.kind == GFMD_OBST_MAP_EXP) {
+    const float zm = o.mapf ? o.mapf[site] : (float)o.map[site];
+    return o.fnorm * (r[2] - (zm + o.fz0));
+  }
+  float dx = r[0] - o.fcx, dy = r[1] - o.fcy, dz = r[2] - o.fcz;
+  dx -= o.flx * rintf(dx / o.flx);
+  dy -= o.fly * rintf(dy / o.fly);
+  return sqrtf(dx * dx + dy * dy + dz * dz) - o.fR;
 }
 
 inline Obst make_obst(const gfmd_obstacle_t *ob, const Geom &g) {
@@ -142,6 +151,21 @@ inline Obst make_obst(const gfmd_obstacle_t *ob, const Geom &g) {
   // 4e-18 eps/sigma, far under any force tolerance
   o.gcut = o.cutoff > 0.0 ? o.cutoff : (o.kind == GFMD_OBST_SPHERE_LJ ? 1e30 : 40.0 * o.sigma);
   o.margin = 10.0 * o.sigma + 1.0;
+  o.fcx = (float)o.cx;
+  o.fcy = (float)o.cy;
+  o.fcz = (float)o.cz;
+  o.fR = (float)o.R;
+  o.flx = (float)o.lx;
+  o.fly = (float)o.ly;
+  o.fax = (float)o.ax;
+  o.fay = (float)o.ay;
+  o.fz0 = (float)o.map_z0;
+  o.fnorm = (float)o.norm;
+  o.fgate_wall = (float)o.gcut + 0.01f * (float)o.gcut + 1e-3f;
+  o.fgate_active = (float)(o.gcut + o.margin);
+  for (int l = 0; l < 8; l++)
+    for (int c = 0; c < 3; c++) o.foff[l][c] = (float)o.off[l][c];
+  o.mapf = nullptr;
   return o;
 }
 
