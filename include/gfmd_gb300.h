@@ -140,6 +140,9 @@ typedef struct {
   double lattice[2];    /* grid spacing along x and y (<= 0: 1) */
   int nlayer;           /* layers (from l = 0) that feel the obstacle (<= 0: all) */
   double layer_offset[8][3];
+  double fz_ext;        /* constant external force along +z on every atom the
+                           obstacle acts on (load control: pressure x area per
+                           atom); energy -fz_ext * sum u_z */
 } gfmd_obstacle_t;
 
 #define GFMD_MIN_CG 0   /* Polak-Ribiere CG, Newton line search (LAMMPS min_style cg
@@ -175,6 +178,25 @@ typedef struct {
  * (src/main/fix_gfmd.cpp:1078-1088) and FixFIRE. */
 int gfmd_minimize(gfmd_handle_t h, const gfmd_obstacle_t *obst, const gfmd_min_params_t *params,
                   double *d_u, gfmd_min_report_t *report);
+
+/* Batched static minimization: n independent surfaces (any grid sizes and
+ * kernels), solved concurrently by CG in one CUDA graph per phase: every
+ * surface is a branch of the graph running its restart and a device-driven
+ * WHILE loop of CG iterations.  Mixed precision when the items' handles are
+ * FP32 and carry an FP64 `refine` handle (all items alike).  params->method
+ * must be GFMD_MIN_CG; params->refine is ignored (per item).  Returns
+ * GFMD_OK when every item converged, else the first failing item's status;
+ * each item's report is filled either way.  No counterpart in the reference
+ * (one surface per LAMMPS run). */
+typedef struct {
+  gfmd_handle_t handle;           /* force evaluation (FP64, or FP32 for mixed) */
+  gfmd_handle_t refine;           /* FP64 handle of the same grid, or NULL */
+  const gfmd_obstacle_t *obstacle;/* may be NULL */
+  double *d_u;                    /* displacements [ndof][nx*ny], device FP64, in/out */
+  gfmd_min_report_t report;       /* out */
+} gfmd_batch_item_t;
+
+int gfmd_minimize_batch(int n, gfmd_batch_item_t *items, const gfmd_min_params_t *params);
 
 /* Damped velocity Verlet (unit masses): v_h = v + dt/2 (f - gamma v),
  * u += dt v_h, v = (v_h + dt/2 f) / (1 + dt gamma/2); gamma = 0 is fix nve.
@@ -230,6 +252,31 @@ int gfmd_kernel_info(gfmd_kernel_t k, int *ndof, int *height);
  * (src/main/gfmd_misc.cpp:32-101, src/main/surface_stiffness.cpp:430-435). */
 int gfmd_kernel_phi(gfmd_kernel_t k, int nx, int ny, int layout, double *phi,
                     double *linf, int nthreads);
+
+/* ---- Self-affine rough surfaces ------------------------------------------
+ * No counterpart in the reference, which only reads height maps
+ * (FixWallMap, src/extras/fix_wall_map.cpp:1123-1190) and low-pass filters
+ * them (:1220-1310).  Random-phase synthesis: on the half spectrum
+ * (kx, ky >= 0) of the nx x ny grid with spacing a,
+ *   C(q) = (q / q_L)^(-2-2H)  for q_L <= q <= q_s, else 0,
+ *   q_L = 2 pi / lambda_long, q_s = 2 pi / lambda_short,
+ *   Z(q) = sqrt(C(q)) exp(2 pi i u(q)), u uniform in [0,1) from a counter-
+ *   based hash of (seed, q) (SplitMix64 finaliser), Hermitian on the ky = 0
+ *   and ky = ny/2 columns,
+ *   h(r) = s * sum_q Z(q) exp(i q.r),  s such that the spectral rms slope
+ *   sqrt(sum_q |q|^2 |Z(q)|^2) equals rms_slope.
+ * Writes h[nx*ny] (x slow, y fast) on the device; synchronous. */
+typedef struct {
+  double lattice;          /* grid spacing a (> 0) */
+  double hurst;            /* Hurst exponent H */
+  double rms_slope;        /* spectral rms slope of the result (> 0) */
+  double lambda_short;     /* short-wavelength cut-off (> 0) */
+  double lambda_long;      /* long-wavelength cut-off (>= lambda_short) */
+  unsigned long long seed;
+} gfmd_surface_params_t;
+
+int gfmd_rough_surface(int nx, int ny, const gfmd_surface_params_t *params, double *d_h,
+                       void *cuda_stream);
 
 #ifdef __cplusplus
 }

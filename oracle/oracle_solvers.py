@@ -28,13 +28,15 @@ SPHERE_EXP, SPHERE_LJ, MAP_EXP = 1, 2, 3
 
 class ObstacleSpec:
     def __init__(self, kind, center=(0, 0, 0), radius=0.0, epsilon=1.0, sigma=1.0, cutoff=0.0,
-                 lattice=(1.0, 1.0), layer_offsets=(), nlayer=0, zmap=None, map_z0=0.0, norm=1):
+                 lattice=(1.0, 1.0), layer_offsets=(), nlayer=0, zmap=None, map_z0=0.0, norm=1,
+                 fz_ext=0.0):
         self.kind, self.c, self.R = kind, np.asarray(center, float), radius
         self.eps, self.sigma, self.cutoff = epsilon, sigma, cutoff
         self.ax, self.ay = lattice
         self.offsets = list(layer_offsets)
         self.nlayer = nlayer
         self.zmap, self.map_z0, self.norm = zmap, map_z0, norm
+        self.fz_ext = fz_ext  # constant +z force per obstacle atom (load control)
         if kind == SPHERE_LJ:
             self.c1 = 48.0 * epsilon * sigma ** 12
             self.c2 = 24.0 * epsilon * sigma ** 6
@@ -92,7 +94,7 @@ def wall(ob: ObstacleSpec | None, u, nx, ny, direction=None, a=0.0):
             E += np.where(m, e, 0.0).sum()
             fdir += np.where(m, (fl * d).sum(0), 0.0).sum()
             curv += np.where(m, cv, 0.0).sum()
-        elif ob.kind == MAP_EXP:
+        if ob.kind == MAP_EXP:
             dz = ob.norm * (r[2] - (ob.zmap + ob.map_z0))
             m = np.ones_like(dz, bool) if ob.cutoff <= 0 else dz < ob.cutoff
             ex = ob.eps * np.exp(-dz / ob.sigma)
@@ -101,6 +103,10 @@ def wall(ob: ObstacleSpec | None, u, nx, ny, direction=None, a=0.0):
             E += np.where(m, ex - ob.offset, 0.0).sum()
             fdir += np.where(m, fz * d[2], 0.0).sum()
             curv += np.where(m, ex / ob.sigma ** 2 * d[2] ** 2, 0.0).sum()
+        if ob.fz_ext != 0.0:
+            f[3 * l + 2] += ob.fz_ext
+            E -= ob.fz_ext * (u[3 * l + 2] + a * d[2]).sum()
+            fdir += ob.fz_ext * d[2].sum()
     return E, f, fdir, curv
 
 

@@ -41,6 +41,7 @@ def gpu_obstacle(spec):
     o.nlayer = spec.nlayer
     o.norm = spec.norm
     o.map_z0 = spec.map_z0
+    o.fz_ext = spec.fz_ext
     for l, off in enumerate(spec.offsets):
         o.layer_offset[l][:] = list(off)
     return o

@@ -4,13 +4,14 @@ The package is a thin host layer over the C ABI of ``libgfmd_gb300.so``
 (include/gfmd_gb300.h).  Import it with
 ``importlib.import_module("user-gfmd_gb300")``.
 """
-from ._lib import GFMDError, MinParams, MinReport, Obstacle, lib  # noqa: F401
+from ._lib import GFMDError, MinParams, MinReport, Obstacle, SurfaceParams, check, lib  # noqa: F401
 from ._lib import (GFMD_OBST_MAP_EXP, GFMD_OBST_NONE, GFMD_OBST_SPHERE_EXP,  # noqa: F401
                    GFMD_OBST_SPHERE_LJ)
 from .solver import (  # noqa: F401
     GFMDSolverGB300,
     StiffnessKernel,
     gfmd_solver_factory,
+    minimize_batch,
     stiffness_kernel_factory,
 )
 
@@ -18,9 +19,12 @@ __all__ = [
     "GFMDError",
     "Obstacle",
     "sphere_obstacle",
+    "rough_surface",
+    "map_obstacle",
     "GFMDSolverGB300",
     "StiffnessKernel",
     "gfmd_solver_factory",
+    "minimize_batch",
     "stiffness_kernel_factory",
     "lib",
 ]
@@ -38,4 +42,27 @@ def sphere_obstacle(center, radius, epsilon, sigma, cutoff=0.0, kind="exp", latt
     o.nlayer = nlayer
     for l, off in enumerate(layer_offsets or []):
         o.layer_offset[l][:] = list(off)
+    return o
+
+
+def rough_surface(out, nx, ny, hurst, rms_slope, lambda_short, lambda_long, seed, lattice=1.0,
+                  stream=0):
+    """Self-affine random-phase height map into the CUDA float64 tensor
+    ``out`` (nx*ny elements, x slow); see gfmd_rough_surface."""
+    p = SurfaceParams(lattice, hurst, rms_slope, lambda_short, lambda_long, seed)
+    check(lib().gfmd_rough_surface(nx, ny, p, out.data_ptr(), stream))
+    return out
+
+
+def map_obstacle(d_map, epsilon, sigma, z0=0.0, norm=-1, cutoff=0.0, nlayer=1) -> Obstacle:
+    """Rigid height map z_map (CUDA float64 tensor, nx*ny) with an
+    exponential wall on dz = norm (r_z - z_map - z0); norm = -1 for an
+    indenter above the surface."""
+    o = Obstacle()
+    o.kind = GFMD_OBST_MAP_EXP
+    o.d_map = d_map.data_ptr()
+    o.map_z0, o.norm = z0, norm
+    o.epsilon, o.sigma, o.cutoff = epsilon, sigma, cutoff
+    o.nlayer = nlayer
+    o.lattice[:] = [1.0, 1.0]
     return o

@@ -49,6 +49,7 @@ class Obstacle(ctypes.Structure):
         ("lattice", ctypes.c_double * 2),
         ("nlayer", ctypes.c_int),
         ("layer_offset", (ctypes.c_double * 3) * 8),
+        ("fz_ext", ctypes.c_double),
     ]
 
 
@@ -89,6 +90,18 @@ class MinReport(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class BatchItem(ctypes.Structure):
+    """gfmd_batch_item_t"""
+
+    _fields_ = [
+        ("handle", ctypes.c_void_p),
+        ("refine", ctypes.c_void_p),
+        ("obstacle", ctypes.POINTER(Obstacle)),
+        ("d_u", ctypes.c_void_p),
+        ("report", MinReport),
+    ]
+
+
 _NAMES = {
     GFMD_EINVAL: "EINVAL",
     GFMD_ENOMEM: "ENOMEM",
@@ -98,6 +111,13 @@ _NAMES = {
     GFMD_ENOTCONVERGED: "ENOTCONVERGED",
     GFMD_ENOPHI: "ENOPHI",
 }
+
+
+class SurfaceParams(ctypes.Structure):
+    """gfmd_surface_params_t."""
+    _fields_ = [("lattice", ctypes.c_double), ("hurst", ctypes.c_double),
+                ("rms_slope", ctypes.c_double), ("lambda_short", ctypes.c_double),
+                ("lambda_long", ctypes.c_double), ("seed", ctypes.c_ulonglong)]
 
 
 class GFMDError(RuntimeError):
@@ -129,9 +149,11 @@ SIGNATURES = {
     "gfmd_solver_info": [_vp, _pi, _pi],
     "gfmd_minimize": [_vp, ctypes.POINTER(Obstacle), ctypes.POINTER(MinParams), _vp,
                       ctypes.POINTER(MinReport)],
+    "gfmd_minimize_batch": [_c_int, ctypes.POINTER(BatchItem), ctypes.POINTER(MinParams)],
     "gfmd_run_dynamics": [_vp, ctypes.POINTER(Obstacle), _c_dbl, _c_dbl, _c_int, _vp, _vp, _vp,
                           ctypes.POINTER(MinReport)],
     "gfmd_post_force_noalloc": [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp],
+    "gfmd_rough_surface": [_c_int, _c_int, ctypes.POINTER(SurfaceParams), _vp, _vp],
     "gfmd_kernel_create": [ctypes.c_char_p, ctypes.POINTER(_vp)],
     "gfmd_kernel_destroy": [_vp],
     "gfmd_kernel_info": [_vp, _pi, _pi],

@@ -43,6 +43,7 @@
 #include <chrono>
 #include <cmath>
 #include <string>
+#include <vector>
 
 #include "gfmd_internal.h"
 #include "gfmd_obstacle.cuh"
@@ -73,6 +74,7 @@ struct CgCtl {
   double ftol_req;          // requested tolerance
   double fmax_restart;      // max |g_i| at the last restart
   int bulk;                 // FP32 phase: tolerance floored at the FP32 noise level
+  int frozen;               // phase ended by the host (FP32 stagnation)
   int it, since, maxit, recompute;
   int ls_it, ls_done;
   int done;                 // 0 running, 1 converged, 2 iteration cap, 3 non-finite
@@ -202,6 +204,7 @@ __global__ void __launch_bounds__(kT, 4) k_restart(Obst o, Geom gm, const Tx *__
   Dot<Tv> gg;
   double ew = 0.0;
   float fmx = 0.0f, femx = 0.0f;
+  const bool has_ext = o.fz_ext != 0.0;
   double fmx_d = 0.0;
   for (int s = blockIdx.x * kT + threadIdx.x; s < N; s += gridDim.x * kT) {
     const int ix = s / gm.ny, iy = s - ix * gm.ny;
@@ -229,7 +232,8 @@ __global__ void __launch_bounds__(kT, 4) k_restart(Obst o, Geom gm, const Tx *__
       for (int c = 0; c < 3; c++) {
         const size_t idx = (size_t)(3 * l + c) * N + s;
         Tv gv;
-        if (hit) gv = (Tv)((double)fel[idx] + fw[c]);
+        const bool ext = has_ext && c == 2 && l < o.nlayer;
+        if (hit || ext) gv = (Tv)((double)fel[idx] + (hit ? fw[c] : 0.0) + (ext ? o.fz_ext : 0.0));
         else gv = (Tv)fel[idx];
         g[idx] = gv;
         h[idx] = gv;
@@ -253,7 +257,8 @@ __global__ void __launch_bounds__(kT, 4) k_restart(Obst o, Geom gm, const Tx *__
     // FP32 state resolves g = f_el + F_w to about eps32 |f_el|: the FP32
     // phase stops at 64 eps32 max|f_el| if that is above the request
     ctl->ftol = ctl->bulk ? fmax(ctl->ftol_req, 64.0 * 5.960464477539063e-8 * res[3]) : ctl->ftol_req;
-    if (!isfinite(res[0])) ctl->done = 3;
+    if (ctl->frozen) ctl->done = 1;
+    else if (!isfinite(res[0])) ctl->done = 3;
     else if (res[2] <= ctl->ftol) ctl->done = 1;
     else if (ctl->it >= ctl->maxit) ctl->done = 2;
     else ctl->done = 0;
@@ -574,63 +579,108 @@ cudaError_t eval_on(gfmd_solver *hh, cudaStream_t st, const void *in, int in_t, 
   return e;
 }
 
-// One phase as a graph: restart (fresh F_el(u), g, h = g) then
-// WHILE(condition) { CG iteration }.  hr evaluates the restart force in Tx,
-// hd the direction force in Tv.
+// One CG problem of a batch.
+struct Item {
+  CgBufs b;
+  gfmd_solver *hp = nullptr;    // force handle (FP32 in the mixed solve)
+  gfmd_solver *hr64 = nullptr;  // FP64 refinement handle (mixed) or NULL
+  Obst o{};
+  double *u = nullptr;          // caller's FP64 displacements
+  bool mixed = false;
+  int evals = 0;
+  int done = 0;                 // phase result
+  int it0 = 0;
+  gfmd_min_report_t rep{};
+};
+
+// Phase kinds: plain FP64 <double, double>; FP32 bulk <float, float>;
+// FP64 refinement <double, float>.
+template <typename Tx, typename Tv> struct PhaseIo {
+  static Tx *x(Item &it, bool refine) {
+    if constexpr (sizeof(Tx) == 4) return it.b.u32;
+    else { (void)refine; return it.u; }
+  }
+};
+
+// One phase of a batch as a graph: a branch per item with its restart (fresh
+// F_el(u), g, h = g; arms the item's loop) followed by a WHILE node over CG
+// iterations.  The branches run concurrently.
 template <typename Tx, typename Tv>
-cudaError_t build_phase(CgBufs &b, gfmd_solver *hr, gfmd_solver *hd, const Obst &o, Tx *x,
-                        cudaGraph_t *graph_out, cudaGraphExec_t *exec_out) {
-  const Geom &gm = hr->g;
-  Tx *fel = reinterpret_cast<Tx *>(b.fel);
-  Tv *g = reinterpret_cast<Tv *>(b.g), *h = reinterpret_cast<Tv *>(b.h), *fKh = reinterpret_cast<Tv *>(b.fKh);
+cudaError_t build_phase(std::vector<Item *> &its, bool refine, cudaStream_t ms, cudaEvent_t fork,
+                        std::vector<cudaEvent_t> &join, cudaGraph_t *graph_out, cudaGraphExec_t *exec_out) {
+  const size_t n = its.size();
   cudaGraph_t top = nullptr;
   RT_CHECK(cudaGraphCreate(&top, 0));
   *graph_out = top;
-  cudaGraphConditionalHandle hc;
-  RT_CHECK(cudaGraphConditionalHandleCreate(&hc, top, 0, cudaGraphCondAssignDefault));
-  RT_CHECK(cudaStreamBeginCaptureToGraph(b.cs, top, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-  cudaError_t e = cudaMemsetAsync(&b.ctl->counter, 0, sizeof(unsigned int), b.cs);
-  if (e == cudaSuccess) e = eval_on(hr, b.cs, x, io_type<Tx>(), fel, io_type<Tx>(), b.d_e, true);
-  if (e == cudaSuccess) {
-    k_restart<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(o, gm, x, fel, g, h, b.active, b.part, b.ctl, hc, 1);
-    e = cudaGetLastError();
-  }
-  cudaGraphNodeParams cp = {};
-  cudaGraphNode_t cnode = nullptr;
-  if (e == cudaSuccess) {
-    cudaStreamCaptureStatus st;
-    const cudaGraphNode_t *deps = nullptr;
-    size_t nd = 0;
-    e = cudaStreamGetCaptureInfo(b.cs, &st, nullptr, nullptr, &deps, nullptr, &nd);
+  std::vector<cudaGraphConditionalHandle> hc(n);
+  for (size_t i = 0; i < n; i++)
+    RT_CHECK(cudaGraphConditionalHandleCreate(&hc[i], top, 0, cudaGraphCondAssignDefault));
+  std::vector<cudaGraph_t> body(n, nullptr);
+  RT_CHECK(cudaStreamBeginCaptureToGraph(ms, top, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  cudaError_t e = cudaEventRecord(fork, ms);
+  for (size_t i = 0; i < n && e == cudaSuccess; i++) {
+    Item &it = *its[i];
+    CgBufs &b = it.b;
+    gfmd_solver *hr = refine ? it.hr64 : it.hp;
+    Tx *x = PhaseIo<Tx, Tv>::x(it, refine);
+    Tx *fel = reinterpret_cast<Tx *>(b.fel);
+    Tv *g = reinterpret_cast<Tv *>(b.g), *h = reinterpret_cast<Tv *>(b.h);
+    e = cudaStreamWaitEvent(b.cs, fork, 0);
+    if (e == cudaSuccess) e = cudaMemsetAsync(&b.ctl->counter, 0, sizeof(unsigned int), b.cs);
+    if (e == cudaSuccess) e = eval_on(hr, b.cs, x, io_type<Tx>(), fel, io_type<Tx>(), b.d_e, true);
     if (e == cudaSuccess) {
-      cp.type = cudaGraphNodeTypeConditional;
-      cp.conditional.handle = hc;
-      cp.conditional.type = cudaGraphCondTypeWhile;
-      cp.conditional.size = 1;
-      e = cudaGraphAddNode(&cnode, top, deps, nullptr, nd, &cp);
+      k_restart<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(it.o, hr->g, x, fel, g, h, b.active, b.part, b.ctl, hc[i], 1);
+      e = cudaGetLastError();
     }
-    if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(b.cs, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (e == cudaSuccess) {
+      cudaStreamCaptureStatus st;
+      const cudaGraphNode_t *deps = nullptr;
+      size_t nd = 0;
+      e = cudaStreamGetCaptureInfo(b.cs, &st, nullptr, nullptr, &deps, nullptr, &nd);
+      cudaGraphNodeParams cp = {};
+      cudaGraphNode_t cnode = nullptr;
+      if (e == cudaSuccess) {
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = hc[i];
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        e = cudaGraphAddNode(&cnode, top, deps, nullptr, nd, &cp);
+      }
+      if (e == cudaSuccess) {
+        body[i] = cp.conditional.phGraph_out[0];
+        e = cudaStreamUpdateCaptureDependencies(b.cs, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies);
+      }
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(join[i], b.cs);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ms, join[i], 0);
   }
   cudaGraph_t got = nullptr;
-  cudaError_t e2 = cudaStreamEndCapture(b.cs, &got);
+  cudaError_t e2 = cudaStreamEndCapture(ms, &got);
   if (e == cudaSuccess) e = e2;
   if (e != cudaSuccess) return e;
-  // loop body
-  cudaGraph_t body = cp.conditional.phGraph_out[0];
-  RT_CHECK(cudaStreamBeginCaptureToGraph(b.cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-  e = eval_on(hd, b.cs, h, io_type<Tv>(), fKh, io_type<Tv>(), b.d_e, false);
-  if (e == cudaSuccess) {
-    k_dirforce<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(o, gm, x, fKh, h, g, b.active, b.part, b.ctl);
-    if (o.kind != GFMD_OBST_NONE)
-      for (int p = 0; p < kLsMax; p++)
-        k_probe<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(o, gm, x, h, b.active, b.part, b.ctl);
-    k_update<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(o, gm, x, h, fKh, g, b.active, b.part, b.ctl, hc, 1);
-    k_dir<Tv><<<b.nblk * 4, kT, 0, b.cs>>>(b.n, h, g, b.ctl);
-    e = cudaGetLastError();
+  // loop bodies
+  for (size_t i = 0; i < n; i++) {
+    Item &it = *its[i];
+    CgBufs &b = it.b;
+    gfmd_solver *hd = it.hp;
+    const Geom &gm = hd->g;
+    Tx *x = PhaseIo<Tx, Tv>::x(it, refine);
+    Tv *g = reinterpret_cast<Tv *>(b.g), *h = reinterpret_cast<Tv *>(b.h), *fKh = reinterpret_cast<Tv *>(b.fKh);
+    RT_CHECK(cudaStreamBeginCaptureToGraph(b.cs, body[i], nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    e = eval_on(hd, b.cs, h, io_type<Tv>(), fKh, io_type<Tv>(), b.d_e, false);
+    if (e == cudaSuccess) {
+      k_dirforce<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(it.o, gm, x, fKh, h, g, b.active, b.part, b.ctl);
+      if (it.o.kind != GFMD_OBST_NONE)
+        for (int p = 0; p < kLsMax; p++)
+          k_probe<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(it.o, gm, x, h, b.active, b.part, b.ctl);
+      k_update<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(it.o, gm, x, h, fKh, g, b.active, b.part, b.ctl, hc[i], 1);
+      k_dir<Tv><<<b.nblk * 4, kT, 0, b.cs>>>(b.n, h, g, b.ctl);
+      e = cudaGetLastError();
+    }
+    e2 = cudaStreamEndCapture(b.cs, &got);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) return e;
   }
-  e2 = cudaStreamEndCapture(b.cs, &got);
-  if (e == cudaSuccess) e = e2;
-  if (e != cudaSuccess) return e;
   return cudaGraphInstantiate(exec_out, top, 0);
 }
 
@@ -643,109 +693,234 @@ struct GraphHolder {
   }
 };
 
-// Runs one phase until it converges, fails or reaches the iteration cap.
-// Returns the phase's done code (1, 2, 3) or -1 on a CUDA error.
-// The FP32 phase also ends when a whole restart chunk has not halved max|g|
-// (it has reached what FP32 state resolves).
+// Runs one phase of the batch until every item has converged, failed or hit
+// the iteration cap (each launch of the graph runs at most `recompute`
+// iterations per item).  In the FP32 bulk phase an item whose whole restart
+// chunk did not halve max|g| is frozen: it has reached what FP32 state
+// resolves.  Returns a CUDA error.
 template <typename Tx, typename Tv>
-int run_phase(CgBufs &b, gfmd_solver *hr, gfmd_solver *hd, const Obst &o, Tx *x, int *evals,
-              cudaError_t *err) {
+cudaError_t run_phase(std::vector<Item *> &its, bool refine, cudaStream_t ms, cudaEvent_t fork,
+                      std::vector<cudaEvent_t> &join) {
   GraphHolder gh;
-  cudaError_t e = build_phase<Tx, Tv>(b, hr, hd, o, x, &gh.g, &gh.x);
-  if (e != cudaSuccess) { *err = e; return -1; }
+  RT_CHECK((build_phase<Tx, Tv>(its, refine, ms, fork, join, &gh.g, &gh.x)));
+  for (Item *it : its) it->it0 = it->b.hctl->it;
   for (;;) {
-    const int it0 = b.hctl->it;
-    e = cudaGraphLaunch(gh.x, b.cs);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(b.hctl, b.ctl, sizeof(CgCtl), cudaMemcpyDeviceToHost, b.cs);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(b.cs);
-    if (e != cudaSuccess) { *err = e; return -1; }
-    *evals += 1 + (b.hctl->it - it0);
-    if (b.hctl->done != 0) return b.hctl->done;
-    if (b.hctl->it == it0) {  // an armed loop always iterates
-      *err = cudaErrorUnknown;
-      return -1;
+    RT_CHECK(cudaGraphLaunch(gh.x, ms));
+    for (Item *it : its) RT_CHECK(cudaMemcpyAsync(it->b.hctl, it->b.ctl, sizeof(CgCtl), cudaMemcpyDeviceToHost, ms));
+    RT_CHECK(cudaStreamSynchronize(ms));
+    bool all = true;
+    for (Item *it : its) {
+      CgCtl &c = *it->b.hctl;
+      it->evals += 1 + (c.it - it->it0);
+      const bool ran = c.it != it->it0;
+      it->it0 = c.it;
+      it->done = c.done;
+      if (c.done != 0) continue;
+      if (!ran) return cudaErrorUnknown;  // an armed loop always iterates
+      if (c.bulk && c.since >= c.recompute && !(c.fmax < 0.5 * c.fmax_restart)) {
+        c.frozen = 1;  // takes effect at the next restart
+        RT_CHECK(cudaMemcpyAsync(&it->b.ctl->frozen, &c.frozen, sizeof(int), cudaMemcpyHostToDevice, ms));
+      }
+      all = false;
     }
-    if (b.hctl->bulk && b.hctl->since >= b.hctl->recompute && !(b.hctl->fmax < 0.5 * b.hctl->fmax_restart))
-      return 1;
+    if (all) return cudaSuccess;
   }
+}
+
+// Validates an item and prepares its buffers and control block.
+int item_init(Item &it, gfmd_solver *hp, gfmd_solver *hr64, const gfmd_obstacle_t *ob, double *u,
+              const gfmd_min_params_t *prm, cudaStream_t ms, std::string &err) {
+  it.hp = hp;
+  it.hr64 = hp->precision == GFMD_PREC_F32 ? hr64 : nullptr;
+  it.u = u;
+  it.mixed = hp->precision == GFMD_PREC_F32;
+  cudaError_t ce = bufs_init(it.b, hp, it.mixed);
+  if (ce != cudaSuccess) {
+    err = cudaGetErrorString(ce);
+    return ce == cudaErrorMemoryAllocation ? GFMD_ENOMEM : GFMD_ECUDA;
+  }
+  it.o = make_obst(ob, hp->g);
+  if (it.o.kind == GFMD_OBST_MAP_EXP) {
+    const size_t nsite = (size_t)hp->g.nx * hp->g.ny;
+    ce = cudaMalloc((void **)&it.b.mapf, sizeof(float) * nsite);
+    if (ce == cudaSuccess) {
+      k_d2f<<<4 * hp->sm_count, 256, 0, ms>>>(nsite, it.o.map, it.b.mapf);
+      it.o.mapf = it.b.mapf;
+    }
+  }
+  CgCtl c{};
+  c.ftol = prm->ftol;
+  c.ftol_req = prm->ftol;
+  c.bulk = it.mixed ? 1 : 0;
+  c.maxit = prm->maxiter > 0 ? prm->maxiter : 100000;
+  c.recompute = std::min(10000, prm->recompute > 0 ? prm->recompute : 50);
+  c.obst = it.o.kind != GFMD_OBST_NONE;
+  *it.b.hctl = c;
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(it.b.ctl, it.b.hctl, sizeof(CgCtl), cudaMemcpyHostToDevice, ms);
+  if (ce == cudaSuccess && it.mixed) k_d2f<<<4 * hp->sm_count, 256, 0, ms>>>(it.b.n, u, it.b.u32);
+  if (ce == cudaSuccess) ce = cudaGetLastError();
+  if (ce != cudaSuccess) {
+    err = cudaGetErrorString(ce);
+    return GFMD_ECUDA;
+  }
+  return GFMD_OK;
+}
+
+struct StreamSet {
+  cudaStream_t ms = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> join;
+  ~StreamSet() {
+    for (cudaEvent_t e : join) cudaEventDestroy(e);
+    if (fork) cudaEventDestroy(fork);
+    if (ms) cudaStreamDestroy(ms);
+  }
+  cudaError_t init(size_t n) {
+    cudaError_t e = cudaStreamCreateWithFlags(&ms, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+    join.assign(n, nullptr);
+    for (size_t i = 0; i < n && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&join[i], cudaEventDisableTiming);
+    return e;
+  }
+};
+
+// Solves the items (all plain FP64, or all mixed); fills each item's report.
+// Returns GFMD_OK or the first failing item's status.
+int solve_batch(std::vector<Item *> &its, const gfmd_min_params_t *prm, cudaStream_t ms,
+                cudaEvent_t fork, std::vector<cudaEvent_t> &join, std::string &err) {
+  const bool mixed = its[0]->mixed;
+  cudaError_t ce;
+  if (!mixed) {
+    ce = run_phase<double, double>(its, false, ms, fork, join);
+  } else {
+    ce = run_phase<float, float>(its, false, ms, fork, join);
+    std::vector<Item *> ref;
+    for (Item *it : its) {
+      if (ce != cudaSuccess) break;
+      k_f2d<<<4 * it->hp->sm_count, 256, 0, ms>>>(it->b.n, it->b.u32, it->u);
+      if (it->done == 1 && it->hr64) {
+        CgCtl &c = *it->b.hctl;
+        c.done = 0;
+        c.bulk = 0;
+        c.frozen = 0;
+        ce = cudaMemcpyAsync(it->b.ctl, &c, sizeof(CgCtl), cudaMemcpyHostToDevice, ms);
+        ref.push_back(it);
+      }
+    }
+    if (ce == cudaSuccess) ce = cudaGetLastError();
+    // FP64 refinement: FP64 restarts, FP32 direction forces
+    if (ce == cudaSuccess && !ref.empty()) ce = run_phase<double, float>(ref, true, ms, fork, join);
+  }
+  if (ce != cudaSuccess) {
+    err = cudaGetErrorString(ce);
+    cudaStreamSynchronize(ms);
+    return GFMD_ECUDA;
+  }
+  int first_bad = GFMD_OK;
+  for (Item *it : its) {
+    // report from a fresh evaluation with the most accurate handle
+    double E = 0.0, fm = 0.0, ff2 = 0.0;
+    ce = report_total_force(it->hr64 ? it->hr64 : it->hp, ms, it->o, it->u, &E, &fm, &ff2);
+    if (ce != cudaSuccess) {
+      err = cudaGetErrorString(ce);
+      return GFMD_ECUDA;
+    }
+    it->evals++;
+    gfmd_min_report_t &r = it->rep;
+    r.iterations = it->b.hctl->it;
+    r.force_evals = it->evals;
+    r.energy = E;
+    r.fmax = fm;
+    r.fnorm = std::sqrt(ff2);
+    int status = it->done == 1 ? GFMD_OK : (it->done == 3 ? GFMD_ENONFINITE : GFMD_ENOTCONVERGED);
+    if (status == GFMD_OK && !(fm <= prm->ftol * 1.0000001)) status = GFMD_ENOTCONVERGED;
+    r.status = status;
+    if (status != GFMD_OK && first_bad == GFMD_OK) {
+      first_bad = status;
+      err = status == GFMD_ENONFINITE ? "non-finite force during CG" : "CG did not reach max|f| <= ftol";
+    }
+  }
+  return first_bad;
 }
 
 }  // namespace
 
 int cg_minimize(gfmd_solver *hp, const gfmd_obstacle_t *ob, const gfmd_min_params_t *prm, double *u,
                 gfmd_min_report_t *rep, std::string &err) {
-  const bool mixed = hp->precision == GFMD_PREC_F32;
-  gfmd_solver *hr64 = prm->refine ? prm->refine : nullptr;
-  CgBufs b;
-  cudaError_t ce = bufs_init(b, hp, mixed);
+  StreamSet ss;
+  cudaError_t ce = ss.init(1);
+  Item it;
+  // order the solve after the caller's stream
+  if (ce == cudaSuccess) ce = cudaEventRecord(ss.fork, hp->stream);
+  if (ce == cudaSuccess) ce = cudaStreamWaitEvent(ss.ms, ss.fork, 0);
   if (ce != cudaSuccess) {
     err = cudaGetErrorString(ce);
-    return ce == cudaErrorMemoryAllocation ? GFMD_ENOMEM : GFMD_ECUDA;
-  }
-  // order the solve after the caller's stream
-  if ((ce = cudaEventRecord(b.ev, hp->stream)) == cudaSuccess) ce = cudaStreamWaitEvent(b.cs, b.ev, 0);
-  Obst o = make_obst(ob, hp->g);
-  if (ce == cudaSuccess && o.kind == GFMD_OBST_MAP_EXP) {
-    const size_t nsite = (size_t)hp->g.nx * hp->g.ny;
-    ce = cudaMalloc((void **)&b.mapf, sizeof(float) * nsite);
-    if (ce == cudaSuccess) {
-      k_d2f<<<4 * hp->sm_count, 256, 0, b.cs>>>(nsite, o.map, b.mapf);
-      o.mapf = b.mapf;
-    }
-  }
-  CgCtl c{};
-  c.ftol = prm->ftol;
-  c.ftol_req = prm->ftol;
-  c.bulk = mixed ? 1 : 0;
-  c.maxit = prm->maxiter > 0 ? prm->maxiter : 100000;
-  c.recompute = std::min(10000, prm->recompute > 0 ? prm->recompute : 50);
-  c.obst = o.kind != GFMD_OBST_NONE;
-  *b.hctl = c;
-  if (ce == cudaSuccess) ce = cudaMemcpyAsync(b.ctl, b.hctl, sizeof(CgCtl), cudaMemcpyHostToDevice, b.cs);
-  int evals = 0, done = -1;
-  const int eb = 4 * hp->sm_count;
-  if (ce == cudaSuccess) {
-    if (!mixed) {
-      done = run_phase<double, double>(b, hp, hp, o, u, &evals, &ce);
-    } else {
-      k_d2f<<<eb, 256, 0, b.cs>>>(b.n, u, b.u32);
-      done = run_phase<float, float>(b, hp, hp, o, b.u32, &evals, &ce);
-      if (done >= 0) {
-        k_f2d<<<eb, 256, 0, b.cs>>>(b.n, b.u32, u);
-        if (done == 1 && hr64) {
-          // FP64 refinement: FP64 restarts, FP32 direction forces
-          b.hctl->done = 0;
-          b.hctl->bulk = 0;
-          ce = cudaMemcpyAsync(b.ctl, b.hctl, sizeof(CgCtl), cudaMemcpyHostToDevice, b.cs);
-          if (ce == cudaSuccess) done = run_phase<double, float>(b, hr64, hp, o, u, &evals, &ce);
-        }
-      }
-    }
-  }
-  if (done < 0 || ce != cudaSuccess) {
-    err = cudaGetErrorString(ce);
-    cudaStreamSynchronize(b.cs);
     return GFMD_ECUDA;
   }
-  // report from a fresh evaluation with the most accurate handle
-  double E = 0.0, fm = 0.0, ff2 = 0.0;
-  ce = report_total_force(hr64 ? hr64 : hp, b.cs, o, u, &E, &fm, &ff2);
-  if (ce == cudaSuccess) ce = cudaEventRecord(b.ev, b.cs);
-  if (ce == cudaSuccess) ce = cudaStreamWaitEvent(hp->stream, b.ev, 0);
-  if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return GFMD_ECUDA; }
-  evals++;
+  int rc = item_init(it, hp, prm->refine, ob, u, prm, ss.ms, err);
+  if (rc != GFMD_OK) return rc;
+  std::vector<Item *> its{&it};
+  rc = solve_batch(its, prm, ss.ms, ss.fork, ss.join, err);
+  if (cudaEventRecord(ss.fork, ss.ms) == cudaSuccess) cudaStreamWaitEvent(hp->stream, ss.fork, 0);
   if (rep) {
-    rep->iterations = b.hctl->it;
-    rep->force_evals = evals;
-    rep->energy = E;
-    rep->fmax = fm;
-    rep->fnorm = std::sqrt(ff2);
+    const double secs = rep->seconds;
+    *rep = it.rep;
+    rep->seconds = secs;
   }
-  int status = done == 1 ? GFMD_OK : (done == 3 ? GFMD_ENONFINITE : GFMD_ENOTCONVERGED);
-  if (status == GFMD_OK && !(fm <= prm->ftol * 1.0000001)) status = GFMD_ENOTCONVERGED;
-  if (status == GFMD_ENOTCONVERGED) err = "CG did not reach max|f| <= ftol";
-  if (status == GFMD_ENONFINITE) err = "non-finite force during CG";
-  return status;
+  return rc;
 }
 
 }  // namespace gfmd
+
+extern "C" int gfmd_minimize_batch(int n, gfmd_batch_item_t *items, const gfmd_min_params_t *prm) {
+  using namespace gfmd;
+  if (n < 1 || !items || !prm) return set_error(GFMD_EINVAL, "gfmd_minimize_batch: bad arguments");
+  if (prm->method != GFMD_MIN_CG) return set_error(GFMD_EINVAL, "gfmd_minimize_batch: only CG is batched");
+  const int prec0 = items[0].handle ? items[0].handle->precision : -1;
+  const bool ref0 = items[0].refine != nullptr;
+  for (int i = 0; i < n; i++) {
+    gfmd_batch_item_t &b = items[i];
+    if (!b.handle || !b.d_u) return set_error(GFMD_EINVAL, "gfmd_minimize_batch: NULL handle or d_u");
+    if (!b.handle->have_phi) return set_error(GFMD_ENOPHI, "gfmd_minimize_batch: no stiffness table uploaded");
+    if (b.handle->precision != prec0 || (b.refine != nullptr) != ref0)
+      return set_error(GFMD_EINVAL, "gfmd_minimize_batch: items must share precision and refinement");
+    if (b.refine) {
+      const Geom &a = b.handle->g, &c = b.refine->g;
+      if (a.nx != c.nx || a.ny != c.ny || a.ndof != c.ndof || !b.refine->have_phi ||
+          b.refine->precision != GFMD_PREC_F64)
+        return set_error(GFMD_EINVAL, "gfmd_minimize_batch: refine handle does not match");
+    }
+    const gfmd_obstacle_t *ob = b.obstacle;
+    if (ob && (ob->kind < GFMD_OBST_NONE || ob->kind > GFMD_OBST_MAP_EXP))
+      return set_error(GFMD_EINVAL, "gfmd_minimize_batch: unknown obstacle kind");
+    if (ob && ob->kind == GFMD_OBST_MAP_EXP && !ob->d_map)
+      return set_error(GFMD_EINVAL, "gfmd_minimize_batch: map obstacle without a map");
+  }
+  const auto t0 = std::chrono::steady_clock::now();
+  StreamSet ss;
+  cudaError_t ce = ss.init((size_t)n);
+  if (ce != cudaSuccess) return set_error(GFMD_ECUDA, std::string("gfmd_minimize_batch: ") + cudaGetErrorString(ce));
+  for (int i = 0; i < n && ce == cudaSuccess; i++) {
+    ce = cudaEventRecord(ss.join[i], items[i].handle->stream);
+    if (ce == cudaSuccess) ce = cudaStreamWaitEvent(ss.ms, ss.join[i], 0);
+  }
+  if (ce != cudaSuccess) return set_error(GFMD_ECUDA, std::string("gfmd_minimize_batch: ") + cudaGetErrorString(ce));
+  std::vector<Item> store((size_t)n);
+  std::vector<Item *> its;
+  std::string err;
+  for (int i = 0; i < n; i++) {
+    int rc = item_init(store[i], items[i].handle, items[i].refine, items[i].obstacle, items[i].d_u, prm, ss.ms, err);
+    if (rc != GFMD_OK) return set_error(rc, "gfmd_minimize_batch: " + err);
+    its.push_back(&store[i]);
+  }
+  const int rc = solve_batch(its, prm, ss.ms, ss.fork, ss.join, err);
+  const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  for (int i = 0; i < n; i++) {
+    items[i].report = store[i].rep;
+    items[i].report.seconds = secs;
+  }
+  if (cudaEventRecord(ss.fork, ss.ms) == cudaSuccess)
+    for (int i = 0; i < n; i++) cudaStreamWaitEvent(items[i].handle->stream, ss.fork, 0);
+  if (rc != GFMD_OK) return set_error(rc, "gfmd_minimize_batch: " + err);
+  return GFMD_OK;
+}

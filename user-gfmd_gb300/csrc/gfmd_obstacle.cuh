@@ -26,6 +26,7 @@ struct Obst {
   double ax, ay, lx, ly;  // lattice spacing, box
   int nlayer;
   double off[8][3];
+  double fz_ext;   // external +z force on each atom of layers l < nlayer
   double gcut;     // effective cutoff on the gap (exp walls without one: 40 sigma)
   double margin;   // extra distance kept in the active-site list
   // FP32 copies for the per-site gating, so sites far from the obstacle cost
@@ -128,6 +129,7 @@ inline Obst make_obst(const gfmd_obstacle_t *ob, const Geom &g) {
   o.map = ob->d_map;
   o.map_z0 = ob->map_z0;
   o.norm = ob->norm == 0 ? 1 : ob->norm;
+  o.fz_ext = ob->fz_ext;
   o.ax = ob->lattice[0] > 0 ? ob->lattice[0] : 1.0;
   o.ay = ob->lattice[1] > 0 ? ob->lattice[1] : 1.0;
   o.lx = o.ax * g.nx;

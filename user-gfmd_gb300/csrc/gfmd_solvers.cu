@@ -121,6 +121,10 @@ __global__ void __launch_bounds__(kRedThreads) k_total_force(Obst o, Geom g, con
         fw[2] = w.f[2];
         acc[0] += w.e;
       }
+      if (l < o.nlayer && o.fz_ext != 0.0) {
+        fw[2] += o.fz_ext;  // load control: constant external force
+        acc[0] -= o.fz_ext * x[(size_t)(3 * l + 2) * N + s];
+      }
       for (int c = 0; c < 3; c++) {
         const size_t idx = (size_t)(3 * l + c) * N + s;
         const double f = fel[idx] + fw[c];

@@ -248,6 +248,35 @@ class GFMDSolverGB300:
             pass
 
 
+def minimize_batch(problems, ftol: float = 1e-6, maxiter: int = 0, recompute: int = 0):
+    """Batched CG (gfmd_minimize_batch): ``problems`` is a list of
+    (solver, u, obstacle_or_None, refine_solver_or_None) with u a CUDA
+    float64 tensor updated in place.  Returns the list of reports; raises
+    GFMDError (with ``.reports``) if any item failed."""
+    n = len(problems)
+    items = (_lib.BatchItem * n)()
+    keep = []
+    for i, (s, u, ob, ref) in enumerate(problems):
+        items[i].handle = s._handle().value
+        items[i].refine = ref._handle().value if ref is not None else None
+        if ob is not None:
+            items[i].obstacle = ctypes.pointer(ob)
+            keep.append(ob)
+        items[i].d_u = _ptr(u)
+    p = _lib.MinParams()
+    p.method = _lib.GFMD_MIN_CG
+    p.ftol = ftol
+    p.maxiter = maxiter
+    p.recompute = recompute
+    rc = lib().gfmd_minimize_batch(n, items, ctypes.byref(p))
+    reports = [items[i].report.as_dict() for i in range(n)]
+    if rc != _lib.GFMD_OK:
+        err = GFMDError(rc, lib().gfmd_last_error().decode(errors="replace"))
+        err.reports = reports
+        raise err
+    return reports
+
+
 _SOLVERS = {"static": "f64", "static/gb300": "f64", "static/gb300/f32": "f32"}
 
 
