@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--no-f64", action="store_true")
     ap.add_argument("--no-static", action="store_true")
     ap.add_argument("--static-n", type=int, default=2048)
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-n", type=int, default=64)
     return ap.parse_args()
 
 
@@ -286,6 +288,87 @@ def static_solve(g, torch, dev, stream, n):
 
 
 # ---------------------------------------------------------------------------
+# Batched static solves: 64 fcc(111) surfaces under rough rigid indenters
+
+BATCH_KERNEL = "ft fcc111 1 1.0 pair-potential 1 1.0 height 128"
+BATCH_SIZES = (64, 128, 256, 384, 512, 1024)
+E_STAR_FCC111 = 1.54  # contact modulus of this kernel (the reference's Hertz fcc111 test)
+
+
+def batched_solve(g, torch, dev, nsurf=64, seed=20261203, ftol=1e-6):
+    """64 independent surfaces, sizes drawn from {64..1024}^2, each indented
+    by a self-affine rigid surface (H = 0.8, rms slope 0.1, cut-offs 4 a and
+    L/2, random phases) under load control p in U[1e-3, 1e-2] E*, exp wall
+    (eps = 1, range 0.5 a) on both atoms of the cell; FP32 CG bulk plus FP64
+    refinement to max|f| <= 1e-6.  Timed twice: one surface after another,
+    and all surfaces in one batched graph (gfmd_minimize_batch)."""
+    rng = np.random.default_rng(seed)
+    sizes = [int(x) for x in rng.choice(BATCH_SIZES, nsurf)]
+    loads = rng.uniform(1e-3, 1e-2, nsurf)
+    k = g.StiffnessKernel(BATCH_KERNEL)
+    d = k.get_dimension()
+    t0 = time.perf_counter()
+    tabs = {n: k.phi_table(n, n, "half") for n in sorted(set(sizes))}
+    t_phi = time.perf_counter() - t0
+    cell_area = 3.0 ** 0.5  # a x a sqrt(3) rectangular cell, two atoms
+    probs = []
+    for i, (n, p) in enumerate(zip(sizes, loads)):
+        half, linf = tabs[n]
+        hs = []
+        for prec in ("f32", "f64"):
+            s = g.gfmd_solver_factory("static/gb300/f32" if prec == "f32" else "static/gb300")
+            s.set_grid_size(n, n, d)
+            s.set_phi(half, "half", linf)
+            hs.append(s)
+        zmap = torch.empty(n * n, dtype=torch.float64, device=dev)
+        g.rough_surface(zmap, n, n, 0.8, 0.1, 4.0, n / 2.0, seed + i)
+        ob = g.map_obstacle(zmap, 1.0, 0.5, z0=-float(zmap.min()), norm=-1, nlayer=2)
+        ob.fz_ext = float(p) * E_STAR_FCC111 * cell_area / 2.0
+        probs.append((hs[0], hs[1], ob, zmap, n))
+    dofs = sum(d * n * n for n in sizes)
+
+    def fresh():
+        return [torch.zeros(d, n * n, dtype=torch.float64, device=dev) for *_, n in probs]
+
+    # warm-up: module load and first graph instantiation
+    small = next(p for p in probs if p[4] == min(sizes))
+    uw = torch.zeros(d, small[4] ** 2, dtype=torch.float64, device=dev)
+    try:
+        g.minimize_batch([(small[0], uw, small[2], small[1])], ftol=ftol, maxiter=3)
+    except g.GFMDError:
+        pass
+    us = fresh()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    seq = [s32.minimize(u, ob, "cg", ftol=ftol, maxiter=50000, refine=s64)
+           for (s32, s64, ob, _, _), u in zip(probs, us)]
+    torch.cuda.synchronize()
+    t_seq = time.perf_counter() - t0
+    ub = fresh()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reps = g.minimize_batch([(s32, u, ob, s64) for (s32, s64, ob, _, _), u in zip(probs, ub)],
+                            ftol=ftol, maxiter=50000)
+    torch.cuda.synchronize()
+    t_bat = time.perf_counter() - t0
+    same = all(torch.equal(a, b) for a, b in zip(us, ub))
+    its = [r["iterations"] for r in reps]
+    return {
+        "config": f"{nsurf} x {BATCH_KERNEL}, sizes {BATCH_SIZES} (seeded), rough indenter "
+                  "H 0.8 rms slope 0.1 cut-offs 4 a / L/2, load p in U[1e-3, 1e-2] E* "
+                  f"(E* = {E_STAR_FCC111}), FP32 CG + FP64 refinement to max|f| <= {ftol}",
+        "sizes": sizes, "dofs_total": dofs,
+        "sequential_seconds": t_seq, "batched_seconds": t_bat, "speedup": t_seq / t_bat,
+        "iterations_total": int(sum(its)), "iterations_max": int(max(its)),
+        "dof_iterations_per_s": float(sum(d * n * n * r["iterations"] for n, r in zip(sizes, reps)) / t_bat),
+        "max_fmax": float(max(r["fmax"] for r in reps)),
+        "all_converged": all(r["status"] == 0 for r in reps) and all(r["status"] == 0 for r in seq),
+        "batched_equals_sequential": same,
+        "phi_table_seconds": t_phi,
+    }
+
+
+# ---------------------------------------------------------------------------
 # GB300 arm
 # ---------------------------------------------------------------------------
 
@@ -404,6 +487,8 @@ def run_gb300(args):
 
     if not args.no_static:
         extra["static_solve"] = static_solve(g, torch, dev, stream, args.static_n)
+    if not args.no_batch:
+        extra["batched_solve"] = batched_solve(g, torch, dev, args.batch_n)
 
     cpu = None
     if rank == 0 and not args.no_cpu:

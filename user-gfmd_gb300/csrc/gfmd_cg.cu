@@ -41,6 +41,8 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cmath>
 #include <string>
 #include <vector>
@@ -74,7 +76,7 @@ struct CgCtl {
   double ftol_req;          // requested tolerance
   double fmax_restart;      // max |g_i| at the last restart
   int bulk;                 // FP32 phase: tolerance floored at the FP32 noise level
-  int frozen;               // phase ended by the host (FP32 stagnation)
+  int parked;               // phase finished: the branch skips its restart and loop
   int it, since, maxit, recompute;
   int ls_it, ls_done;
   int done;                 // 0 running, 1 converged, 2 iteration cap, 3 non-finite
@@ -188,6 +190,13 @@ __device__ __forceinline__ float gap_of(const Obst &o, int ix, int iy, int l, co
 
 __device__ __forceinline__ bool wall_near(const Obst &o, float ge) { return ge < o.fgate_wall; }
 
+// The FP32 bulk phase evaluates a map wall in FP32 (its force depends on the
+// atom height alone, and every atom under a rough indenter is in range: FP64
+// exponentials per atom would bound the phase); FP64 phases use FP64.
+template <typename Tx> __device__ __forceinline__ bool map_in_f32(const Obst &o) {
+  return sizeof(Tx) == 4 && o.kind == GFMD_OBST_MAP_EXP;
+}
+
 __device__ __forceinline__ void set_loop(cudaGraphConditionalHandle hc, int use, unsigned int v) {
   if (use) cudaGraphSetConditional(hc, v);
 }
@@ -214,7 +223,16 @@ __global__ void __launch_bounds__(kT, 4) k_restart(Obst o, Geom gm, const Tx *__
       for (int c = 0; c < 3; c++) femx = fmaxf(femx, fabsf((float)fel[(size_t)(3 * l + c) * N + s]));
       double fw[3];
       bool hit = false;
-      if (l < o.nlayer && o.kind != GFMD_OBST_NONE) {
+      if (l < o.nlayer && map_in_f32<Tx>(o)) {
+        float e, fz;
+        map_wall_f(o, s, (float)x[(size_t)(3 * l + 2) * N + s] + o.foff[l][2], e, fz);
+        nearflag = true;
+        ew += e;
+        fw[0] = 0.0;
+        fw[1] = 0.0;
+        fw[2] = fz;
+        hit = true;
+      } else if (l < o.nlayer && o.kind != GFMD_OBST_NONE) {
         const float ge = gap_of(o, ix, iy, l, x, N, s);
         if (ge < o.fgate_active) nearflag = true;
         if (wall_near(o, ge)) {
@@ -257,8 +275,7 @@ __global__ void __launch_bounds__(kT, 4) k_restart(Obst o, Geom gm, const Tx *__
     // FP32 state resolves g = f_el + F_w to about eps32 |f_el|: the FP32
     // phase stops at 64 eps32 max|f_el| if that is above the request
     ctl->ftol = ctl->bulk ? fmax(ctl->ftol_req, 64.0 * 5.960464477539063e-8 * res[3]) : ctl->ftol_req;
-    if (ctl->frozen) ctl->done = 1;
-    else if (!isfinite(res[0])) ctl->done = 3;
+    if (!isfinite(res[0])) ctl->done = 3;
     else if (res[2] <= ctl->ftol) ctl->done = 1;
     else if (ctl->it >= ctl->maxit) ctl->done = 2;
     else ctl->done = 0;
@@ -288,7 +305,19 @@ __global__ void __launch_bounds__(kT) k_dirforce(Obst o, Geom gm, const Tx *__re
         gh.add(g[idx], hv);
       }
     }
-    if (o.kind != GFMD_OBST_NONE && active[s]) {
+    if (map_in_f32<Tx>(o)) {
+      float cwf = 0.0f, fhf = 0.0f;
+      for (int l = 0; l < o.nlayer; l++) {
+        const size_t iz = (size_t)(3 * l + 2) * N + s;
+        float e, fz;
+        map_wall_f(o, s, (float)x[iz] + o.foff[l][2], e, fz);
+        const float hz = (float)h[iz];
+        cwf += fz * o.fnorm * o.finv_sigma * hz * hz;  // d2E/dz2 = F / sigma
+        fhf += fz * hz;
+      }
+      cw += cwf;
+      fw0h += fhf;
+    } else if (o.kind != GFMD_OBST_NONE && active[s]) {
       const int ix = s / gm.ny, iy = s - ix * gm.ny;
       for (int l = 0; l < o.nlayer; l++) {
         double r[3], d[3];
@@ -332,6 +361,20 @@ __global__ void __launch_bounds__(kT) k_probe(Obst o, Geom gm, const Tx *__restr
   const int N = gm.nx * gm.ny;
   double dfh = 0.0, cw = 0.0;
   for (int s = blockIdx.x * kT + threadIdx.x; s < N; s += gridDim.x * kT) {
+    if (map_in_f32<Tx>(o)) {
+      float dfh_f = 0.0f, cw_f = 0.0f;
+      for (int l = 0; l < o.nlayer; l++) {
+        const size_t iz = (size_t)(3 * l + 2) * N + s;
+        const float hz = (float)h[iz];
+        float e, fz;
+        map_wall_f(o, s, (float)x[iz] + (float)a * hz + o.foff[l][2], e, fz);
+        dfh_f += fz * hz;
+        cw_f += fz * o.fnorm * o.finv_sigma * hz * hz;
+      }
+      dfh += dfh_f;
+      cw += cw_f;
+      continue;
+    }
     if (!active[s]) continue;
     const int ix = s / gm.ny, iy = s - ix * gm.ny;
     for (int l = 0; l < o.nlayer; l++) {
@@ -448,7 +491,14 @@ __global__ void __launch_bounds__(kT, 4) k_update(Obst o, Geom gm, Tx *__restric
         xn[c] = xv[c] + a * (Tx)hv[c];
         gn[c] = go[c] + av * fk[c];
       }
-      if (obst && l < o.nlayer) {
+      if (obst && l < o.nlayer && map_in_f32<Tx>(o)) {
+        float e1, f1, e0, f0;
+        map_wall_f(o, s, (float)xn[2] + o.foff[l][2], e1, f1);
+        map_wall_f(o, s, (float)xv[2] + o.foff[l][2], e0, f0);
+        nearflag = true;
+        ew += e1;
+        gn[2] = gn[2] + (Tv)(f1 - f0);
+      } else if (obst && l < o.nlayer) {
         const float ge_new = gap_reg(o, ix, iy, l, s, xn);
         const float ge_old = gap_reg(o, ix, iy, l, s, xv);
         if (ge_new < o.fgate_active) nearflag = true;
@@ -519,54 +569,118 @@ __global__ void k_d2f(size_t n, const double *__restrict__ a, float *__restrict_
     b[i] = (float)a[i];
 }
 
+// Arms a branch's restart unless the branch is parked.
+__global__ void k_gate(const CgCtl *ctl, cudaGraphConditionalHandle hif) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) cudaGraphSetConditional(hif, ctl->parked ? 0u : 1u);
+}
+
+// Final report from FP64 elastic forces fel of u: total force
+// f = fel + F_w(u) + external; sums: E_w + E_ext, |f|^2; max |f_i|.
+__global__ void __launch_bounds__(kT) k_report(Obst o, Geom gm, const double *__restrict__ x,
+                                                const double *__restrict__ fel, double *__restrict__ part,
+                                                CgCtl *ctl, double *__restrict__ out) {
+  const int N = gm.nx * gm.ny;
+  const int nl = gm.ndof / 3;
+  double ew = 0.0, f2 = 0.0, fm = 0.0;
+  for (int s = blockIdx.x * kT + threadIdx.x; s < N; s += gridDim.x * kT) {
+    const int ix = s / gm.ny, iy = s - ix * gm.ny;
+    for (int l = 0; l < nl; l++) {
+      double fw[3] = {0.0, 0.0, 0.0};
+      if (l < o.nlayer) {
+        if (o.kind != GFMD_OBST_NONE) {
+          double r[3], d[3];
+          atom_pos<double, double>(o, ix, iy, l, x, nullptr, N, s, 0.0, r, d);
+          const WallOut w = wall_eval(o, ix, iy, s, r, d);
+          fw[0] = w.f[0];
+          fw[1] = w.f[1];
+          fw[2] = w.f[2];
+          ew += w.e;
+        }
+        fw[2] += o.fz_ext;
+        ew -= o.fz_ext * x[(size_t)(3 * l + 2) * N + s];
+      }
+      for (int c = 0; c < 3; c++) {
+        const double f = fel[(size_t)(3 * l + c) * N + s] + fw[c];
+        f2 += f * f;
+        fm = fmax(fm, fabs(f));
+      }
+    }
+  }
+  const double acc[3] = {ew, f2, fm};
+  __shared__ double res[3];
+  if (!reduce_last<2, 1>(acc, part, &ctl->counter, res)) return;
+  if (threadIdx.x < 3) out[threadIdx.x] = res[threadIdx.x];
+}
+
 // ---- host side ---------------------------------------------------------------
+
+// GFMD_TRACE=1 prints the host-side phases of a solve (setup, graph build,
+// launches, report) to stderr.
+bool trace_on() {
+  static const bool on = [] {
+    const char *v = std::getenv("GFMD_TRACE");
+    return v && v[0] && v[0] != '0';
+  }();
+  return on;
+}
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
 
 template <typename T> constexpr int io_type() { return sizeof(T) == 8 ? 0 : 1; }
 
+// Device state of one CG problem, carved from one allocation.
 struct CgBufs {
   cudaStream_t cs = nullptr;
   int nblk = 0;
   size_t n = 0;
-  void *fel = nullptr;      // n doubles (holds float or double)
+  void *arena = nullptr;
+  void *fel = nullptr;      // n doubles: elastic force of a restart (float or double)
   void *g = nullptr, *h = nullptr, *fKh = nullptr;  // n doubles each (Tv)
-  float *u32 = nullptr;
+  float *u32 = nullptr;     // FP32 displacements of the mixed solve
   float *mapf = nullptr;    // FP32 copy of a map obstacle (gating)
   unsigned char *active = nullptr;
   double *part = nullptr;
-  double *d_e = nullptr;
+  double *d_e = nullptr;    // energy of an evaluation; [1..3] report scalars
   CgCtl *ctl = nullptr;
-  CgCtl *hctl = nullptr;  // pinned
-  cudaEvent_t ev = nullptr;
+  CgCtl *hctl = nullptr;    // pinned
   ~CgBufs() {
-    for (void *p : {fel, g, h, fKh, (void *)u32, (void *)mapf, (void *)active, (void *)part, (void *)d_e,
-                    (void *)ctl})
-      if (p) cudaFree(p);
+    if (arena) cudaFree(arena);
     if (hctl) cudaFreeHost(hctl);
-    if (ev) cudaEventDestroy(ev);
     if (cs) cudaStreamDestroy(cs);
   }
 };
 
-cudaError_t bufs_init(CgBufs &b, gfmd_solver *h, bool mixed) {
+cudaError_t bufs_init(CgBufs &b, gfmd_solver *h, bool mixed, bool map) {
   const Geom &g = h->g;
   b.n = (size_t)g.ndof * g.nx * g.ny;
   const size_t nsite = (size_t)g.nx * g.ny;
   b.nblk = (int)std::max<size_t>(1, std::min<size_t>((size_t)h->sm_count * 4, (nsite + kT - 1) / kT));
+  auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+  const size_t vb = up(sizeof(double) * b.n);
+  size_t off[10], tot = 0;
+  const size_t sz[10] = {vb, vb, vb, vb, mixed ? up(sizeof(float) * b.n) : 0, map ? up(sizeof(float) * nsite) : 0,
+                         up(nsite), up(sizeof(double) * kQ * b.nblk), up(sizeof(double) * 4), up(sizeof(CgCtl))};
+  for (int k = 0; k < 10; k++) {
+    off[k] = tot;
+    tot += sz[k];
+  }
   cudaError_t e = cudaStreamCreateWithFlags(&b.cs, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b.ev, cudaEventDisableTiming);
-  const size_t vb = sizeof(double) * b.n;
-  if (e == cudaSuccess) e = cudaMalloc(&b.fel, vb);
-  if (e == cudaSuccess) e = cudaMalloc(&b.g, vb);
-  if (e == cudaSuccess) e = cudaMalloc(&b.h, vb);
-  if (e == cudaSuccess) e = cudaMalloc(&b.fKh, vb);
-  if (e == cudaSuccess && mixed) e = cudaMalloc((void **)&b.u32, sizeof(float) * b.n);
-  if (e == cudaSuccess) e = cudaMalloc((void **)&b.active, nsite);
-  if (e == cudaSuccess) e = cudaMalloc((void **)&b.part, sizeof(double) * kQ * b.nblk);
-  if (e == cudaSuccess) e = cudaMalloc((void **)&b.d_e, sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc((void **)&b.ctl, sizeof(CgCtl));
+  if (e == cudaSuccess) e = cudaMalloc(&b.arena, tot);
   if (e == cudaSuccess) e = cudaMallocHost((void **)&b.hctl, sizeof(CgCtl));
-  if (e == cudaSuccess) e = cudaMemsetAsync(b.active, 0, nsite, b.cs);
-  return e;
+  if (e != cudaSuccess) return e;
+  char *a = static_cast<char *>(b.arena);
+  b.fel = a + off[0];
+  b.g = a + off[1];
+  b.h = a + off[2];
+  b.fKh = a + off[3];
+  b.u32 = mixed ? reinterpret_cast<float *>(a + off[4]) : nullptr;
+  b.mapf = map ? reinterpret_cast<float *>(a + off[5]) : nullptr;
+  b.active = reinterpret_cast<unsigned char *>(a + off[6]);
+  b.part = reinterpret_cast<double *>(a + off[7]);
+  b.d_e = reinterpret_cast<double *>(a + off[8]);
+  b.ctl = reinterpret_cast<CgCtl *>(a + off[9]);
+  return cudaSuccess;
 }
 
 // Force evaluation on stream st with handle hh.
@@ -593,18 +707,34 @@ struct Item {
   gfmd_min_report_t rep{};
 };
 
-// Phase kinds: plain FP64 <double, double>; FP32 bulk <float, float>;
-// FP64 refinement <double, float>.
-template <typename Tx, typename Tv> struct PhaseIo {
-  static Tx *x(Item &it, bool refine) {
-    if constexpr (sizeof(Tx) == 4) return it.b.u32;
-    else { (void)refine; return it.u; }
-  }
-};
+// Displacements a phase works on: FP32 copy in the bulk phase, else u.
+template <typename Tx> Tx *phase_x(Item &it) {
+  if constexpr (sizeof(Tx) == 4) return it.b.u32;
+  else return it.u;
+}
 
-// One phase of a batch as a graph: a branch per item with its restart (fresh
-// F_el(u), g, h = g; arms the item's loop) followed by a WHILE node over CG
-// iterations.  The branches run concurrently.
+// Adds a conditional node of the given type after the capture's current
+// dependencies on stream st; returns its body graph.
+cudaError_t add_cond(cudaStream_t st, cudaGraph_t top, cudaGraphConditionalHandle hc,
+                     cudaGraphConditionalNodeType type, cudaGraph_t *body) {
+  cudaStreamCaptureStatus cs;
+  const cudaGraphNode_t *deps = nullptr;
+  size_t nd = 0;
+  RT_CHECK(cudaStreamGetCaptureInfo(st, &cs, nullptr, nullptr, &deps, nullptr, &nd));
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = hc;
+  cp.conditional.type = type;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node = nullptr;
+  RT_CHECK(cudaGraphAddNode(&node, top, deps, nullptr, nd, &cp));
+  *body = cp.conditional.phGraph_out[0];
+  return cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+}
+
+// One phase of a batch as a graph.  Per item, concurrently:
+//   k_gate -> IF(not parked) { restart: fresh F_el(u), g, h = g; arms the
+//   loop } -> WHILE(armed) { CG iteration }.
 template <typename Tx, typename Tv>
 cudaError_t build_phase(std::vector<Item *> &its, bool refine, cudaStream_t ms, cudaEvent_t fork,
                         std::vector<cudaEvent_t> &join, cudaGraph_t *graph_out, cudaGraphExec_t *exec_out) {
@@ -612,45 +742,23 @@ cudaError_t build_phase(std::vector<Item *> &its, bool refine, cudaStream_t ms, 
   cudaGraph_t top = nullptr;
   RT_CHECK(cudaGraphCreate(&top, 0));
   *graph_out = top;
-  std::vector<cudaGraphConditionalHandle> hc(n);
-  for (size_t i = 0; i < n; i++)
-    RT_CHECK(cudaGraphConditionalHandleCreate(&hc[i], top, 0, cudaGraphCondAssignDefault));
-  std::vector<cudaGraph_t> body(n, nullptr);
+  std::vector<cudaGraphConditionalHandle> hif(n), hwh(n);
+  for (size_t i = 0; i < n; i++) {
+    RT_CHECK(cudaGraphConditionalHandleCreate(&hif[i], top, 0, cudaGraphCondAssignDefault));
+    RT_CHECK(cudaGraphConditionalHandleCreate(&hwh[i], top, 0, cudaGraphCondAssignDefault));
+  }
+  std::vector<cudaGraph_t> bif(n, nullptr), bwh(n, nullptr);
   RT_CHECK(cudaStreamBeginCaptureToGraph(ms, top, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
   cudaError_t e = cudaEventRecord(fork, ms);
   for (size_t i = 0; i < n && e == cudaSuccess; i++) {
-    Item &it = *its[i];
-    CgBufs &b = it.b;
-    gfmd_solver *hr = refine ? it.hr64 : it.hp;
-    Tx *x = PhaseIo<Tx, Tv>::x(it, refine);
-    Tx *fel = reinterpret_cast<Tx *>(b.fel);
-    Tv *g = reinterpret_cast<Tv *>(b.g), *h = reinterpret_cast<Tv *>(b.h);
+    CgBufs &b = its[i]->b;
     e = cudaStreamWaitEvent(b.cs, fork, 0);
-    if (e == cudaSuccess) e = cudaMemsetAsync(&b.ctl->counter, 0, sizeof(unsigned int), b.cs);
-    if (e == cudaSuccess) e = eval_on(hr, b.cs, x, io_type<Tx>(), fel, io_type<Tx>(), b.d_e, true);
     if (e == cudaSuccess) {
-      k_restart<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(it.o, hr->g, x, fel, g, h, b.active, b.part, b.ctl, hc[i], 1);
+      k_gate<<<1, 32, 0, b.cs>>>(b.ctl, hif[i]);
       e = cudaGetLastError();
     }
-    if (e == cudaSuccess) {
-      cudaStreamCaptureStatus st;
-      const cudaGraphNode_t *deps = nullptr;
-      size_t nd = 0;
-      e = cudaStreamGetCaptureInfo(b.cs, &st, nullptr, nullptr, &deps, nullptr, &nd);
-      cudaGraphNodeParams cp = {};
-      cudaGraphNode_t cnode = nullptr;
-      if (e == cudaSuccess) {
-        cp.type = cudaGraphNodeTypeConditional;
-        cp.conditional.handle = hc[i];
-        cp.conditional.type = cudaGraphCondTypeWhile;
-        cp.conditional.size = 1;
-        e = cudaGraphAddNode(&cnode, top, deps, nullptr, nd, &cp);
-      }
-      if (e == cudaSuccess) {
-        body[i] = cp.conditional.phGraph_out[0];
-        e = cudaStreamUpdateCaptureDependencies(b.cs, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies);
-      }
-    }
+    if (e == cudaSuccess) e = add_cond(b.cs, top, hif[i], cudaGraphCondTypeIf, &bif[i]);
+    if (e == cudaSuccess) e = add_cond(b.cs, top, hwh[i], cudaGraphCondTypeWhile, &bwh[i]);
     if (e == cudaSuccess) e = cudaEventRecord(join[i], b.cs);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(ms, join[i], 0);
   }
@@ -658,22 +766,34 @@ cudaError_t build_phase(std::vector<Item *> &its, bool refine, cudaStream_t ms, 
   cudaError_t e2 = cudaStreamEndCapture(ms, &got);
   if (e == cudaSuccess) e = e2;
   if (e != cudaSuccess) return e;
-  // loop bodies
   for (size_t i = 0; i < n; i++) {
     Item &it = *its[i];
     CgBufs &b = it.b;
-    gfmd_solver *hd = it.hp;
+    gfmd_solver *hr = refine ? it.hr64 : it.hp, *hd = it.hp;
     const Geom &gm = hd->g;
-    Tx *x = PhaseIo<Tx, Tv>::x(it, refine);
+    Tx *x = phase_x<Tx>(it);
+    Tx *fel = reinterpret_cast<Tx *>(b.fel);
     Tv *g = reinterpret_cast<Tv *>(b.g), *h = reinterpret_cast<Tv *>(b.h), *fKh = reinterpret_cast<Tv *>(b.fKh);
-    RT_CHECK(cudaStreamBeginCaptureToGraph(b.cs, body[i], nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    // restart
+    RT_CHECK(cudaStreamBeginCaptureToGraph(b.cs, bif[i], nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    e = cudaMemsetAsync(&b.ctl->counter, 0, sizeof(unsigned int), b.cs);
+    if (e == cudaSuccess) e = eval_on(hr, b.cs, x, io_type<Tx>(), fel, io_type<Tx>(), b.d_e, true);
+    if (e == cudaSuccess) {
+      k_restart<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(it.o, gm, x, fel, g, h, b.active, b.part, b.ctl, hwh[i], 1);
+      e = cudaGetLastError();
+    }
+    e2 = cudaStreamEndCapture(b.cs, &got);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) return e;
+    // iteration
+    RT_CHECK(cudaStreamBeginCaptureToGraph(b.cs, bwh[i], nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
     e = eval_on(hd, b.cs, h, io_type<Tv>(), fKh, io_type<Tv>(), b.d_e, false);
     if (e == cudaSuccess) {
       k_dirforce<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(it.o, gm, x, fKh, h, g, b.active, b.part, b.ctl);
       if (it.o.kind != GFMD_OBST_NONE)
         for (int p = 0; p < kLsMax; p++)
           k_probe<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(it.o, gm, x, h, b.active, b.part, b.ctl);
-      k_update<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(it.o, gm, x, h, fKh, g, b.active, b.part, b.ctl, hc[i], 1);
+      k_update<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(it.o, gm, x, h, fKh, g, b.active, b.part, b.ctl, hwh[i], 1);
       k_dir<Tv><<<b.nblk * 4, kT, 0, b.cs>>>(b.n, h, g, b.ctl);
       e = cudaGetLastError();
     }
@@ -694,36 +814,51 @@ struct GraphHolder {
 };
 
 // Runs one phase of the batch until every item has converged, failed or hit
-// the iteration cap (each launch of the graph runs at most `recompute`
-// iterations per item).  In the FP32 bulk phase an item whose whole restart
-// chunk did not halve max|g| is frozen: it has reached what FP32 state
-// resolves.  Returns a CUDA error.
+// the iteration cap; each launch of the graph runs at most `recompute`
+// iterations per item, and items that finished are parked (their branches
+// do nothing in later launches).  In the FP32 bulk phase an item whose whole
+// restart chunk did not halve max|g| is parked as converged: it has reached
+// what FP32 state resolves.
 template <typename Tx, typename Tv>
 cudaError_t run_phase(std::vector<Item *> &its, bool refine, cudaStream_t ms, cudaEvent_t fork,
                       std::vector<cudaEvent_t> &join) {
   GraphHolder gh;
+  const double t0 = now_s();
   RT_CHECK((build_phase<Tx, Tv>(its, refine, ms, fork, join, &gh.g, &gh.x)));
+  const double t1 = now_s();
+  int launches = 0;
   for (Item *it : its) it->it0 = it->b.hctl->it;
   for (;;) {
+    launches++;
     RT_CHECK(cudaGraphLaunch(gh.x, ms));
     for (Item *it : its) RT_CHECK(cudaMemcpyAsync(it->b.hctl, it->b.ctl, sizeof(CgCtl), cudaMemcpyDeviceToHost, ms));
     RT_CHECK(cudaStreamSynchronize(ms));
     bool all = true;
     for (Item *it : its) {
       CgCtl &c = *it->b.hctl;
+      if (c.parked) continue;
       it->evals += 1 + (c.it - it->it0);
       const bool ran = c.it != it->it0;
       it->it0 = c.it;
-      it->done = c.done;
-      if (c.done != 0) continue;
-      if (!ran) return cudaErrorUnknown;  // an armed loop always iterates
-      if (c.bulk && c.since >= c.recompute && !(c.fmax < 0.5 * c.fmax_restart)) {
-        c.frozen = 1;  // takes effect at the next restart
-        RT_CHECK(cudaMemcpyAsync(&it->b.ctl->frozen, &c.frozen, sizeof(int), cudaMemcpyHostToDevice, ms));
+      if (c.done == 0) {
+        if (!ran) return cudaErrorUnknown;  // an armed loop always iterates
+        if (!(c.bulk && c.since >= c.recompute && !(c.fmax < 0.5 * c.fmax_restart))) {
+          all = false;
+          continue;
+        }
+        c.done = 1;  // FP32 stagnation: the bulk phase is over for this item
       }
-      all = false;
+      it->done = c.done;
+      c.parked = 1;
+      RT_CHECK(cudaMemcpyAsync(it->b.ctl, &c, sizeof(CgCtl), cudaMemcpyHostToDevice, ms));
     }
-    if (all) return cudaSuccess;
+    if (all) {
+      if (trace_on())
+        std::fprintf(stderr, "gfmd cg phase <%s,%s> items %zu: graph build %.3f s, %d launches %.3f s\n",
+                     sizeof(Tx) == 8 ? "f64" : "f32", sizeof(Tv) == 8 ? "f64" : "f32", its.size(), t1 - t0,
+                     launches, now_s() - t1);
+      return cudaSuccess;
+    }
   }
 }
 
@@ -734,19 +869,18 @@ int item_init(Item &it, gfmd_solver *hp, gfmd_solver *hr64, const gfmd_obstacle_
   it.hr64 = hp->precision == GFMD_PREC_F32 ? hr64 : nullptr;
   it.u = u;
   it.mixed = hp->precision == GFMD_PREC_F32;
-  cudaError_t ce = bufs_init(it.b, hp, it.mixed);
+  it.o = make_obst(ob, hp->g);
+  const bool map = it.o.kind == GFMD_OBST_MAP_EXP;
+  cudaError_t ce = bufs_init(it.b, hp, it.mixed, map);
   if (ce != cudaSuccess) {
     err = cudaGetErrorString(ce);
     return ce == cudaErrorMemoryAllocation ? GFMD_ENOMEM : GFMD_ECUDA;
   }
-  it.o = make_obst(ob, hp->g);
-  if (it.o.kind == GFMD_OBST_MAP_EXP) {
-    const size_t nsite = (size_t)hp->g.nx * hp->g.ny;
-    ce = cudaMalloc((void **)&it.b.mapf, sizeof(float) * nsite);
-    if (ce == cudaSuccess) {
-      k_d2f<<<4 * hp->sm_count, 256, 0, ms>>>(nsite, it.o.map, it.b.mapf);
-      it.o.mapf = it.b.mapf;
-    }
+  const size_t nsite = (size_t)hp->g.nx * hp->g.ny;
+  ce = cudaMemsetAsync(it.b.active, 0, nsite, ms);
+  if (ce == cudaSuccess && map) {
+    k_d2f<<<4 * hp->sm_count, 256, 0, ms>>>(nsite, it.o.map, it.b.mapf);
+    it.o.mapf = it.b.mapf;
   }
   CgCtl c{};
   c.ftol = prm->ftol;
@@ -802,7 +936,7 @@ int solve_batch(std::vector<Item *> &its, const gfmd_min_params_t *prm, cudaStre
         CgCtl &c = *it->b.hctl;
         c.done = 0;
         c.bulk = 0;
-        c.frozen = 0;
+        c.parked = 0;
         ce = cudaMemcpyAsync(it->b.ctl, &c, sizeof(CgCtl), cudaMemcpyHostToDevice, ms);
         ref.push_back(it);
       }
@@ -811,27 +945,40 @@ int solve_batch(std::vector<Item *> &its, const gfmd_min_params_t *prm, cudaStre
     // FP64 refinement: FP64 restarts, FP32 direction forces
     if (ce == cudaSuccess && !ref.empty()) ce = run_phase<double, float>(ref, true, ms, fork, join);
   }
+  // reports from fresh FP64 (or the item's own precision) evaluations
+  const double tr = now_s();
+  for (Item *it : its) {
+    if (ce != cudaSuccess) break;
+    gfmd_solver *hh = it->hr64 ? it->hr64 : it->hp;
+    double *fel = reinterpret_cast<double *>(it->b.fel);
+    ce = cudaMemsetAsync(&it->b.ctl->counter, 0, sizeof(unsigned int), ms);
+    if (ce == cudaSuccess) ce = eval_on(hh, ms, it->u, 0, fel, 0, it->b.d_e, true);
+    if (ce == cudaSuccess) {
+      k_report<<<it->b.nblk, kT, 0, ms>>>(it->o, hh->g, it->u, fel, it->b.part, it->b.ctl, it->b.d_e + 1);
+      ce = cudaGetLastError();
+    }
+  }
+  std::vector<double> sc(4 * its.size());
+  for (size_t i = 0; i < its.size() && ce == cudaSuccess; i++)
+    ce = cudaMemcpyAsync(&sc[4 * i], its[i]->b.d_e, 4 * sizeof(double), cudaMemcpyDeviceToHost, ms);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(ms);
   if (ce != cudaSuccess) {
     err = cudaGetErrorString(ce);
     cudaStreamSynchronize(ms);
     return GFMD_ECUDA;
   }
+  if (trace_on()) std::fprintf(stderr, "gfmd cg reports: %.3f s\n", now_s() - tr);
   int first_bad = GFMD_OK;
-  for (Item *it : its) {
-    // report from a fresh evaluation with the most accurate handle
-    double E = 0.0, fm = 0.0, ff2 = 0.0;
-    ce = report_total_force(it->hr64 ? it->hr64 : it->hp, ms, it->o, it->u, &E, &fm, &ff2);
-    if (ce != cudaSuccess) {
-      err = cudaGetErrorString(ce);
-      return GFMD_ECUDA;
-    }
+  for (size_t i = 0; i < its.size(); i++) {
+    Item *it = its[i];
     it->evals++;
+    const double fm = sc[4 * i + 3];
     gfmd_min_report_t &r = it->rep;
     r.iterations = it->b.hctl->it;
     r.force_evals = it->evals;
-    r.energy = E;
+    r.energy = sc[4 * i] + sc[4 * i + 1];
     r.fmax = fm;
-    r.fnorm = std::sqrt(ff2);
+    r.fnorm = std::sqrt(sc[4 * i + 2]);
     int status = it->done == 1 ? GFMD_OK : (it->done == 3 ? GFMD_ENONFINITE : GFMD_ENOTCONVERGED);
     if (status == GFMD_OK && !(fm <= prm->ftol * 1.0000001)) status = GFMD_ENOTCONVERGED;
     r.status = status;
@@ -908,11 +1055,13 @@ extern "C" int gfmd_minimize_batch(int n, gfmd_batch_item_t *items, const gfmd_m
   std::vector<Item> store((size_t)n);
   std::vector<Item *> its;
   std::string err;
+  const double ti = now_s();
   for (int i = 0; i < n; i++) {
     int rc = item_init(store[i], items[i].handle, items[i].refine, items[i].obstacle, items[i].d_u, prm, ss.ms, err);
     if (rc != GFMD_OK) return set_error(rc, "gfmd_minimize_batch: " + err);
     its.push_back(&store[i]);
   }
+  if (trace_on()) std::fprintf(stderr, "gfmd cg setup of %d items: %.3f s\n", n, now_s() - ti);
   const int rc = solve_batch(its, prm, ss.ms, ss.fork, ss.join, err);
   const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   for (int i = 0; i < n; i++) {

@@ -35,8 +35,23 @@ struct Obst {
   float fgate_wall;    // evaluate the wall below this gap estimate
   float fgate_active;  // keep the site in the line-search set below this
   float foff[8][3];
+  float feps, finv_sigma, foffset, fgcut;  // map wall in FP32
   const float *mapf;   // FP32 copy of the map (may be NULL: then map is read)
 };
+
+// Exponential map wall in FP32 on atom height rz at site s: energy and z force.
+__device__ __forceinline__ void map_wall_f(const Obst &o, size_t s, float rz, float &e, float &fz) {
+  const float zm = (o.mapf ? o.mapf[s] : (float)o.map[s]) + o.fz0;
+  const float dz = o.fnorm * (rz - zm);
+  if (dz >= o.fgcut) {
+    e = 0.0f;
+    fz = 0.0f;
+    return;
+  }
+  const float ex = o.feps * expf(-dz * o.finv_sigma);
+  e = ex - o.foffset;
+  fz = o.fnorm * ex * o.finv_sigma;
+}
 
 struct WallOut {
   double e;        // energy
@@ -168,6 +183,10 @@ inline Obst make_obst(const gfmd_obstacle_t *ob, const Geom &g) {
   for (int l = 0; l < 8; l++)
     for (int c = 0; c < 3; c++) o.foff[l][c] = (float)o.off[l][c];
   o.mapf = nullptr;
+  o.feps = (float)o.eps;
+  o.finv_sigma = o.sigma > 0.0 ? (float)(1.0 / o.sigma) : 0.0f;
+  o.foffset = (float)o.offset;
+  o.fgcut = (float)o.gcut;
   return o;
 }
 
