@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--no-static", action="store_true")
     ap.add_argument("--static-n", type=int, default=2048)
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-dynamics", action="store_true")
+    ap.add_argument("--dyn-steps", type=int, default=10000)
     ap.add_argument("--batch-n", type=int, default=64)
     return ap.parse_args()
 
@@ -288,6 +290,35 @@ def static_solve(g, torch, dev, stream, n):
 
 
 # ---------------------------------------------------------------------------
+# Damped dynamics on the force-evaluation workload
+
+def dynamics_run(torch, dev, s32, s64, u_h, nsteps, dt=0.01, gamma=0.1, ncheck=200):
+    """Velocity Verlet with damping gamma = 0.1, dt = 0.01 from the seeded
+    Gaussian displacements (v = 0) on the 2048^2 fcc(100) four-layer kernel:
+    FP32 state and forces with FP64 energy reductions, all steps in one
+    graph-captured launch.  The energy trajectory is checked against the FP64
+    path over the first `ncheck` steps."""
+    def run(s, n):
+        u = torch.from_numpy(u_h).to(dev)
+        v = torch.zeros_like(u)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e, rep = s.run_dynamics(u, v, dt, gamma, n)
+        torch.cuda.synchronize()
+        return e, time.perf_counter() - t0
+    run(s32, 3)  # warm-up: graph instantiation
+    e32, t32 = run(s32, nsteps)
+    e64c, t64c = run(s64, ncheck)
+    diff = float(np.abs(e32[:ncheck + 1] - e64c).max() / np.abs(e64c).max())
+    return {"config": f"{nsteps} steps, dt {dt}, gamma {gamma}, u ~ N(0, 0.01 a) seeded, v = 0",
+            "steps_per_s": nsteps / t32, "ms_per_step": 1e3 * t32 / nsteps, "seconds": t32,
+            "energy_first": float(e32[0]), "energy_last": float(e32[-1]),
+            "monotone_decay": bool(np.all(np.diff(e32) <= 1e-12 * abs(e32[0]))),
+            "max_rel_energy_diff_vs_fp64_first_%d_steps" % ncheck: diff,
+            "fp64_ms_per_step": 1e3 * t64c / ncheck}
+
+
+# ---------------------------------------------------------------------------
 # Batched static solves: 64 fcc(111) surfaces under rough rigid indenters
 
 BATCH_KERNEL = "ft fcc111 1 1.0 pair-potential 1 1.0 height 128"
@@ -456,7 +487,10 @@ def run_gb300(args):
         extra["f64_path"] = {"value": 1000.0 / ms64, "unit": "evals/s", "ms_per_step": ms64,
                              "dtype": "f64"}
         extra["error_vs_f64"] = {"rel_l2_force": rel, "rel_energy": rele}
-        del s64, u64, f64
+        del u64, f64
+        if not args.no_dynamics:
+            extra["dynamics"] = dynamics_run(torch, dev, s, s64, u_h, args.dyn_steps)
+        del s64
 
     # end to end through the reference-facing call on host buffers
     e2e = None

@@ -196,3 +196,46 @@ def test_solver_status_codes():
     with pytest.raises(g.GFMDError) as ei:
         s.minimize(bad, None, "cg", maxiter=5)
     assert ei.value.code == 4
+
+
+@pytest.mark.parametrize("obstacle", ["sphere", "map"])
+def test_fp32_dynamics_tracks_fp64(obstacle):
+    nx = ny = 64
+    d, half, full, linf = tables(KERNEL_FCC2, nx, ny)
+    rng = np.random.default_rng(31)
+    u0 = rng.normal(0, 0.01, (d, nx * ny))
+    v0 = np.zeros_like(u0)
+    g = gfmd_pkg()
+    keep = None
+    if obstacle == "sphere":
+        o = gpu_obstacle(osv.ObstacleSpec(osv.SPHERE_EXP, center=(32.0, 32.0, 20.4), radius=20.0,
+                                          epsilon=0.05, sigma=0.5, cutoff=3.0,
+                                          layer_offsets=[(0, 0, 0), (0.5, 0.5, -0.7071)]))
+    else:
+        keep = torch.empty(nx * ny, dtype=torch.float64, device="cuda")
+        g.rough_surface(keep, nx, ny, 0.8, 0.1, 4.0, 32.0, 3)
+        o = g.map_obstacle(keep, 0.05, 0.5, z0=-float(keep.min()) + 0.2, norm=-1, nlayer=1)
+        o.fz_ext = 1e-3
+    out = {}
+    for prec in ("f64", "f32"):
+        s = _solver(nx, ny, d, half, linf, prec)
+        u = torch.from_numpy(u0).cuda()
+        v = torch.from_numpy(v0).cuda()
+        e, rep = s.run_dynamics(u, v, 0.01, 0.1, 300, o)
+        out[prec] = (u.cpu().numpy(), e)
+    (u64, e64), (u32, e32) = out["f64"], out["f32"]
+    assert np.abs(e32 - e64).max() <= 1e-5 * np.abs(e64).max()
+    assert rel_l2(u32, u64) <= 1e-5
+    assert e64[-1] < e64[0]  # damped
+
+
+def test_fp32_nve_energy_conservation():
+    nx = ny = 32
+    d, half, full, linf = tables(KERNEL_FCC2, nx, ny)
+    s = _solver(nx, ny, d, half, linf, "f32")
+    rng = np.random.default_rng(5)
+    u = torch.from_numpy(rng.uniform(-0.1, 0.1, (d, nx * ny))).cuda()
+    v = torch.zeros_like(u)
+    e, rep = s.run_dynamics(u, v, 0.01, 0.0, 5000)
+    assert rep["iterations"] == 5000
+    assert np.abs(e - e.mean()).max() / abs(e.mean()) < 1e-4

@@ -1,7 +1,7 @@
 // Solver loops around the force evaluation, resident on the GPU:
 //   static  - FIRE (FixFIRE, src/cuda/fix_fire.cpp:117-297); conjugate
 //             gradients live in gfmd_cg.cu;
-//   dynamic - damped velocity Verlet (fix nve plus linear damping).
+//   dynamic - damped velocity Verlet lives in gfmd_dynamics.cu.
 // Obstacles (gfmd_obstacle.cuh) act on every atom of the grid.
 //
 // State vectors here are FP64 [ndof][nx*ny]; the elastic forces come from the
@@ -138,16 +138,6 @@ __global__ void __launch_bounds__(kRedThreads) k_total_force(Obst o, Geom g, con
   block_reduce(acc, 2, true, part);
 }
 
-// sums: a.b
-__global__ void __launch_bounds__(kRedThreads) k_dot(size_t n, const double *__restrict__ a,
-                                                     const double *__restrict__ b,
-                                                     double *__restrict__ part) {
-  double acc[1] = {0.0};
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    acc[0] += a[i] * b[i];
-  block_reduce(acc, 1, false, part);
-}
-
 // FIRE, first half (FixFIRE::initial_integrate): v += dtf f, |v| per atom
 // limited to vlimit, u += dt v.
 __global__ void k_fire_first(Geom g, double *__restrict__ x, double *__restrict__ v,
@@ -206,31 +196,6 @@ __global__ void k_axpby(size_t n, double *__restrict__ v, const double *__restri
                         double b) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     v[i] = a * v[i] + b * f[i];
-}
-
-// Damped velocity Verlet, first half: vh = v + dt/2 (f - gamma v); u += dt vh.
-__global__ void k_verlet_first(size_t n, double *__restrict__ x, double *__restrict__ v,
-                               const double *__restrict__ f, double dt, double gamma) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const double vh = v[i] + 0.5 * dt * (f[i] - gamma * v[i]);
-    v[i] = vh;
-    x[i] += dt * vh;
-  }
-}
-
-// Second half: v = (vh + dt/2 f) / (1 + dt gamma/2); sums: v.v (kinetic x 2)
-__global__ void __launch_bounds__(kRedThreads) k_verlet_second(size_t n, double *__restrict__ v,
-                                                               const double *__restrict__ f,
-                                                               double dt, double gamma,
-                                                               double *__restrict__ part) {
-  double acc[1] = {0.0};
-  const double den = 1.0 / (1.0 + 0.5 * dt * gamma);
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const double vn = (v[i] + 0.5 * dt * f[i]) * den;
-    v[i] = vn;
-    acc[0] += vn * vn;
-  }
-  block_reduce(acc, 1, false, part);
 }
 
 // ---------------------------------------------------------------------------
@@ -430,50 +395,6 @@ int gfmd_minimize(gfmd_handle_t h, const gfmd_obstacle_t *obst, const gfmd_min_p
     rep->status = rc;
   }
   if (rc != GFMD_OK) return gfmd::set_error(rc, "gfmd_minimize: " + err);
-  return GFMD_OK;
-}
-
-int gfmd_run_dynamics(gfmd_handle_t h, const gfmd_obstacle_t *obst, double dt, double gamma,
-                      int nsteps, double *d_u, double *d_v, double *energies,
-                      gfmd_min_report_t *rep) {
-  using namespace gfmd;
-  if (!h || !d_u || !d_v || nsteps < 0 || !(dt > 0.0) || gamma < 0.0)
-    return set_error(GFMD_EINVAL, "gfmd_run_dynamics: bad argument");
-  if (!h->have_phi) return set_error(GFMD_ENOPHI, "gfmd_run_dynamics: no stiffness table uploaded");
-  auto t0 = std::chrono::steady_clock::now();
-  Work w;
-  cudaError_t ce = work_init(w, h, 2);  // fel, f
-  if (ce != cudaSuccess) return set_error(GFMD_ENOMEM, std::string("gfmd_run_dynamics: ") + cudaGetErrorString(ce));
-  double *fel = w.bufs[0], *f = w.bufs[1];
-  const Obst o = make_obst(obst, h->g);
-  double E = 0.0, fmax = 0.0;
-  ce = total_force(w, h, o, d_u, fel, f, &E, &fmax, nullptr);
-  int evals = 1;
-  for (int step = 0; step <= nsteps && ce == cudaSuccess; step++) {
-    // kinetic energy of the current v
-    k_dot<<<w.nblk, kRedThreads, 0, w.st>>>(w.n, d_v, d_v, w.part);
-    if ((ce = fetch(w, 1, false)) != cudaSuccess) break;
-    const double ekin = 0.5 * w.hres[0];
-    if (energies) energies[step] = E + ekin;
-    if (!std::isfinite(E + ekin)) {
-      return set_error(GFMD_ENONFINITE, "gfmd_run_dynamics: non-finite energy");
-    }
-    if (step == nsteps) break;
-    k_verlet_first<<<w.nblk, kRedThreads, 0, w.st>>>(w.n, d_u, d_v, f, dt, gamma);
-    if ((ce = total_force(w, h, o, d_u, fel, f, &E, &fmax, nullptr)) != cudaSuccess) break;
-    evals++;
-    k_verlet_second<<<w.nblk, kRedThreads, 0, w.st>>>(w.n, d_v, f, dt, gamma, w.part);
-  }
-  if (ce != cudaSuccess) return set_error(GFMD_ECUDA, std::string("gfmd_run_dynamics: ") + cudaGetErrorString(ce));
-  if (rep) {
-    rep->iterations = nsteps;
-    rep->force_evals = evals;
-    rep->energy = E;
-    rep->fmax = fmax;
-    rep->fnorm = 0.0;
-    rep->status = GFMD_OK;
-    rep->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-  }
   return GFMD_OK;
 }
 
