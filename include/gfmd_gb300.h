@@ -184,7 +184,8 @@ int gfmd_minimize(gfmd_handle_t h, const gfmd_obstacle_t *obst, const gfmd_min_p
  * surface is a branch of the graph running its restart and a device-driven
  * WHILE loop of CG iterations.  Mixed precision when the items' handles are
  * FP32 and carry an FP64 `refine` handle (all items alike).  params->method
- * must be GFMD_MIN_CG; params->refine is ignored (per item).  Returns
+ * must be GFMD_MIN_CG; params->refine is ignored (per item); every handle
+ * may appear in one item only (each owns its scratch).  Returns
  * GFMD_OK when every item converged, else the first failing item's status;
  * each item's report is filled either way.  No counterpart in the reference
  * (one surface per LAMMPS run). */

@@ -90,3 +90,52 @@ def test_batch_rejects_mixed_precisions():
     with pytest.raises(g.GFMDError) as ei:
         g.minimize_batch([(a, u1, None, None), (b, u2, None, None)])
     assert ei.value.code == 1
+
+
+def test_batch_rejects_a_handle_in_two_items():
+    g = gfmd_pkg()
+    nx = ny = 16
+    d, half, full, linf = tables(KERNEL_SC, nx, ny)
+    a = _solver(nx, ny, d, half, linf, "f64")
+    u1 = torch.zeros(d, nx * ny, dtype=torch.float64, device="cuda")
+    u2 = torch.zeros_like(u1)
+    with pytest.raises(g.GFMDError) as ei:
+        g.minimize_batch([(a, u1, None, None), (a, u2, None, None)])
+    assert ei.value.code == 1
+
+
+_DIRECT = r"""
+import sys, numpy as np, torch
+sys.path.insert(0, sys.argv[1])
+from solver_cases import KERNEL_SC, gpu_obstacle, sphere_spec, tables
+from conftest import gfmd_pkg
+nx = ny = 32
+d, half, full, linf = tables(KERNEL_SC, nx, ny)
+outs = []
+for prec in ("f64", "f32"):
+    s = gfmd_pkg().gfmd_solver_factory("static/gb300" if prec == "f64" else "static/gb300/f32")
+    s.set_grid_size(nx, ny, d); s.set_phi(half, "half", linf)
+    r = None
+    if prec == "f32":
+        r = gfmd_pkg().gfmd_solver_factory("static/gb300"); r.set_grid_size(nx, ny, d); r.set_phi(half, "half", linf)
+    u = torch.zeros(d, nx * ny, dtype=torch.float64, device="cuda")
+    rep = s.minimize(u, gpu_obstacle(sphere_spec(nx, ny, R=8.0, pen=0.3, cutoff=4.0)), "cg", ftol=1e-8, refine=r)
+    outs.append(u.cpu().numpy())
+np.save(sys.argv[2], np.stack(outs))
+"""
+
+
+def test_direct_launch_mode_matches_graphs(tmp_path):
+    import os
+    import subprocess
+    import sys
+    here = os.path.dirname(__file__)
+    script = tmp_path / "direct.py"
+    script.write_text(_DIRECT)
+    res = {}
+    for mode in ("0", "1"):
+        out = tmp_path / f"u{mode}.npy"
+        env = dict(os.environ, GFMD_NO_GRAPHS=mode)
+        subprocess.run([sys.executable, str(script), here, str(out)], check=True, env=env, timeout=300)
+        res[mode] = np.load(out)
+    assert np.array_equal(res["0"], res["1"])

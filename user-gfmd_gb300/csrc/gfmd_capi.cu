@@ -50,6 +50,8 @@ void release(gfmd_solver *h) {
                   h->d_counter};
   for (void *p : ptrs)
     if (p) cudaFree(p);
+  if (h->ws) cudaFree(h->ws);
+  if (h->ws_host) cudaFreeHost(h->ws_host);
   delete h;
 }
 

@@ -511,7 +511,8 @@ __global__ void __launch_bounds__(kT) k_report(Obst o, Geom gm, const double *__
     for (int l = 0; l < nl; l++) {
       double fw[3] = {0.0, 0.0, 0.0};
       if (l < o.nlayer) {
-        if (o.kind != GFMD_OBST_NONE) {
+        if (o.kind == GFMD_OBST_MAP_EXP ||
+            (o.kind != GFMD_OBST_NONE && wall_near(o, gap_of(o, ix, iy, l, x, N, s)))) {
           double r[3], d[3];
           atom_pos<double, double>(o, ix, iy, l, x, nullptr, N, s, 0.0, r, d);
           const WallOut w = wall_eval(o, ix, iy, s, r, d);
@@ -553,12 +554,12 @@ double now_s() {
 
 template <typename T> constexpr int io_type() { return sizeof(T) == 8 ? 0 : 1; }
 
-// Device state of one CG problem, carved from one allocation.
+// Device state of one CG problem, carved from the handle's workspace (kept
+// between solves, grown when a solve needs more).
 struct CgBufs {
   cudaStream_t cs = nullptr;
   int nblk = 0;
   size_t n = 0;
-  void *arena = nullptr;
   void *fel = nullptr;      // n doubles: elastic force of a restart (float or double)
   void *g = nullptr, *h = nullptr, *fKh = nullptr;  // n doubles each (Tv)
   float *u32 = nullptr;     // FP32 displacements of the mixed solve
@@ -569,8 +570,6 @@ struct CgBufs {
   CgCtl *ctl = nullptr;
   CgCtl *hctl = nullptr;    // pinned
   ~CgBufs() {
-    if (arena) cudaFree(arena);
-    if (hctl) cudaFreeHost(hctl);
     if (cs) cudaStreamDestroy(cs);
   }
 };
@@ -590,10 +589,17 @@ cudaError_t bufs_init(CgBufs &b, gfmd_solver *h, bool mixed, bool map) {
     tot += sz[k];
   }
   cudaError_t e = cudaStreamCreateWithFlags(&b.cs, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaMalloc(&b.arena, tot);
-  if (e == cudaSuccess) e = cudaMallocHost((void **)&b.hctl, sizeof(CgCtl));
+  if (e == cudaSuccess && h->ws_bytes < tot) {
+    if (h->ws) cudaFree(h->ws);
+    h->ws = nullptr;
+    h->ws_bytes = 0;
+    e = cudaMalloc(&h->ws, tot);
+    if (e == cudaSuccess) h->ws_bytes = tot;
+  }
+  if (e == cudaSuccess && !h->ws_host) e = cudaMallocHost(&h->ws_host, sizeof(CgCtl));
   if (e != cudaSuccess) return e;
-  char *a = static_cast<char *>(b.arena);
+  b.hctl = static_cast<CgCtl *>(h->ws_host);
+  char *a = static_cast<char *>(h->ws);
   b.fel = a + off[0];
   b.g = a + off[1];
   b.h = a + off[2];
@@ -656,6 +662,38 @@ cudaError_t add_cond(cudaStream_t st, cudaGraph_t top, cudaGraphConditionalHandl
   return cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
 }
 
+// Restart of one item on stream st: fresh F_el(u), g = f_el + F_w + f_ext,
+// h = g; arms the item's loop through hwh when use_hc.
+template <typename Tx, typename Tv>
+cudaError_t enqueue_restart(Item &it, bool refine, cudaStream_t st, cudaGraphConditionalHandle hwh, int use_hc) {
+  CgBufs &b = it.b;
+  gfmd_solver *hr = refine ? it.hr64 : it.hp;
+  Tx *x = phase_x<Tx>(it);
+  Tx *fel = reinterpret_cast<Tx *>(b.fel);
+  Tv *g = reinterpret_cast<Tv *>(b.g), *h = reinterpret_cast<Tv *>(b.h);
+  RT_CHECK(cudaMemsetAsync(&b.ctl->counter, 0, sizeof(unsigned int), st));
+  RT_CHECK(eval_on(hr, st, x, io_type<Tx>(), fel, io_type<Tx>(), b.d_e, true));
+  k_restart<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, it.hp->g, x, fel, g, h, b.active, b.part, b.ctl, hwh, use_hc);
+  return cudaGetLastError();
+}
+
+// One CG iteration of one item on stream st.
+template <typename Tx, typename Tv>
+cudaError_t enqueue_iteration(Item &it, cudaStream_t st, cudaGraphConditionalHandle hwh, int use_hc) {
+  CgBufs &b = it.b;
+  gfmd_solver *hd = it.hp;
+  const Geom &gm = hd->g;
+  Tx *x = phase_x<Tx>(it);
+  Tv *g = reinterpret_cast<Tv *>(b.g), *h = reinterpret_cast<Tv *>(b.h), *fKh = reinterpret_cast<Tv *>(b.fKh);
+  RT_CHECK(eval_on(hd, st, h, io_type<Tv>(), fKh, io_type<Tv>(), b.d_e, false));
+  k_dirforce<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, gm, x, fKh, h, g, b.active, b.part, b.ctl);
+  if (it.o.kind != GFMD_OBST_NONE)
+    for (int p = 0; p < kLsMax; p++) k_probe<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, gm, x, h, b.active, b.part, b.ctl);
+  k_update<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, gm, x, h, fKh, g, b.active, b.part, b.ctl, hwh, use_hc);
+  k_dir<Tv><<<b.nblk * 4, kT, 0, st>>>(b.n, h, g, b.ctl);
+  return cudaGetLastError();
+}
+
 // One phase of a batch as a graph.  Per item, concurrently:
 //   k_gate -> IF(not parked) { restart: fresh F_el(u), g, h = g; arms the
 //   loop } -> WHILE(armed) { CG iteration }.
@@ -691,41 +729,52 @@ cudaError_t build_phase(std::vector<Item *> &its, bool refine, cudaStream_t ms, 
   if (e == cudaSuccess) e = e2;
   if (e != cudaSuccess) return e;
   for (size_t i = 0; i < n; i++) {
-    Item &it = *its[i];
-    CgBufs &b = it.b;
-    gfmd_solver *hr = refine ? it.hr64 : it.hp, *hd = it.hp;
-    const Geom &gm = hd->g;
-    Tx *x = phase_x<Tx>(it);
-    Tx *fel = reinterpret_cast<Tx *>(b.fel);
-    Tv *g = reinterpret_cast<Tv *>(b.g), *h = reinterpret_cast<Tv *>(b.h), *fKh = reinterpret_cast<Tv *>(b.fKh);
-    // restart
-    RT_CHECK(cudaStreamBeginCaptureToGraph(b.cs, bif[i], nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-    e = cudaMemsetAsync(&b.ctl->counter, 0, sizeof(unsigned int), b.cs);
-    if (e == cudaSuccess) e = eval_on(hr, b.cs, x, io_type<Tx>(), fel, io_type<Tx>(), b.d_e, true);
-    if (e == cudaSuccess) {
-      k_restart<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(it.o, gm, x, fel, g, h, b.active, b.part, b.ctl, hwh[i], 1);
-      e = cudaGetLastError();
-    }
-    e2 = cudaStreamEndCapture(b.cs, &got);
+    cudaStream_t st = its[i]->b.cs;
+    RT_CHECK(cudaStreamBeginCaptureToGraph(st, bif[i], nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    e = enqueue_restart<Tx, Tv>(*its[i], refine, st, hwh[i], 1);
+    e2 = cudaStreamEndCapture(st, &got);
     if (e == cudaSuccess) e = e2;
     if (e != cudaSuccess) return e;
-    // iteration
-    RT_CHECK(cudaStreamBeginCaptureToGraph(b.cs, bwh[i], nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-    e = eval_on(hd, b.cs, h, io_type<Tv>(), fKh, io_type<Tv>(), b.d_e, false);
-    if (e == cudaSuccess) {
-      k_dirforce<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(it.o, gm, x, fKh, h, g, b.active, b.part, b.ctl);
-      if (it.o.kind != GFMD_OBST_NONE)
-        for (int p = 0; p < kLsMax; p++)
-          k_probe<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(it.o, gm, x, h, b.active, b.part, b.ctl);
-      k_update<Tx, Tv><<<b.nblk, kT, 0, b.cs>>>(it.o, gm, x, h, fKh, g, b.active, b.part, b.ctl, hwh[i], 1);
-      k_dir<Tv><<<b.nblk * 4, kT, 0, b.cs>>>(b.n, h, g, b.ctl);
-      e = cudaGetLastError();
-    }
-    e2 = cudaStreamEndCapture(b.cs, &got);
+    RT_CHECK(cudaStreamBeginCaptureToGraph(st, bwh[i], nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    e = enqueue_iteration<Tx, Tv>(*its[i], st, hwh[i], 1);
+    e2 = cudaStreamEndCapture(st, &got);
     if (e == cudaSuccess) e = e2;
     if (e != cudaSuccess) return e;
   }
   return cudaGraphInstantiate(exec_out, top, 0);
+}
+
+// GFMD_NO_GRAPHS=1: the same kernels in the same order, launched directly
+// with the loop decisions taken on the host after every restart and
+// iteration (one synchronization each).  Results are identical to the graph
+// mode; it exists for profilers that do not attribute kernels inside
+// conditional graph nodes.
+bool no_graphs() {
+  static const bool on = [] {
+    const char *v = std::getenv("GFMD_NO_GRAPHS");
+    return v && v[0] && v[0] != '0';
+  }();
+  return on;
+}
+
+template <typename Tx, typename Tv>
+cudaError_t run_launch_direct(std::vector<Item *> &its, bool refine, cudaStream_t ms) {
+  const cudaGraphConditionalHandle none = 0;
+  for (Item *it : its) {
+    CgCtl &c = *it->b.hctl;
+    RT_CHECK(cudaMemcpyAsync(&c, it->b.ctl, sizeof(CgCtl), cudaMemcpyDeviceToHost, ms));
+    RT_CHECK(cudaStreamSynchronize(ms));
+    if (c.parked) continue;
+    RT_CHECK((enqueue_restart<Tx, Tv>(*it, refine, ms, none, 0)));
+    RT_CHECK(cudaMemcpyAsync(&c, it->b.ctl, sizeof(CgCtl), cudaMemcpyDeviceToHost, ms));
+    RT_CHECK(cudaStreamSynchronize(ms));
+    while (c.done == 0 && c.since < c.recompute) {
+      RT_CHECK((enqueue_iteration<Tx, Tv>(*it, ms, none, 0)));
+      RT_CHECK(cudaMemcpyAsync(&c, it->b.ctl, sizeof(CgCtl), cudaMemcpyDeviceToHost, ms));
+      RT_CHECK(cudaStreamSynchronize(ms));
+    }
+  }
+  return cudaSuccess;
 }
 
 struct GraphHolder {
@@ -748,13 +797,15 @@ cudaError_t run_phase(std::vector<Item *> &its, bool refine, cudaStream_t ms, cu
                       std::vector<cudaEvent_t> &join) {
   GraphHolder gh;
   const double t0 = now_s();
-  RT_CHECK((build_phase<Tx, Tv>(its, refine, ms, fork, join, &gh.g, &gh.x)));
+  const bool direct = no_graphs();
+  if (!direct) RT_CHECK((build_phase<Tx, Tv>(its, refine, ms, fork, join, &gh.g, &gh.x)));
   const double t1 = now_s();
   int launches = 0;
   for (Item *it : its) it->it0 = it->b.hctl->it;
   for (;;) {
     launches++;
-    RT_CHECK(cudaGraphLaunch(gh.x, ms));
+    if (direct) RT_CHECK((run_launch_direct<Tx, Tv>(its, refine, ms)));
+    else RT_CHECK(cudaGraphLaunch(gh.x, ms));
     for (Item *it : its) RT_CHECK(cudaMemcpyAsync(it->b.hctl, it->b.ctl, sizeof(CgCtl), cudaMemcpyDeviceToHost, ms));
     RT_CHECK(cudaStreamSynchronize(ms));
     bool all = true;
@@ -952,6 +1003,10 @@ extern "C" int gfmd_minimize_batch(int n, gfmd_batch_item_t *items, const gfmd_m
   for (int i = 0; i < n; i++) {
     gfmd_batch_item_t &b = items[i];
     if (!b.handle || !b.d_u) return set_error(GFMD_EINVAL, "gfmd_minimize_batch: NULL handle or d_u");
+    for (int j = 0; j < i; j++)  // each handle owns its scratch: one item per handle
+      if (items[j].handle == b.handle || (b.refine && items[j].refine == b.refine) ||
+          items[j].handle == b.refine || (items[j].refine && items[j].refine == b.handle))
+        return set_error(GFMD_EINVAL, "gfmd_minimize_batch: a handle appears in two items");
     if (!b.handle->have_phi) return set_error(GFMD_ENOPHI, "gfmd_minimize_batch: no stiffness table uploaded");
     if (b.handle->precision != prec0 || (b.refine != nullptr) != ref0)
       return set_error(GFMD_EINVAL, "gfmd_minimize_batch: items must share precision and refinement");

@@ -89,6 +89,11 @@ struct gfmd_solver {
   unsigned *d_counter = nullptr;  // blocks finished in the column kernel
   int fast_rpost = 0;
   double bytes = 0.0;
+
+  // solver workspace, kept between solves (gfmd_cg.cu)
+  void *ws = nullptr;
+  size_t ws_bytes = 0;
+  void *ws_host = nullptr;   // pinned control block
 };
 
 namespace gfmd {
