@@ -279,6 +279,37 @@ typedef struct {
 int gfmd_rough_surface(int nx, int ny, const gfmd_surface_params_t *params, double *d_h,
                        void *cuda_stream);
 
+/* ---- Learned warm start ----------------------------------------------------
+ * No counterpart in the reference.  A BF16 convolutional encoder-decoder
+ * (4 levels, base_ch channels at full resolution, 2 base_ch below; periodic
+ * 3x3 convolutions, 2x2 average pooling, nearest upsampling with additive
+ * skips) mapping in_ch input channels to out_ch output channels, run and
+ * trained by the library's own tensor-core kernels (BF16 operands, FP32
+ * accumulation, FP32 master weights, Adam).  Tensors are device FP32 NHWC
+ * [batch][H][W][C], H and W multiples of 8.  Not thread-safe per handle. */
+typedef struct gfmd_ws_net *gfmd_ws_handle_t;
+
+int gfmd_ws_create(int in_ch, int out_ch, int base_ch, unsigned long long seed, gfmd_ws_handle_t *out);
+int gfmd_ws_destroy(gfmd_ws_handle_t net);
+int gfmd_ws_set_stream(gfmd_ws_handle_t net, void *cuda_stream);
+int gfmd_ws_num_params(gfmd_ws_handle_t net, long long *count);
+/* Copy parameters and/or the last gradient to host FP32 arrays (may be NULL);
+ * layout per layer: W[cout][9][cin] (tap = 3 (dy+1) + (dx+1)), then b[cout]. */
+int gfmd_ws_get_params(gfmd_ws_handle_t net, float *host_w, float *host_grad);
+int gfmd_ws_set_params(gfmd_ws_handle_t net, const float *host_w);
+int gfmd_ws_forward(gfmd_ws_handle_t net, int batch, int H, int W, const float *d_in, float *d_out);
+/* Forward, mean-squared-error loss against d_target, backward; the gradient
+ * stays in the handle for gfmd_ws_adam_step; *loss (may be NULL) is FP64. */
+int gfmd_ws_loss_grad(gfmd_ws_handle_t net, int batch, int H, int W, const float *d_in,
+                      const float *d_target, double *loss);
+int gfmd_ws_adam_step(gfmd_ws_handle_t net, float lr, float beta1, float beta2, float eps);
+/* Layout conversions between a solver grid [channels][nsite] (FP64) and one
+ * NHWC image (FP32), with a scale factor. */
+int gfmd_ws_to_nhwc(const double *d_u, int channels, int nsite, float scale, float *d_out,
+                    void *cuda_stream);
+int gfmd_ws_from_nhwc(const float *d_in, int channels, int nsite, double scale, double *d_u,
+                      void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -15,7 +15,11 @@ from .solver import (  # noqa: F401
     stiffness_kernel_factory,
 )
 
+from .warmstart import WarmStart, WarmStartNet  # noqa: F401
+
 __all__ = [
+    "WarmStart",
+    "WarmStartNet",
     "GFMDError",
     "Obstacle",
     "sphere_obstacle",

@@ -154,6 +154,17 @@ SIGNATURES = {
                           ctypes.POINTER(MinReport)],
     "gfmd_post_force_noalloc": [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp],
     "gfmd_rough_surface": [_c_int, _c_int, ctypes.POINTER(SurfaceParams), _vp, _vp],
+    "gfmd_ws_create": [_c_int, _c_int, _c_int, ctypes.c_ulonglong, ctypes.POINTER(_vp)],
+    "gfmd_ws_destroy": [_vp],
+    "gfmd_ws_set_stream": [_vp, _vp],
+    "gfmd_ws_num_params": [_vp, ctypes.POINTER(ctypes.c_longlong)],
+    "gfmd_ws_get_params": [_vp, _vp, _vp],
+    "gfmd_ws_set_params": [_vp, _vp],
+    "gfmd_ws_forward": [_vp, _c_int, _c_int, _c_int, _vp, _vp],
+    "gfmd_ws_loss_grad": [_vp, _c_int, _c_int, _c_int, _vp, _vp, _pd],
+    "gfmd_ws_adam_step": [_vp, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float],
+    "gfmd_ws_to_nhwc": [_vp, _c_int, _c_int, ctypes.c_float, _vp, _vp],
+    "gfmd_ws_from_nhwc": [_vp, _c_int, _c_int, _c_dbl, _vp, _vp],
     "gfmd_kernel_create": [ctypes.c_char_p, ctypes.POINTER(_vp)],
     "gfmd_kernel_destroy": [_vp],
     "gfmd_kernel_info": [_vp, _pi, _pi],
