@@ -58,6 +58,9 @@ def parse():
     ap.add_argument("--static-n", type=int, default=2048)
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-dynamics", action="store_true")
+    ap.add_argument("--no-warmstart", action="store_true")
+    ap.add_argument("--ws-full", action="store_true",
+                    help="warm start at the full configuration: 2000 pairs at 512^2, 4096^2, 32 loads")
     ap.add_argument("--dyn-steps", type=int, default=10000)
     ap.add_argument("--batch-n", type=int, default=64)
     return ap.parse_args()
@@ -319,6 +322,76 @@ def dynamics_run(torch, dev, s32, s64, u_h, nsteps, dt=0.01, gamma=0.1, ncheck=2
 
 
 # ---------------------------------------------------------------------------
+# Learned warm start
+
+WS_KERNEL = "ft sc100 1.0 1 pair-potential 2 1.0 1.0 height 128"
+E_STAR_SC100 = 8.0 / 3.0
+
+
+def warmstart_run(g, torch, dev, n_train=256, n_pairs=256, epochs=20, n_apply=1024, n_loads=4,
+                  seed=20261203):
+    """Rough contacts on the sc(100) kernel (H = 0.7, rms slope 0.2, cut-offs
+    4 a and 256 a, random phases; load-controlled, p log-uniform in
+    [1e-4, 1e-2] E*): training pairs from the batched mixed-precision solver
+    at n_train^2, the BF16 network trained on the GPU by the library's own
+    kernels, then held-out solves at n_apply^2 from a cold start (u = 0) and
+    from the network's guess, both to max|f| <= 1e-6."""
+    W = importlib.import_module("user-gfmd_gb300.warmstart")
+    rc = W.RoughContact(WS_KERNEL, 0.7, 0.2, 4.0, 256.0, E_STAR_SC100)
+    rng = np.random.default_rng(seed)
+    loads = 10 ** rng.uniform(-4, -2, n_pairs)
+    t0 = time.perf_counter()
+    zs, us, reps = rc.solve_many(g, torch, n_train, loads, list(range(seed, seed + n_pairs)))
+    torch.cuda.synchronize()
+    t_gen = time.perf_counter() - t0
+    hs = float(torch.stack([z - z.min() for z in zs]).std())
+    usc = float(torch.stack([u[2] for u in us]).std())
+    ws = W.WarmStart(3, 32, 1, h_scale=hs, u_scale=usc)
+    X = ws.features(torch, zs, loads, n_train, n_train)
+    T = ws.targets(torch, us, n_train, n_train)
+    del us, zs
+    t0 = time.perf_counter()
+    losses = ws.train(torch, X, T, epochs=epochs, batch=8, lr=2e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    del X, T
+    tl = 10 ** np.linspace(-4, -2, n_loads)
+    ts = list(range(seed + 10_000, seed + 10_000 + n_loads))
+    rc.solvers(g, n_apply)  # stiffness table generated outside both timings
+    t0 = time.perf_counter()
+    _, ucold, cold = rc.solve_many(g, torch, n_apply, tl, ts, chunk=1)
+    torch.cuda.synchronize()
+    t_cold = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    guesses, errs = [], []
+    for p, sd, ut in zip(tl, ts, ucold):
+        z, _ = rc.problem(g, torch, n_apply, p, sd)
+        u = torch.zeros(3, n_apply * n_apply, dtype=torch.float64, device=dev)
+        ws.initial_guess(torch, z, p, n_apply, n_apply, u)
+        guesses.append(u)
+        errs.append(float((u[2] - ut[2]).norm() / ut[2].norm()))
+    _, uwarm, warm = rc.solve_many(g, torch, n_apply, tl, ts, chunk=1, guesses=guesses)
+    torch.cuda.synchronize()
+    t_warm = time.perf_counter() - t0
+    agree = max(float((a - b).norm() / a.norm()) for a, b in zip(ucold, uwarm))
+    return {
+        "config": f"{WS_KERNEL}; network 4 levels, 32 base channels, BF16 tensor-core kernels; "
+                  f"{n_pairs} pairs at {n_train}^2, {epochs} epochs; applied at {n_apply}^2 on "
+                  f"{n_loads} held-out loads in [1e-4, 1e-2] E*",
+        "pair_generation_seconds": t_gen, "pair_iterations_mean": float(np.mean([r["iterations"] for r in reps])),
+        "train_seconds": t_train, "loss_first_epoch": losses[0], "loss_last_epoch": losses[-1],
+        "guess_rel_error_uz": errs,
+        "cold_iterations": [r["iterations"] for r in cold], "warm_iterations": [r["iterations"] for r in warm],
+        "cold_seconds": t_cold, "warm_seconds_incl_inference": t_warm,
+        "speedup_warm_vs_cold": t_cold / t_warm,
+        "iteration_ratio_warm_vs_cold": float(sum(r["iterations"] for r in warm) /
+                                              max(1, sum(r["iterations"] for r in cold))),
+        "solutions_agree_rel": agree,
+        "all_converged": all(r["status"] == 0 for r in cold + warm),
+    }
+
+
+# ---------------------------------------------------------------------------
 # Batched static solves: 64 fcc(111) surfaces under rough rigid indenters
 
 BATCH_KERNEL = "ft fcc111 1 1.0 pair-potential 1 1.0 height 128"
@@ -523,6 +596,11 @@ def run_gb300(args):
         extra["static_solve"] = static_solve(g, torch, dev, stream, args.static_n)
     if not args.no_batch:
         extra["batched_solve"] = batched_solve(g, torch, dev, args.batch_n)
+    if not args.no_warmstart:
+        if args.ws_full:
+            extra["warmstart"] = warmstart_run(g, torch, dev, 512, 2000, 10, 4096, 32)
+        else:
+            extra["warmstart"] = warmstart_run(g, torch, dev)
 
     cpu = None
     if rank == 0 and not args.no_cpu:

@@ -85,3 +85,41 @@ def test_gpu_training_reduces_loss():
         net.loss_grad(x, t)
         net.adam_step(3e-3)
     assert net.loss_grad(x, t) < 0.2 * first
+
+
+@pytest.mark.gpu
+def test_warm_started_solve_converges_to_the_cold_solution(capsys):
+    """Pairs from the solver, training on the GPU, and the solver as judge:
+    from the network's guess it converges to the same minimum as from u = 0
+    (the iteration counts of both are reported)."""
+    torch = pytest.importorskip("torch")
+    from importlib import import_module
+    g = gfmd_pkg()
+    W = import_module(g.__name__ + ".warmstart")
+    rc = W.RoughContact("ft sc100 1.0 1 pair-potential 2 1.0 1.0 height 16", 0.7, 0.2, 4.0, 32.0, 8.0 / 3.0)
+    n = 64
+    rng = np.random.default_rng(2)
+    loads = 10 ** rng.uniform(-3, -2, 32)
+    zs, us, reps = rc.solve_many(g, torch, n, loads, list(range(100, 132)))
+    assert all(r["status"] == 0 for r in reps)
+    hs = float(torch.stack([z - z.min() for z in zs]).std())
+    usc = float(torch.stack([u[2] for u in us]).std())
+    ws = W.WarmStart(3, 8, 1, h_scale=hs, u_scale=usc)
+    X = ws.features(torch, zs, loads, n, n)
+    T = ws.targets(torch, us, n, n)
+    losses = ws.train(torch, X, T, epochs=8, batch=4, lr=3e-3)
+    assert losses[-1] < 0.5 * losses[0]
+    tl, ts = [3e-3, 8e-3], [900, 901]
+    _, ucold, cold = rc.solve_many(g, torch, n, tl, ts)
+    guesses = []
+    for p, sd in zip(tl, ts):
+        z, _ = rc.problem(g, torch, n, p, sd)
+        u = torch.zeros(3, n * n, dtype=torch.float64, device="cuda")
+        guesses.append(ws.initial_guess(torch, z, p, n, n, u).clone())
+    _, uwarm, warm = rc.solve_many(g, torch, n, tl, ts, guesses=guesses)
+    for a, b, r in zip(ucold, uwarm, warm):
+        assert r["status"] == 0 and r["fmax"] <= 1e-6
+        assert float((a - b).norm() / a.norm()) <= 1e-4
+    with capsys.disabled():
+        print(f"\nwarm start: cold iterations {[r['iterations'] for r in cold]}, "
+              f"warm {[r['iterations'] for r in warm]}")

@@ -127,3 +127,62 @@ class WarmStart:
             if log:
                 log(ep, losses[-1])
         return losses
+
+
+# ---------------------------------------------------------------------------
+# Rough-contact problems and solver-generated training pairs
+
+class RoughContact:
+    """Load-controlled contact of a rigid self-affine indenter (exponential
+    map wall of strength ``eps`` and range ``sigma`` above the surface, its
+    lowest point touching the undeformed surface) with an elastic surface
+    under the external pressure ``load * e_star`` (per site area ``area``)."""
+
+    def __init__(self, kernel_args, hurst, rms_slope, lambda_short, lambda_long, e_star,
+                 eps=1.0, sigma=0.5, area=1.0, nlayer=1):
+        self.kernel_args = kernel_args
+        self.hurst, self.rms_slope = hurst, rms_slope
+        self.lambda_short, self.lambda_long = lambda_short, lambda_long
+        self.e_star, self.eps, self.sigma, self.area, self.nlayer = e_star, eps, sigma, area, nlayer
+        self._tables = {}
+
+    def solvers(self, g, n):
+        """(FP32, FP64) handles for an n x n grid (tables generated once per n)."""
+        if n not in self._tables:
+            k = g.StiffnessKernel(self.kernel_args)
+            self._tables[n] = (k.get_dimension(),) + k.phi_table(n, n, "half")
+        d, half, linf = self._tables[n]
+        out = []
+        for name in ("static/gb300/f32", "static/gb300"):
+            s = g.gfmd_solver_factory(name)
+            s.set_grid_size(n, n, d)
+            s.set_phi(half, "half", linf)
+            out.append(s)
+        return out[0], out[1], d
+
+    def problem(self, g, torch, n, load, seed, device="cuda"):
+        """(height map, obstacle) for an n x n grid."""
+        z = torch.empty(n * n, dtype=torch.float64, device=device)
+        g.rough_surface(z, n, n, self.hurst, self.rms_slope, self.lambda_short, self.lambda_long, seed)
+        ob = g.map_obstacle(z, self.eps, self.sigma, z0=-float(z.min()), norm=-1, nlayer=self.nlayer)
+        ob.fz_ext = float(load) * self.e_star * self.area / self.nlayer
+        return z, ob
+
+    def solve_many(self, g, torch, n, loads, seeds, ftol=1e-6, chunk=32, guesses=None):
+        """Solves the problems (batched, mixed precision); returns
+        (height maps, displacements, reports)."""
+        zs, us, reps = [], [], []
+        for c0 in range(0, len(loads), chunk):
+            items, keep = [], []
+            for i in range(c0, min(len(loads), c0 + chunk)):
+                s32, s64, d = self.solvers(g, n)
+                z, ob = self.problem(g, torch, n, loads[i], seeds[i])
+                u = torch.zeros(d, n * n, dtype=torch.float64, device="cuda")
+                if guesses is not None:
+                    u.copy_(guesses[i])
+                items.append((s32, u, ob, s64))
+                keep.append(z)
+            reps += g.minimize_batch(items, ftol=ftol, maxiter=50000)
+            zs += keep
+            us += [it[1] for it in items]
+        return zs, us, reps
