@@ -239,11 +239,14 @@ def run_reference(args):
 STATIC_KERNEL = "ft fcc100 1.0 1 pair-potential 1 1.0 height 128"
 
 
-def static_solve(g, torch, dev, stream, n):
+def static_solve(g, torch, dev, stream, n, shift=0.01):
     """Hertz-like indentation of a 2048^2 fcc(100) surface (E* = 1.39 kernel
     of the reference's tests/TEST_Hertz_fcc100_128x128): rigid sphere
     R = 100 a centred on the grid, exponential wall e = exp(-g / 0.5 a) on
-    the gap, 1.0 a penetration, CG to max|f_i| <= 1e-6."""
+    the gap, 1.0 a penetration, CG to max|f_i| <= 1e-6 from u = 0.  Paths:
+    plain FP64 CG (the baseline), FP32 CG + FP64 refinement, and the same
+    preconditioned by (Phi + shift)^{-1} (the reference's min_style cg/gfmd).
+    Displacement errors are against an FP64 solution converged to 1e-10."""
     k = g.StiffnessKernel(STATIC_KERNEL)
     d = k.get_dimension()
     half, linf = k.phi_table(n, n, "half")
@@ -258,36 +261,33 @@ def static_solve(g, torch, dev, stream, n):
         return s
 
     s64, s32 = solver("f64"), solver("f32")
+    p64, p32 = s64.make_preconditioner(shift), s32.make_preconditioner(shift)
     out = {"config": f"{STATIC_KERNEL}, {n}x{n}, sphere R=100 a, exp wall range 0.5 a, "
                      "penetration 1.0 a, CG to max|f| <= 1e-6 (ftol), cold start u = 0; "
-                     "each path warmed by one untimed 3-iteration solve"}
-    for s, ref in ((s64, None), (s32, s64)):  # module load, first graph instantiation
+                     "each path warmed by one untimed 3-iteration solve",
+           "preconditioner_shift": shift}
+    # reference: FP64, preconditioned, converged far below the tolerance
+    uref = torch.zeros(d, n * n, dtype=torch.float64, device=dev)
+    s64.minimize(uref, ob, "cg", ftol=1e-10, maxiter=50000, precond=p64)
+    paths = {"plain_fp64": (s64, None, None), "mixed_fp32_fp64_refine": (s32, s64, None),
+             "mixed_preconditioned": (s32, s64, p32)}
+    for name, (s, ref, pre) in paths.items():
         uw = torch.zeros(d, n * n, dtype=torch.float64, device=dev)
         try:
-            s.minimize(uw, ob, "cg", ftol=1e-6, maxiter=3, refine=ref)
+            s.minimize(uw, ob, "cg", ftol=1e-6, maxiter=3, refine=ref, precond=pre)
         except g.GFMDError:
             pass
-    u64 = torch.zeros(d, n * n, dtype=torch.float64, device=dev)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    r64 = s64.minimize(u64, ob, "cg", ftol=1e-6, maxiter=50000)
-    torch.cuda.synchronize()
-    t64 = time.perf_counter() - t0
-    um = torch.zeros_like(u64)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    rm = s32.minimize(um, ob, "cg", ftol=1e-6, maxiter=50000, refine=s64)
-    torch.cuda.synchronize()
-    tm = time.perf_counter() - t0
-    err = float(torch.linalg.norm(um - u64) / torch.linalg.norm(u64))
-    out["plain_fp64"] = {"seconds": t64, "iterations": r64["iterations"],
-                         "force_evals": r64["force_evals"], "fmax": r64["fmax"],
-                         "energy": r64["energy"]}
-    out["mixed_fp32_fp64_refine"] = {"seconds": tm, "iterations": rm["iterations"],
-                                     "force_evals": rm["force_evals"], "fmax": rm["fmax"],
-                                     "energy": rm["energy"],
-                                     "rel_displacement_error_vs_fp64": err}
-    out["speedup"] = t64 / tm
+        u = torch.zeros(d, n * n, dtype=torch.float64, device=dev)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = s.minimize(u, ob, "cg", ftol=1e-6, maxiter=50000, refine=ref, precond=pre)
+        torch.cuda.synchronize()
+        out[name] = {"seconds": time.perf_counter() - t0, "iterations": r["iterations"],
+                     "force_evals": r["force_evals"], "fmax": r["fmax"], "energy": r["energy"],
+                     "rel_displacement_error": float(torch.linalg.norm(u - uref) / torch.linalg.norm(uref))}
+    t64 = out["plain_fp64"]["seconds"]
+    out["speedup_mixed"] = t64 / out["mixed_fp32_fp64_refine"]["seconds"]
+    out["speedup"] = t64 / out["mixed_preconditioned"]["seconds"]
     out["unit"] = "s"
     return out
 

@@ -160,6 +160,10 @@ typedef struct {
   /* FIRE parameters (<= 0: the defaults of FixFIRE, src/cuda/fix_fire.cpp:63-69) */
   int fire_minsteps;
   double fire_incfac, fire_decfac, fire_mix, fire_mixdec, fire_dtmax, fire_dt, fire_xlimit;
+  gfmd_handle_t precond; /* CG: optional preconditioner from gfmd_make_preconditioner
+                            (same grid and precision as the handle): Polak-Ribiere
+                            on z = (Phi + shift)^{-1} g, the reference's min_style
+                            cg/gfmd (src/extras/min_cg_gfmd.cpp:96-207) */
 } gfmd_min_params_t;
 
 typedef struct {
@@ -171,6 +175,14 @@ typedef struct {
   double fnorm;         /* |f|_2 at the end (LAMMPS' fnorm) */
   double seconds;       /* wall time of the call */
 } gfmd_min_report_t;
+
+/* Preconditioner for CG: a new handle (same grid and precision) whose force
+ * evaluation returns -(Phi(q) + shift I)^{-1} u(q), no gamma-point term.
+ * Restates precondition_gradient (src/main/gfmd_misc.h:40-133) with
+ * Cavg = shift I; the block inverses are computed once, on the host, from
+ * h's uploaded table.  shift > 0 (it regularizes q = 0 and stands in for the
+ * obstacle stiffness).  Destroy with gfmd_destroy. */
+int gfmd_make_preconditioner(gfmd_handle_t h, double shift, gfmd_handle_t *out);
 
 /* Static minimization of elastic + obstacle energy from the displacements in
  * d_u (device, [ndof][nx*ny], FP64; updated in place).  Replaces LAMMPS'
@@ -195,6 +207,7 @@ typedef struct {
   const gfmd_obstacle_t *obstacle;/* may be NULL */
   double *d_u;                    /* displacements [ndof][nx*ny], device FP64, in/out */
   gfmd_min_report_t report;       /* out */
+  gfmd_handle_t precond;          /* optional preconditioner (all items alike) */
 } gfmd_batch_item_t;
 
 int gfmd_minimize_batch(int n, gfmd_batch_item_t *items, const gfmd_min_params_t *params);

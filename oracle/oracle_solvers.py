@@ -177,6 +177,93 @@ def cg(elastic, ob, u, nx, ny, ftol=1e-6, maxiter=100000, recompute=50):
                "fmax": np.abs(f).max(), "fnorm": np.sqrt((f * f).sum())}
 
 
+def pcg(elastic, precond, ob, u, nx, ny, ftol=1e-6, maxiter=100000, recompute=50):
+    """Preconditioned Polak-Ribiere CG of the reference's min_style cg/gfmd
+    (src/extras/min_cg_gfmd.cpp:96-207): z = precond(g) = (Phi + c)^{-1} g,
+    beta = max(0, z.(g - g_old) / (g_old.z_old)), h = z + beta h, reset to
+    h = z when h.g <= 0; the line search and the restarts every `recompute`
+    iterations are those of ``cg``.  Returns (u, report)."""
+    u = u.copy()
+    it = evals = 0
+
+    def restart():
+        nonlocal evals
+        fel, _ = elastic(u, True)
+        evals += 1
+        _, fw, _, _ = wall(ob, u, nx, ny)
+        g = fel + fw
+        z = precond(g)
+        return fel, g, z, z.copy(), (g * z).sum()
+
+    fel, g, z, h, gz = restart()
+    since = 0
+    while True:
+        if np.abs(g).max() <= ftol or it >= maxiter:
+            break
+        fKh, _ = elastic(h, False)
+        evals += 1
+        Kh = -fKh
+        hKh = (h * Kh).sum()
+        felh = (fel * h).sum()
+        a, lo, hi = 0.0, 0.0, -1.0
+        for _ in range(16):
+            fwh = cw = 0.0
+            if ob is not None:
+                _, _, fwh, cw = wall(ob, u, nx, ny, h, a)
+            gdir = felh - a * hKh + fwh
+            curv = hKh + cw
+            if gdir > 0:
+                lo = a
+            else:
+                hi = a
+            an = a + gdir / curv if curv > 0 else -1.0
+            if hi >= 0 and (an <= lo or an >= hi or an < 0):
+                an = 0.5 * (lo + hi)
+            elif an < 0:
+                an = 2 * lo if lo > 0 else 1e-3
+            step = abs(an - a)
+            a = an
+            if step <= 1e-6 * abs(a) or ob is None:
+                break
+        u += a * h
+        fel -= a * Kh
+        _, fw, _, _ = wall(ob, u, nx, ny)
+        gn = fel + fw
+        it += 1
+        since += 1
+        if since >= recompute:
+            fel, g, z, h, gz = restart()
+            since = 0
+            continue
+        zn = precond(gn)
+        zg = (zn * gn).sum()
+        beta = max(0.0, (zg - (zn * g).sum()) / gz)
+        hg = (h * gn).sum()
+        if not zg + beta * hg > 0:
+            beta = 0.0
+        h = zn + beta * h
+        g, gz = gn, zg
+    fel, E_el = elastic(u, True)
+    E_w, fw, _, _ = wall(ob, u, nx, ny)
+    f = fel + fw
+    return u, {"iterations": it, "force_evals": evals + 1, "energy": E_el + E_w,
+               "fmax": np.abs(f).max(), "fnorm": np.sqrt((f * f).sum())}
+
+
+def preconditioner(full, nx, ny, shift, post_force):
+    """z = (Phi(q) + shift I)^{-1} g(q) with the oracle's force routine on the
+    inverted full table (restates precondition_gradient, gfmd_misc.h:40-133)."""
+    N = nx * ny
+    d = full.shape[-1]
+    inv = np.linalg.inv(full * N + shift * np.eye(d)[None]) / N
+    zero = np.zeros(d // 3)
+
+    def apply(g):
+        f, _, _ = post_force(inv, zero, g, nx, ny)
+        return -f
+    return apply
+
+
 def fire(elastic, ob, u, nx, ny, ftol=1e-6, maxiter=100000, minsteps=10, incfac=1.2,
          decfac=0.5, mix_in=0.1, mixdec=0.99, dtmax=0.001, dt=None, xlimit=0.0):
     """FixFIRE (src/cuda/fix_fire.cpp:117-297) with unit masses."""

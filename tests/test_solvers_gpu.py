@@ -239,3 +239,39 @@ def test_fp32_nve_energy_conservation():
     e, rep = s.run_dynamics(u, v, 0.01, 0.0, 5000)
     assert rep["iterations"] == 5000
     assert np.abs(e - e.mean()).max() / abs(e.mean()) < 1e-4
+
+
+def test_preconditioner_matches_oracle():
+    from conftest import oracle_post_force
+    nx, ny = 32, 24
+    d, half, full, linf = tables(KERNEL_FCC2, nx, ny)
+    s = _solver(nx, ny, d, half, linf)
+    p = s.make_preconditioner(0.1)
+    rng = np.random.default_rng(8)
+    g = rng.normal(0, 1, (d, nx * ny))
+    f = np.empty_like(g)
+    p.post_force(g, f)
+    z = osv.preconditioner(full, nx, ny, 0.1, oracle_post_force)(g)
+    assert rel_l2(-f, z) <= 1e-10
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_preconditioned_cg_matches_oracle(prec):
+    from conftest import oracle_post_force
+    nx = ny = 32
+    d, half, full, linf, ob = _problem()
+    el = oracle_elastic(full, linf, nx, ny)
+    zp = osv.preconditioner(full, nx, ny, 0.05, oracle_post_force)
+    u_ref, r_ref = osv.pcg(el, zp, ob, np.zeros((d, nx * ny)), nx, ny, ftol=1e-8)
+    _, r_cg = osv.cg(el, ob, np.zeros((d, nx * ny)), nx, ny, ftol=1e-8)
+    s = _solver(nx, ny, d, half, linf, prec)
+    ref = _solver(nx, ny, d, half, linf, "f64") if prec == "f32" else None
+    pre = s.make_preconditioner(0.05)
+    o, _ = _gpu_obst(ob)
+    u = torch.zeros(d, nx * ny, dtype=torch.float64, device="cuda")
+    rep = s.minimize(u, o, "cg", ftol=1e-8, refine=ref, precond=pre)
+    assert rep["fmax"] <= 1e-8
+    assert rel_l2(u.cpu().numpy(), u_ref) <= 1e-6
+    assert r_ref["iterations"] < r_cg["iterations"]  # preconditioning pays
+    if prec == "f64":
+        assert rep["iterations"] <= 1.5 * r_ref["iterations"] + 5

@@ -70,6 +70,7 @@ class MinParams(ctypes.Structure):
         ("fire_dtmax", ctypes.c_double),
         ("fire_dt", ctypes.c_double),
         ("fire_xlimit", ctypes.c_double),
+        ("precond", ctypes.c_void_p),
     ]
 
 
@@ -99,6 +100,7 @@ class BatchItem(ctypes.Structure):
         ("obstacle", ctypes.POINTER(Obstacle)),
         ("d_u", ctypes.c_void_p),
         ("report", MinReport),
+        ("precond", ctypes.c_void_p),
     ]
 
 
@@ -149,6 +151,7 @@ SIGNATURES = {
     "gfmd_solver_info": [_vp, _pi, _pi],
     "gfmd_minimize": [_vp, ctypes.POINTER(Obstacle), ctypes.POINTER(MinParams), _vp,
                       ctypes.POINTER(MinReport)],
+    "gfmd_make_preconditioner": [_vp, _c_dbl, ctypes.POINTER(_vp)],
     "gfmd_minimize_batch": [_c_int, ctypes.POINTER(BatchItem), ctypes.POINTER(MinParams)],
     "gfmd_run_dynamics": [_vp, ctypes.POINTER(Obstacle), _c_dbl, _c_dbl, _c_int, _vp, _vp, _vp,
                           ctypes.POINTER(MinReport)],

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <complex>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -410,6 +411,112 @@ int gfmd_set_phi(gfmd_handle_t h, const double *phi, int layout, const double *l
   CK(cudaMemcpy(h->d_linf, lf.data(), sizeof(double) * lf.size(), cudaMemcpyHostToDevice),
      "gfmd_set_phi: linf");
   h->have_phi = true;
+  return GFMD_OK;
+}
+
+int gfmd_make_preconditioner(gfmd_handle_t h, double shift, gfmd_handle_t *out) {
+  if (!h || !out) return fail(GFMD_EINVAL, "gfmd_make_preconditioner: NULL argument");
+  *out = nullptr;
+  if (!h->have_phi) return fail(GFMD_ENOPHI, "gfmd_make_preconditioner: no stiffness table uploaded");
+  if (!(shift > 0.0) || !std::isfinite(shift)) return fail(GFMD_EINVAL, "gfmd_make_preconditioner: shift must be > 0");
+  const gfmd::Geom &g = h->g;
+  gfmd_handle_t p = nullptr;
+  int rc = gfmd_create(g.nx, g.ny, g.ndof, h->precision, &p);
+  if (rc != GFMD_OK) return rc;
+  if (p->fast != h->fast) {  // same parameters give the same path
+    release(p);
+    return fail(GFMD_ECUDA, "gfmd_make_preconditioner: path mismatch");
+  }
+  const int D = g.ndof, D2 = D * D;
+  const size_t nslot = (size_t)g.nyc * g.nxp, nel = nslot * D2;
+  const bool f64 = h->precision == GFMD_PREC_F64;
+  std::vector<double> tab(nel);
+  {
+    std::vector<float> tf;
+    cudaError_t e;
+    if (f64) {
+      e = cudaMemcpy(tab.data(), h->d_phi, nel * 8, cudaMemcpyDeviceToHost);
+    } else {
+      tf.resize(nel);
+      e = cudaMemcpy(tf.data(), h->d_phi, nel * 4, cudaMemcpyDeviceToHost);
+      for (size_t i = 0; i < nel; i++) tab[i] = tf[i];
+    }
+    if (e != cudaSuccess) {
+      release(p);
+      return cuda_fail(e, "gfmd_make_preconditioner: download");
+    }
+  }
+  const double N = (double)g.nx * (double)g.ny;
+  const bool fused = h->fast;
+  bool ok = true;
+  parallel_for((long)nslot, [&](long a, long b) {
+    std::vector<std::complex<double>> A(D2), I(D2);
+    for (long t = a; t < b; t++) {
+      const int ky = (int)(t / g.nxp), xs = (int)(t % g.nxp);
+      const size_t base = fused ? ((size_t)ky * (g.nxp / 32) + xs / 32) * D2 * 32 + (xs % 32)
+                                : (size_t)ky * D2 * g.nxp + xs;
+      const size_t ps = fused ? 32 : (size_t)g.nxp;
+      // Hermitian block Phi = N * table, plus the shift
+      for (int i = 0; i < D; i++) A[i * D + i] = N * tab[base + (size_t)i * ps] + shift;
+      int q = D;
+      for (int i = 0; i < D; i++)
+        for (int j = i + 1; j < D; j++) {
+          const std::complex<double> v(N * tab[base + (size_t)q * ps], N * tab[base + (size_t)(q + 1) * ps]);
+          A[i * D + j] = v;
+          A[j * D + i] = std::conj(v);
+          q += 2;
+        }
+      // Gauss-Jordan inverse (Hermitian positive definite: no pivoting)
+      for (int i = 0; i < D2; i++) I[i] = 0.0;
+      for (int i = 0; i < D; i++) I[i * D + i] = 1.0;
+      for (int c = 0; c < D; c++) {
+        const std::complex<double> piv = A[c * D + c];
+        if (!(std::abs(piv) > 0.0)) { ok = false; break; }
+        const std::complex<double> ip = 1.0 / piv;
+        for (int k = 0; k < D; k++) {
+          A[c * D + k] *= ip;
+          I[c * D + k] *= ip;
+        }
+        for (int r = 0; r < D; r++) {
+          if (r == c) continue;
+          const std::complex<double> f = A[r * D + c];
+          if (f == 0.0) continue;
+          for (int k = 0; k < D; k++) {
+            A[r * D + k] -= f * A[c * D + k];
+            I[r * D + k] -= f * I[c * D + k];
+          }
+        }
+      }
+      // pack M / N (Hermitian part)
+      for (int i = 0; i < D; i++) tab[base + (size_t)i * ps] = I[i * D + i].real() / N;
+      q = D;
+      for (int i = 0; i < D; i++)
+        for (int j = i + 1; j < D; j++) {
+          const std::complex<double> v = 0.5 * (I[i * D + j] + std::conj(I[j * D + i])) / N;
+          tab[base + (size_t)q * ps] = v.real();
+          tab[base + (size_t)(q + 1) * ps] = v.imag();
+          q += 2;
+        }
+    }
+  });
+  if (!ok) {
+    release(p);
+    return fail(GFMD_ENONFINITE, "gfmd_make_preconditioner: singular block");
+  }
+  cudaError_t e;
+  if (f64) {
+    e = cudaMemcpy(p->d_phi, tab.data(), nel * 8, cudaMemcpyHostToDevice);
+  } else {
+    std::vector<float> tf(nel);
+    for (size_t i = 0; i < nel; i++) tf[i] = (float)tab[i];
+    e = cudaMemcpy(p->d_phi, tf.data(), nel * 4, cudaMemcpyHostToDevice);
+  }
+  if (e != cudaSuccess) {
+    release(p);
+    return cuda_fail(e, "gfmd_make_preconditioner: upload");
+  }
+  p->have_phi = true;
+  *out = p;
   return GFMD_OK;
 }
 

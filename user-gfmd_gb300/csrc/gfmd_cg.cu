@@ -74,7 +74,8 @@ struct CgCtl {
   double gg;                // g.g of the current gradient
   double fmax;              // max |g_i|
   double ew;                // obstacle energy at the last update
-  double beta;              // next direction: h = g + beta h
+  double beta;              // next direction: h = g + beta h (h = z + beta h with a preconditioner)
+  double hg;                // h_old . g_new (descent check of the preconditioned direction)
   double ftol;              // tolerance of the running phase
   double ftol_req;          // requested tolerance
   double fmax_restart;      // max |g_i| at the last restart
@@ -381,7 +382,8 @@ __device__ __forceinline__ float gap_reg(const Obst &o, int ix, int iy, int l, s
 template <typename Tx, typename Tv>
 __global__ void __launch_bounds__(kT, 4) k_update(Obst o, Geom gm, Tx *__restrict__ x,
                                                    const Tv *__restrict__ h, const Tv *__restrict__ fKh,
-                                                   Tv *__restrict__ g, unsigned char *__restrict__ active,
+                                                   Tv *__restrict__ g, Tv *__restrict__ gp,
+                                                   unsigned char *__restrict__ active,
                                                    double *__restrict__ part, CgCtl *ctl,
                                                    cudaGraphConditionalHandle hc, int use_hc) {
   const double ad = ctl->a;
@@ -447,6 +449,7 @@ __global__ void __launch_bounds__(kT, 4) k_update(Obst o, Geom gm, Tx *__restric
         else fmx_d = fmax(fmx_d, fabs(gn[c]));
         x[idx] = xn[c];
         g[idx] = gn[c];
+        if (gp) gp[idx] = go[c];  // previous gradient (preconditioned Polak-Ribiere)
       }
     }
     active[s] = nearflag ? 1 : 0;
@@ -456,13 +459,17 @@ __global__ void __launch_bounds__(kT, 4) k_update(Obst o, Geom gm, Tx *__restric
   if (!reduce_last<4, 1>(acc, part, &ctl->counter, res)) return;
   if (threadIdx.x == 0) {
     const double gg_new = res[0], g_gold = res[1], h_g = res[2];
-    const double gg_old = ctl->gg;
-    double beta = gg_old > 0.0 ? (gg_new - g_gold) / gg_old : 0.0;  // Polak-Ribiere
-    if (beta < 0.0) beta = 0.0;
-    // new direction h' = g + beta h must descend: h'.g = gg_new + beta h.g > 0
-    if (!(gg_new + beta * h_g > 0.0)) beta = 0.0;
-    ctl->beta = beta;
-    ctl->gg = gg_new;
+    if (!gp) {
+      const double gg_old = ctl->gg;
+      double beta = gg_old > 0.0 ? (gg_new - g_gold) / gg_old : 0.0;  // Polak-Ribiere
+      if (beta < 0.0) beta = 0.0;
+      // new direction h' = g + beta h must descend: h'.g = gg_new + beta h.g > 0
+      if (!(gg_new + beta * h_g > 0.0)) beta = 0.0;
+      ctl->beta = beta;
+      ctl->gg = gg_new;
+    } else {
+      ctl->hg = h_g;  // beta follows from the preconditioned gradient (k_pcg_beta)
+    }
     ctl->ew = res[3];
     ctl->fmax = res[4];
     ctl->it += 1;
@@ -482,6 +489,58 @@ __global__ void __launch_bounds__(kT) k_dir(size_t n, Tv *__restrict__ h, const 
   const Tv beta = (Tv)ctl->beta;
   for (size_t i = blockIdx.x * (size_t)kT + threadIdx.x; i < n; i += (size_t)gridDim.x * kT)
     h[i] = g[i] + beta * h[i];
+}
+
+// Preconditioned CG.  The preconditioner handle's force evaluation of g
+// returns mz = -z, z = (Phi + c)^{-1} g.
+// Restart: h = z; g.z.
+template <typename Tv>
+__global__ void __launch_bounds__(kT) k_pcg_init(size_t n, const Tv *__restrict__ g, const Tv *__restrict__ mz,
+                                                  Tv *__restrict__ h, double *__restrict__ part, CgCtl *ctl) {
+  Dot<Tv> gz;
+  for (size_t i = blockIdx.x * (size_t)kT + threadIdx.x; i < n; i += (size_t)gridDim.x * kT) {
+    const Tv z = -mz[i];
+    h[i] = z;
+    gz.add(g[i], z);
+  }
+  const double acc[1] = {gz.get()};
+  __shared__ double res[1];
+  if (!reduce_last<1, 0>(acc, part, &ctl->counter, res)) return;
+  if (threadIdx.x == 0) ctl->gg = res[0];
+}
+
+// After the update: beta = max(0, z.(g - g_old) / (g_old.z_old)) with the
+// descent check h'.g = z.g + beta h.g > 0 (min_cg_gfmd.cpp:172-196).
+template <typename Tv>
+__global__ void __launch_bounds__(kT) k_pcg_beta(size_t n, const Tv *__restrict__ g, const Tv *__restrict__ gp,
+                                                  const Tv *__restrict__ mz, double *__restrict__ part,
+                                                  CgCtl *ctl) {
+  Dot<Tv> zg, zgo;
+  for (size_t i = blockIdx.x * (size_t)kT + threadIdx.x; i < n; i += (size_t)gridDim.x * kT) {
+    const Tv z = -mz[i];
+    zg.add(z, g[i]);
+    zgo.add(z, gp[i]);
+  }
+  const double acc[2] = {zg.get(), zgo.get()};
+  __shared__ double res[2];
+  if (!reduce_last<2, 0>(acc, part, &ctl->counter, res)) return;
+  if (threadIdx.x == 0) {
+    const double old = ctl->gg;
+    double beta = old > 0.0 ? (res[0] - res[1]) / old : 0.0;
+    if (!(beta > 0.0)) beta = 0.0;
+    if (!(res[0] + beta * ctl->hg > 0.0)) beta = 0.0;
+    ctl->beta = beta;
+    ctl->gg = res[0];
+  }
+}
+
+// h = z + beta h
+template <typename Tv>
+__global__ void __launch_bounds__(kT) k_dir_pcg(size_t n, Tv *__restrict__ h, const Tv *__restrict__ mz,
+                                                 const CgCtl *ctl) {
+  const Tv beta = (Tv)ctl->beta;
+  for (size_t i = blockIdx.x * (size_t)kT + threadIdx.x; i < n; i += (size_t)gridDim.x * kT)
+    h[i] = beta * h[i] - mz[i];
 }
 
 __global__ void k_f2d(size_t n, const float *__restrict__ a, double *__restrict__ b) {
@@ -562,6 +621,7 @@ struct CgBufs {
   size_t n = 0;
   void *fel = nullptr;      // n doubles: elastic force of a restart (float or double)
   void *g = nullptr, *h = nullptr, *fKh = nullptr;  // n doubles each (Tv)
+  void *mz = nullptr, *gp = nullptr;  // preconditioned CG: -z and the previous g (Tv)
   float *u32 = nullptr;     // FP32 displacements of the mixed solve
   float *mapf = nullptr;    // FP32 copy of a map obstacle (gating)
   unsigned char *active = nullptr;
@@ -574,17 +634,18 @@ struct CgBufs {
   }
 };
 
-cudaError_t bufs_init(CgBufs &b, gfmd_solver *h, bool mixed, bool map) {
+cudaError_t bufs_init(CgBufs &b, gfmd_solver *h, bool mixed, bool map, bool pcg) {
   const Geom &g = h->g;
   b.n = (size_t)g.ndof * g.nx * g.ny;
   const size_t nsite = (size_t)g.nx * g.ny;
   b.nblk = (int)std::max<size_t>(1, std::min<size_t>((size_t)h->sm_count * 4, (nsite + kT - 1) / kT));
   auto up = [](size_t x) { return (x + 255) / 256 * 256; };
   const size_t vb = up(sizeof(double) * b.n);
-  size_t off[10], tot = 0;
-  const size_t sz[10] = {vb, vb, vb, vb, mixed ? up(sizeof(float) * b.n) : 0, map ? up(sizeof(float) * nsite) : 0,
-                         up(nsite), up(sizeof(double) * kQ * b.nblk), up(sizeof(double) * 4), up(sizeof(CgCtl))};
-  for (int k = 0; k < 10; k++) {
+  size_t off[12], tot = 0;
+  const size_t sz[12] = {vb, vb, vb, vb, mixed ? up(sizeof(float) * b.n) : 0, map ? up(sizeof(float) * nsite) : 0,
+                         up(nsite), up(sizeof(double) * kQ * b.nblk), up(sizeof(double) * 4), up(sizeof(CgCtl)),
+                         pcg ? vb : 0, pcg ? vb : 0};
+  for (int k = 0; k < 12; k++) {
     off[k] = tot;
     tot += sz[k];
   }
@@ -610,6 +671,8 @@ cudaError_t bufs_init(CgBufs &b, gfmd_solver *h, bool mixed, bool map) {
   b.part = reinterpret_cast<double *>(a + off[7]);
   b.d_e = reinterpret_cast<double *>(a + off[8]);
   b.ctl = reinterpret_cast<CgCtl *>(a + off[9]);
+  b.mz = pcg ? a + off[10] : nullptr;
+  b.gp = pcg ? a + off[11] : nullptr;
   return cudaSuccess;
 }
 
@@ -628,6 +691,7 @@ struct Item {
   CgBufs b;
   gfmd_solver *hp = nullptr;    // force handle (FP32 in the mixed solve)
   gfmd_solver *hr64 = nullptr;  // FP64 refinement handle (mixed) or NULL
+  gfmd_solver *hpre = nullptr;  // preconditioner handle or NULL
   Obst o{};
   double *u = nullptr;          // caller's FP64 displacements
   bool mixed = false;
@@ -674,6 +738,11 @@ cudaError_t enqueue_restart(Item &it, bool refine, cudaStream_t st, cudaGraphCon
   RT_CHECK(cudaMemsetAsync(&b.ctl->counter, 0, sizeof(unsigned int), st));
   RT_CHECK(eval_on(hr, st, x, io_type<Tx>(), fel, io_type<Tx>(), b.d_e, true));
   k_restart<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, it.hp->g, x, fel, g, h, b.active, b.part, b.ctl, hwh, use_hc);
+  if (it.hpre) {
+    Tv *mz = reinterpret_cast<Tv *>(b.mz);
+    RT_CHECK(eval_on(it.hpre, st, g, io_type<Tv>(), mz, io_type<Tv>(), b.d_e, false));
+    k_pcg_init<Tv><<<b.nblk, kT, 0, st>>>(b.n, g, mz, h, b.part, b.ctl);
+  }
   return cudaGetLastError();
 }
 
@@ -689,8 +758,16 @@ cudaError_t enqueue_iteration(Item &it, cudaStream_t st, cudaGraphConditionalHan
   k_dirforce<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, gm, x, fKh, h, g, b.active, b.part, b.ctl);
   if (it.o.kind != GFMD_OBST_NONE)
     for (int p = 0; p < kLsMax; p++) k_probe<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, gm, x, h, b.active, b.part, b.ctl);
-  k_update<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, gm, x, h, fKh, g, b.active, b.part, b.ctl, hwh, use_hc);
-  k_dir<Tv><<<b.nblk * 4, kT, 0, st>>>(b.n, h, g, b.ctl);
+  Tv *gp = it.hpre ? reinterpret_cast<Tv *>(b.gp) : nullptr;
+  k_update<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, gm, x, h, fKh, g, gp, b.active, b.part, b.ctl, hwh, use_hc);
+  if (it.hpre) {
+    Tv *mz = reinterpret_cast<Tv *>(b.mz);
+    RT_CHECK(eval_on(it.hpre, st, g, io_type<Tv>(), mz, io_type<Tv>(), b.d_e, false));
+    k_pcg_beta<Tv><<<b.nblk, kT, 0, st>>>(b.n, g, gp, mz, b.part, b.ctl);
+    k_dir_pcg<Tv><<<b.nblk * 4, kT, 0, st>>>(b.n, h, mz, b.ctl);
+  } else {
+    k_dir<Tv><<<b.nblk * 4, kT, 0, st>>>(b.n, h, g, b.ctl);
+  }
   return cudaGetLastError();
 }
 
@@ -838,15 +915,16 @@ cudaError_t run_phase(std::vector<Item *> &its, bool refine, cudaStream_t ms, cu
 }
 
 // Validates an item and prepares its buffers and control block.
-int item_init(Item &it, gfmd_solver *hp, gfmd_solver *hr64, const gfmd_obstacle_t *ob, double *u,
-              const gfmd_min_params_t *prm, cudaStream_t ms, std::string &err) {
+int item_init(Item &it, gfmd_solver *hp, gfmd_solver *hr64, gfmd_solver *hpre, const gfmd_obstacle_t *ob,
+              double *u, const gfmd_min_params_t *prm, cudaStream_t ms, std::string &err) {
   it.hp = hp;
+  it.hpre = hpre;
   it.hr64 = hp->precision == GFMD_PREC_F32 ? hr64 : nullptr;
   it.u = u;
   it.mixed = hp->precision == GFMD_PREC_F32;
   it.o = make_obst(ob, hp->g);
   const bool map = it.o.kind == GFMD_OBST_MAP_EXP;
-  cudaError_t ce = bufs_init(it.b, hp, it.mixed, map);
+  cudaError_t ce = bufs_init(it.b, hp, it.mixed, map, hpre != nullptr);
   if (ce != cudaSuccess) {
     err = cudaGetErrorString(ce);
     return ce == cudaErrorMemoryAllocation ? GFMD_ENOMEM : GFMD_ECUDA;
@@ -979,7 +1057,7 @@ int cg_minimize(gfmd_solver *hp, const gfmd_obstacle_t *ob, const gfmd_min_param
     err = cudaGetErrorString(ce);
     return GFMD_ECUDA;
   }
-  int rc = item_init(it, hp, prm->refine, ob, u, prm, ss.ms, err);
+  int rc = item_init(it, hp, prm->refine, prm->precond, ob, u, prm, ss.ms, err);
   if (rc != GFMD_OK) return rc;
   std::vector<Item *> its{&it};
   rc = solve_batch(its, prm, ss.ms, ss.fork, ss.join, err);
@@ -1016,6 +1094,17 @@ extern "C" int gfmd_minimize_batch(int n, gfmd_batch_item_t *items, const gfmd_m
           b.refine->precision != GFMD_PREC_F64)
         return set_error(GFMD_EINVAL, "gfmd_minimize_batch: refine handle does not match");
     }
+    if (b.precond) {
+      const Geom &a = b.handle->g, &c = b.precond->g;
+      if (a.nx != c.nx || a.ny != c.ny || a.ndof != c.ndof || !b.precond->have_phi ||
+          b.precond->precision != b.handle->precision)
+        return set_error(GFMD_EINVAL, "gfmd_minimize_batch: preconditioner does not match");
+      for (int j = 0; j < n; j++)
+        if (j != i && (items[j].precond == b.precond || items[j].handle == b.precond || items[j].refine == b.precond))
+          return set_error(GFMD_EINVAL, "gfmd_minimize_batch: a handle appears in two items");
+    }
+    if ((b.precond != nullptr) != (items[0].precond != nullptr))
+      return set_error(GFMD_EINVAL, "gfmd_minimize_batch: items must share preconditioning");
     const gfmd_obstacle_t *ob = b.obstacle;
     if (ob && (ob->kind < GFMD_OBST_NONE || ob->kind > GFMD_OBST_MAP_EXP))
       return set_error(GFMD_EINVAL, "gfmd_minimize_batch: unknown obstacle kind");
@@ -1036,7 +1125,8 @@ extern "C" int gfmd_minimize_batch(int n, gfmd_batch_item_t *items, const gfmd_m
   std::string err;
   const double ti = now_s();
   for (int i = 0; i < n; i++) {
-    int rc = item_init(store[i], items[i].handle, items[i].refine, items[i].obstacle, items[i].d_u, prm, ss.ms, err);
+    int rc = item_init(store[i], items[i].handle, items[i].refine, items[i].precond, items[i].obstacle,
+                       items[i].d_u, prm, ss.ms, err);
     if (rc != GFMD_OK) return set_error(rc, "gfmd_minimize_batch: " + err);
     its.push_back(&store[i]);
   }

@@ -380,6 +380,12 @@ int gfmd_minimize(gfmd_handle_t h, const gfmd_obstacle_t *obst, const gfmd_min_p
     if (a.nx != b.nx || a.ny != b.ny || a.ndof != b.ndof || !prm->refine->have_phi)
       return gfmd::set_error(GFMD_EINVAL, "gfmd_minimize: refine handle does not match");
   }
+  if (prm->precond) {
+    const gfmd::Geom &a = h->g, &b = prm->precond->g;
+    if (a.nx != b.nx || a.ny != b.ny || a.ndof != b.ndof || !prm->precond->have_phi ||
+        prm->precond->precision != h->precision || prm->precond == h || prm->precond == prm->refine)
+      return gfmd::set_error(GFMD_EINVAL, "gfmd_minimize: preconditioner does not match");
+  }
   if (obst && obst->kind == GFMD_OBST_MAP_EXP && !obst->d_map)
     return gfmd::set_error(GFMD_EINVAL, "gfmd_minimize: map obstacle without a map");
   if (obst && (obst->kind < GFMD_OBST_NONE || obst->kind > GFMD_OBST_MAP_EXP))

@@ -168,8 +168,19 @@ class GFMDSolverGB300:
         fn = lib().gfmd_force_f64 if self.precision == "f64" else lib().gfmd_force_f32
         check(fn(self._handle(), _ptr(u), _ptr(f), _ptr(epot)))
 
+    def make_preconditioner(self, shift: float) -> "GFMDSolverGB300":
+        """A handle applying -(Phi + shift)^{-1} (gfmd_make_preconditioner),
+        for ``minimize(..., precond=...)``."""
+        out = GFMDSolverGB300(self.precision, name=self.name + "/precond")
+        h = ctypes.c_void_p()
+        check(lib().gfmd_make_preconditioner(self._handle(), shift, ctypes.byref(h)))
+        out._h = h
+        out.nx, out.ny, out.ndof = self.nx, self.ny, self.ndof
+        return out
+
     def minimize(self, u, obstacle=None, method: str = "cg", ftol: float = 1e-6,
-                 maxiter: int = 0, refine: "GFMDSolverGB300 | None" = None, **fire) -> dict:
+                 maxiter: int = 0, refine: "GFMDSolverGB300 | None" = None,
+                 precond: "GFMDSolverGB300 | None" = None, **fire) -> dict:
         """Static minimization from the displacements in u (CUDA float64
         tensor [ndof, nx*ny], updated in place); returns the report.  Raises
         GFMDError on failure (e.g. ENOTCONVERGED)."""
@@ -178,6 +189,7 @@ class GFMDSolverGB300:
         p.ftol = ftol
         p.maxiter = maxiter
         p.refine = refine._handle().value if refine is not None else None
+        p.precond = precond._handle().value if precond is not None else None
         for k, v in fire.items():
             setattr(p, "fire_" + k, v)
         rep = _lib.MinReport()
@@ -250,15 +262,18 @@ class GFMDSolverGB300:
 
 def minimize_batch(problems, ftol: float = 1e-6, maxiter: int = 0, recompute: int = 0):
     """Batched CG (gfmd_minimize_batch): ``problems`` is a list of
-    (solver, u, obstacle_or_None, refine_solver_or_None) with u a CUDA
+    (solver, u, obstacle_or_None, refine_solver_or_None[, precond]) with u a CUDA
     float64 tensor updated in place.  Returns the list of reports; raises
     GFMDError (with ``.reports``) if any item failed."""
     n = len(problems)
     items = (_lib.BatchItem * n)()
     keep = []
-    for i, (s, u, ob, ref) in enumerate(problems):
+    for i, prob in enumerate(problems):
+        s, u, ob, ref = prob[:4]
+        pre = prob[4] if len(prob) > 4 else None
         items[i].handle = s._handle().value
         items[i].refine = ref._handle().value if ref is not None else None
+        items[i].precond = pre._handle().value if pre is not None else None
         if ob is not None:
             items[i].obstacle = ctypes.pointer(ob)
             keep.append(ob)
