@@ -373,6 +373,9 @@ def warmstart_run(g, torch, dev, n_train=256, n_pairs=256, epochs=20, n_apply=10
     _, uwarm, warm = rc.solve_many(g, torch, n_apply, tl, ts, chunk=1, guesses=guesses)
     torch.cuda.synchronize()
     t_warm = time.perf_counter() - t0
+    # with the preconditioned solver
+    _, _, pcold = rc.solve_many(g, torch, n_apply, tl, ts, chunk=1, shift=0.01)
+    _, _, pwarm = rc.solve_many(g, torch, n_apply, tl, ts, chunk=1, guesses=guesses, shift=0.01)
     agree = max(float((a - b).norm() / a.norm()) for a, b in zip(ucold, uwarm))
     return {
         "config": f"{WS_KERNEL}; network 4 levels, 32 base channels, BF16 tensor-core kernels; "
@@ -387,6 +390,8 @@ def warmstart_run(g, torch, dev, n_train=256, n_pairs=256, epochs=20, n_apply=10
         "iteration_ratio_warm_vs_cold": float(sum(r["iterations"] for r in warm) /
                                               max(1, sum(r["iterations"] for r in cold))),
         "solutions_agree_rel": agree,
+        "preconditioned_cold_iterations": [r["iterations"] for r in pcold],
+        "preconditioned_warm_iterations": [r["iterations"] for r in pwarm],
         "all_converged": all(r["status"] == 0 for r in cold + warm),
     }
 
@@ -457,12 +462,30 @@ def batched_solve(g, torch, dev, nsurf=64, seed=20261203, ftol=1e-6):
     t_bat = time.perf_counter() - t0
     same = all(torch.equal(a, b) for a, b in zip(us, ub))
     its = [r["iterations"] for r in reps]
+    # the same batch, preconditioned CG (shift 0.01)
+    pres = [s32.make_preconditioner(0.01) for (s32, _, _, _, _) in probs]
+    up_ = fresh()
+    try:
+        g.minimize_batch([(s32, u, ob, s64, p) for (s32, s64, ob, _, _), u, p in zip(probs, up_, pres)],
+                         ftol=ftol, maxiter=3)
+    except g.GFMDError:
+        pass
+    up_ = fresh()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    repp = g.minimize_batch([(s32, u, ob, s64, p) for (s32, s64, ob, _, _), u, p in zip(probs, up_, pres)],
+                            ftol=ftol, maxiter=50000)
+    torch.cuda.synchronize()
+    t_pcg = time.perf_counter() - t0
     return {
         "config": f"{nsurf} x {BATCH_KERNEL}, sizes {BATCH_SIZES} (seeded), rough indenter "
                   "H 0.8 rms slope 0.1 cut-offs 4 a / L/2, load p in U[1e-3, 1e-2] E* "
                   f"(E* = {E_STAR_FCC111}), FP32 CG + FP64 refinement to max|f| <= {ftol}",
         "sizes": sizes, "dofs_total": dofs,
         "sequential_seconds": t_seq, "batched_seconds": t_bat, "speedup": t_seq / t_bat,
+        "batched_preconditioned_seconds": t_pcg,
+        "preconditioned_iterations_total": int(sum(r["iterations"] for r in repp)),
+        "preconditioned_all_converged": all(r["status"] == 0 for r in repp),
         "iterations_total": int(sum(its)), "iterations_max": int(max(its)),
         "dof_iterations_per_s": float(sum(d * n * n * r["iterations"] for n, r in zip(sizes, reps)) / t_bat),
         "max_fmax": float(max(r["fmax"] for r in reps)),

@@ -146,8 +146,9 @@ class RoughContact:
         self.e_star, self.eps, self.sigma, self.area, self.nlayer = e_star, eps, sigma, area, nlayer
         self._tables = {}
 
-    def solvers(self, g, n):
-        """(FP32, FP64) handles for an n x n grid (tables generated once per n)."""
+    def solvers(self, g, n, shift=0.0):
+        """(FP32, FP64, ndof[, FP32 preconditioner]) for an n x n grid
+        (tables generated once per n)."""
         if n not in self._tables:
             k = g.StiffnessKernel(self.kernel_args)
             self._tables[n] = (k.get_dimension(),) + k.phi_table(n, n, "half")
@@ -158,6 +159,8 @@ class RoughContact:
             s.set_grid_size(n, n, d)
             s.set_phi(half, "half", linf)
             out.append(s)
+        if shift > 0.0:
+            return out[0], out[1], d, out[0].make_preconditioner(shift)
         return out[0], out[1], d
 
     def problem(self, g, torch, n, load, seed, device="cuda"):
@@ -168,19 +171,20 @@ class RoughContact:
         ob.fz_ext = float(load) * self.e_star * self.area / self.nlayer
         return z, ob
 
-    def solve_many(self, g, torch, n, loads, seeds, ftol=1e-6, chunk=32, guesses=None):
-        """Solves the problems (batched, mixed precision); returns
-        (height maps, displacements, reports)."""
+    def solve_many(self, g, torch, n, loads, seeds, ftol=1e-6, chunk=32, guesses=None, shift=0.0):
+        """Solves the problems (batched, mixed precision; preconditioned CG
+        when shift > 0); returns (height maps, displacements, reports)."""
         zs, us, reps = [], [], []
         for c0 in range(0, len(loads), chunk):
             items, keep = [], []
             for i in range(c0, min(len(loads), c0 + chunk)):
-                s32, s64, d = self.solvers(g, n)
+                hs = self.solvers(g, n, shift)
+                s32, s64, d = hs[:3]
                 z, ob = self.problem(g, torch, n, loads[i], seeds[i])
                 u = torch.zeros(d, n * n, dtype=torch.float64, device="cuda")
                 if guesses is not None:
                     u.copy_(guesses[i])
-                items.append((s32, u, ob, s64))
+                items.append((s32, u, ob, s64) + tuple(hs[3:]))
                 keep.append(z)
             reps += g.minimize_batch(items, ftol=ftol, maxiter=50000)
             zs += keep
