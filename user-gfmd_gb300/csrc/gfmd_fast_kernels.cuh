@@ -12,8 +12,8 @@
 //                    positions, backward DIT FFT (digit-reversed -> natural),
 //                    so the spectrum is never reordered; energy partials are
 //                    summed in a fixed order by the last block to finish;
-//   k_row_inv_fast   rows: half spectrum gathered into digit-reversed slots,
-//                    complex-to-real pre-split in place, DIT backward FFT.
+//   k_row_inv_fast   rows: half spectrum gathered and pre-split (complex to
+//                    real) straight into digit-reversed slots, DIT backward FFT.
 //
 // Shared memory holds each transform under the XOR swizzle
 // p -> p ^ ((p >> 4) & 15), a bijection on [0, n) for n a power of two that
@@ -293,33 +293,31 @@ __global__ void __launch_bounds__(kRowThreads, sizeof(T) == 4 ? 3 : 2)
   C<T> *sm = reinterpret_cast<C<T> *>(smem_raw + (size_t)p.tsize * sizeof(E) + srev_bytes(n));
   load_table(tab, tab_g, p.tsize);
   make_srev(srev, p);
+  cp_async_wait_all();  // the twiddle table
   __syncthreads();
-  const int cs = n + 1;  // spare slot n holds X[n]
+  const int cs = n + 1;  // row pitch (one spare slot)
   const int dof = blockIdx.y;
   const int ix0 = blockIdx.x * rb;
   const int nr = rb, lgrb = __ffs(rb) - 1;
-  // gather X[ky] into digit-reversed slots; X[n] into the spare slot
-  const int tot = nr * (n + 1);
-  for (int i = threadIdx.x; i < tot; i += blockDim.x) {
-    const int ky = i >> lgrb, r = i & (nr - 1);
-    const int slot = ky == n ? n : srev[ky];
-    cp_async<sizeof(C<T>)>(&sm[(size_t)r * cs + slot], &W[((size_t)ky * g.ndof + dof) * g.nxp + ix0 + r]);
-  }
-  cp_async_wait_all();
-  __syncthreads();
-  // Z[k] = (X[k] + conj X[n-k]) + i e^{+2 pi i k/ny} (X[k] - conj X[n-k]),
-  // each thread owning the pair (k, n-k); imaginary parts of X[0], X[n] dropped
+  // Gather fused with the complex-to-real pre-split, lanes over the block's
+  // rows (16 lanes read 128 contiguous bytes of W per wavevector, and their
+  // shared-memory stores land in distinct banks):
+  //   Z[k] = (X[k] + conj X[n-k]) + i e^{+2 pi i k/ny} (X[k] - conj X[n-k]),
+  // each thread owning the pair (k, n-k); imaginary parts of X[0], X[n] dropped.
   const E *post = tab + p.tpost;
   const int half = n / 2 + 1;
+  const C<T> *Wd = W + (size_t)dof * g.nxp + ix0;
+  const size_t kstride = (size_t)g.ndof * g.nxp;
+#pragma unroll 4
   for (int i = threadIdx.x; i < nr * half; i += blockDim.x) {
-    const int r = i / half, k = i - r * half;
+    const int r = i & (nr - 1), k = i >> lgrb;
     C<T> *row = sm + (size_t)r * cs;
+    const C<T> xk = Wd[(size_t)k * kstride + r];
+    const C<T> xm = Wd[(size_t)(n - k) * kstride + r];  // k = 0: X[n]
     if (k == 0) {
-      C<T> x0 = row[0], xn = row[n];
-      row[0] = mk<T>(x0.x + xn.x, x0.x - xn.x);
+      row[0] = mk<T>(xk.x + xm.x, xk.x - xm.x);  // slot of k = 0 is 0
     } else {
       const int pk = srev[k], pm = srev[n - k];
-      C<T> xk = row[pk], xm = row[pm];
       {
         C<T> xc = cconj<T>(xm);
         C<T> A = cadd<T>(xk, xc), B = csub<T>(xk, xc);
