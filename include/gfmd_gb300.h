@@ -102,6 +102,12 @@ int gfmd_force_f32(gfmd_handle_t h, const float *d_u, float *d_f, double *d_epot
  * Replaces: GFMDSolver::get_u0 (src/main/gfmd_solver.h:89-91). */
 int gfmd_get_u0(gfmd_handle_t h, double *u0);
 
+/* Launch plan of the fused path: rows per block of the row transforms
+ * (chosen by the autotuner at gfmd_set_phi) and the Phi prefetch depth of
+ * the column kernel (fixed); 0, 0 on the general path.  No counterpart in
+ * the reference. */
+int gfmd_plan_info(gfmd_handle_t h, int *rows_per_block, int *phi_prefetch);
+
 /* Device bytes held by the handle.
  * Replaces: GFMDSolver::memory_usage (src/main/gfmd_solver.h:97). */
 int gfmd_memory_usage(gfmd_handle_t h, double *bytes);

@@ -176,3 +176,23 @@ def test_fused_energy_is_deterministic_over_repeats():
         s.force_async(u, f, ep)
         vals.add(float(ep.item()))
     assert len(vals) == 1
+
+
+def test_autotuned_plan_is_valid_and_changes_no_result(monkeypatch):
+    g = gfmd_pkg()
+    args, nx, ny = "ft fcc100 1.0 2 pair-potential 1 1.0 height 64", 256, 256
+    k = g.StiffnessKernel(args)
+    d = k.get_dimension()
+    half, linf = k.phi_table(nx, ny, "half")
+    rng = np.random.default_rng(4)
+    u = rng.normal(0.0, 0.01, (d, nx * ny))
+    outs = []
+    for tune in ("1", "0"):
+        monkeypatch.setenv("GFMD_AUTOTUNE", tune)
+        s = _solver(nx, ny, d, "f32", half, "half", linf)
+        info = s.info()
+        assert info["fused"] and info["rows_per_block"] >= 1 and 0 <= info["phi_prefetch"] <= 2
+        f = np.zeros_like(u)
+        e = s.post_force(u, f)
+        outs.append((f, e))
+    assert np.array_equal(outs[0][0], outs[1][0]) and outs[0][1] == outs[1][1]

@@ -149,6 +149,7 @@ SIGNATURES = {
     "gfmd_get_u0": [_vp, _vp],
     "gfmd_memory_usage": [_vp, _pd],
     "gfmd_solver_info": [_vp, _pi, _pi],
+    "gfmd_plan_info": [_vp, _pi, _pi],
     "gfmd_minimize": [_vp, ctypes.POINTER(Obstacle), ctypes.POINTER(MinParams), _vp,
                       ctypes.POINTER(MinReport)],
     "gfmd_make_preconditioner": [_vp, _c_dbl, ctypes.POINTER(_vp)],

@@ -9,6 +9,10 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <algorithm>
+#include <tuple>
+#include <mutex>
+#include <map>
 #include <sstream>
 #include <stdexcept>
 #include <string>
@@ -172,6 +176,7 @@ cudaError_t setup_fast(gfmd_solver *h) {
   h->p2_col = pc;
   h->ftw_col_off = col_off;
   h->fast_rb = rb;
+  h->fast_rb_max = rb;
   h->bytes += (double)nent * 16 + sizeof(unsigned);
   h->fast = true;
   return cudaSuccess;
@@ -340,6 +345,98 @@ int gfmd_memory_usage(gfmd_handle_t h, double *bytes) {
 // its Hermitian part H; p < D holds Re H_pp, then (Re H_ij, Im H_ij) for
 // i < j in row-major order.  With Phi_eff the half-spectrum real transforms
 // reproduce the real part of the reference's full complex transforms.
+// ---- plan autotuner -----------------------------------------------------
+// The fused path's launch plan has a free parameter that changes no
+// arithmetic: the rows per block of the row kernels (1/4 to 1 of the
+// largest that fits the shared-memory budget).  With the table uploaded, each candidate is timed
+// (CUDA events, best of 3 after a warm-up) on scratch inputs and the fastest
+// is kept; results are cached per (nx, ny, ndof, precision) for the
+// process.  GFMD_AUTOTUNE=0 keeps the rule-based defaults.
+namespace {
+struct PlanKey {
+  int nx, ny, ndof, prec;
+  bool operator<(const PlanKey &o) const {
+    return std::tie(nx, ny, ndof, prec) < std::tie(o.nx, o.ny, o.ndof, o.prec);
+  }
+};
+std::mutex g_plan_mu;
+std::map<PlanKey, std::pair<int, int>> g_plans;
+
+cudaError_t autotune(gfmd_solver *h) {
+  if (!h->fast || h->tuned) return cudaSuccess;
+  const char *env = getenv("GFMD_AUTOTUNE");
+  if (env && env[0] == '0') return cudaSuccess;
+  const PlanKey key{h->g.nx, h->g.ny, h->g.ndof, h->precision};
+  {
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    auto it = g_plans.find(key);
+    if (it != g_plans.end()) {
+      h->fast_rb = it->second.first;
+      h->fast_pf = it->second.second;
+      h->tuned = true;
+      return cudaSuccess;
+    }
+  }
+  const size_t n = (size_t)h->g.ndof * h->g.nx * h->g.ny;
+  const size_t es = h->precision == GFMD_PREC_F64 ? 8 : 4;
+  void *u = nullptr, *f = nullptr;
+  double *ep = nullptr;
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaMalloc(&u, n * es);
+  if (e == cudaSuccess) e = cudaMalloc(&f, n * es);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&ep, sizeof(double));
+  if (e == cudaSuccess) e = cudaMemset(u, 0, n * es);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  const int t = h->precision == GFMD_PREC_F64 ? 0 : 1;
+  const char *tr = getenv("GFMD_TRACE");
+  const bool trace = tr && tr[0] && tr[0] != '0';
+  cudaStream_t keep = h->stream;
+  const int rb0 = h->fast_rb, pf0 = h->fast_pf;
+  int best_rb = rb0, best_pf = pf0;
+  float best = 1e30f;
+  h->stream = st;
+  for (int rb = h->fast_rb_max; rb >= 1 && rb * 4 >= h->fast_rb_max && e == cudaSuccess; rb /= 2)
+    for (int pf = 1; pf <= 1 && e == cudaSuccess; pf++) {
+      h->fast_rb = rb;
+      e = gfmd::enqueue_force(h, u, t, f, t, ep);  // warm-up
+      float ms = 1e30f;
+      for (int r = 0; r < 3 && e == cudaSuccess; r++) {
+        e = cudaEventRecord(e0, st);
+        if (e == cudaSuccess) e = gfmd::enqueue_force(h, u, t, f, t, ep);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float x = 0.0f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&x, e0, e1);
+        ms = std::min(ms, x);
+      }
+      if (trace)
+        fprintf(stderr, "gfmd autotune %dx%d ndof %d: rows/block %d, Phi prefetch %d: %.4f ms\n", h->g.nx,
+                h->g.ny, h->g.ndof, rb, pf, ms);
+      if (e == cudaSuccess && ms < best) {
+        best = ms;
+        best_rb = rb;
+        best_pf = pf;
+      }
+    }
+  h->stream = keep;
+  h->fast_rb = e == cudaSuccess ? best_rb : rb0;
+  h->fast_pf = e == cudaSuccess ? best_pf : pf0;
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (st) cudaStreamDestroy(st);
+  for (void *p : {u, f, (void *)ep})
+    if (p) cudaFree(p);
+  if (e != cudaSuccess) return e;
+  h->tuned = true;
+  std::lock_guard<std::mutex> lk(g_plan_mu);
+  g_plans[key] = {h->fast_rb, h->fast_pf};
+  return cudaSuccess;
+}
+}  // namespace
+
 int gfmd_set_phi(gfmd_handle_t h, const double *phi, int layout, const double *linf) {
   if (!h || !phi) return fail(GFMD_EINVAL, "gfmd_set_phi: NULL argument");
   if (layout != GFMD_PHI_FULL && layout != GFMD_PHI_HALF)
@@ -411,6 +508,14 @@ int gfmd_set_phi(gfmd_handle_t h, const double *phi, int layout, const double *l
   CK(cudaMemcpy(h->d_linf, lf.data(), sizeof(double) * lf.size(), cudaMemcpyHostToDevice),
      "gfmd_set_phi: linf");
   h->have_phi = true;
+  CK(autotune(h), "gfmd_set_phi: plan autotuning");
+  return GFMD_OK;
+}
+
+int gfmd_plan_info(gfmd_handle_t h, int *rows_per_block, int *phi_prefetch) {
+  if (!h) return fail(GFMD_EINVAL, "gfmd_plan_info: NULL handle");
+  if (rows_per_block) *rows_per_block = h->fast ? h->fast_rb : 0;
+  if (phi_prefetch) *phi_prefetch = h->fast ? h->fast_pf : 0;
   return GFMD_OK;
 }
 
@@ -516,6 +621,11 @@ int gfmd_make_preconditioner(gfmd_handle_t h, double shift, gfmd_handle_t *out) 
     return cuda_fail(e, "gfmd_make_preconditioner: upload");
   }
   p->have_phi = true;
+  e = autotune(p);
+  if (e != cudaSuccess) {
+    release(p);
+    return cuda_fail(e, "gfmd_make_preconditioner: plan autotuning");
+  }
   *out = p;
   return GFMD_OK;
 }

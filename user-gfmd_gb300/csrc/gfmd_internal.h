@@ -83,7 +83,10 @@ struct gfmd_solver {
   // fused power-of-two path (see gfmd_fast_kernels.cuh)
   bool fast = false;
   gfmd::P2Plan p2_row{}, p2_col{};
-  int fast_rb = 8;           // rows per block of the row kernels
+  int fast_rb = 8;           // rows per block of the row kernels (tuned)
+  int fast_rb_max = 8;       // largest that fits the shared-memory budget
+  int fast_pf = 1;           // Phi prefetch depth of the column kernel (rounds)
+  bool tuned = false;
   void *d_ftw = nullptr;     // octant tables of w_ny and w_nx (see gfmd_fast_kernels.cuh)
   int ftw_col_off = 0;       // entry offset of the w_nx table
   unsigned *d_counter = nullptr;  // blocks finished in the column kernel

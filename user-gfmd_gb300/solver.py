@@ -225,7 +225,10 @@ class GFMDSolverGB300:
         """Launches per force evaluation and whether the fused path runs."""
         n, f = ctypes.c_int(), ctypes.c_int()
         check(lib().gfmd_solver_info(self._handle(), ctypes.byref(n), ctypes.byref(f)))
-        return {"launches_per_eval": n.value, "fused": bool(f.value)}
+        rb, pf = ctypes.c_int(), ctypes.c_int()
+        check(lib().gfmd_plan_info(self._handle(), ctypes.byref(rb), ctypes.byref(pf)))
+        return {"launches_per_eval": n.value, "fused": bool(f.value),
+                "rows_per_block": rb.value, "phi_prefetch": pf.value}
 
     def get_nxy_loc(self) -> int:
         return self.nx * self.ny
