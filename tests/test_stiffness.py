@@ -89,3 +89,22 @@ def test_phi_is_hermitian_and_inversion_symmetric():
     P = phi.reshape(nx, ny, 12, 12)
     Pm = P[(-np.arange(nx)) % nx][:, (-np.arange(ny)) % ny]
     assert np.abs(Pm - np.conj(P)).max() < 1e-15
+
+
+def test_phi_table_cache_round_trip(tmp_path):
+    g = gfmd_pkg()
+    k = g.StiffnessKernel("ft fcc100 1.0 2 pair-potential 1 1.0 height 16")
+    phi, linf = k.phi_table_cached(16, 12, str(tmp_path))
+    files = list(tmp_path.iterdir())
+    assert len(files) == 1
+    phi2, linf2 = k.phi_table_cached(16, 12, str(tmp_path))  # from the file
+    assert np.array_equal(phi, phi2) and np.array_equal(linf, linf2)
+    ref, _ = k.phi_table(16, 12, "half")
+    assert np.array_equal(phi, ref)
+    # a different kernel, grid or layout is a different key; a corrupt file is a miss
+    assert g.PhiTableFile.read(str(files[0]), "ft fcc100 1.0 2 pair-potential 1 1.0 height 17", 16, 12, "half") is None
+    assert g.PhiTableFile.read(str(files[0]), k.args, 16, 14, "half") is None
+    files[0].write_bytes(files[0].read_bytes()[:100])
+    assert g.PhiTableFile.read(str(files[0]), k.args, 16, 12, "half") is None
+    phi3, _ = k.phi_table_cached(16, 12, str(tmp_path))
+    assert np.array_equal(phi3, ref)

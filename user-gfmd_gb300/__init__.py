@@ -9,6 +9,7 @@ from ._lib import (GFMD_OBST_MAP_EXP, GFMD_OBST_NONE, GFMD_OBST_SPHERE_EXP,  # n
                    GFMD_OBST_SPHERE_LJ)
 from .solver import (  # noqa: F401
     GFMDSolverGB300,
+    PhiTableFile,
     StiffnessKernel,
     gfmd_solver_factory,
     minimize_batch,
@@ -27,6 +28,7 @@ __all__ = [
     "map_obstacle",
     "GFMDSolverGB300",
     "StiffnessKernel",
+    "PhiTableFile",
     "gfmd_solver_factory",
     "minimize_batch",
     "stiffness_kernel_factory",

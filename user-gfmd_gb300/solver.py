@@ -17,6 +17,9 @@ Everything runs through the C ABI of ``libgfmd_gb300.so``; errors surface as
 from __future__ import annotations
 
 import ctypes
+import hashlib
+import os
+import struct
 
 import numpy as np
 
@@ -90,9 +93,78 @@ class StiffnessKernel:
         check(lib().gfmd_kernel_phi(self._h, nx, ny, lay, _ptr(phi), _ptr(linf), nthreads))
         return phi, linf
 
+    def phi_table_cached(self, nx: int, ny: int, cache_dir: str, layout: str = "half", nthreads: int = 0):
+        """``phi_table`` through an on-disk cache (``PhiTableFile``): the file
+        for (kernel arguments, nx, ny, layout) is read if present and valid,
+        else the table is generated and written."""
+        path = PhiTableFile.path(cache_dir, self.args, nx, ny, layout)
+        got = PhiTableFile.read(path, self.args, nx, ny, layout)
+        if got is not None:
+            return got
+        phi, linf = self.phi_table(nx, ny, layout, nthreads)
+        PhiTableFile.write(path, self.args, nx, ny, layout, phi, linf)
+        return phi, linf
+
     def get_force_at_gamma_point(self) -> np.ndarray:
         _, linf = self.phi_table(1, 1, "full")
         return linf
+
+
+class PhiTableFile:
+    """Versioned binary Phi(q) table: a 64-byte little-endian header
+    (magic b"GFMDPHI\\0", format version, nx, ny, ndof, layout 0 = half /
+    1 = full, payload bytes, SHA-256 prefix of the kernel arguments), the
+    complex128 table as ``phi_table`` returns it, then linf (float64).
+    Files are written to a temporary name and renamed, so a reader never
+    sees a partial table; a header that does not match is a cache miss."""
+
+    MAGIC = b"GFMDPHI\0"
+    VERSION = 1
+    _HDR = struct.Struct("<8sIiiiiQ24s")
+
+    @staticmethod
+    def key(args: str, nx: int, ny: int, layout: str) -> bytes:
+        canon = " ".join(args.split())
+        return hashlib.sha256(f"{canon}|{nx}|{ny}|{layout}".encode()).digest()[:24]
+
+    @classmethod
+    def path(cls, cache_dir: str, args: str, nx: int, ny: int, layout: str) -> str:
+        return os.path.join(cache_dir, f"phi_{cls.key(args, nx, ny, layout).hex()[:32]}_{nx}x{ny}_{layout}.bin")
+
+    @classmethod
+    def write(cls, path: str, args: str, nx: int, ny: int, layout: str, phi, linf) -> None:
+        phi = np.ascontiguousarray(phi, np.complex128)
+        linf = np.ascontiguousarray(linf, np.float64)
+        hdr = cls._HDR.pack(cls.MAGIC, cls.VERSION, nx, ny, phi.shape[-1], 0 if layout == "half" else 1,
+                            phi.nbytes + linf.nbytes, cls.key(args, nx, ny, layout))
+        os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
+        tmp = f"{path}.tmp{os.getpid()}"
+        with open(tmp, "wb") as fh:
+            fh.write(hdr.ljust(64, b"\0"))
+            fh.write(phi.tobytes())
+            fh.write(linf.tobytes())
+        os.replace(tmp, path)
+
+    @classmethod
+    def read(cls, path: str, args: str, nx: int, ny: int, layout: str):
+        if not os.path.exists(path):
+            return None
+        with open(path, "rb") as fh:
+            raw = fh.read(64)
+            if len(raw) < 64:
+                return None
+            magic, ver, fx, fy, nd, lay, nb, key = cls._HDR.unpack(raw[:cls._HDR.size])
+            if (magic != cls.MAGIC or ver != cls.VERSION or (fx, fy) != (nx, ny)
+                    or lay != (0 if layout == "half" else 1) or key != cls.key(args, nx, ny, layout)):
+                return None
+            body = fh.read()
+        shape = (nx, ny // 2 + 1, nd, nd) if layout == "half" else (nx * ny, nd, nd)
+        nphi = int(np.prod(shape)) * 16
+        if len(body) != nb or nb != nphi + (nd // 3) * 8:
+            return None
+        phi = np.frombuffer(body[:nphi], np.complex128).reshape(shape).copy()
+        linf = np.frombuffer(body[nphi:], np.float64).copy()
+        return phi, linf
 
 
 def stiffness_kernel_factory(keyword: str, *args: str) -> StiffnessKernel:
