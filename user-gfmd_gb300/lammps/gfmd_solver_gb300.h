@@ -1,0 +1,50 @@
+// USER-GFMD solver style "static/gb300": the reference's GFMDSolver interface
+// (src/main/gfmd_solver.h:34-123) implemented over the C ABI of
+// libgfmd_gb300 (include/gfmd_gb300.h).  Drop into USER-GFMD's src/solvers/
+// and register in gfmd_solver_factory (src/main/gfmd_solver.cpp:209-256):
+//   else if (!strcmp(solver_name, "static/gb300"))
+//     solver = new GFMDSolverGB300(lmp, narg, carg, arg);
+// Input syntax is unchanged (`fix ... gfmd ... solver static/gb300`, or the
+// `static` style with `-sf gb300`).  One rank owns the whole grid.
+#ifndef GFMD_SOLVER_GB300_H
+#define GFMD_SOLVER_GB300_H
+
+#include "gfmd_gb300.h"
+#include "gfmd_solver.h"
+
+namespace LAMMPS_NS {
+
+class GFMDSolverGB300 : public GFMDSolver {
+ public:
+  // Optional argument (carg points at it in arg): "f32" for the FP32
+  // compensated-twiddle evaluation; FP64 otherwise.
+  GFMDSolverGB300(LAMMPS *lmp, int narg, int *carg, char **arg);
+  ~GFMDSolverGB300() override;
+
+  void set_grid_size(int nx, int ny, int ndof) override;
+  // GFMDSolverStatic::set_kernel (src/solvers/gfmd_solver_static.cpp:90-136):
+  // the table from fill_phi_buffer, uploaded once
+  void set_kernel(StiffnessKernel *kernel, bool normalize = true) override;
+  // GFMDSolverStatic::post_force (gfmd_solver_static.cpp:145-249); u and f
+  // are FixGFMD's contiguous double** [ndof][nxy] (memory->create)
+  double post_force(void *u, void *f, char *dump_prefix) override;
+  // GFMDSolverStatic::prec_gradient (gfmd_solver_static.cpp:253-269) for a
+  // diagonal constant Cavg = c I: gP = N^2 (Phi + N c)^{-1} g, the operator the
+  // reference applies with its 1/N-scaled table and unnormalised transforms
+  void prec_gradient(double *cavg, double **g, double **gP) override;
+  double memory_usage() override;
+
+  gfmd_handle_t handle() const { return h_; }
+
+ private:
+  gfmd_handle_t h_ = nullptr;
+  gfmd_handle_t pre_ = nullptr;  // preconditioner of the last shift
+  double pre_shift_ = -1.0;
+  int precision_ = GFMD_PREC_F64;
+  double *scratch_ = nullptr;
+  void check(int rc);
+};
+
+}  // namespace LAMMPS_NS
+
+#endif
