@@ -1,13 +1,14 @@
 // Damped velocity Verlet (fix nve with linear damping; gamma = 0 is fix nve)
 // on the GPU, all steps in one CUDA graph:
 //   prologue   f_el = F_el(u); k_second (no kick): f = f_el + F_w(u) + f_ext,
-//              E(0) = E_el + E_w + E_ext + |v|^2 / 2
+//              E(0) = E_el + E_w + E_ext + |v|^2 / 2, then the first half
+//              of step 1: v_h = v + dt/2 (f - gamma v); u += dt v_h
 //   WHILE(step < nsteps) {
-//     k_first    v_h = v + dt/2 (f - gamma v); u += dt v_h
 //     f_el = F_el(u)                 (the handle's force evaluation)
 //     k_second   f = f_el + F_w(u) + f_ext; v = (v_h + dt/2 f) / (1 + dt gamma/2);
 //                E(step) in FP64 by the last block, which also advances the
-//                step and sets the loop condition
+//                step and sets the loop condition; then, unless this was the
+//                last step, the first half of the next one in the same pass
 //   }
 // The state is held in the handle's precision: FP32 handles run FP32 u, v, f
 // with FP32 forces and FP64 energy reductions (kinetic energy as a
@@ -39,18 +40,6 @@ struct DynCtl {
   int status;  // 0 running/ok, 3 non-finite energy
   unsigned int counter;
 };
-
-template <typename T>
-__global__ void __launch_bounds__(kT) k_first(size_t n, T *__restrict__ u, T *__restrict__ v,
-                                               const T *__restrict__ f, T dt, T gamma) {
-  const T hdt = (T)0.5 * dt;
-  for (size_t i = blockIdx.x * (size_t)kT + threadIdx.x; i < n; i += (size_t)gridDim.x * kT) {
-    const T vv = v[i];
-    const T vh = vv + hdt * (f[i] - gamma * vv);
-    v[i] = vh;
-    u[i] = u[i] + dt * vh;
-  }
-}
 
 // Obstacle force on atom (site s, layer l) into fw, energy into e.
 template <typename T>
@@ -95,8 +84,11 @@ __device__ __forceinline__ bool atom_wall(const Obst &o, int ix, int iy, int l, 
 
 // f = f_el + F_w(u) + f_ext; with kick, v = (v + dt/2 f) / (1 + dt gamma/2);
 // energy of the state into energies[step] (advancing step first with kick).
+// Unless this was the last step, the first half of the next step follows in
+// the same pass (v_h = v + dt/2 (f - gamma v), u += dt v_h), so a step costs
+// one evaluation and one pass over the state.
 template <typename T>
-__global__ void __launch_bounds__(kT) k_second(Obst o, Geom gm, const T *__restrict__ u, T *__restrict__ v,
+__global__ void __launch_bounds__(kT) k_second(Obst o, Geom gm, T *__restrict__ u, T *__restrict__ v,
                                                 const T *__restrict__ fel, T *__restrict__ f, T dt, T gamma,
                                                 int kick, const double *__restrict__ d_eel,
                                                 double *__restrict__ energies, double *__restrict__ part,
@@ -107,6 +99,8 @@ __global__ void __launch_bounds__(kT) k_second(Obst o, Geom gm, const T *__restr
   const T hdt = (T)0.5 * dt;
   const T den = (T)1 / ((T)1 + hdt * gamma);
   const bool obst = o.kind != GFMD_OBST_NONE || o.fz_ext != 0.0;
+  // read before the last block advances the step: is there a next step?
+  const bool next = (ctl->step + (kick ? 1 : 0)) < ctl->nsteps;
   Dot<T> vv, ff;
   double ew = 0.0;
   float fm = 0.0f;
@@ -122,13 +116,17 @@ __global__ void __launch_bounds__(kT) k_second(Obst o, Geom gm, const T *__restr
         if (hit) fv = (T)((double)fv + fw[c]);
         f[idx] = fv;
         T vn = v[idx];
-        if (kick) {
-          vn = (vn + hdt * fv) * den;
-          v[idx] = vn;
-        }
+        if (kick) vn = (vn + hdt * fv) * den;
         vv.add(vn, vn);
         ff.add(fv, fv);
         fm = fmaxf(fm, fabsf((float)fv));
+        if (next) {
+          const T vh = vn + hdt * (fv - gamma * vn);
+          v[idx] = vh;
+          u[idx] = u[idx] + dt * vh;
+        } else if (kick) {
+          v[idx] = vn;
+        }
       }
     }
   }
@@ -268,7 +266,6 @@ cudaError_t run_t(gfmd_solver *h, const Obst &o0, double dt, double gamma, int n
   if (e == cudaSuccess) e = e2;
   if (e != cudaSuccess) return e;
   DT_CHECK(cudaStreamBeginCaptureToGraph(b.cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-  k_first<T><<<nblk * 4, kT, 0, b.cs>>>(n, u, v, f, (T)dt, (T)gamma);
   e = eval_dyn(h, b.cs, u, fel, t, scal);
   if (e == cudaSuccess) {
     k_second<T><<<nblk, kT, 0, b.cs>>>(o, gm, u, v, fel, f, (T)dt, (T)gamma, 1, scal, en, part, ctl, scal + 1, hc, 1);
