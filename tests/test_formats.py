@@ -1,0 +1,80 @@
+"""Reference file formats: height maps (FixWallMap::read_map/write_map) and
+the real- and reciprocal-space grid dumps (FixGFMD::dump,
+GFMDSolverFFT::dump)."""
+import importlib
+
+import numpy as np
+import pytest
+
+from conftest import gfmd_pkg, half_to_full, oracle_post_force
+
+fmt = importlib.import_module("user-gfmd_gb300.formats")
+
+
+def test_map_round_trip_and_reference_column_rule(tmp_path):
+    rng = np.random.default_rng(1)
+    z = rng.normal(0, 1, (12, 12))
+    p = tmp_path / "map.matrix"
+    fmt.write_map(str(p), z)
+    lines = p.read_text().splitlines()
+    assert len(lines) == 12 and lines[0].endswith(" ") and "%f " % z[0, 0] in lines[0]
+    back = fmt.read_map(str(p))
+    assert back.shape == (12, 12)
+    assert np.allclose(back, z, atol=5e-7)  # "%f" keeps six decimals
+    # the reader counts columns in the first line and assumes a square map
+    p.write_text("1 2 3\n4 5 6\n7 8 9\n10 11\n")
+    assert np.array_equal(fmt.read_map(str(p)), np.arange(1, 10, dtype=float).reshape(3, 3))
+    p.write_text("1 2 3")
+    with pytest.raises(ValueError):
+        fmt.read_map(str(p))
+
+
+def test_real_space_dump_layout(tmp_path):
+    nx, ny, d = 4, 3, 3
+    rng = np.random.default_rng(2)
+    u = rng.normal(0, 1, (d, nx * ny))
+    f = rng.normal(0, 1, (d, nx * ny))
+    base = fmt.write_real_space_dump(str(tmp_path / "gfmd"), 100, u, f, nx, ny)
+    assert base.endswith("gfmd.100")
+    first = (tmp_path / "gfmd.100.r.u0.out").read_text().splitlines()
+    assert len(first) == ny  # one line per iy, nx values
+    assert first[0] == "".join(" %20.10e " % u[0, ix * ny] for ix in range(nx))
+    for i in range(d):
+        assert np.allclose(fmt.read_grid(f"{base}.r.u{i}.out", nx, ny), u[i], rtol=1e-9)
+        assert np.allclose(fmt.read_grid(f"{base}.r.f{i}.out", nx, ny), f[i], rtol=1e-9)
+    assert np.allclose(fmt.read_grid(f"{base}.r.e.out", nx, ny), (u * f).sum(0), rtol=1e-9)
+
+
+def test_q_space_dump_matches_the_force_evaluation(tmp_path):
+    nx, ny = 8, 6
+    k = gfmd_pkg().StiffnessKernel("ft fcc100 1.0 2 pair-potential 1 1.0 height 16")
+    d = k.get_dimension()
+    half, linf = k.phi_table(nx, ny, "half")
+    full = half_to_full(half, nx, ny)
+    assert np.allclose(fmt.half_to_full(half, nx, ny), full)
+    rng = np.random.default_rng(3)
+    u = rng.normal(0, 0.1, (d, nx * ny))
+    fmt.write_q_space_dump(str(tmp_path / "dq"), u, full, nx, ny)
+    Fr = np.stack([fmt.read_grid(str(tmp_path / f"dq.q.f{i}.real.out"), nx, ny) for i in range(d)])
+    Fi = np.stack([fmt.read_grid(str(tmp_path / f"dq.q.f{i}.imag.out"), nx, ny) for i in range(d)])
+    # f(r) = -sum_q F(q) exp(+i q.r) is the oracle force (no gamma-point term)
+    fq = -np.fft.ifft2((Fr + 1j * Fi).reshape(d, nx, ny)).real.reshape(d, nx * ny) * nx * ny
+    f_ref, _, _ = oracle_post_force(full, np.zeros(d // 3), u, nx, ny)
+    assert np.allclose(fq, f_ref, rtol=1e-8, atol=1e-9 * np.abs(f_ref).max())  # 11 digits in the file
+    e = fmt.read_grid(str(tmp_path / "dq.q.e.out"), nx, ny).sum()
+    _, E, _ = oracle_post_force(full, np.zeros(d // 3), u, nx, ny)
+    assert abs(0.5 * e - E) <= 1e-8 * abs(E)  # E = 1/2 sum Re(u conj F) with no linf
+
+
+@pytest.mark.gpu
+def test_post_force_writes_the_q_space_dump(tmp_path):
+    nx, ny = 16, 12
+    g = gfmd_pkg()
+    k = g.StiffnessKernel("ft fcc100 1.0 2 pair-potential 1 1.0 height 16")
+    s = g.gfmd_solver_factory("static")
+    s.set_grid_size(nx, ny, k.get_dimension())
+    s.set_kernel(k)
+    u = np.random.default_rng(4).normal(0, 0.1, (k.get_dimension(), nx * ny))
+    f = np.empty_like(u)
+    s.post_force(u, f, dump_prefix=str(tmp_path / "step"))
+    assert (tmp_path / "step.q.u0.real.out").exists() and (tmp_path / "step.q.e.out").exists()

@@ -1,0 +1,118 @@
+"""File formats of the reference that sit either side of the hot path.
+
+* Height maps (FixWallMap::read_map / write_map,
+  src/extras/fix_wall_map.cpp:1121-1213): whitespace-separated text, one
+  line per x, ny values per line; the reader counts the columns of the
+  first line (a token starts with an alphanumeric character, '-' or 'e'
+  after a blank), assumes a square map and reads nx*nx values with x
+  slow; the writer prints "%f " per value and a newline per x.
+* Real-space grid dumps (FixGFMD::dump, src/main/fix_gfmd.cpp:1948-2009):
+  for dump prefix P and step s, files P.s.r.u<i>.out and P.s.r.f<i>.out per
+  degree of freedom and P.s.r.uP.out, .fP.out, .e.out (|u|^2, |f|^2, u.f per
+  site); each line is one y (iy), each value " %20.10e " over x.
+* Reciprocal-space dumps written by the solver when post_force gets a dump
+  prefix (GFMDSolverFFT::dump, src/solvers/gfmd_solver_fft.cpp:209-285):
+  P.q.u<i>.real.out / .imag.out with u(q) (forward transform, unscaled),
+  P.q.f<i>.real.out / .imag.out with F(q) = Phi(q) u(q) (the table scaled by
+  1/(nx ny)), and P.q.uP.out, .fP.out, .e.out with sum |u|^2, sum |F|^2 and
+  Re sum u conj(F) per wavevector; same line layout.
+
+Grids here are [ndof][nx*ny] arrays with index ix*ny + iy, as on the solver.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def _count_columns(line: str) -> int:
+    n, last = 0, " "
+    for c in line:
+        if (c.isalnum() or c in "-e") and last == " ":
+            n += 1
+        last = c
+    return n
+
+
+def read_map(path: str) -> np.ndarray:
+    """Height map as FixWallMap::read_map reads it: [nx, nx], x slow."""
+    with open(path) as fh:
+        first = fh.readline()
+        if not first.endswith("\n"):
+            raise ValueError(f"{path}: could not read map file")
+        nx = _count_columns(first.rstrip("\n"))
+        if nx <= 0:
+            raise ValueError(f"{path}: no columns in the first line")
+        values = np.array((first + fh.read()).split(), dtype=np.float64)
+    if values.size < nx * nx:
+        raise ValueError(f"{path}: error reading map file ({values.size} values for {nx} x {nx})")
+    return values[:nx * nx].reshape(nx, nx)
+
+
+def write_map(path: str, zmap) -> None:
+    """FixWallMap::write_map: "%f " per value, one line per x."""
+    z = np.asarray(zmap, np.float64)
+    with open(path, "w") as fh:
+        for row in z:
+            fh.write("".join("%f " % v for v in row))
+            fh.write("\n")
+
+
+def _write_grid(path: str, values, nx: int, ny: int) -> None:
+    g = np.asarray(values, np.float64).reshape(nx, ny)
+    with open(path, "w") as fh:
+        for iy in range(ny):
+            fh.write("".join(" %20.10e " % v for v in g[:, iy]))
+            fh.write("\n")
+
+
+def read_grid(path: str, nx: int, ny: int) -> np.ndarray:
+    """One dump file back as [nx*ny] (index ix*ny + iy)."""
+    a = np.loadtxt(path, ndmin=2)
+    if a.shape != (ny, nx):
+        raise ValueError(f"{path}: expected {ny} lines of {nx} values, got {a.shape}")
+    return a.T.reshape(nx * ny).copy()
+
+
+def write_real_space_dump(prefix: str, step: int, u, f, nx: int, ny: int) -> str:
+    """FixGFMD::dump; returns the file prefix P.s."""
+    u = np.asarray(u, np.float64)
+    f = np.asarray(f, np.float64)
+    base = f"{prefix}.{step}"
+    for i in range(u.shape[0]):
+        _write_grid(f"{base}.r.u{i}.out", u[i], nx, ny)
+        _write_grid(f"{base}.r.f{i}.out", f[i], nx, ny)
+    _write_grid(f"{base}.r.uP.out", (u * u).sum(0), nx, ny)
+    _write_grid(f"{base}.r.fP.out", (f * f).sum(0), nx, ny)
+    _write_grid(f"{base}.r.e.out", (u * f).sum(0), nx, ny)
+    return base
+
+
+def write_q_space_dump(dump_prefix: str, u, phi_full, nx: int, ny: int) -> None:
+    """GFMDSolverFFT::dump for displacements u [ndof][nx*ny] and the full
+    Phi table [nx*ny][ndof][ndof] scaled by 1/(nx ny)."""
+    u = np.asarray(u, np.float64)
+    d = u.shape[0]
+    uq = np.fft.fft2(u.reshape(d, nx, ny)).reshape(d, nx * ny)   # exp(-i q.r), unscaled
+    Fq = np.einsum("qij,jq->iq", np.asarray(phi_full), uq)
+    for i in range(d):
+        _write_grid(f"{dump_prefix}.q.u{i}.real.out", uq[i].real, nx, ny)
+        _write_grid(f"{dump_prefix}.q.u{i}.imag.out", uq[i].imag, nx, ny)
+        _write_grid(f"{dump_prefix}.q.f{i}.real.out", Fq[i].real, nx, ny)
+        _write_grid(f"{dump_prefix}.q.f{i}.imag.out", Fq[i].imag, nx, ny)
+    _write_grid(f"{dump_prefix}.q.uP.out", (np.abs(uq) ** 2).sum(0), nx, ny)
+    _write_grid(f"{dump_prefix}.q.fP.out", (np.abs(Fq) ** 2).sum(0), nx, ny)
+    _write_grid(f"{dump_prefix}.q.e.out", (uq * np.conj(Fq)).sum(0).real, nx, ny)
+
+
+def half_to_full(half, nx: int, ny: int) -> np.ndarray:
+    """[nx, ny//2+1, d, d] half-spectrum table -> [nx*ny, d, d] full table,
+    Phi(-q) = conj Phi(q) for the wavevectors the half spectrum omits."""
+    half = np.asarray(half)
+    d = half.shape[-1]
+    full = np.empty((nx, ny, d, d), dtype=np.complex128)
+    nyc = ny // 2 + 1
+    full[:, :nyc] = half
+    kx = (-np.arange(nx)) % nx
+    for ky in range(nyc, ny):
+        full[:, ky] = np.conj(half[kx, ny - ky])
+    return full.reshape(nx * ny, d, d)

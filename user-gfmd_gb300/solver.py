@@ -208,9 +208,13 @@ class GFMDSolverGB300:
             phi = phi * float(self.nx * self.ny)
         self.set_phi(phi, "half", linf)
 
+    # host copy of the table kept for q-space dumps up to this size
+    DUMP_TABLE_BYTES = 256 << 20
+
     def set_phi(self, phi: np.ndarray, layout: str = "full", linf=None) -> None:
         """Upload a table already scaled by 1/(nx*ny)."""
         phi = np.ascontiguousarray(phi, dtype=np.complex128)
+        self._dump_table = (phi, layout) if phi.nbytes <= self.DUMP_TABLE_BYTES else None
         lay = _lib.GFMD_PHI_FULL if layout == "full" else _lib.GFMD_PHI_HALF
         lf = None if linf is None else np.ascontiguousarray(linf, dtype=np.float64)
         check(lib().gfmd_set_phi(self._handle(), _ptr(phi), lay, None if lf is None else _ptr(lf)))
@@ -220,8 +224,19 @@ class GFMDSolverGB300:
         check(lib().gfmd_set_stream(self._handle(), addr))
 
     def post_force(self, u, f, dump_prefix=None) -> float:
+        """Elastic forces of u into f, energy returned.  With ``dump_prefix``
+        the reciprocal-space dump of GFMDSolverFFT::dump is written as well
+        (formats.write_q_space_dump; needs the table on the host)."""
         if dump_prefix is not None:
-            raise GFMDError(_lib.GFMD_EINVAL, "q-space dumps are not supported by this solver")
+            tab = getattr(self, "_dump_table", None)
+            if tab is None:
+                raise GFMDError(_lib.GFMD_EINVAL, "q-space dumps need a table of at most "
+                                f"{self.DUMP_TABLE_BYTES >> 20} MiB kept by set_phi")
+            from . import formats
+            phi, layout = tab
+            full = formats.half_to_full(phi, self.nx, self.ny) if layout == "half" else phi
+            uh = u.detach().cpu().numpy() if hasattr(u, "detach") else np.asarray(u)
+            formats.write_q_space_dump(dump_prefix, uh, full, self.nx, self.ny)
         e = ctypes.c_double()
         if _is_device(u) and _is_device(f):
             check(lib().gfmd_post_force(self._handle(), _ptr(u), _ptr(f), ctypes.byref(e)))
