@@ -273,6 +273,29 @@ int gfmd_kernel_info(gfmd_kernel_t k, int *ndof, int *height);
 int gfmd_kernel_phi(gfmd_kernel_t k, int nx, int ny, int layout, double *phi,
                     double *linf, int nthreads);
 
+/* ---- Atom list <-> grid -------------------------------------------------
+ * For a fix that keeps its atoms on the device (one rank owning the grid).
+ * gid: [natoms][3] ints (ix, iy, iu) as atom->gid; x, xeq, v: [natoms][3].
+ * Replaces: FixGFMD::pre_force, orthogonal box (src/main/fix_gfmd.cpp:659-858):
+ * u[3 iu + c][ix' ny + iy'] = x - xeq (minimum image in x, y), with
+ * ix' = (ix - dxshift) mod nx, iy' = (iy - dyshift) mod ny; v (may be NULL)
+ * copied into vgrid the same way.  d_slot_count (may be NULL): [ndof/3][nx*ny]
+ * int scratch that, when given, checks that atoms and slots match one to one.
+ * status (host, may be NULL): [0] atoms with iu outside [0, ndof/3), [1] empty
+ * slots, [2] slots filled twice or more (-1 without d_slot_count).
+ * GFMD_EINVAL when any of them is nonzero.  Synchronizes the stream. */
+int gfmd_atoms_to_grid(int natoms, const double *d_x, const double *d_xeq, const double *d_v,
+                       const int *d_gid, int nx, int ny, int ndof, double xprd, double yprd,
+                       int dxshift, int dyshift, double *d_u, double *d_vgrid, int *d_slot_count,
+                       int *status, void *cuda_stream);
+/* Replaces: FixGFMD::grid_to_list (src/main/fix_gfmd.cpp:952-1074): the grid
+ * force f[3 iu + c][ix ny + iy] of every atom into (accumulate: added to)
+ * d_fatoms [natoms][3]; fsum (host, may be NULL) gets the force summed over
+ * the atoms (FP64, fixed order).  GFMD_EINVAL for ids outside the grid.
+ * Synchronizes the stream. */
+int gfmd_grid_to_atoms(int natoms, const int *d_gid, const double *d_f, int nx, int ny, int ndof,
+                       double *d_fatoms, int accumulate, double *fsum, void *cuda_stream);
+
 /* ---- Self-affine rough surfaces ------------------------------------------
  * No counterpart in the reference, which only reads height maps
  * (FixWallMap, src/extras/fix_wall_map.cpp:1123-1190) and low-pass filters

@@ -10,6 +10,8 @@ from ._lib import (GFMD_OBST_MAP_EXP, GFMD_OBST_NONE, GFMD_OBST_SPHERE_EXP,  # n
 from .solver import (  # noqa: F401
     GFMDSolverGB300,
     PhiTableFile,
+    atoms_to_grid,
+    grid_to_atoms,
     StiffnessKernel,
     gfmd_solver_factory,
     minimize_batch,
@@ -29,6 +31,8 @@ __all__ = [
     "GFMDSolverGB300",
     "StiffnessKernel",
     "PhiTableFile",
+    "atoms_to_grid",
+    "grid_to_atoms",
     "gfmd_solver_factory",
     "minimize_batch",
     "stiffness_kernel_factory",

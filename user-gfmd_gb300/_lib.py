@@ -157,6 +157,9 @@ SIGNATURES = {
     "gfmd_run_dynamics": [_vp, ctypes.POINTER(Obstacle), _c_dbl, _c_dbl, _c_int, _vp, _vp, _vp,
                           ctypes.POINTER(MinReport)],
     "gfmd_post_force_noalloc": [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp],
+    "gfmd_atoms_to_grid": [_c_int, _vp, _vp, _vp, _vp, _c_int, _c_int, _c_int, _c_dbl, _c_dbl, _c_int,
+                           _c_int, _vp, _vp, _vp, _pi, _vp],
+    "gfmd_grid_to_atoms": [_c_int, _vp, _vp, _c_int, _c_int, _c_int, _vp, _c_int, _pd, _vp],
     "gfmd_rough_surface": [_c_int, _c_int, ctypes.POINTER(SurfaceParams), _vp, _vp],
     "gfmd_ws_create": [_c_int, _c_int, _c_int, ctypes.c_ulonglong, ctypes.POINTER(_vp)],
     "gfmd_ws_destroy": [_vp],

@@ -382,6 +382,34 @@ def minimize_batch(problems, ftol: float = 1e-6, maxiter: int = 0, recompute: in
     return reports
 
 
+def atoms_to_grid(x, xeq, gid, nx, ny, ndof, box, u, v=None, vgrid=None, shift=(0, 0), check=True,
+                  stream=0):
+    """gfmd_atoms_to_grid on CUDA tensors: x, xeq, v [natoms, 3] float64, gid
+    [natoms, 3] int32, u (and vgrid) [ndof, nx*ny] float64.  With ``check``
+    the atoms must fill the grid slots one to one.  Returns the status."""
+    import torch
+    st = (ctypes.c_int * 3)()
+    slots = torch.empty((ndof // 3) * nx * ny, dtype=torch.int32, device=u.device) if check else None
+    rc = lib().gfmd_atoms_to_grid(x.shape[0], _ptr(x), _ptr(xeq), _ptr(v) if v is not None else None, _ptr(gid),
+                                  nx, ny, ndof, float(box[0]), float(box[1]), int(shift[0]), int(shift[1]),
+                                  _ptr(u), _ptr(vgrid) if vgrid is not None else None,
+                                  _ptr(slots) if slots is not None else None, st, stream)
+    status = {"bad_ids": st[0], "empty_slots": st[1], "duplicate_slots": st[2]}
+    if rc != _lib.GFMD_OK:
+        err = GFMDError(rc, lib().gfmd_last_error().decode(errors="replace"))
+        err.status = status
+        raise err
+    return status
+
+
+def grid_to_atoms(gid, f, nx, ny, ndof, fatoms, accumulate=False, stream=0):
+    """gfmd_grid_to_atoms on CUDA tensors; returns the summed force (3,)."""
+    s = (ctypes.c_double * 3)()
+    check(lib().gfmd_grid_to_atoms(gid.shape[0], _ptr(gid), _ptr(f), nx, ny, ndof, _ptr(fatoms),
+                                   1 if accumulate else 0, s, stream))
+    return np.array(list(s))
+
+
 _SOLVERS = {"static": "f64", "static/gb300": "f64", "static/gb300/f32": "f32"}
 
 
