@@ -35,6 +35,10 @@ CASES = [
     ("fcc111_h128_64x37", "ft fcc111 1 1.0 pair-potential 1 1.0 height 128", 64, 37, False),
     ("sc100_nnn_h128_32x32", "ft sc100 1 1.0 pair-potential 2 1.0 1.0 height 128", 32, 32, False),
     ("fcc100x2_h64_36x36", "ft fcc100 1.0 2 pair-potential 1 1.0 height 64", 36, 36, False),
+    # the analytic styles (SC100StiffnessKernel, FCC100StiffnessKernel)
+    ("sc100_analytic_h16_9x7", "sc100 height 16", 9, 7, True),
+    ("fcc100x4_analytic_h10_6x8", "fcc100 4 1.0 0.3 0.1 height 10", 6, 8, True),
+    ("fcc100x2_kappa_normal_8x8", "fcc100 x 2 1.0 0.2 0.3 0.1 0.1 0.05 normal -1 height 10", 8, 8, True),
 ]
 
 SEED = 20261203

@@ -7,16 +7,18 @@ import pytest
 from conftest import golden_cases, gfmd_pkg, load_golden
 
 
-def _ft_cases():
+def _table_cases():
+    """Fixtures that carry the reference's full Phi table: the `ft` style and
+    the analytic sc100 and fcc100 styles."""
     out = []
     for p in golden_cases():
         c = load_golden(p)
-        if "phi" in c and str(c["args"]).startswith("ft "):
+        if "phi" in c:
             out.append(p)
     return out
 
 
-@pytest.mark.parametrize("path", _ft_cases(), ids=lambda p: os.path.basename(p)[:-4])
+@pytest.mark.parametrize("path", _table_cases(), ids=lambda p: os.path.basename(p)[:-4])
 def test_phi_table_matches_reference(path):
     c = load_golden(path)
     nx, ny = int(c["nx"]), int(c["ny"])
@@ -63,6 +65,14 @@ def test_pair_potential_linf_keyword_gives_zero_gamma_force():
         "ft sc100 abc 1 pair-potential 1 1.0",
         "ft sc100 1.0 1 pair-potential 1 1.0 height 8 extra",
         "ft sc100 1.0 1 pair-potential 4 1 1 1 1",
+        "fcc100",
+        "fcc100 5 1.0",
+        "fcc100 2 1.0 0.3",
+        "fcc100 x 1 1.0",
+        "fcc100 1 abc",
+        "fcc100 2 1.0 0 0 normal 0",
+        "fcc100 1 1.0 height 4 extra",
+        "sc100 extra",
     ],
 )
 def test_malformed_kernel_arguments_raise(args):
@@ -70,6 +80,17 @@ def test_malformed_kernel_arguments_raise(args):
     with pytest.raises(g.GFMDError) as ei:
         g.StiffnessKernel(args)
     assert ei.value.code == 1
+
+
+def test_analytic_fcc100_linf_is_the_gamma_point_force():
+    # FCC100StiffnessKernel::get_force_at_gamma_point returns the `linf`
+    # values (fcc100_stiffness.cpp:482-487); they must sum to zero
+    g = gfmd_pkg()
+    k = g.StiffnessKernel("fcc100 2 1.0 0.0 0.0 linf 0.05 -0.05 height 4")
+    assert np.array_equal(k.get_force_at_gamma_point(), np.array([0.05, -0.05]))
+    assert k.get_dimension() == 6
+    with pytest.raises(g.GFMDError):
+        g.StiffnessKernel("fcc100 2 1.0 0.0 0.0 linf 0.1 0.1")
 
 
 def test_singular_nn_only_simple_cubic_is_reported():

@@ -241,6 +241,7 @@ void CrystalSurface::compute_neighbor_list(double rcut) {
 StiffnessKernel *StiffnessKernel::create(const std::vector<std::string> &tok, size_t &pos) {
   if (pos >= tok.size()) throw std::runtime_error("missing stiffness kernel keyword");
   const std::string kw = tok[pos++];
+  if (kw == "sc100" || kw == "fcc100") return create_analytic(kw, tok, pos);
   if (kw != "ft")
     throw std::runtime_error("stiffness kernel '" + kw +
                              "' has no table producer here; pass its table to gfmd_set_phi");
@@ -333,6 +334,196 @@ StiffnessKernel *StiffnessKernel::create(const std::vector<std::string> &tok, si
   return k;
 }
 
+// ---- the analytic styles -----------------------------------------------------
+
+// SC100StiffnessKernel (src/stiffness_kernels/sc100_stiffness.cpp:137-160):
+//   sc100 [height N]
+// FCC100StiffnessKernel (src/stiffness_kernels/fcc100_stiffness.cpp:57-242):
+//   fcc100 [x] nu k1 [kappa1] [k2 [kappa2] k3 [kappa3]] {height N | linf l1..l_nu |
+//          normal +-1 | mulphase m}
+// (one spring constant for nu = 1, three otherwise; kappas with `x`).
+StiffnessKernel *StiffnessKernel::create_analytic(const std::string &kw, const std::vector<std::string> &tok,
+                                                  size_t &pos) {
+  StiffnessKernel *k = new StiffnessKernel();
+  try {
+    k->name_ = kw;
+    if (kw == "sc100") {
+      k->kind_ = kSC100;
+      k->nu_ = 1;
+      if (pos + 1 < tok.size() && tok[pos] == "height") {
+        pos++;
+        k->height_ = (int)parse_int(tok, pos, "height", 0, 0);
+      }
+    } else {
+      k->kind_ = kFCC100;
+      if (pos >= tok.size()) throw std::runtime_error("fcc100: expected the number of interacting neighbors");
+      bool x = false;
+      if (!tok[pos].empty() && tok[pos].back() == 'x') {
+        x = true;
+        pos++;
+      }
+      k->nu_ = (int)parse_int(tok, pos, "number of layers", 1, 4);
+      const int nk = k->nu_ == 1 ? 1 : 3;
+      for (int i = 0; i < nk; i++) {
+        k->k_[i] = parse_double(tok, pos, "spring constant", 0, 0);
+        if (x) k->kappa_[i] = parse_double(tok, pos, "spring constant", 0, 0);
+      }
+      k->linf_.assign(k->nu_, 0.0);
+      bool found = true;
+      while (pos + 1 < tok.size() && found) {
+        found = false;
+        if (tok[pos] == "height") {
+          pos++;
+          k->height_ = (int)parse_int(tok, pos, "height", 0, 0);
+          found = true;
+        } else if (tok[pos] == "linf") {
+          pos++;
+          double sum = 0.0;
+          for (int i = 0; i < k->nu_; i++) {
+            k->linf_[i] = parse_double(tok, pos, "linf", 0, 0);
+            sum += k->linf_[i];
+          }
+          if (std::fabs(sum) > 1e-12) throw std::runtime_error("linear force contributions must sum to zero");
+          found = true;
+        } else if (tok[pos] == "normal") {
+          pos++;
+          k->z_ = (int)parse_int(tok, pos, "surface normal", -1, 1);
+          if (k->z_ != 1 && k->z_ != -1) throw std::runtime_error("surface normal must be +1 or -1");
+          found = true;
+        } else if (tok[pos] == "mulphase") {
+          pos++;
+          parse_double(tok, pos, "mulphase", 0, 0);  // parsed, not used by the matrices
+          found = true;
+        }
+      }
+    }
+    k->dim_ = 3 * k->nu_;
+  } catch (...) {
+    delete k;
+    throw;
+  }
+  return k;
+}
+
+void StiffnessKernel::analytic_layers(double qx, double qy, cplx *D, double *xc, double *yc) const {
+  const int nu = nu_;
+  auto B = [&](int r, int c) { return D + 9 * (size_t)(r * (nu + 1) + c); };
+  for (size_t i = 0; i < 9 * (size_t)(nu + 1) * (nu + 1); i++) D[i] = {0.0, 0.0};
+  for (int i = 0; i < nu; i++) xc[i] = yc[i] = 0.0;
+  auto re = [](cplx *M, int a, int b) -> double & { return M[3 * a + b].re; };
+  auto im = [](cplx *M, int a, int b) -> double & { return M[3 * a + b].im; };
+  const double cx = std::cos(qx), cy = std::cos(qy), sx = std::sin(qx), sy = std::sin(qy);
+  if (kind_ == kSC100) {
+    // SC100StiffnessKernel::get_per_layer_dynamical_matrices (sc100_stiffness.cpp:167-227)
+    cplx *U0 = B(0, 0), *U = B(0, 1), *V0 = B(1, 0), *V = B(1, 1);
+    re(U, 0, 0) = 6 - 2 * cx * (1 + cy);
+    re(U, 1, 1) = 6 - 2 * cy * (1 + cx);
+    re(U, 2, 2) = 6;
+    re(U, 0, 1) = 2 * sx * sy;
+    re(U, 1, 0) = 2 * sx * sy;
+    re(U0, 0, 0) = 5 - 2 * cx * (1 + cy);
+    re(U0, 1, 1) = 5 - 2 * cy * (1 + cx);
+    re(U0, 2, 2) = 3;
+    re(U0, 0, 1) = 2 * sx * sy;
+    re(U0, 1, 0) = 2 * sx * sy;
+    re(V, 0, 0) = -cx;
+    re(V, 1, 1) = -cy;
+    re(V, 2, 2) = -1 - cx - cy;
+    im(V, 0, 2) = sx;
+    im(V, 1, 2) = sy;
+    im(V, 2, 0) = sx;
+    im(V, 2, 1) = sy;
+    std::memcpy(V0, V, 9 * sizeof(cplx));  // pair potential: V0 = V
+    return;
+  }
+  // FCC100StiffnessKernel::get_per_layer_dynamical_matrices (fcc100_stiffness.cpp:276-480),
+  // the equations of the reference's PRB appendix (A12-A30) in its arithmetic order
+  const double cx2 = std::cos(qx / 2), cy2 = std::cos(qy / 2), sx2 = std::sin(qx / 2), sy2 = std::sin(qy / 2);
+  const double sqrt2 = std::sqrt(2.0);
+  const double *k = k_, *kap = kappa_;
+  const int z = z_;
+  cplx *U0 = B(0, 0), *U = B(0, nu), *V0 = B(1, 0), *V = B(1, nu), *W = B(2 < nu + 1 ? 2 : 0, nu);
+  // nearest neighbours (A12-A17)
+  re(U, 0, 0) = k[0] * (4 - 2 * cx) + kap[0] * (8 - 2 * cy);
+  re(U, 1, 1) = k[0] * (4 - 2 * cy) + kap[0] * (8 - 2 * cx);
+  re(U, 2, 2) = k[0] * 4 + kap[0] * (8 - 2 * cx - 2 * cy);
+  re(U0, 0, 0) = re(U, 0, 0) - k[0] * 1 - kap[0] * 3;
+  re(U0, 1, 1) = re(U, 1, 1) - k[0] * 1 - kap[0] * 3;
+  re(U0, 2, 2) = re(U, 2, 2) - k[0] * 2 - kap[0] * 2;
+  re(V, 0, 0) = -k[0] * cx2 * cy2 - kap[0] * 3 * cx2 * cy2;
+  re(V, 1, 1) = -k[0] * cx2 * cy2 - kap[0] * 3 * cx2 * cy2;
+  re(V, 2, 2) = -k[0] * 2 * cx2 * cy2 - kap[0] * 2 * cx2 * cy2;
+  re(V, 0, 1) = k[0] * sx2 * sy2 - kap[0] * sx2 * sy2;
+  im(V, 0, 2) = z * (k[0] * sqrt2 * sx2 * cy2 - kap[0] * sqrt2 * sx2 * cy2);
+  im(V, 1, 2) = z * (k[0] * sqrt2 * cx2 * sy2 - kap[0] * sqrt2 * cx2 * sy2);
+  re(V, 1, 0) = k[0] * sx2 * sy2 - kap[0] * sx2 * sy2;
+  im(V, 2, 0) = z * (k[0] * sqrt2 * sx2 * cy2 - kap[0] * sqrt2 * sx2 * cy2);
+  im(V, 2, 1) = z * (k[0] * sqrt2 * cx2 * sy2 - kap[0] * sqrt2 * cx2 * sy2);
+  if (nu >= 2) {
+    // second and third neighbours, a full cell vertically (A21-A30)
+    cplx *U1 = B(0, 1);
+    double u2[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    u2[0] = k[1] * (2 - 2 * cx * cy) + kap[1] * (4 - 2 * cx * cy) + k[2] * 8 + kap[2] * 16;
+    u2[4] = k[1] * (2 - 2 * cx * cy) + kap[1] * (4 - 2 * cx * cy) + k[2] * 8 + kap[2] * 16;
+    u2[8] = k[1] * 2 + kap[1] * (4 - 4 * cx * cy) + k[2] * 8 + kap[2] * 16;
+    u2[1] = k[1] * 2 * sx * sy - kap[1] * 2 * sx * sy;
+    u2[3] = k[1] * 2 * sx * sy - kap[1] * 2 * sx * sy;
+    for (int a = 0; a < 9; a++) {
+      U0[a].re += u2[a];
+      U[a].re += u2[a];
+    }
+    std::memcpy(U1, U, 9 * sizeof(cplx));
+    re(U0, 0, 0) -= kap[1] + k[2] * 4 + kap[2] * 8;
+    re(U0, 1, 1) -= kap[1] + k[2] * 4 + kap[2] * 8;
+    re(U0, 2, 2) -= k[1] + k[2] * 4 + kap[2] * 8;
+    re(U1, 0, 0) -= kap[1] + k[2] * 2 / 3 + kap[2] * 10 / 3;
+    re(U1, 1, 1) -= kap[1] + k[2] * 2 / 3 + kap[2] * 10 / 3;
+    re(U1, 2, 2) -= k[1] + k[2] * 8 / 3 + kap[2] * 4 / 3;
+    re(V, 0, 0) += -k[2] * 1 / 3 * cx2 * cy2 * (-10 + 18 * cx + 2 * cy) -
+                   kap[2] * 1 / 3 * cx2 * cy2 * (-14 + 6 * cx + 22 * cy);
+    re(V, 1, 1) += -k[2] * 1 / 3 * cx2 * cy2 * (-10 + 2 * cx + 18 * cy) -
+                   kap[2] * 1 / 3 * cx2 * cy2 * (-14 + 22 * cx + 6 * cy);
+    re(V, 2, 2) += -k[2] * 2 / 3 * cx2 * cy2 * (-2 + 2 * (cx + cy)) -
+                   kap[2] * 2 / 3 * cx2 * cy2 * (-10 + 10 * (cx + cy));
+    re(V, 0, 1) += -k[2] * (-2 - 2 * (cx + cy)) * sx2 * sy2 - kap[2] * (2 + 2 * (cx + cy)) * sx2 * sy2;
+    im(V, 0, 2) += z * (-k[2] * 1 / 3 * sqrt2 * cy2 * (-2 - 2 * (3 * cx + cy)) * sx2 -
+                        kap[2] * 1 / 3 * sqrt2 * cy2 * (2 + 2 * (3 * cx + cy)) * sx2);
+    im(V, 1, 2) += z * (-k[2] * 1 / 3 * sqrt2 * cx2 * (-2 - 2 * (cx + 3 * cy)) * sy2 -
+                        kap[2] * 1 / 3 * sqrt2 * cx2 * (2 + 2 * (cx + 3 * cy)) * sy2);
+    re(V, 1, 0) += -k[2] * (-2 - 2 * (cx + cy)) * sx2 * sy2 - kap[2] * (2 + 2 * (cx + cy)) * sx2 * sy2;
+    im(V, 2, 0) += z * (-k[2] * 1 / 3 * sqrt2 * cy2 * (-2 - 2 * (3 * cx + cy)) * sx2 -
+                        kap[2] * 1 / 3 * sqrt2 * cy2 * (2 + 2 * (3 * cx + cy)) * sx2);
+    im(V, 2, 1) += z * (-k[2] * 1 / 3 * sqrt2 * cx2 * (-2 - 2 * (cx + 3 * cy)) * sy2 -
+                        kap[2] * 1 / 3 * sqrt2 * cx2 * (2 + 2 * (cx + 3 * cy)) * sy2);
+    re(W, 0, 0) = -kap[1] - k[2] * 2 / 3 * cx - kap[2] * (4 * cx / 3 + 2 * cy);
+    re(W, 1, 1) = -kap[1] - k[2] * 2 / 3 * cy - kap[2] * (2 * cx + 4 * cy / 3);
+    re(W, 2, 2) = -k[1] - k[2] * 4 / 3 * (cx + cy) - kap[2] * 2 / 3 * (cx + cy);
+    im(W, 0, 2) = z * (k[2] * 2 / 3 * sqrt2 * sx - kap[2] * 2 / 3 * sqrt2 * sx);
+    im(W, 1, 2) = z * (k[2] * 2 / 3 * sqrt2 * sy - kap[2] * 2 / 3 * sqrt2 * sy);
+    im(W, 2, 0) = z * (k[2] * 2 / 3 * sqrt2 * sx - kap[2] * 2 / 3 * sqrt2 * sx);
+    im(W, 2, 1) = z * (k[2] * 2 / 3 * sqrt2 * sy - kap[2] * 2 / 3 * sqrt2 * sy);
+  }
+  // pair potential: the per-layer V, W equal the bulk ones; U2, U3 too
+  std::memcpy(V0, V, 9 * sizeof(cplx));
+  if (nu > 1) {
+    std::memcpy(B(1, 1), V, 9 * sizeof(cplx));
+    std::memcpy(B(2, 0), W, 9 * sizeof(cplx));
+    std::memcpy(B(2, 1), W, 9 * sizeof(cplx));
+  }
+  if (nu > 2) {
+    std::memcpy(B(0, 2), U, 9 * sizeof(cplx));
+    std::memcpy(B(1, 2), V, 9 * sizeof(cplx));
+    std::memcpy(B(2, 2), W, 9 * sizeof(cplx));
+  }
+  if (nu > 3) {
+    std::memcpy(B(0, 3), U, 9 * sizeof(cplx));
+    std::memcpy(B(1, 3), V, 9 * sizeof(cplx));
+    std::memcpy(B(2, 3), W, 9 * sizeof(cplx));
+  }
+  if (nu == 2 || nu == 4) xc[1] = yc[1] = 0.5;
+  if (nu == 4) xc[3] = yc[3] = 0.5;
+}
+
 // FCPairPotential::offsite: D = -k e(x)e - kappa (1 - e(x)e).
 void StiffnessKernel::offsite(const LatticeNeighbor &n, double *D) const {
   double e[3] = {n.r[0] / n.rnorm, n.r[1] / n.rnorm, n.r[2] / n.rnorm};
@@ -376,6 +567,49 @@ void StiffnessKernel::pre_compute() {
 void StiffnessKernel::dynamical_matrices(double qx, double qy, cplx *U0, cplx *U, cplx *V) const {
   const int d = dim_;
   for (int i = 0; i < d * d; i++) U0[i] = U[i] = V[i] = {0.0, 0.0};
+  if (kind_ != kFT) {
+    // StiffnessKernel::get_dynamical_matrices (src/main/surface_stiffness.cpp:112-270):
+    // cell-level U0, U (upper triangle from the per-layer blocks, lower by
+    // conjugate transpose) and V (lower triangle), with the phase of the
+    // lateral shift between layers
+    const int nu = nu_;
+    cplx Dl[9 * 25];
+    double xc[4], yc[4];
+    analytic_layers(qx, qy, Dl, xc, yc);
+    auto blk = [&](int r, int c) { return Dl + 9 * (size_t)(r * (nu + 1) + c); };
+    auto phase = [&](int i, int j) {
+      const double a = (xc[j] - xc[i]) * qx + (yc[j] - yc[i]) * qy;
+      return cplx{std::cos(a), std::sin(a)};
+    };
+    for (int i = 0; i < nu; i++)
+      for (int j = i; j < nu; j++) {
+        const int r = j - i;
+        if (r > nu) continue;
+        const cplx *m1 = blk(r, i), *m2 = blk(r, nu);
+        const cplx f = i == j ? cplx{1.0, 0.0} : phase(i, j);
+        for (int a = 0; a < 3; a++)
+          for (int b = 0; b < 3; b++) {
+            const cplx p1 = cmul(f, m1[3 * a + b]), p2 = cmul(f, m2[3 * a + b]);
+            U0[(3 * i + a) * d + 3 * j + b] = i == j ? m1[3 * a + b] : p1;
+            U[(3 * i + a) * d + 3 * j + b] = i == j ? m2[3 * a + b] : p2;
+            if (i != j) {
+              const cplx q1 = cmul(f, m1[3 * b + a]), q2 = cmul(f, m2[3 * b + a]);
+              U0[(3 * j + a) * d + 3 * i + b] = {q1.re, -q1.im};
+              U[(3 * j + a) * d + 3 * i + b] = {q2.re, -q2.im};
+            }
+          }
+      }
+    for (int i = 0; i < nu; i++)
+      for (int j = 0; j <= i; j++) {
+        const int r = nu + j - i;
+        if (r > nu) continue;
+        const cplx *m = blk(r, nu);
+        const cplx f = phase(i, j);
+        for (int a = 0; a < 3; a++)
+          for (int b = 0; b < 3; b++) V[(3 * i + a) * d + 3 * j + b] = cmul(f, m[3 * a + b]);
+      }
+    return;
+  }
   const int nn = (int)surf_.neigh.size();
   for (int n = 0; n < nn; n++) {
     const LatticeNeighbor &nb = surf_.neigh[n];

@@ -1,6 +1,6 @@
 // Host-side Phi(q) table producer for the `ft` stiffness-kernel style with the
 // `pair-potential` force-constant model on the sc100, fcc100 and fcc111
-// crystal surfaces.
+// crystal surfaces, and for the analytic `sc100` and `fcc100` styles.
 //
 // Reference behaviour restated (USER-GFMD):
 //   surfaces             src/surfaces/{sc100,fcc100,fcc111}_surface.cpp,
@@ -15,6 +15,11 @@
 //   transfer matrix      greens_function_transfer_matrix_stiffness + iterate_Gnn
 //                        (src/main/surface_stiffness.cpp:493-548, 811-873)
 //   table fill           fill_phi_buffer (src/main/gfmd_misc.cpp:32-101)
+//   analytic styles      SC100StiffnessKernel (src/stiffness_kernels/sc100_stiffness.cpp:137-227),
+//                        FCC100StiffnessKernel (src/stiffness_kernels/fcc100_stiffness.cpp:57-487),
+//                        cell matrices from per-layer blocks in
+//                        StiffnessKernel::get_dynamical_matrices
+//                        (src/main/surface_stiffness.cpp:112-270)
 //
 // It exists so that a machine without the reference tree can still build the
 // tables the force path needs; inside LAMMPS the reference's own
@@ -60,6 +65,8 @@ class StiffnessKernel {
   // tok[pos] (the keyword) and advances pos past what it consumed.
   // Throws std::runtime_error with a message on malformed input.
   static StiffnessKernel *create(const std::vector<std::string> &tok, size_t &pos);
+  static StiffnessKernel *create_analytic(const std::string &kw, const std::vector<std::string> &tok,
+                                          size_t &pos);
 
   int ndof() const { return dim_; }
   int height() const { return height_; }
@@ -69,7 +76,12 @@ class StiffnessKernel {
   // (src/force_constants/fc_pair_potential.cpp:184-191) does not override
   // ForceConstants::linear (src/main/force_constants.cpp:88-94), so
   // FTStiffnessKernel::get_force_at_gamma_point returns zeros.
-  std::vector<double> linf() const { return std::vector<double>(surf_.nat, 0.0); }
+  // The analytic fcc100 style returns its `linf` values
+  // (FCC100StiffnessKernel::get_force_at_gamma_point, fcc100_stiffness.cpp:482-487).
+  std::vector<double> linf() const {
+    if (kind_ == kFCC100) return linf_;
+    return std::vector<double>(kind_ == kFT ? surf_.nat : nu_, 0.0);
+  }
   // The values given with the `linf` keyword.
   const std::vector<double> &linf_keyword() const { return linf_; }
   const std::string &name() const { return name_; }
@@ -82,6 +94,11 @@ class StiffnessKernel {
   bool stiffness(double qx, double qy, cplx *phi, cplx *work) const;
 
  private:
+  // `ft` (force constants on a crystal surface) or the analytic styles
+  enum Kind { kFT, kSC100, kFCC100 };
+  Kind kind_ = kFT;
+  int nu_ = 1;      // layers of the analytic styles
+  int z_ = 1;       // surface normal of the analytic fcc100 style
   std::string name_;
   CrystalSurface surf_;
   int dim_ = 3;
@@ -90,6 +107,10 @@ class StiffnessKernel {
   std::vector<double> linf_;
   std::vector<double> D0ii_, D1ii_, Dij_;  // on-site (per atom) and off-site (per neighbour)
 
+  // Per-layer blocks of the analytic styles in (nu+1)^2 slots of 9 entries
+  // (row 0: U0..U_{nu-1}, U; row 1: V0.., V; row 2: W0.., W) and the lateral
+  // shift of every layer in cell units.
+  void analytic_layers(double qx, double qy, cplx *D, double *xc, double *yc) const;
   void offsite(const LatticeNeighbor &n, double *D) const;
   void onsite(int i, int ab, double *D) const;
   void pre_compute();
