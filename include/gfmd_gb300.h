@@ -255,14 +255,23 @@ int gfmd_post_force_noalloc(int nx, int ny, int ndof, const double *d_phi_half,
 /* Parse the stiffness-kernel part of a `fix gfmd` line, e.g.
  * "ft fcc100 1.0 2 pair-potential 1 1.0 height 64".  Supported here: the
  * `ft` style on the sc100, fcc100 and fcc111 surfaces with `pair-potential`
- * force constants.  Other styles are produced by the reference's own
- * fill_phi_buffer and uploaded with gfmd_set_phi.
+ * force constants, the analytic `sc100` and `fcc100` styles, and the
+ * continuum `isotropic` and `nonperiodic` styles.  Other styles are produced
+ * by the reference's own fill_phi_buffer and uploaded with gfmd_set_phi.
  * Replaces: stiffness_kernel_factory (src/main/surface_stiffness.cpp:440-481). */
 int gfmd_kernel_create(const char *args, gfmd_kernel_t *out);
 int gfmd_kernel_destroy(gfmd_kernel_t k);
 
 /* Kernel dimension ndof (get_dimension) and substrate height (get_height). */
 int gfmd_kernel_info(gfmd_kernel_t k, int *ndof, int *height);
+
+/* Lateral box lengths of the surface (LAMMPS domain->xprd, domain->yprd),
+ * which the isotropic (q = 0 term, square boxes only) and nonperiodic (grid
+ * spacing xprd/nx, yprd/ny) styles read.  0 (the default) means one length
+ * unit per grid point, xprd = nx and yprd = ny of each table filled.
+ * Replaces: the Domain pointer handed to stiffness_kernel_factory
+ * (src/main/surface_stiffness.cpp:440-444). */
+int gfmd_kernel_set_box(gfmd_kernel_t k, double xprd, double yprd);
 
 /* Fill a Phi table for an nx x ny grid, scaled by 1/(nx*ny), in
  * GFMD_PHI_FULL or GFMD_PHI_HALF layout (host memory the caller allocates:

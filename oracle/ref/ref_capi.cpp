@@ -27,6 +27,7 @@ using namespace LAMMPS_NS;
 namespace {
 
 thread_local std::string g_last_error;
+thread_local double g_box_x = 1.0, g_box_y = 1.0;
 
 struct Env {
   Error error;
@@ -42,6 +43,7 @@ struct Env {
     lmp.domain = &domain;
     lmp.update = &update;
     lmp.screen = nullptr;
+    domain.set_cell(g_box_x, g_box_y, 1.0);
   }
 };
 
@@ -90,6 +92,15 @@ int gref_kernel_info(const char *args, int *ndof, int *height) {
     g_last_error = e.what();
     return -1;
   }
+}
+
+/* Box lengths (LAMMPS' domain->xprd, yprd; the isotropic and nonperiodic
+ * kernels read them) of every later call on this thread; default 1 x 1 as
+ * the reference's Domain stub. */
+int gref_set_box(double xprd, double yprd) {
+  g_box_x = xprd;
+  g_box_y = yprd;
+  return 0;
 }
 
 /* Full-grid Phi(q) table exactly as fill_phi_buffer leaves it

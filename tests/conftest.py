@@ -66,6 +66,15 @@ def load_golden(path):
     return {k: z[k] for k in z.files}
 
 
+def kernel_for(c):
+    """The stiffness kernel of a fixture, with the box lengths the reference
+    ran it in when the fixture stores them (isotropic, nonperiodic)."""
+    k = gfmd_pkg().StiffnessKernel(str(c["args"]))
+    if "xprd" in c:
+        k.set_box(float(c["xprd"]), float(c["yprd"]))
+    return k
+
+
 def rel_l2(a, b):
     a = np.asarray(a, np.float64)
     b = np.asarray(b, np.float64)

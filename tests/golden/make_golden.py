@@ -39,7 +39,16 @@ CASES = [
     ("sc100_analytic_h16_9x7", "sc100 height 16", 9, 7, True),
     ("fcc100x4_analytic_h10_6x8", "fcc100 4 1.0 0.3 0.1 height 10", 6, 8, True),
     ("fcc100x2_kappa_normal_8x8", "fcc100 x 2 1.0 0.2 0.3 0.1 0.1 0.05 normal -1 height 10", 8, 8, True),
+    # the continuum styles, with the box of the reference's tests (one length
+    # unit per grid point: xprd = nx, yprd = ny)
+    ("isotropic_nu03_12x12", "isotropic 0.3 1.0 1.0", 12, 12, True),
+    ("nonperiodic_nu03_9x7", "nonperiodic 0.3 1.0", 9, 7, True),
+    ("nonperiodic_nu025_16x12", "nonperiodic 0.25 2.0", 16, 12, True),
+    ("nonperiodic_nu03_63x63", "nonperiodic 0.3 1.0", 63, 63, False),
 ]
+
+# kernels that read the box lengths; the fixtures store them as xprd, yprd
+BOX_STYLES = ("isotropic", "nonperiodic")
 
 SEED = 20261203
 
@@ -53,6 +62,8 @@ def load_ref() -> ctypes.CDLL:
 
 
 def run_case(L, args: str, nx: int, ny: int, seed: int):
+    box = (float(nx), float(ny)) if args.split()[0] in BOX_STYLES else (1.0, 1.0)
+    L.gref_set_box(ctypes.c_double(box[0]), ctypes.c_double(box[1]))
     nd, ht = ctypes.c_int(), ctypes.c_int()
     if L.gref_kernel_info(args.encode(), ctypes.byref(nd), ctypes.byref(ht)):
         raise RuntimeError(L.gref_last_error().decode())
@@ -80,6 +91,8 @@ def main() -> int:
         d, h, phi, linf, u, f, e, u0 = run_case(L, args, nx, ny, SEED + i)
         out = dict(args=np.array(args), nx=nx, ny=ny, ndof=d, height=h, u=u, f=f,
                    epot=np.array(e), u0=u0, linf=linf)
+        if args.split()[0] in BOX_STYLES:
+            out["xprd"], out["yprd"] = np.array(float(nx)), np.array(float(ny))
         if keep_phi:
             out["phi"] = phi
         path = os.path.join(HERE, f"{name}.npz")

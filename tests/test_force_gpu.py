@@ -9,7 +9,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import (golden_cases, gfmd_pkg, half_to_full, load_golden, oracle_post_force,
+from conftest import (golden_cases, gfmd_pkg, kernel_for, half_to_full, load_golden, oracle_post_force,
                       rel_l2)
 
 torch = pytest.importorskip("torch")
@@ -22,7 +22,7 @@ FP32_TOL = 5e-6
 def _phi(c, nx, ny):
     if "phi" in c:
         return c["phi"], "full", c["linf"]
-    k = gfmd_pkg().StiffnessKernel(str(c["args"]))
+    k = kernel_for(c)
     phi, linf = k.phi_table(nx, ny, "half")
     return phi, "half", linf
 

@@ -8,7 +8,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import (golden_cases, gfmd_pkg, half_to_full, load_golden, oracle,
+from conftest import (golden_cases, gfmd_pkg, kernel_for, half_to_full, load_golden, oracle,
                       oracle_post_force, rel_l2)
 
 
@@ -46,7 +46,7 @@ def test_oracle_matches_reference_fixture(path):
     if "phi" in c:
         phi = c["phi"]
     else:
-        k = gfmd_pkg().StiffnessKernel(str(c["args"]))
+        k = kernel_for(c)
         phi, _ = k.phi_table(nx, ny, "full")
     f, e, u0 = oracle_post_force(phi, c["linf"], c["u"], nx, ny)
     assert rel_l2(f, c["f"]) <= 1e-12
@@ -64,7 +64,7 @@ def test_energy_identity_without_linf():
 def test_half_table_expands_to_reference_table():
     c = load_golden(os.path.join(os.path.dirname(__file__), "golden", "fcc100x2_h64_12x10.npz"))
     nx, ny = int(c["nx"]), int(c["ny"])
-    k = gfmd_pkg().StiffnessKernel(str(c["args"]))
+    k = kernel_for(c)
     half, _ = k.phi_table(nx, ny, "half")
     full = half_to_full(half, nx, ny)
     assert np.abs(full - c["phi"]).max() <= 1e-13 * np.abs(c["phi"]).max()

@@ -2,7 +2,7 @@
 import numpy as np
 import pytest
 
-from conftest import gfmd_pkg, rel_l2
+from conftest import gfmd_pkg, half_to_full, rel_l2
 from solver_cases import (KERNEL_FCC2, KERNEL_SC, gpu_obstacle, oracle_elastic, osv,
                           sphere_spec, tables)
 
@@ -275,3 +275,43 @@ def test_preconditioned_cg_matches_oracle(prec):
     assert r_ref["iterations"] < r_cg["iterations"]  # preconditioning pays
     if prec == "f64":
         assert rep["iterations"] <= 1.5 * r_ref["iterations"] + 5
+
+
+def test_hertz_on_the_nonperiodic_kernel_matches_oracle():
+    # tests/TEST_Hertz_nonperiodic_64x64 of the reference: nonperiodic 0.3 1.0,
+    # Lennard-Jones sphere R = 100, CG to max|f| <= 1e-6; the GPU minimum
+    # against the oracle's and the reference's Hertz residual bound
+    from test_continuum_kernels import hertz_residual, hertz_sphere
+
+    n = 64
+    k = gfmd_pkg().StiffnessKernel("nonperiodic 0.3 1.0")
+    k.set_box(n, n)
+    half, linf = k.phi_table(n, n, "half")
+    el = oracle_elastic(half_to_full(half, n, n), linf, n, n)
+    ob = hertz_sphere()
+    u_ref, r_ref = osv.cg(el, ob, np.zeros((3, n * n)), n, n, ftol=1e-6)
+    s = _solver(n, n, 3, half, linf)
+    o, keep = _gpu_obst(ob)
+    u = torch.zeros(3, n * n, dtype=torch.float64, device="cuda")
+    rep = s.minimize(u, o, "cg", ftol=1e-6)
+    assert rep["fmax"] <= 1e-6
+    assert rel_l2(u.cpu().numpy(), u_ref) <= 1e-5
+    f = np.zeros((3, n * n))
+    s.post_force(u.cpu().numpy(), f)
+    res, _ = hertz_residual(f[2].reshape(n, n), n, n)
+    assert res < 1e-2
+
+
+def test_nve_energy_conservation_on_the_nonperiodic_kernel():
+    # tests/TEST_energy_conservation_nonperiodic: 15 x 15, random displacements
+    # of 0.1, dt = 0.01, |E - <E>| / <E> < 1e-4
+    n = 15
+    k = gfmd_pkg().StiffnessKernel("nonperiodic 0.3 1.0")
+    k.set_box(n, n)
+    half, linf = k.phi_table(n, n, "half")
+    s = _solver(n, n, 3, half, linf)
+    rng = np.random.default_rng(12472634)
+    u = torch.from_numpy(rng.uniform(-0.1, 0.1, (3, n * n))).cuda()
+    v = torch.zeros_like(u)
+    e, _ = s.run_dynamics(u, v, 0.01, 0.0, 20000)
+    assert np.abs(e - e.mean()).max() / abs(e.mean()) < 1e-4

@@ -4,7 +4,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import golden_cases, gfmd_pkg, load_golden
+from conftest import golden_cases, gfmd_pkg, kernel_for, load_golden
 
 
 def _table_cases():
@@ -22,7 +22,7 @@ def _table_cases():
 def test_phi_table_matches_reference(path):
     c = load_golden(path)
     nx, ny = int(c["nx"]), int(c["ny"])
-    k = gfmd_pkg().StiffnessKernel(str(c["args"]))
+    k = kernel_for(c)
     assert k.get_dimension() == int(c["ndof"])
     assert k.get_height() == int(c["height"])
     phi, linf = k.phi_table(nx, ny, "full")

@@ -175,6 +175,7 @@ SIGNATURES = {
     "gfmd_kernel_create": [ctypes.c_char_p, ctypes.POINTER(_vp)],
     "gfmd_kernel_destroy": [_vp],
     "gfmd_kernel_info": [_vp, _pi, _pi],
+    "gfmd_kernel_set_box": [_vp, ctypes.c_double, ctypes.c_double],
     "gfmd_kernel_phi": [_vp, _c_int, _c_int, _c_int, _vp, _vp, _c_int],
 }
 

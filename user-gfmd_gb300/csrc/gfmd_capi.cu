@@ -727,6 +727,14 @@ int gfmd_kernel_info(gfmd_kernel_t k, int *ndof, int *height) {
   return GFMD_OK;
 }
 
+int gfmd_kernel_set_box(gfmd_kernel_t k, double xprd, double yprd) {
+  if (!k) return fail(GFMD_EINVAL, "gfmd_kernel_set_box: NULL kernel");
+  if (!(xprd >= 0.0) || !(yprd >= 0.0) || !std::isfinite(xprd) || !std::isfinite(yprd))
+    return fail(GFMD_EINVAL, "gfmd_kernel_set_box: box lengths must be finite and >= 0");
+  k->k->set_box(xprd, yprd);
+  return GFMD_OK;
+}
+
 int gfmd_kernel_phi(gfmd_kernel_t k, int nx, int ny, int layout, double *phi, double *linf,
                     int nthreads) {
   if (!k || !phi) return fail(GFMD_EINVAL, "gfmd_kernel_phi: NULL argument");

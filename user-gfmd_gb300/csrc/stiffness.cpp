@@ -242,6 +242,7 @@ StiffnessKernel *StiffnessKernel::create(const std::vector<std::string> &tok, si
   if (pos >= tok.size()) throw std::runtime_error("missing stiffness kernel keyword");
   const std::string kw = tok[pos++];
   if (kw == "sc100" || kw == "fcc100") return create_analytic(kw, tok, pos);
+  if (kw == "isotropic" || kw == "nonperiodic") return create_continuum(kw, tok, pos);
   if (kw != "ft")
     throw std::runtime_error("stiffness kernel '" + kw +
                              "' has no table producer here; pass its table to gfmd_set_phi");
@@ -332,6 +333,138 @@ StiffnessKernel *StiffnessKernel::create(const std::vector<std::string> &tok, si
     throw;
   }
   return k;
+}
+
+// ---- the continuum styles ----------------------------------------------------
+
+// IsotropicStiffnessKernel (src/stiffness_kernels/isotropic_stiffness.cpp:43-87):
+//   isotropic nu mu gamma      (height 1 when 0 < gamma < 1e6, else 0)
+// NonperiodicStiffnessKernel (src/stiffness_kernels/nonperiodic_stiffness.cpp:44-102):
+//   nonperiodic nu mu          (height 1)
+StiffnessKernel *StiffnessKernel::create_continuum(const std::string &kw, const std::vector<std::string> &tok,
+                                                   size_t &pos) {
+  StiffnessKernel *k = new StiffnessKernel();
+  try {
+    k->name_ = kw;
+    k->nu_ = 1;
+    k->dim_ = 3;
+    k->poisson_ = parse_double(tok, pos, "Poisson number", 0, 0);
+    k->shear_ = parse_double(tok, pos, "shear modulus", 0, 0);
+    if (kw == "isotropic") {
+      k->kind_ = kIsotropic;
+      k->gamma_ = parse_double(tok, pos, "gamma", 0, 0);
+      k->height_ = (k->gamma_ > 0.0 && k->gamma_ < 1e6) ? 1 : 0;
+    } else {
+      k->kind_ = kNonperiodic;
+      k->height_ = 1;
+    }
+  } catch (...) {
+    delete k;
+    throw;
+  }
+  return k;
+}
+
+// Surface Green's function of an isotropic elastic half-space in Fourier
+// space (q in radians per grid spacing), inverted to a stiffness; at q = 0 the
+// finite-box compliance diag((1/2 + 1/(2(1-nu))) xprd, same, xprd)/(gamma pi).
+// Follows IsotropicStiffnessKernel::get_stiffness_matrix
+// (isotropic_stiffness.cpp:91-146); the shear modulus is mu, the Poisson
+// number nu, and 2 - 1/alpha = 2 nu, 1 - 1/alpha = 2 nu - 1 with
+// alpha = 1/(2(1-nu)).
+bool StiffnessKernel::isotropic(double qx, double qy, double xprd, double yprd, cplx *phi) const {
+  (void)yprd;
+  const double alpha = 1.0 / (2.0 * (1.0 - poisson_));
+  for (int i = 0; i < 9; i++) phi[i] = {0.0, 0.0};
+  if (std::fabs(qx) <= 1e-6 && std::fabs(qy) <= 1e-6) {
+    const double cz = xprd / (gamma_ * kPi);
+    phi[0].re = (alpha + 0.5) * cz;
+    phi[4].re = phi[0].re;
+    phi[8].re = cz;
+    return invert(3, phi);
+  }
+  const double q2 = qx * qx + qy * qy, q = std::sqrt(q2);
+  const double mu = shear_, nu = poisson_;
+  const double inplane = 2.0 * nu / (2.0 * mu * q * q2);  // (2 - 1/alpha) / (2 mu q^3)
+  const double normal = (2.0 * nu - 1.0) / (2.0 * mu * q2);  // (1 - 1/alpha) / (2 mu q^2)
+  phi[0].re = 1.0 / (mu * q) - qx * qx * inplane;
+  phi[4].re = 1.0 / (mu * q) - qy * qy * inplane;
+  phi[8].re = 1.0 / (2.0 * mu * alpha * q);
+  phi[1].re = phi[3].re = -qx * qy * inplane;
+  phi[2].im = -qx * normal;
+  phi[5].im = -qy * normal;
+  phi[6].im = qx * normal;
+  phi[7].im = qy * normal;
+  return invert(3, phi);
+}
+
+namespace {
+
+// Y * ln(X + r), r = |(X, Y)|, zero on the line Y = 0; for X < 0 through
+// X + r = Y^2 / (r - X), which has no cancellation.
+double y_log_x_plus_r(double Y, double X) {
+  if (Y == 0.0) return 0.0;
+  const double r = std::sqrt(X * X + Y * Y);
+  return Y * (X >= 0.0 ? std::log(X + r) : std::log(Y * Y / (r - X)));
+}
+
+// X * atan(Y / X) + Y/2 * ln(X^2 + Y^2): an antiderivative in X and Y of X / r^2.
+double prim_x_over_r2(double X, double Y) {
+  const double r2 = X * X + Y * Y;
+  double v = X == 0.0 ? 0.0 : X * std::atan(Y / X);
+  if (Y != 0.0) v += 0.5 * Y * std::log(r2);
+  return v;
+}
+
+}  // namespace
+
+// Displacements at the surface of an isotropic half-space (shear modulus mu,
+// Poisson number nu) under a unit force spread uniformly over one grid cell
+// [-dx/2, dx/2] x [-dy/2, dy/2], at the grid point offset (i dx, j dy).  The
+// point-force solutions of Boussinesq (normal) and Cerruti (tangential), in
+// the reference's orientation (z and the normal force positive away from the
+// solid), are, with c = (1 - 2 nu) / (4 pi mu) and r = |(x, y)|:
+//   normal force P:       u_x = c P x/r^2,  u_y = c P y/r^2,
+//                         u_z = (1 - nu) P / (2 pi mu r)
+//   tangential force Q_x: u_x = Q_x/(2 pi mu) ((1 - nu)/r + nu x^2/r^3),
+//                         u_y = Q_x/(2 pi mu) nu x y/r^3,  u_z = -c Q_x x/r^2
+// (Q_y by symmetry).  Their integrals over the cell are closed-form corner
+// sums of antiderivatives F with d2F/dxdy = integrand:
+//   1/r -> x ln(y + r) + y ln(x + r),   x/r^2 -> x atan(y/x) + y/2 ln r^2,
+//   x^2/r^3 -> y ln(x + r),             x y/r^3 -> -r.
+// The reference integrates the same solutions over two triangles per cell
+// (sq_uniform_PQ, src/stiffness_kernels/li_berger.cpp:453-459, after Li and
+// Berger, J. Elasticity 63, 137 (2001)); both are exact up to rounding.
+void StiffnessKernel::nonperiodic_green(int i, int j, double dx, double dy, double *G) const {
+  const double mu = shear_, nu = poisson_;
+  const double a = 0.5 * dx, b = 0.5 * dy;
+  const double x[2] = {i * dx - a, i * dx + a}, y[2] = {j * dy - b, j * dy + b};
+  double inv_r = 0, x_r2 = 0, y_r2 = 0, xx_r3 = 0, yy_r3 = 0, xy_r3 = 0;
+  for (int cx = 0; cx < 2; cx++)
+    for (int cy = 0; cy < 2; cy++) {
+      const double sgn = (cx == cy) ? 1.0 : -1.0;
+      const double X = x[cx], Y = y[cy];
+      const double xl = y_log_x_plus_r(X, Y), yl = y_log_x_plus_r(Y, X);  // X ln(Y+r), Y ln(X+r)
+      inv_r += sgn * (xl + yl);
+      x_r2 += sgn * prim_x_over_r2(X, Y);
+      y_r2 += sgn * prim_x_over_r2(Y, X);
+      xx_r3 += sgn * yl;
+      yy_r3 += sgn * xl;
+      xy_r3 -= sgn * std::sqrt(X * X + Y * Y);
+    }
+  // unit total force: traction 1/(dx dy) over the cell
+  const double t = 1.0 / (dx * dy);
+  const double c = (1.0 - 2.0 * nu) / (4.0 * kPi * mu) * t, s = t / (2.0 * kPi * mu);
+  // columns: traction x, y, z
+  G[0] = s * ((1.0 - nu) * inv_r + nu * xx_r3);
+  G[3] = s * nu * xy_r3;
+  G[6] = -c * x_r2;
+  G[1] = s * nu * xy_r3;
+  G[4] = s * ((1.0 - nu) * inv_r + nu * yy_r3);
+  G[7] = -c * y_r2;
+  G[2] = c * x_r2;
+  G[5] = c * y_r2;
+  G[8] = (1.0 - nu) * s * inv_r;
 }
 
 // ---- the analytic styles -----------------------------------------------------
@@ -686,14 +819,141 @@ bool StiffnessKernel::stiffness(double qx, double qy, cplx *phi, cplx *work) con
   return true;
 }
 
+namespace {
+
+// Complex DFT of any length n on the host: recursive mixed-radix decimation
+// in time over the prime factors of n, out[k] = sum_t in[t] exp(sign 2 pi i
+// t k / n), unscaled.  Cost n * (sum of the prime factors).
+class HostDFT {
+ public:
+  HostDFT(int n, int sign) : n_(n), tw_(n) {
+    for (int t = 0; t < n; t++) {
+      const double a = 2.0 * kPi * t / n;
+      tw_[t] = {std::cos(a), sign * std::sin(a)};
+    }
+    int m = n;
+    for (int p = 2; p * p <= m; p++)
+      while (m % p == 0) {
+        f_.push_back(p);
+        m /= p;
+      }
+    if (m > 1) f_.push_back(m);
+  }
+  // in: n entries with the given stride; out: n contiguous entries.
+  void run(const cplx *in, int stride, cplx *out) const {
+    if (n_ == 1) {
+      out[0] = in[0];
+      return;
+    }
+    std::vector<cplx> acc(f_.empty() ? 1 : *std::max_element(f_.begin(), f_.end()));
+    rec(in, stride, out, n_, 0, acc.data());
+  }
+
+ private:
+  int n_;
+  std::vector<cplx> tw_;
+  std::vector<int> f_;
+  // DFT of length n = p * m of in[0], in[stride], ...: p sub-transforms of
+  // length m over every p-th input, then the radix-p combination.
+  void rec(const cplx *in, int stride, cplx *out, int n, size_t fi, cplx *acc) const {
+    if (n == 1) {
+      out[0] = in[0];
+      return;
+    }
+    const int p = f_[fi], m = n / p, step = n_ / n;
+    for (int r = 0; r < p; r++) rec(in + (size_t)r * stride, stride * p, out + (size_t)r * m, m, fi + 1, acc);
+    for (int k = 0; k < m; k++) {
+      for (int q = 0; q < p; q++) {
+        cplx v = {0.0, 0.0};
+        for (int r = 0; r < p; r++) {
+          const cplx w = tw_[((size_t)r * (k + (size_t)q * m) % n) * step];
+          v = {v.re + out[r * m + k].re * w.re - out[r * m + k].im * w.im,
+               v.im + out[r * m + k].re * w.im + out[r * m + k].im * w.re};
+        }
+        acc[q] = v;
+      }
+      for (int q = 0; q < p; q++) out[q * m + k] = acc[q];
+    }
+  }
+};
+
+template <class F>
+void parallel_for(int n, int nthreads, F f) {
+  std::atomic<int> next(0);
+  auto worker = [&]() {
+    for (int i; (i = next.fetch_add(1)) < n;) f(i);
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < nthreads; t++) th.emplace_back(worker);
+  worker();
+  for (auto &t : th) t.join();
+}
+
+// NonperiodicStiffnessKernel::create_and_fill_buffer
+// (src/stiffness_kernels/nonperiodic_stiffness.cpp:106-208): the real-space
+// Green's function on the minimum-image grid, off-diagonal entries zeroed on
+// the far row and column of an even dimension (so the transform stays
+// Hermitian), a 2-D transform with exp(+i) per entry, and a 3x3 inverse per
+// wavevector.  Only the stored ky columns are transformed along x.
+std::string fill_nonperiodic(const StiffnessKernel &k, int nx, int ny, int layout, double *phi,
+                             int nthreads) {
+  const double xprd = k.box_x() > 0.0 ? k.box_x() : nx, yprd = k.box_y() > 0.0 ? k.box_y() : ny;
+  const double dx = xprd / nx, dy = yprd / ny;
+  const int nyc = layout == 0 ? ny : ny / 2 + 1;
+  const size_t nxy = (size_t)nx * ny;
+  std::vector<cplx> g(9 * nxy);  // [entry][ix][iy], transformed along y in place
+  const HostDFT fy(ny, +1), fx(nx, +1);
+  parallel_for(nx, nthreads, [&](int ix) {
+    const int i = ix <= nx / 2 ? ix : ix - nx;
+    std::vector<cplx> row(ny), out(ny);
+    double G[9];
+    std::vector<double> rows(9 * (size_t)ny);
+    for (int iy = 0; iy < ny; iy++) {
+      const int j = iy <= ny / 2 ? iy : iy - ny;
+      k.nonperiodic_green(i, j, dx, dy, G);
+      if ((nx % 2 == 0 && ix == nx / 2) || (ny % 2 == 0 && iy == ny / 2))
+        G[1] = G[2] = G[3] = G[5] = G[6] = G[7] = 0.0;
+      for (int e = 0; e < 9; e++) rows[e * (size_t)ny + iy] = G[e];
+    }
+    for (int e = 0; e < 9; e++) {
+      for (int iy = 0; iy < ny; iy++) row[iy] = {rows[e * (size_t)ny + iy], 0.0};
+      fy.run(row.data(), 1, out.data());
+      std::memcpy(&g[e * nxy + (size_t)ix * ny], out.data(), sizeof(cplx) * ny);
+    }
+  });
+  std::atomic<int> singular(0);
+  const double inv = 1.0 / ((double)nx * (double)ny);
+  parallel_for(nyc, nthreads, [&](int iy) {
+    std::vector<cplx> col(9 * (size_t)nx);
+    for (int e = 0; e < 9; e++) fx.run(&g[e * nxy + iy], ny, &col[e * (size_t)nx]);
+    cplx m[9];
+    for (int ix = 0; ix < nx; ix++) {
+      for (int e = 0; e < 9; e++) m[e] = col[e * (size_t)nx + ix];
+      if (!invert(3, m)) singular.store(1);
+      double *o = phi + 2 * ((size_t)ix * nyc + iy) * 9;
+      for (int e = 0; e < 9; e++) {
+        o[2 * e] = m[e].re * inv;
+        o[2 * e + 1] = m[e].im * inv;
+      }
+    }
+  });
+  if (singular.load()) return "singular matrix while computing the stiffness kernel";
+  return std::string();
+}
+
+}  // namespace
+
 std::string fill_phi_table(const StiffnessKernel &k, int nx, int ny, int layout, double *phi,
                            int nthreads) {
   if (nx < 1 || ny < 1) return "grid dimensions must be positive";
   if (layout != 0 && layout != 1) return "unknown table layout";
+  if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
+  if (k.is_nonperiodic()) return fill_nonperiodic(k, nx, ny, layout, phi, nthreads);
+  const double xprd = k.box_x() > 0.0 ? k.box_x() : nx, yprd = k.box_y() > 0.0 ? k.box_y() : ny;
+  if (k.is_isotropic() && xprd != yprd) return "isotropic kernel works with square surfaces only";
   const int d = k.ndof(), d2 = d * d;
   const int nyc = layout == 0 ? ny : ny / 2 + 1;
   const double inv = 1.0 / ((double)nx * (double)ny);
-  if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
   std::atomic<int> next(0);
   std::atomic<int> bad_ix(-1), bad_herm(-1);
   auto worker = [&]() {
@@ -705,7 +965,9 @@ std::string fill_phi_table(const StiffnessKernel &k, int nx, int ny, int layout,
       double qx = (ix <= nx / 2) ? 2.0 * kPi * ix / nx : 2.0 * kPi * (ix - nx) / nx;
       for (int iy = 0; iy < nyc; iy++) {
         double qy = (iy <= ny / 2) ? 2.0 * kPi * iy / ny : 2.0 * kPi * (iy - ny) / ny;
-        if (!k.stiffness(qx, qy, p.data(), work.data())) {
+        const bool ok = k.is_isotropic() ? k.isotropic(qx, qy, xprd, yprd, p.data())
+                                         : k.stiffness(qx, qy, p.data(), work.data());
+        if (!ok) {
           bad_ix.store(ix);
           return;
         }

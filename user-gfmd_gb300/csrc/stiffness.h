@@ -1,6 +1,7 @@
 // Host-side Phi(q) table producer for the `ft` stiffness-kernel style with the
 // `pair-potential` force-constant model on the sc100, fcc100 and fcc111
-// crystal surfaces, and for the analytic `sc100` and `fcc100` styles.
+// crystal surfaces, for the analytic `sc100` and `fcc100` styles, and for the
+// continuum `isotropic` and `nonperiodic` styles.
 //
 // Reference behaviour restated (USER-GFMD):
 //   surfaces             src/surfaces/{sc100,fcc100,fcc111}_surface.cpp,
@@ -20,6 +21,8 @@
 //                        cell matrices from per-layer blocks in
 //                        StiffnessKernel::get_dynamical_matrices
 //                        (src/main/surface_stiffness.cpp:112-270)
+//   continuum styles     IsotropicStiffnessKernel (src/stiffness_kernels/isotropic_stiffness.cpp:43-146),
+//                        NonperiodicStiffnessKernel (src/stiffness_kernels/nonperiodic_stiffness.cpp:44-242)
 //
 // It exists so that a machine without the reference tree can still build the
 // tables the force path needs; inside LAMMPS the reference's own
@@ -67,6 +70,23 @@ class StiffnessKernel {
   static StiffnessKernel *create(const std::vector<std::string> &tok, size_t &pos);
   static StiffnessKernel *create_analytic(const std::string &kw, const std::vector<std::string> &tok,
                                           size_t &pos);
+  static StiffnessKernel *create_continuum(const std::string &kw, const std::vector<std::string> &tok,
+                                           size_t &pos);
+
+  // Lateral box lengths (LAMMPS domain->xprd, yprd), read by the isotropic
+  // and nonperiodic styles.  Zero (the default) means one lattice spacing per
+  // grid point: xprd = nx, yprd = ny of the table being filled.
+  void set_box(double xprd, double yprd) { box_x_ = xprd; box_y_ = yprd; }
+  double box_x() const { return box_x_; }
+  double box_y() const { return box_y_; }
+  bool is_isotropic() const { return kind_ == kIsotropic; }
+  bool is_nonperiodic() const { return kind_ == kNonperiodic; }
+  // Isotropic elastic half-space at one wavevector (3x3); false if singular.
+  bool isotropic(double qx, double qy, double xprd, double yprd, cplx *phi) const;
+  // Real-space surface Green's function of the nonperiodic style at grid
+  // offset (i, j) with spacing (dx, dy): G[3*a + b] = displacement a under
+  // unit force b spread uniformly over one dx x dy cell.
+  void nonperiodic_green(int i, int j, double dx, double dy, double *G) const;
 
   int ndof() const { return dim_; }
   int height() const { return height_; }
@@ -94,9 +114,12 @@ class StiffnessKernel {
   bool stiffness(double qx, double qy, cplx *phi, cplx *work) const;
 
  private:
-  // `ft` (force constants on a crystal surface) or the analytic styles
-  enum Kind { kFT, kSC100, kFCC100 };
+  // `ft` (force constants on a crystal surface), the analytic lattice styles,
+  // or the continuum styles
+  enum Kind { kFT, kSC100, kFCC100, kIsotropic, kNonperiodic };
   Kind kind_ = kFT;
+  double poisson_ = 0.0, shear_ = 1.0, gamma_ = 1.0;  // isotropic / nonperiodic
+  double box_x_ = 0.0, box_y_ = 0.0;
   int nu_ = 1;      // layers of the analytic styles
   int z_ = 1;       // surface normal of the analytic fcc100 style
   std::string name_;

@@ -64,6 +64,16 @@ class StiffnessKernel:
             lib().gfmd_kernel_destroy(h)
             self._h = ctypes.c_void_p()
 
+    def set_box(self, xprd: float, yprd: float) -> None:
+        """Lateral box lengths (LAMMPS ``domain->xprd``, ``yprd``) for the
+        isotropic and nonperiodic styles; 0 means one unit per grid point."""
+        check(lib().gfmd_kernel_set_box(self._h, float(xprd), float(yprd)))
+        self._box = (float(xprd), float(yprd))
+
+    def _cache_key(self) -> str:
+        box = getattr(self, "_box", (0.0, 0.0))
+        return self.args if box == (0.0, 0.0) else f"{self.args} box {box[0]!r} {box[1]!r}"
+
     def get_dimension(self) -> int:
         return self._ndof
 
@@ -97,12 +107,13 @@ class StiffnessKernel:
         """``phi_table`` through an on-disk cache (``PhiTableFile``): the file
         for (kernel arguments, nx, ny, layout) is read if present and valid,
         else the table is generated and written."""
-        path = PhiTableFile.path(cache_dir, self.args, nx, ny, layout)
-        got = PhiTableFile.read(path, self.args, nx, ny, layout)
+        key = self._cache_key()
+        path = PhiTableFile.path(cache_dir, key, nx, ny, layout)
+        got = PhiTableFile.read(path, key, nx, ny, layout)
         if got is not None:
             return got
         phi, linf = self.phi_table(nx, ny, layout, nthreads)
-        PhiTableFile.write(path, self.args, nx, ny, layout, phi, linf)
+        PhiTableFile.write(path, key, nx, ny, layout, phi, linf)
         return phi, linf
 
     def get_force_at_gamma_point(self) -> np.ndarray:
