@@ -190,6 +190,23 @@ typedef struct {
  * obstacle stiffness).  Destroy with gfmd_destroy. */
 int gfmd_make_preconditioner(gfmd_handle_t h, double shift, gfmd_handle_t *out);
 
+/* Preconditioned gradient, device buffers [ndof][nx*ny] FP64, on h's stream:
+ *   gP = IFFT( (Phi(q) + Cavg)^{-1} FFT(g) )
+ * with Phi(q) the uploaded table (divided by nx*ny) and both transforms
+ * unscaled, as the reference computes it.  Cavg: ndof*ndof doubles (host),
+ * symmetric, added to every block.  The block inverses are built on the host
+ * on the first call and again whenever Cavg or the table changes.
+ * As in the reference, when ndof > 3 only the first three components are
+ * preconditioned and the others are returned as nx*ny*g (the reference's
+ * loop writes back three components, src/main/gfmd_misc.h:121-124).
+ * Replaces: GFMDSolverStatic::prec_gradient (src/solvers/gfmd_solver_static.cpp:253-269)
+ * with precondition_gradient<DEF_G> (src/main/gfmd_misc.h:40-133). */
+int gfmd_prec_gradient(gfmd_handle_t h, const double *cavg, const double *d_g, double *d_gP);
+
+/* The same on host buffers [ndof][nx*ny] (copies in and out inside the call).
+ * Replaces: GFMDSolverStatic::prec_gradient with FixGFMD's CPU double** buffers. */
+int gfmd_prec_gradient_host(gfmd_handle_t h, const double *cavg, const double *g, double *gP);
+
 /* Static minimization of elastic + obstacle energy from the displacements in
  * d_u (device, [ndof][nx*ny], FP64; updated in place).  Replaces LAMMPS'
  * minimize driving fix gfmd through min_pre_force/min_post_force

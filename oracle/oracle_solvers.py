@@ -264,6 +264,22 @@ def preconditioner(full, nx, ny, shift, post_force):
     return apply
 
 
+def prec_gradient(full, cavg, g, nx, ny):
+    """GFMDSolverStatic::prec_gradient (src/solvers/gfmd_solver_static.cpp:253-269):
+    gP = IFFT((Phi(q) + Cavg)^{-1} FFT(g)), table `full` [nx*ny, d, d] as
+    fill_phi_buffer leaves it (divided by nx*ny), both transforms unscaled
+    (forward exp(-i), backward exp(+i)).  For d > 3 precondition_gradient<DEF_G>
+    writes back three components only (src/main/gfmd_misc.h:121-124): the other
+    components leave the transform pair as nx*ny*g."""
+    d = g.shape[0]
+    gq = np.fft.fft2(g.reshape(d, nx, ny), axes=(1, 2)).reshape(d, -1)
+    M = np.linalg.inv(full + np.asarray(cavg, float)[None])
+    out = np.einsum("qij,jq->iq", M, gq)
+    if d > 3:
+        out[3:] = gq[3:]
+    return (np.fft.ifft2(out.reshape(d, nx, ny), axes=(1, 2)) * (nx * ny)).real.reshape(d, -1)
+
+
 def fire(elastic, ob, u, nx, ny, ftol=1e-6, maxiter=100000, minsteps=10, incfac=1.2,
          decfac=0.5, mix_in=0.1, mixdec=0.99, dtmax=0.001, dt=None, xlimit=0.0):
     """FixFIRE (src/cuda/fix_fire.cpp:117-297) with unit masses."""

@@ -159,4 +159,57 @@ int gref_post_force(const char *args, int nx, int ny, const double *u,
   }
 }
 
+/* One call of the reference's GFMDSolverStatic::prec_gradient
+ * (src/solvers/gfmd_solver_static.cpp:253-269): gP from g and Cavg
+ * (ndof*ndof), both [ndof][nx*ny]. */
+int gref_prec_gradient(const char *args, int nx, int ny, const double *cavg,
+                       const double *g, double *gP) {
+  try {
+    Env env;
+    Args a(args);
+    std::unique_ptr<StiffnessKernel> k(make_kernel(env, a));
+    int ndof = k->get_dimension();
+    int nxy = nx * ny;
+    int carg = 0;
+    GFMDSolverStatic solver(&env.lmp, 0, &carg, nullptr);
+    solver.set_grid_size(nx, ny, ndof);
+    solver.set_kernel(k.get(), true);
+    double **gb, **pb;
+    env.memory.create(gb, ndof, nxy, "gref:g");
+    env.memory.create(pb, ndof, nxy, "gref:gP");
+    std::memcpy(&gb[0][0], g, sizeof(double) * (size_t)ndof * nxy);
+    std::vector<double> c(cavg, cavg + (size_t)ndof * ndof);
+    solver.prec_gradient(c.data(), gb, pb);
+    std::memcpy(gP, &pb[0][0], sizeof(double) * (size_t)ndof * nxy);
+    env.memory.destroy(gb);
+    env.memory.destroy(pb);
+    return 0;
+  } catch (const std::exception &e) {
+    g_last_error = e.what();
+    return -1;
+  }
+}
+
+/* GFMDSolverFFT::dump_stiffness (greens = 0) or dump_greens_function
+ * (greens = 1) of a static solver on an nx x ny grid
+ * (src/solvers/gfmd_solver_fft.cpp:294-420); the files go to the current
+ * directory. */
+int gref_dump(const char *args, int nx, int ny, int greens) {
+  try {
+    Env env;
+    Args a(args);
+    std::unique_ptr<StiffnessKernel> k(make_kernel(env, a));
+    int carg = 0;
+    GFMDSolverStatic solver(&env.lmp, 0, &carg, nullptr);
+    solver.set_grid_size(nx, ny, k->get_dimension());
+    solver.set_kernel(k.get(), true);
+    if (greens) solver.dump_greens_function();
+    else solver.dump_stiffness();
+    return 0;
+  } catch (const std::exception &e) {
+    g_last_error = e.what();
+    return -1;
+  }
+}
+
 }  // extern "C"

@@ -1,7 +1,8 @@
 """Generate the golden fixtures of tests/golden/ from the reference itself.
 
-Runs the reference's own, unmodified ``fill_phi_buffer`` and
-``GFMDSolverStatic::post_force`` through oracle/_ref/libgfmdref.so (built
+Runs the reference's own, unmodified ``fill_phi_buffer``,
+``GFMDSolverStatic::post_force``, ``GFMDSolverStatic::prec_gradient`` and the
+``GFMDSolverFFT`` stiffness / Green's function dumps through oracle/_ref/libgfmdref.so (built
 from the reference sources by oracle/ref/Makefile; needs the reference tree,
 so this script runs only where it is present).  Each fixture stores the
 kernel arguments, the grid, seeded displacements, the reference's forces,
@@ -52,6 +53,12 @@ BOX_STYLES = ("isotropic", "nonperiodic")
 
 SEED = 20261203
 
+# GFMDSolverStatic::prec_gradient fixtures (tests/golden/prec/): kernel, grid
+PREC_CASES = [
+    ("prec_sc100_nnn_h16_8x6", "ft sc100 1 1.0 pair-potential 2 1.0 1.0 height 16", 8, 6),
+    ("prec_fcc100x2_h8_6x8", "ft fcc100 1.0 2 pair-potential 1 1.0 height 8", 6, 8),
+]
+
 
 def load_ref() -> ctypes.CDLL:
     if not os.path.exists(REF_LIB):
@@ -85,8 +92,61 @@ def run_case(L, args: str, nx: int, ny: int, seed: int):
     return d, ht.value, phi, linf, u, f, e.value, u0
 
 
+def run_prec_case(L, args: str, nx: int, ny: int, seed: int):
+    L.gref_set_box(ctypes.c_double(1.0), ctypes.c_double(1.0))
+    nd, ht = ctypes.c_int(), ctypes.c_int()
+    if L.gref_kernel_info(args.encode(), ctypes.byref(nd), ctypes.byref(ht)):
+        raise RuntimeError(L.gref_last_error().decode())
+    d = nd.value
+    rng = np.random.default_rng(seed)
+    g = rng.normal(0.0, 1.0, (d, nx * ny))
+    c = rng.normal(0.0, 0.1, (d, d))
+    cavg = c + c.T + 0.5 * np.eye(d)
+    gP = np.zeros_like(g)
+    if L.gref_prec_gradient(args.encode(), nx, ny, cavg.ctypes.data_as(ctypes.c_void_p),
+                            g.ctypes.data_as(ctypes.c_void_p), gP.ctypes.data_as(ctypes.c_void_p)):
+        raise RuntimeError(L.gref_last_error().decode())
+    return dict(args=np.array(args), nx=nx, ny=ny, ndof=d, cavg=cavg, g=g, gP=gP)
+
+
+# GFMDSolverFFT::dump_stiffness / dump_greens_function fixtures
+# (tests/golden/dumps/): the reference's files as text, kernel and grid
+DUMP_CASES = [
+    ("dump_fcc100x2_h8_5x3", "ft fcc100 1.0 2 pair-potential 1 1.0 height 8", 5, 3),
+]
+
+
+def run_dump_case(L, args: str, nx: int, ny: int):
+    import tempfile
+    L.gref_set_box(ctypes.c_double(1.0), ctypes.c_double(1.0))
+    out = dict(args=np.array(args), nx=nx, ny=ny)
+    cwd = os.getcwd()
+    for greens in (0, 1):
+        with tempfile.TemporaryDirectory() as d:
+            os.chdir(d)
+            try:
+                if L.gref_dump(args.encode(), nx, ny, greens):
+                    raise RuntimeError(L.gref_last_error().decode())
+                for fn in sorted(os.listdir(d)):
+                    with open(fn) as fh:
+                        out["file:" + fn] = np.array(fh.read())
+            finally:
+                os.chdir(cwd)
+    return out
+
+
 def main() -> int:
     L = load_ref()
+    os.makedirs(os.path.join(HERE, "dumps"), exist_ok=True)
+    for name, args, nx, ny in DUMP_CASES:
+        path = os.path.join(HERE, "dumps", f"{name}.npz")
+        np.savez_compressed(path, **run_dump_case(L, args, nx, ny))
+        print(f"{name} -> {os.path.getsize(path)} bytes")
+    os.makedirs(os.path.join(HERE, "prec"), exist_ok=True)
+    for i, (name, args, nx, ny) in enumerate(PREC_CASES):
+        path = os.path.join(HERE, "prec", f"{name}.npz")
+        np.savez_compressed(path, **run_prec_case(L, args, nx, ny, SEED + 100 + i))
+        print(f"{name} -> {os.path.getsize(path)} bytes")
     for i, (name, args, nx, ny, keep_phi) in enumerate(CASES):
         d, h, phi, linf, u, f, e, u0 = run_case(L, args, nx, ny, SEED + i)
         out = dict(args=np.array(args), nx=nx, ny=ny, ndof=d, height=h, u=u, f=f,

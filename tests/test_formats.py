@@ -78,3 +78,59 @@ def test_post_force_writes_the_q_space_dump(tmp_path):
     f = np.empty_like(u)
     s.post_force(u, f, dump_prefix=str(tmp_path / "step"))
     assert (tmp_path / "step.q.u0.real.out").exists() and (tmp_path / "step.q.e.out").exists()
+
+
+def _dump_fixtures():
+    import glob
+    import os
+    return sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "dumps", "*.npz")))
+
+
+def _check_dump_dir(directory, c):
+    # same files, same line and column layout, values within the "%e" digits
+    # (noise-level entries of a table, ~1e-18, differ between any two
+    # computations of it, hence a floor at 1e-12 of the dump's largest value)
+    import os
+    want = {k[5:]: str(c[k]) for k in c if k.startswith("file:")}
+    stem = "g" if any(k.startswith("g") for k in os.listdir(directory)) else "phi"
+    mine = {fn: open(os.path.join(directory, fn)).read() for fn in os.listdir(directory)}
+    assert set(mine) == {k for k in want if k.startswith(stem)}
+    scale = max(np.abs(np.array(want[fn].split(), float)).max(initial=0.0) for fn in mine)
+    for fn, text in mine.items():
+        ref = want[fn]
+        assert [len(l.split()) for l in text.split("\n")] == [len(l.split()) for l in ref.split("\n")]
+        assert all(l == "" or (l.startswith(" ") and l.endswith(" ")) for l in text.split("\n"))
+        a = np.array(text.split(), float)
+        b = np.array(ref.split(), float)
+        if b.size:
+            assert np.abs(a - b).max() <= 1e-6 * np.abs(b).max() + 1e-12 * scale
+
+
+@pytest.mark.parametrize("path", _dump_fixtures(), ids=lambda p: p.rsplit("/", 1)[-1][:-4])
+def test_stiffness_and_greens_dumps_match_the_reference(path, tmp_path):
+    from conftest import kernel_for, load_golden
+    c = load_golden(path)
+    nx, ny = int(c["nx"]), int(c["ny"])
+    full, _ = kernel_for(c).phi_table(nx, ny, "full")
+    for greens in (False, True):
+        d = tmp_path / ("g" if greens else "phi")
+        d.mkdir()
+        fmt.write_stiffness_dump(str(d), full, nx, ny, greens=greens)
+        _check_dump_dir(str(d), c)
+
+
+@pytest.mark.gpu
+def test_solver_dump_stiffness_and_greens_function(tmp_path):
+    from conftest import kernel_for, load_golden
+    path = _dump_fixtures()[0]
+    c = load_golden(path)
+    nx, ny = int(c["nx"]), int(c["ny"])
+    k = kernel_for(c)
+    s = gfmd_pkg().gfmd_solver_factory("static/gb300")
+    s.set_grid_size(nx, ny, k.get_dimension())
+    s.set_kernel(k)
+    for greens in (False, True):
+        d = tmp_path / ("g" if greens else "phi")
+        d.mkdir()
+        (s.dump_greens_function if greens else s.dump_stiffness)(str(d))
+        _check_dump_dir(str(d), c)

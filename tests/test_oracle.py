@@ -3,6 +3,7 @@
 The golden fixtures hold forces, energies and u(q=0) of the reference's
 unmodified GFMDSolverStatic::post_force (see tests/golden/make_golden.py).
 """
+import glob
 import os
 
 import numpy as np
@@ -68,3 +69,20 @@ def test_half_table_expands_to_reference_table():
     half, _ = k.phi_table(nx, ny, "half")
     full = half_to_full(half, nx, ny)
     assert np.abs(full - c["phi"]).max() <= 1e-13 * np.abs(c["phi"]).max()
+
+
+def prec_cases():
+    return sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "prec", "*.npz")))
+
+
+@pytest.mark.parametrize("path", prec_cases(), ids=lambda p: os.path.basename(p)[:-4])
+def test_oracle_prec_gradient_matches_reference_fixture(path):
+    # the fixtures hold the reference's own GFMDSolverStatic::prec_gradient
+    # output (tests/golden/make_golden.py), including its ndof > 3 behaviour
+    from solver_cases import osv
+
+    c = load_golden(path)
+    nx, ny = int(c["nx"]), int(c["ny"])
+    full, _ = kernel_for(c).phi_table(nx, ny, "full")
+    gP = osv.prec_gradient(full, c["cavg"], c["g"], nx, ny)
+    assert rel_l2(gP, c["gP"]) <= 1e-12

@@ -315,3 +315,40 @@ def test_nve_energy_conservation_on_the_nonperiodic_kernel():
     v = torch.zeros_like(u)
     e, _ = s.run_dynamics(u, v, 0.01, 0.0, 20000)
     assert np.abs(e - e.mean()).max() / abs(e.mean()) < 1e-4
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_prec_gradient_matches_reference_fixture(prec):
+    # GFMDSolverStatic::prec_gradient of the reference (fixtures from its own
+    # code, tests/golden/prec/), through gfmd_prec_gradient; the same Cavg
+    # again (cached inverses), another Cavg (rebuilt), a new table (rebuilt)
+    import glob
+    import os
+
+    from conftest import kernel_for, load_golden
+
+    tol = 1e-11 if prec == "f64" else 2e-5
+    paths = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "prec", "*.npz")))
+    assert paths
+    for path in paths:
+        c = load_golden(path)
+        nx, ny, d = int(c["nx"]), int(c["ny"]), int(c["ndof"])
+        half, linf = kernel_for(c).phi_table(nx, ny, "half")
+        s = _solver(nx, ny, d, half, linf, prec)
+        g = torch.from_numpy(c["g"]).cuda()
+        gP = torch.empty_like(g)
+        for _ in range(2):
+            gP.fill_(0.0)
+            s.prec_gradient(c["cavg"], g, gP)
+            torch.cuda.synchronize()
+            assert rel_l2(gP.cpu().numpy(), c["gP"]) <= tol
+        full = half_to_full(half, nx, ny)
+        c2 = c["cavg"] + 0.3 * np.eye(d)
+        s.prec_gradient(c2, g, gP)
+        assert rel_l2(gP.cpu().numpy(), osv.prec_gradient(full, c2, c["g"], nx, ny)) <= tol
+        s.set_phi(2.0 * half, "half", linf)
+        s.prec_gradient(c2, g, gP)
+        assert rel_l2(gP.cpu().numpy(), osv.prec_gradient(2.0 * full, c2, c["g"], nx, ny)) <= tol
+        g_ = gfmd_pkg()
+        with pytest.raises(g_.GFMDError):
+            s.prec_gradient(c2 + np.triu(np.ones((d, d)), 1), g, gP)  # not symmetric

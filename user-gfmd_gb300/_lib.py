@@ -153,6 +153,8 @@ SIGNATURES = {
     "gfmd_minimize": [_vp, ctypes.POINTER(Obstacle), ctypes.POINTER(MinParams), _vp,
                       ctypes.POINTER(MinReport)],
     "gfmd_make_preconditioner": [_vp, _c_dbl, ctypes.POINTER(_vp)],
+    "gfmd_prec_gradient": [_vp, _vp, _vp, _vp],
+    "gfmd_prec_gradient_host": [_vp, _vp, _vp, _vp],
     "gfmd_minimize_batch": [_c_int, ctypes.POINTER(BatchItem), ctypes.POINTER(MinParams)],
     "gfmd_run_dynamics": [_vp, ctypes.POINTER(Obstacle), _c_dbl, _c_dbl, _c_int, _vp, _vp, _vp,
                           ctypes.POINTER(MinReport)],

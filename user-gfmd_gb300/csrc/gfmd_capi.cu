@@ -10,6 +10,7 @@
 #include <cstring>
 #include <memory>
 #include <algorithm>
+#include <atomic>
 #include <tuple>
 #include <mutex>
 #include <map>
@@ -57,6 +58,7 @@ void release(gfmd_solver *h) {
     if (p) cudaFree(p);
   if (h->ws) cudaFree(h->ws);
   if (h->ws_host) cudaFreeHost(h->ws_host);
+  release(h->prec_grad);
   delete h;
 }
 
@@ -439,6 +441,9 @@ cudaError_t autotune(gfmd_solver *h) {
 
 int gfmd_set_phi(gfmd_handle_t h, const double *phi, int layout, const double *linf) {
   if (!h || !phi) return fail(GFMD_EINVAL, "gfmd_set_phi: NULL argument");
+  release(h->prec_grad);  // built from the previous table
+  h->prec_grad = nullptr;
+  h->prec_cavg.clear();
   if (layout != GFMD_PHI_FULL && layout != GFMD_PHI_HALF)
     return fail(GFMD_EINVAL, "gfmd_set_phi: unknown layout");
   const gfmd::Geom &g = h->g;
@@ -519,18 +524,33 @@ int gfmd_plan_info(gfmd_handle_t h, int *rows_per_block, int *phi_prefetch) {
   return GFMD_OK;
 }
 
-int gfmd_make_preconditioner(gfmd_handle_t h, double shift, gfmd_handle_t *out) {
-  if (!h || !out) return fail(GFMD_EINVAL, "gfmd_make_preconditioner: NULL argument");
+}  // extern "C"
+
+// dst[i] = s * src[i], grid-stride
+__global__ void k_scaled_copy(const double *__restrict__ src, double *__restrict__ dst, size_t n, double s) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = s * src[i];
+}
+
+// A new handle on h's grid and precision whose force evaluation applies
+// -scale * A(q)^{-1}, A(q) = block(Phi table entry of h) built by `fill`
+// (which receives the Hermitian block of h's table as uploaded, i.e. already
+// divided by nx*ny, and may change it in place).  The inverse is Gauss-Jordan
+// without pivoting (A Hermitian positive definite); its Hermitian part is
+// packed.  Returns a GFMD status; `who` prefixes messages.
+template <typename Fill>
+static int inverse_table_handle(gfmd_handle_t h, const char *who, double scale, Fill fill,
+                                gfmd_handle_t *out) {
   *out = nullptr;
-  if (!h->have_phi) return fail(GFMD_ENOPHI, "gfmd_make_preconditioner: no stiffness table uploaded");
-  if (!(shift > 0.0) || !std::isfinite(shift)) return fail(GFMD_EINVAL, "gfmd_make_preconditioner: shift must be > 0");
+  const std::string w(who);
+  if (!h->have_phi) return fail(GFMD_ENOPHI, w + ": no stiffness table uploaded");
   const gfmd::Geom &g = h->g;
   gfmd_handle_t p = nullptr;
   int rc = gfmd_create(g.nx, g.ny, g.ndof, h->precision, &p);
   if (rc != GFMD_OK) return rc;
   if (p->fast != h->fast) {  // same parameters give the same path
     release(p);
-    return fail(GFMD_ECUDA, "gfmd_make_preconditioner: path mismatch");
+    return fail(GFMD_ECUDA, w + ": path mismatch");
   }
   const int D = g.ndof, D2 = D * D;
   const size_t nslot = (size_t)g.nyc * g.nxp, nel = nslot * D2;
@@ -548,12 +568,11 @@ int gfmd_make_preconditioner(gfmd_handle_t h, double shift, gfmd_handle_t *out) 
     }
     if (e != cudaSuccess) {
       release(p);
-      return cuda_fail(e, "gfmd_make_preconditioner: download");
+      return cuda_fail(e, (w + ": download").c_str());
     }
   }
-  const double N = (double)g.nx * (double)g.ny;
   const bool fused = h->fast;
-  bool ok = true;
+  std::atomic<bool> ok(true);
   parallel_for((long)nslot, [&](long a, long b) {
     std::vector<std::complex<double>> A(D2), I(D2);
     for (long t = a; t < b; t++) {
@@ -561,22 +580,26 @@ int gfmd_make_preconditioner(gfmd_handle_t h, double shift, gfmd_handle_t *out) 
       const size_t base = fused ? ((size_t)ky * (g.nxp / 32) + xs / 32) * D2 * 32 + (xs % 32)
                                 : (size_t)ky * D2 * g.nxp + xs;
       const size_t ps = fused ? 32 : (size_t)g.nxp;
-      // Hermitian block Phi = N * table, plus the shift
-      for (int i = 0; i < D; i++) A[i * D + i] = N * tab[base + (size_t)i * ps] + shift;
+      // Hermitian block of the uploaded table
+      for (int i = 0; i < D; i++) A[i * D + i] = tab[base + (size_t)i * ps];
       int q = D;
       for (int i = 0; i < D; i++)
         for (int j = i + 1; j < D; j++) {
-          const std::complex<double> v(N * tab[base + (size_t)q * ps], N * tab[base + (size_t)(q + 1) * ps]);
+          const std::complex<double> v(tab[base + (size_t)q * ps], tab[base + (size_t)(q + 1) * ps]);
           A[i * D + j] = v;
           A[j * D + i] = std::conj(v);
           q += 2;
         }
+      fill(A.data());
       // Gauss-Jordan inverse (Hermitian positive definite: no pivoting)
       for (int i = 0; i < D2; i++) I[i] = 0.0;
       for (int i = 0; i < D; i++) I[i * D + i] = 1.0;
       for (int c = 0; c < D; c++) {
         const std::complex<double> piv = A[c * D + c];
-        if (!(std::abs(piv) > 0.0)) { ok = false; break; }
+        if (!(std::abs(piv) > 0.0) || !std::isfinite(std::abs(piv))) {
+          ok = false;
+          break;
+        }
         const std::complex<double> ip = 1.0 / piv;
         for (int k = 0; k < D; k++) {
           A[c * D + k] *= ip;
@@ -592,12 +615,12 @@ int gfmd_make_preconditioner(gfmd_handle_t h, double shift, gfmd_handle_t *out) 
           }
         }
       }
-      // pack M / N (Hermitian part)
-      for (int i = 0; i < D; i++) tab[base + (size_t)i * ps] = I[i * D + i].real() / N;
+      // pack scale * inverse (Hermitian part)
+      for (int i = 0; i < D; i++) tab[base + (size_t)i * ps] = scale * I[i * D + i].real();
       q = D;
       for (int i = 0; i < D; i++)
         for (int j = i + 1; j < D; j++) {
-          const std::complex<double> v = 0.5 * (I[i * D + j] + std::conj(I[j * D + i])) / N;
+          const std::complex<double> v = 0.5 * scale * (I[i * D + j] + std::conj(I[j * D + i]));
           tab[base + (size_t)q * ps] = v.real();
           tab[base + (size_t)(q + 1) * ps] = v.imag();
           q += 2;
@@ -606,7 +629,7 @@ int gfmd_make_preconditioner(gfmd_handle_t h, double shift, gfmd_handle_t *out) 
   });
   if (!ok) {
     release(p);
-    return fail(GFMD_ENONFINITE, "gfmd_make_preconditioner: singular block");
+    return fail(GFMD_ENONFINITE, w + ": singular block");
   }
   cudaError_t e;
   if (f64) {
@@ -618,15 +641,78 @@ int gfmd_make_preconditioner(gfmd_handle_t h, double shift, gfmd_handle_t *out) 
   }
   if (e != cudaSuccess) {
     release(p);
-    return cuda_fail(e, "gfmd_make_preconditioner: upload");
+    return cuda_fail(e, (w + ": upload").c_str());
   }
   p->have_phi = true;
   e = autotune(p);
   if (e != cudaSuccess) {
     release(p);
-    return cuda_fail(e, "gfmd_make_preconditioner: plan autotuning");
+    return cuda_fail(e, (w + ": plan autotuning").c_str());
   }
   *out = p;
+  return GFMD_OK;
+}
+
+extern "C" {
+
+int gfmd_make_preconditioner(gfmd_handle_t h, double shift, gfmd_handle_t *out) {
+  if (!h || !out) return fail(GFMD_EINVAL, "gfmd_make_preconditioner: NULL argument");
+  *out = nullptr;
+  if (!(shift > 0.0) || !std::isfinite(shift)) return fail(GFMD_EINVAL, "gfmd_make_preconditioner: shift must be > 0");
+  // (Phi + shift)^{-1} / N with Phi = N * table: the force path's unscaled
+  // transform pair then applies -(Phi + shift)^{-1}
+  const double N = (double)h->g.nx * (double)h->g.ny;
+  const int D = h->g.ndof;
+  return inverse_table_handle(h, "gfmd_make_preconditioner", 1.0 / N,
+                              [&](std::complex<double> *A) {
+                                for (int i = 0; i < D * D; i++) A[i] *= N;
+                                for (int i = 0; i < D; i++) A[i * D + i] += shift;
+                              },
+                              out);
+}
+
+int gfmd_prec_gradient(gfmd_handle_t h, const double *cavg, const double *d_g, double *d_gP) {
+  if (!h || !cavg || !d_g || !d_gP) return fail(GFMD_EINVAL, "gfmd_prec_gradient: NULL argument");
+  if (d_g == d_gP) return fail(GFMD_EINVAL, "gfmd_prec_gradient: g and gP must not alias");
+  const int D = h->g.ndof;
+  for (int i = 0; i < D; i++)
+    for (int j = 0; j < D; j++) {
+      const double a = cavg[i * D + j], b = cavg[j * D + i];
+      if (!std::isfinite(a)) return fail(GFMD_EINVAL, "gfmd_prec_gradient: Cavg holds NaN or Inf");
+      if (std::fabs(a - b) > 1e-12 * (std::fabs(a) + std::fabs(b)))
+        return fail(GFMD_EINVAL, "gfmd_prec_gradient: Cavg must be symmetric");
+    }
+  std::vector<double> c(cavg, cavg + (size_t)D * D);
+  if (!h->prec_grad || h->prec_cavg != c) {
+    release(h->prec_grad);
+    h->prec_grad = nullptr;
+    h->prec_cavg.clear();
+    gfmd_handle_t p = nullptr;
+    // the reference's operator (Phi(q)/N + Cavg)^{-1} between unscaled
+    // transforms; the force path applies -table, so the table is -M
+    int rc = inverse_table_handle(h, "gfmd_prec_gradient", -1.0,
+                                  [&](std::complex<double> *A) {
+                                    for (int i = 0; i < D * D; i++) A[i] += c[i];
+                                  },
+                                  &p);
+    if (rc != GFMD_OK) return rc;
+    h->prec_grad = p;
+    h->prec_cavg = c;
+  }
+  h->prec_grad->stream = h->stream;
+  cudaError_t e = gfmd::enqueue_force_opts(h->prec_grad, d_g, 0, d_gP, 0, h->prec_grad->d_scal, false);
+  if (e != cudaSuccess) return cuda_fail(e, "gfmd_prec_gradient");
+  if (D > 3) {
+    // precondition_gradient<DEF_G> writes back only three components for
+    // ndof > 3 (gfmd_misc.h:121-124); the others leave the unscaled
+    // transform pair as nx*ny*g
+    const size_t nxy = (size_t)h->g.nx * h->g.ny, n = (size_t)(D - 3) * nxy;
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)std::max(1, h->sm_count) * 8);
+    k_scaled_copy<<<blocks, 256, 0, h->stream>>>(d_g + 3 * nxy, d_gP + 3 * nxy, n,
+                                                  (double)h->g.nx * (double)h->g.ny);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "gfmd_prec_gradient");
+  }
   return GFMD_OK;
 }
 
@@ -681,6 +767,21 @@ int gfmd_post_force_host(gfmd_handle_t h, const double *u, double *f, double *ep
   CK(cudaStreamSynchronize(h->stream), "gfmd_post_force_host");
   if (!std::isfinite(e)) return fail(GFMD_ENONFINITE, "gfmd_post_force_host: energy is not finite");
   if (epot) *epot = e;
+  return GFMD_OK;
+}
+
+int gfmd_prec_gradient_host(gfmd_handle_t h, const double *cavg, const double *g, double *gP) {
+  if (!h || !cavg || !g || !gP) return fail(GFMD_EINVAL, "gfmd_prec_gradient_host: NULL argument");
+  const size_t n = (size_t)h->g.ndof * h->g.nx * h->g.ny;
+  if (!h->d_io) CK(cudaMalloc(&h->d_io, 2 * n * sizeof(double)), "gfmd_prec_gradient_host: staging");
+  double *dg = reinterpret_cast<double *>(h->d_io), *dp = dg + n;
+  CK(cudaMemcpyAsync(dg, g, n * sizeof(double), cudaMemcpyHostToDevice, h->stream),
+     "gfmd_prec_gradient_host: copy in");
+  int rc = gfmd_prec_gradient(h, cavg, dg, dp);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(gP, dp, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream),
+     "gfmd_prec_gradient_host: copy out");
+  CK(cudaStreamSynchronize(h->stream), "gfmd_prec_gradient_host");
   return GFMD_OK;
 }
 

@@ -97,6 +97,11 @@ struct gfmd_solver {
   void *ws = nullptr;
   size_t ws_bytes = 0;
   void *ws_host = nullptr;   // pinned control block
+
+  // handle applying (Phi/(nx ny) + Cavg)^{-1}, built by gfmd_prec_gradient for
+  // the Cavg it holds; dropped when the table changes
+  gfmd_solver *prec_grad = nullptr;
+  std::vector<double> prec_cavg;
 };
 
 namespace gfmd {

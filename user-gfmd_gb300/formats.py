@@ -16,6 +16,14 @@
   P.q.f<i>.real.out / .imag.out with F(q) = Phi(q) u(q) (the table scaled by
   1/(nx ny)), and P.q.uP.out, .fP.out, .e.out with sum |u|^2, sum |F|^2 and
   Re sum u conj(F) per wavevector; same line layout.
+* Stiffness and Green's function dumps (GFMDSolverFFT::dump_stiffness,
+  dump_greens_function, src/solvers/gfmd_solver_fft.cpp:294-420): files
+  phi<i><j>.real.out / .imag.out (g<i><j>... for the Green's function, the
+  inverse of each block of the table scaled by 1/(nx ny)) with " %e " per
+  value; the table's blocks are read in storage order, ny lines of nx values
+  (line j holds blocks j*nx .. j*nx + nx - 1); phitr/gtr .real/.imag.out
+  hold one empty line per line of the other files (the reference computes a
+  trace there but writes nothing else).
 
 Grids here are [ndof][nx*ny] arrays with index ix*ny + iy, as on the solver.
 """
@@ -102,6 +110,29 @@ def write_q_space_dump(dump_prefix: str, u, phi_full, nx: int, ny: int) -> None:
     _write_grid(f"{dump_prefix}.q.uP.out", (np.abs(uq) ** 2).sum(0), nx, ny)
     _write_grid(f"{dump_prefix}.q.fP.out", (np.abs(Fq) ** 2).sum(0), nx, ny)
     _write_grid(f"{dump_prefix}.q.e.out", (uq * np.conj(Fq)).sum(0).real, nx, ny)
+
+
+def write_stiffness_dump(directory: str, phi_full, nx: int, ny: int, greens: bool = False) -> None:
+    """dump_stiffness (greens False) or dump_greens_function (greens True)
+    of a full table [nx*ny, d, d] (scaled by 1/(nx ny)) into `directory`.
+    A singular block raises numpy.linalg.LinAlgError (the reference aborts)."""
+    import os
+
+    tab = np.asarray(phi_full, np.complex128).reshape(nx * ny, *np.shape(phi_full)[-2:])
+    d = tab.shape[-1]
+    if greens:
+        tab = np.linalg.inv(tab)
+    stem = "g" if greens else "phi"
+    blocks = tab.reshape(ny, nx, d, d)
+    for i in range(d):
+        for j in range(d):
+            for part, vals in (("real", blocks[:, :, i, j].real), ("imag", blocks[:, :, i, j].imag)):
+                with open(os.path.join(directory, f"{stem}{i}{j}.{part}.out"), "w") as fh:
+                    for row in vals:
+                        fh.write("".join(" %e " % v for v in row) + "\n")
+    for part in ("real", "imag"):
+        with open(os.path.join(directory, f"{stem}tr.{part}.out"), "w") as fh:
+            fh.write("\n" * ny)
 
 
 def half_to_full(half, nx: int, ny: int) -> np.ndarray:

@@ -20,9 +20,7 @@ GFMDSolverGB300::GFMDSolverGB300(LAMMPS *lmp, int narg, int *carg, char **arg) :
 }
 
 GFMDSolverGB300::~GFMDSolverGB300() {
-  if (pre_) gfmd_destroy(pre_);
   if (h_) gfmd_destroy(h_);
-  delete[] scratch_;
 }
 
 void GFMDSolverGB300::check(int rc) {
@@ -44,9 +42,6 @@ void GFMDSolverGB300::set_kernel(StiffnessKernel *kernel, bool normalize) {
   kernel->get_force_at_gamma_point(linf.data());
   check(gfmd_set_phi(h_, reinterpret_cast<double *>(&phi[0][0]), GFMD_PHI_FULL, linf.data()));
   destroy_complex_operator_buffer(phi);  // the library keeps its own packed copy
-  if (pre_) gfmd_destroy(pre_);
-  pre_ = nullptr;
-  pre_shift_ = -1.0;
 }
 
 double GFMDSolverGB300::post_force(void *u, void *f, char *dump_prefix) {
@@ -58,30 +53,11 @@ double GFMDSolverGB300::post_force(void *u, void *f, char *dump_prefix) {
 }
 
 void GFMDSolverGB300::prec_gradient(double *cavg, double **g, double **gP) {
-  const int nsq = ndof * ndof;
-  for (int i = 0; i < nsq; i++)
-    if (cavg[i] != ((i % (ndof + 1)) == 0 ? cavg[0] : 0.0))
-      error->all(FLERR, "static/gb300 preconditions with Cavg = c I only");
-  const double N = (double)nx * (double)ny;
-  const double shift = N * cavg[0];
-  if (!pre_ || shift != pre_shift_) {
-    if (pre_) gfmd_destroy(pre_);
-    pre_ = nullptr;
-    check(gfmd_make_preconditioner(h_, shift, &pre_));
-    pre_shift_ = shift;
-  }
-  const size_t n = (size_t)ndof * nxy_loc;
-  if (!scratch_) scratch_ = new double[n];
-  double e = 0.0;
-  // the handle's evaluation returns -(Phi + shift)^{-1} g
-  check(gfmd_post_force_host(pre_, &g[0][0], scratch_, &e));
-  const double s = -N * N;
-  for (size_t i = 0; i < n; i++) gP[0][i] = s * scratch_[i];
+  check(gfmd_prec_gradient_host(h_, cavg, &g[0][0], &gP[0][0]));
 }
 
 double GFMDSolverGB300::memory_usage() {
-  double b = 0.0, p = 0.0;
+  double b = 0.0;
   if (h_) gfmd_memory_usage(h_, &b);
-  if (pre_) gfmd_memory_usage(pre_, &p);
-  return b + p;
+  return b;
 }

@@ -28,9 +28,9 @@ class GFMDSolverGB300 : public GFMDSolver {
   // GFMDSolverStatic::post_force (gfmd_solver_static.cpp:145-249); u and f
   // are FixGFMD's contiguous double** [ndof][nxy] (memory->create)
   double post_force(void *u, void *f, char *dump_prefix) override;
-  // GFMDSolverStatic::prec_gradient (gfmd_solver_static.cpp:253-269) for a
-  // diagonal constant Cavg = c I: gP = N^2 (Phi + N c)^{-1} g, the operator the
-  // reference applies with its 1/N-scaled table and unnormalised transforms
+  // GFMDSolverStatic::prec_gradient (gfmd_solver_static.cpp:253-269):
+  // gP = IFFT((Phi/N + Cavg)^{-1} FFT(g)), unnormalised transforms, Cavg a
+  // symmetric ndof x ndof matrix (gfmd_prec_gradient_host)
   void prec_gradient(double *cavg, double **g, double **gP) override;
   double memory_usage() override;
 
@@ -38,10 +38,7 @@ class GFMDSolverGB300 : public GFMDSolver {
 
  private:
   gfmd_handle_t h_ = nullptr;
-  gfmd_handle_t pre_ = nullptr;  // preconditioner of the last shift
-  double pre_shift_ = -1.0;
   int precision_ = GFMD_PREC_F64;
-  double *scratch_ = nullptr;
   void check(int rc);
 };
 

@@ -230,6 +230,30 @@ class GFMDSolverGB300:
         lf = None if linf is None else np.ascontiguousarray(linf, dtype=np.float64)
         check(lib().gfmd_set_phi(self._handle(), _ptr(phi), lay, None if lf is None else _ptr(lf)))
 
+    def _host_table(self, who: str):
+        tab = getattr(self, "_dump_table", None)
+        if tab is None:
+            raise GFMDError(_lib.GFMD_EINVAL, f"{who} needs a table of at most "
+                            f"{self.DUMP_TABLE_BYTES >> 20} MiB kept by set_phi")
+        from . import formats
+        phi, layout = tab
+        return formats.half_to_full(phi, self.nx, self.ny) if layout == "half" else phi
+
+    def dump_stiffness(self, directory: str = ".") -> None:
+        """phi<i><j>.{real,imag}.out of the uploaded table (GFMDSolverFFT::dump_stiffness)."""
+        from . import formats
+        formats.write_stiffness_dump(directory, self._host_table("dump_stiffness"), self.nx, self.ny)
+
+    def dump_greens_function(self, directory: str = ".") -> None:
+        """g<i><j>.{real,imag}.out, the inverse of every block of the table
+        (GFMDSolverFFT::dump_greens_function)."""
+        from . import formats
+        try:
+            formats.write_stiffness_dump(directory, self._host_table("dump_greens_function"),
+                                         self.nx, self.ny, greens=True)
+        except np.linalg.LinAlgError as ex:
+            raise GFMDError(_lib.GFMD_ENONFINITE, f"dump_greens_function: singular block ({ex})")
+
     def set_stream(self, stream) -> None:
         addr = stream if isinstance(stream, int) else int(getattr(stream, "cuda_stream", 0))
         check(lib().gfmd_set_stream(self._handle(), addr))
@@ -275,6 +299,17 @@ class GFMDSolverGB300:
         out._h = h
         out.nx, out.ny, out.ndof = self.nx, self.ny, self.ndof
         return out
+
+    def prec_gradient(self, cavg, g, gP) -> None:
+        """gP = IFFT((Phi(q) + Cavg)^{-1} FFT(g)), [ndof, nx*ny] float64 CUDA
+        tensors (gfmd_prec_gradient) or contiguous host arrays
+        (gfmd_prec_gradient_host); Cavg is a symmetric ndof x ndof matrix
+        (GFMDSolverStatic::prec_gradient)."""
+        c = np.ascontiguousarray(np.broadcast_to(np.asarray(cavg, np.float64), (self.ndof, self.ndof)))
+        if _is_device(g):
+            check(lib().gfmd_prec_gradient(self._handle(), _ptr(c), _ptr(g), _ptr(gP)))
+        else:
+            check(lib().gfmd_prec_gradient_host(self._handle(), _ptr(c), _ptr(g), _ptr(gP)))
 
     def minimize(self, u, obstacle=None, method: str = "cg", ftol: float = 1e-6,
                  maxiter: int = 0, refine: "GFMDSolverGB300 | None" = None,
