@@ -154,9 +154,11 @@ typedef struct {
 #define GFMD_MIN_CG 0   /* Polak-Ribiere CG, Newton line search (LAMMPS min_style cg
                            as used on fix gfmd by tests/TEST_Hertz_x/lammps.in) */
 #define GFMD_MIN_FIRE 1 /* FIRE (FixFIRE, src/cuda/fix_fire.cpp:117-297) */
+#define GFMD_MIN_TR 2   /* trust region on the preconditioned gradient (min_style
+                           tr/gfmd, src/extras/min_tr_gfmd.cpp:95-241) */
 
 typedef struct {
-  int method;           /* GFMD_MIN_CG or GFMD_MIN_FIRE */
+  int method;           /* GFMD_MIN_CG, GFMD_MIN_FIRE or GFMD_MIN_TR */
   double ftol;          /* converged when max |f_i| <= ftol (per component) */
   int maxiter;          /* <= 0: 100000 */
   int recompute;        /* CG: recompute F_el(u) from scratch every n iterations (<= 0: 50) */
@@ -169,7 +171,11 @@ typedef struct {
   gfmd_handle_t precond; /* CG: optional preconditioner from gfmd_make_preconditioner
                             (same grid and precision as the handle): Polak-Ribiere
                             on z = (Phi + shift)^{-1} g, the reference's min_style
-                            cg/gfmd (src/extras/min_cg_gfmd.cpp:96-207) */
+                            cg/gfmd (src/extras/min_cg_gfmd.cpp:96-207);
+                            TR: the preconditioner of the step (none: identity) */
+  /* TR parameters (<= 0: defaults): largest trust radius (LAMMPS min_modify
+     dmax, default 0.1) and the acceptance ratio (0.01, min_tr_gfmd.cpp:76) */
+  double tr_dmax, tr_rho_tol;
 } gfmd_min_params_t;
 
 typedef struct {

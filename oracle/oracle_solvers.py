@@ -14,6 +14,7 @@ Reference behaviour restated:
              src/extras/fix_wall_map.cpp:686-817);
   FIRE       FixFIRE::initial_integrate / final_integrate
              (src/cuda/fix_fire.cpp:117-297);
+  TR         MinTRGFMD::iterate (src/extras/min_tr_gfmd.cpp:95-241);
   CG         Polak-Ribiere conjugate gradients (LAMMPS min_style cg, which
              the reference's Hertz tests run on fix gfmd) with a Newton line
              search along the direction;
@@ -278,6 +279,57 @@ def prec_gradient(full, cavg, g, nx, ny):
     if d > 3:
         out[3:] = gq[3:]
     return (np.fft.ifft2(out.reshape(d, nx, ny), axes=(1, 2)) * (nx * ny)).real.reshape(d, -1)
+
+
+def tr(elastic, precond, ob, u, nx, ny, ftol=1e-6, maxiter=100000, dmax=0.1, rho_tol=0.01):
+    """Trust region on the preconditioned force (MinTRGFMD::iterate,
+    src/extras/min_tr_gfmd.cpp:95-241): step a h, h = P f, a = min(1,
+    delta/sqrt(g.h)); accepted when (E_prev - E) >= rho_tol (a - a^2/2) g.h,
+    else undone with delta = a sqrt(g.h)/2; after acceptance delta =
+    min(2 delta, max(delta/2, 2|dE| / (min(1/2, 1 - delta/(2 sqrt(g.h))) sqrt(g.h)))).
+    P: callable (preconditioned force) or None (identity).  Converged when
+    max|f_i| <= ftol."""
+    u = u.copy()
+
+    def total(v):
+        fe, ee = elastic(v, True)
+        ew, fw, _, _ = wall(ob, v, nx, ny)
+        return fe + fw, ee + ew
+
+    f, E = total(u)
+    evals, it = 1, 0
+    P = precond if precond is not None else (lambda x: x.copy())
+    if np.abs(f).max() > ftol:
+        h = P(f)
+        g = f.copy()
+        gg = float((g * h).sum())
+        delta = min(dmax, np.sqrt(gg))
+        Eprev = E
+    while np.abs(f).max() > ftol and it < maxiter:
+        sg = np.sqrt(gg)
+        a = min(1.0, delta / sg)
+        u += a * h
+        f, E = total(u)
+        evals += 1
+        it += 1
+        if np.abs(f).max() <= ftol:
+            break
+        rho = (Eprev - E) / ((a - 0.5 * a * a) * gg)
+        if not rho >= rho_tol:
+            delta = 0.5 * a * sg
+            u -= a * h
+            f = g.copy()
+            E = Eprev
+        else:
+            fac = 2.0 * abs(E - Eprev) / (min(0.5, 1.0 - delta / (2.0 * sg)) * sg)
+            delta = min(2.0 * delta, max(0.5 * delta, fac))
+            Eprev = E
+            h = P(f)
+            g = f.copy()
+            gg = float((g * h).sum())
+    f, E = total(u)
+    return u, {"iterations": it, "force_evals": evals, "energy": E, "fmax": np.abs(f).max(),
+               "fnorm": np.sqrt((f * f).sum())}
 
 
 def fire(elastic, ob, u, nx, ny, ftol=1e-6, maxiter=100000, minsteps=10, incfac=1.2,

@@ -279,8 +279,10 @@ def test_preconditioned_cg_matches_oracle(prec):
 
 def test_hertz_on_the_nonperiodic_kernel_matches_oracle():
     # tests/TEST_Hertz_nonperiodic_64x64 of the reference: nonperiodic 0.3 1.0,
-    # Lennard-Jones sphere R = 100, CG to max|f| <= 1e-6; the GPU minimum
-    # against the oracle's and the reference's Hertz residual bound
+    # Lennard-Jones sphere R = 100; the GPU minimum against the oracle's and
+    # the reference's Hertz residual bound.  Solved to max|f| <= 1e-9: at the
+    # reference's 1e-6 the soft lateral modes of this table leave the two
+    # converged displacements 1e-5 apart
     from test_continuum_kernels import hertz_residual, hertz_sphere
 
     n = 64
@@ -289,13 +291,13 @@ def test_hertz_on_the_nonperiodic_kernel_matches_oracle():
     half, linf = k.phi_table(n, n, "half")
     el = oracle_elastic(half_to_full(half, n, n), linf, n, n)
     ob = hertz_sphere()
-    u_ref, r_ref = osv.cg(el, ob, np.zeros((3, n * n)), n, n, ftol=1e-6)
+    u_ref, r_ref = osv.cg(el, ob, np.zeros((3, n * n)), n, n, ftol=1e-9)
     s = _solver(n, n, 3, half, linf)
     o, keep = _gpu_obst(ob)
     u = torch.zeros(3, n * n, dtype=torch.float64, device="cuda")
-    rep = s.minimize(u, o, "cg", ftol=1e-6)
-    assert rep["fmax"] <= 1e-6
-    assert rel_l2(u.cpu().numpy(), u_ref) <= 1e-5
+    rep = s.minimize(u, o, "cg", ftol=1e-9)
+    assert rep["fmax"] <= 1e-9
+    assert rel_l2(u.cpu().numpy(), u_ref) <= 1e-7
     f = np.zeros((3, n * n))
     s.post_force(u.cpu().numpy(), f)
     res, _ = hertz_residual(f[2].reshape(n, n), n, n)
@@ -352,3 +354,39 @@ def test_prec_gradient_matches_reference_fixture(prec):
         g_ = gfmd_pkg()
         with pytest.raises(g_.GFMDError):
             s.prec_gradient(c2 + np.triu(np.ones((d, d)), 1), g, gP)  # not symmetric
+
+
+@pytest.mark.parametrize("with_precond", [True, False])
+def test_trust_region_matches_oracle(with_precond):
+    from conftest import oracle_post_force
+
+    nx = ny = 32
+    d, half, full, linf, ob = _problem(osv.SPHERE_EXP)
+    el = oracle_elastic(full, linf, nx, ny)
+    u0 = np.zeros((d, nx * ny))
+    P = osv.preconditioner(full, nx, ny, 0.05, oracle_post_force) if with_precond else None
+    u_ref, r_ref = osv.tr(el, P, ob, u0, nx, ny, ftol=1e-8, maxiter=20000)
+    s = _solver(nx, ny, d, half, linf)
+    pre = s.make_preconditioner(0.05) if with_precond else None
+    o, keep = _gpu_obst(ob)
+    u = torch.zeros(d, nx * ny, dtype=torch.float64, device="cuda")
+    rep = s.minimize(u, o, "tr", ftol=1e-8, maxiter=20000, precond=pre)
+    assert rep["fmax"] <= 1e-8
+    assert rel_l2(u.cpu().numpy(), u_ref) <= 1e-6
+    assert abs(rep["energy"] - r_ref["energy"]) <= 1e-9 * abs(r_ref["energy"])
+    assert abs(rep["iterations"] - r_ref["iterations"]) <= max(2, r_ref["iterations"] // 20)
+
+
+def test_mixed_precision_trust_region_with_fp64_refinement():
+    nx = ny = 32
+    d, half, full, linf, ob = _problem(osv.SPHERE_EXP)
+    el = oracle_elastic(full, linf, nx, ny)
+    u_ref, r_ref = osv.cg(el, ob, np.zeros((d, nx * ny)), nx, ny, ftol=1e-8)
+    s32 = _solver(nx, ny, d, half, linf, "f32")
+    s64 = _solver(nx, ny, d, half, linf)
+    pre = s32.make_preconditioner(0.05)
+    o, keep = _gpu_obst(ob)
+    u = torch.zeros(d, nx * ny, dtype=torch.float64, device="cuda")
+    rep = s32.minimize(u, o, "tr", ftol=1e-8, precond=pre, refine=s64)
+    assert rep["fmax"] <= 1e-8
+    assert rel_l2(u.cpu().numpy(), u_ref) <= 1e-6

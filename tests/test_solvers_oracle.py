@@ -52,3 +52,24 @@ def test_oracle_nve_conserves_energy():
     u0 = np.random.default_rng(3).normal(0, 0.1, (d, nx * ny))
     _, _, e = osv.verlet(el, None, u0, np.zeros_like(u0), nx, ny, 0.01, 0.0, 2000)
     assert np.abs(e - e.mean()).max() / abs(e.mean()) < 1e-4
+
+
+def test_oracle_trust_region_reaches_the_cg_minimum():
+    # MinTRGFMD restated: with the (Phi + shift)^{-1} preconditioner and
+    # without one (steepest descent in a trust region)
+    from conftest import oracle_post_force
+
+    nx = ny = 32
+    d, half, full, linf = tables(KERNEL_SC, nx, ny)
+    el = oracle_elastic(full, linf, nx, ny)
+    ob = sphere_spec(nx, ny, R=6.0, pen=0.3, cutoff=4.0)
+    u0 = np.zeros((d, nx * ny))
+    ucg, rcg = osv.cg(el, ob, u0, nx, ny, ftol=1e-8)
+    P = osv.preconditioner(full, nx, ny, 0.05, oracle_post_force)
+    up, rp = osv.tr(el, P, ob, u0, nx, ny, ftol=1e-8)
+    un, rn = osv.tr(el, None, ob, u0, nx, ny, ftol=1e-8, maxiter=20000)
+    for u, r in ((up, rp), (un, rn)):
+        assert r["fmax"] <= 1e-8
+        assert np.linalg.norm(u - ucg) <= 1e-5 * np.linalg.norm(ucg)
+        assert abs(r["energy"] - rcg["energy"]) <= 1e-9 * abs(rcg["energy"])
+    assert rp["iterations"] < rn["iterations"] / 10

@@ -31,6 +31,7 @@ GFMD_OBST_SPHERE_LJ = 2
 GFMD_OBST_MAP_EXP = 3
 GFMD_MIN_CG = 0
 GFMD_MIN_FIRE = 1
+GFMD_MIN_TR = 2
 
 
 class Obstacle(ctypes.Structure):
@@ -71,6 +72,8 @@ class MinParams(ctypes.Structure):
         ("fire_dt", ctypes.c_double),
         ("fire_xlimit", ctypes.c_double),
         ("precond", ctypes.c_void_p),
+        ("tr_dmax", ctypes.c_double),
+        ("tr_rho_tol", ctypes.c_double),
     ]
 
 
@@ -101,6 +104,8 @@ class BatchItem(ctypes.Structure):
         ("d_u", ctypes.c_void_p),
         ("report", MinReport),
         ("precond", ctypes.c_void_p),
+        ("tr_dmax", ctypes.c_double),
+        ("tr_rho_tol", ctypes.c_double),
     ]
 
 

@@ -198,6 +198,21 @@ __global__ void k_axpby(size_t n, double *__restrict__ v, const double *__restri
     v[i] = a * v[i] + b * f[i];
 }
 
+// dst = s * src
+__global__ void k_scale(size_t n, double *__restrict__ dst, const double *__restrict__ src, double s) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = s * src[i];
+}
+
+// partials of sum a.b
+__global__ void __launch_bounds__(kRedThreads) k_dot(size_t n, const double *__restrict__ a,
+                                                     const double *__restrict__ b, double *__restrict__ part) {
+  double acc[1] = {0.0};
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    acc[0] += a[i] * b[i];
+  block_reduce(acc, 1, false, part);
+}
+
 // ---------------------------------------------------------------------------
 // Host-side driver state.
 
@@ -358,6 +373,107 @@ int fire_solve(gfmd_solver *hp, const gfmd_obstacle_t *ob, const gfmd_min_params
   return status;
 }
 
+// ---- static: trust region ---------------------------------------------------
+// MinTRGFMD::iterate (src/extras/min_tr_gfmd.cpp:95-241): a step a*h along
+// the preconditioned force h = P f, a = min(1, delta/sqrt(g.h)); the step is
+// accepted when the energy drop is at least rho_tol of the model's
+// (a - a^2/2) g.h, else undone with the radius halved to a sqrt(g.h)/2; on
+// acceptance the radius becomes min(2 delta, max(delta/2,
+// 2|dE| / (min(1/2, 1 - delta/(2 sqrt(g.h))) sqrt(g.h)))).  P is the
+// preconditioner handle (-(Phi + shift)^{-1} as a force evaluation, so h is
+// minus its output) or the identity.  Convergence is max|f_i| <= ftol as for
+// the other methods (the reference's loop tests |f|_2 against LAMMPS' ftol,
+// and has an energy criterion that the reference's tests switch off with
+// etol = 0).
+int tr_solve(gfmd_solver *hp, const gfmd_obstacle_t *ob, const gfmd_min_params_t *prm,
+             double *u, gfmd_min_report_t *rep, std::string &err) {
+  Work w;
+  cudaError_t ce = work_init(w, hp, 5);  // fel, f, g, h, Pf
+  if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return ce == cudaErrorMemoryAllocation ? GFMD_ENOMEM : GFMD_ECUDA; }
+  double *fel = w.bufs[0], *f = w.bufs[1], *g = w.bufs[2], *h = w.bufs[3], *pf = w.bufs[4];
+  const Obst o = make_obst(ob, hp->g);
+  const double dmax = prm->tr_dmax > 0 ? prm->tr_dmax : 0.1;
+  const double rho_tol = prm->tr_rho_tol > 0 ? prm->tr_rho_tol : 0.01;
+  const int maxit = prm->maxiter > 0 ? prm->maxiter : 100000;
+  const size_t bytes = sizeof(double) * w.n;
+  gfmd_solver *hh = hp;
+  int evals = 0, it = 0, status = GFMD_ENOTCONVERGED;
+  double E = 0.0, Eprev = 0.0, fmax = 0.0, f2 = 0.0, gg = 0.0, delta = 0.0;
+  bool refining = false;
+  // h = P f, gg = f.h, g = f
+  auto precondition = [&]() -> cudaError_t {
+    if (prm->precond) {
+      RT(elastic(w, prm->precond, f, pf, false, nullptr));
+      evals++;
+      k_scale<<<w.nblk, kRedThreads, 0, w.st>>>(w.n, h, pf, -1.0);
+    } else {
+      RT(cudaMemcpyAsync(h, f, bytes, cudaMemcpyDeviceToDevice, w.st));
+    }
+    RT(cudaMemcpyAsync(g, f, bytes, cudaMemcpyDeviceToDevice, w.st));
+    k_dot<<<w.nblk, kRedThreads, 0, w.st>>>(w.n, g, h, w.part);
+    RT(fetch(w, 1, false));
+    gg = w.hres[0];
+    return cudaSuccess;
+  };
+  auto restart = [&]() -> cudaError_t {
+    RT(total_force(w, hh, o, u, fel, f, &E, &fmax, &f2));
+    evals++;
+    Eprev = E;
+    if (fmax <= prm->ftol || !std::isfinite(fmax)) return cudaSuccess;
+    RT(precondition());
+    delta = std::min(dmax, std::sqrt(gg));
+    return cudaSuccess;
+  };
+  ce = restart();
+  while (ce == cudaSuccess) {
+    if (!std::isfinite(fmax) || !std::isfinite(E)) { status = GFMD_ENONFINITE; break; }
+    if (fmax <= prm->ftol) {
+      if (prm->refine && !refining) {
+        refining = true;
+        hh = prm->refine;
+        if ((ce = restart()) != cudaSuccess) break;
+        continue;
+      }
+      status = GFMD_OK;
+      break;
+    }
+    if (it >= maxit) break;
+    if (!(gg > 0.0)) { status = GFMD_ENONFINITE; err = "the preconditioned gradient is not a descent direction"; break; }
+    const double sg = std::sqrt(gg), a = std::min(1.0, delta / sg);
+    k_axpby<<<w.nblk, kRedThreads, 0, w.st>>>(w.n, u, h, 1.0, a);
+    if ((ce = total_force(w, hh, o, u, fel, f, &E, &fmax, &f2)) != cudaSuccess) break;
+    evals++;
+    it++;
+    if (fmax <= prm->ftol) continue;  // converged at the new point
+    const double rho = (Eprev - E) / ((a - 0.5 * a * a) * gg);
+    if (!(rho >= rho_tol)) {
+      // declined: undo the step, keep the old gradient, shrink the radius
+      delta = 0.5 * a * sg;
+      k_axpby<<<w.nblk, kRedThreads, 0, w.st>>>(w.n, u, h, 1.0, -a);
+      if ((ce = cudaMemcpyAsync(f, g, bytes, cudaMemcpyDeviceToDevice, w.st)) != cudaSuccess) break;
+      E = Eprev;
+    } else {
+      const double fac = 2.0 * std::fabs(E - Eprev) / (std::min(0.5, 1.0 - delta / (2.0 * sg)) * sg);
+      delta = std::min(2.0 * delta, std::max(0.5 * delta, fac));
+      Eprev = E;
+      if ((ce = precondition()) != cudaSuccess) break;
+    }
+  }
+  if (ce == cudaSuccess && status != GFMD_ENONFINITE)
+    ce = total_force(w, hh, o, u, fel, f, &E, &fmax, &f2);  // fresh forces at the end point
+  if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return GFMD_ECUDA; }
+  if (rep) {
+    rep->iterations = it;
+    rep->force_evals = evals;
+    rep->energy = E;
+    rep->fmax = fmax;
+    rep->fnorm = std::sqrt(f2);
+  }
+  if (status == GFMD_ENOTCONVERGED) err = "trust region reached the iteration cap before max|f| <= ftol";
+  if (status == GFMD_ENONFINITE && err.empty()) err = "non-finite force during the trust-region solve";
+  return status;
+}
+
 }  // namespace
 
 cudaError_t report_total_force(gfmd_solver *hh, cudaStream_t st, const Obst &o, const double *u,
@@ -395,6 +511,7 @@ int gfmd_minimize(gfmd_handle_t h, const gfmd_obstacle_t *obst, const gfmd_min_p
   int rc;
   if (prm->method == GFMD_MIN_CG) rc = gfmd::cg_minimize(h, obst, prm, d_u, rep, err);
   else if (prm->method == GFMD_MIN_FIRE) rc = gfmd::fire_solve(h, obst, prm, d_u, rep, err);
+  else if (prm->method == GFMD_MIN_TR) rc = gfmd::tr_solve(h, obst, prm, d_u, rep, err);
   else return gfmd::set_error(GFMD_EINVAL, "gfmd_minimize: unknown method");
   if (rep) {
     rep->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

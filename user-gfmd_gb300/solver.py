@@ -318,13 +318,16 @@ class GFMDSolverGB300:
         tensor [ndof, nx*ny], updated in place); returns the report.  Raises
         GFMDError on failure (e.g. ENOTCONVERGED)."""
         p = _lib.MinParams()
-        p.method = _lib.GFMD_MIN_CG if method == "cg" else _lib.GFMD_MIN_FIRE
+        methods = {"cg": _lib.GFMD_MIN_CG, "fire": _lib.GFMD_MIN_FIRE, "tr": _lib.GFMD_MIN_TR}
+        if method not in methods:
+            raise ValueError(f"unknown method {method!r}")
+        p.method = methods[method]
         p.ftol = ftol
         p.maxiter = maxiter
         p.refine = refine._handle().value if refine is not None else None
         p.precond = precond._handle().value if precond is not None else None
-        for k, v in fire.items():
-            setattr(p, "fire_" + k, v)
+        for k, v in fire.items():  # FIRE parameters by name; TR ones as tr_dmax, tr_rho_tol
+            setattr(p, k if k.startswith("tr_") else "fire_" + k, v)
         rep = _lib.MinReport()
         ob = ctypes.byref(obstacle) if obstacle is not None else None
         rc = lib().gfmd_minimize(self._handle(), ob, ctypes.byref(p), _ptr(u), ctypes.byref(rep))
