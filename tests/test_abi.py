@@ -51,3 +51,41 @@ def test_solver_factory_names():
     assert g.gfmd_solver_factory("static/gb300/f32").precision == "f32"
     with pytest.raises(g.GFMDError):
         g.gfmd_solver_factory("nosuch")
+
+
+# ctypes mirror -> C typedef of include/gfmd_gb300.h
+_STRUCTS = {"Obstacle": "gfmd_obstacle_t", "MinParams": "gfmd_min_params_t",
+            "MinReport": "gfmd_min_report_t", "BatchItem": "gfmd_batch_item_t",
+            "SurfaceParams": "gfmd_surface_params_t"}
+
+
+def test_ctypes_structs_match_the_c_layout(tmp_path):
+    # sizeof and every field's offset, from the C compiler on the header
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    from importlib import import_module
+
+    lib = import_module("user-gfmd_gb300._lib")
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "gfmd_gb300.h"', "int main(void) {"]
+    for py, c in _STRUCTS.items():
+        lines.append(f'  printf("{py} size %zu\\n", sizeof({c}));')
+        for name, _ in getattr(lib, py)._fields_:
+            lines.append(f'  printf("{py} {name} %zu\\n", offsetof({c}, {name}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.check_call([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    got = {}
+    for line in subprocess.check_output([str(exe)], text=True).splitlines():
+        py, name, v = line.split()
+        got[(py, name)] = int(v)
+    for py in _STRUCTS:
+        S = getattr(lib, py)
+        assert got[(py, "size")] == ctypes.sizeof(S), py
+        for name, _ in S._fields_:
+            assert got[(py, name)] == getattr(S, name).offset, (py, name)

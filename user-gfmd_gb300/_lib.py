@@ -104,8 +104,6 @@ class BatchItem(ctypes.Structure):
         ("d_u", ctypes.c_void_p),
         ("report", MinReport),
         ("precond", ctypes.c_void_p),
-        ("tr_dmax", ctypes.c_double),
-        ("tr_rho_tol", ctypes.c_double),
     ]
 
 
