@@ -605,6 +605,23 @@ def run_gb300(args):
         e2e = {"value": ws / dt, "unit": "evals/s", "h2d_bytes_per_step": nb,
                "d2h_bytes_per_step": nb + 8,
                "call": "gfmd_post_force_host (FP64 host buffers, pinned)"}
+        # the host link this call is bound by: plain pinned copies of the same
+        # bytes (one direction at a time, as the call needs u before f)
+        ud = torch.empty(uh.shape, dtype=uh.dtype, device=dev)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        h2d = d2h = 0.0
+        for _ in range(3):
+            ev[0].record()
+            ud.copy_(uh, non_blocking=True)
+            ev[1].record()
+            fh.copy_(ud, non_blocking=True)
+            ev[2].record()
+            torch.cuda.synchronize()
+            h2d, d2h = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+        del ud
+        e2e["link"] = {"h2d_gbs": nb / (h2d * 1e-3) / 1e9, "d2h_gbs": nb / (d2h * 1e-3) / 1e9,
+                       "bound_evals_per_s": ws / ((h2d + d2h + ms) * 1e-3),
+                       "note": "ceiling = 1 / (H2D + D2H copy time of the step's bytes + device time)"}
 
     peak, peak_kind = measured_peaks()
     sz = 4 if args.precision == "f32" else 8

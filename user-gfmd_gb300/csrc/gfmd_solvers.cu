@@ -397,9 +397,13 @@ int tr_solve(gfmd_solver *hp, const gfmd_obstacle_t *ob, const gfmd_min_params_t
   const int maxit = prm->maxiter > 0 ? prm->maxiter : 100000;
   const size_t bytes = sizeof(double) * w.n;
   gfmd_solver *hh = hp;
-  int evals = 0, it = 0, status = GFMD_ENOTCONVERGED;
+  int evals = 0, it = 0, status = GFMD_ENOTCONVERGED, rejects = 0;
   double E = 0.0, Eprev = 0.0, fmax = 0.0, f2 = 0.0, gg = 0.0, delta = 0.0;
   bool refining = false;
+  // With a refine handle, the first (bulk) phase ends when max|f| <= ftol, or
+  // when its energies can no longer rank a step: the model decrease below
+  // the FP32 noise of the energy (64 ulp of |E|), or 32 rejections in a row.
+  const double e_noise = hp->precision == GFMD_PREC_F32 ? 64.0 * 5.960464477539063e-8 : 0.0;
   // h = P f, gg = f.h, g = f
   auto precondition = [&]() -> cudaError_t {
     if (prm->precond) {
@@ -440,6 +444,14 @@ int tr_solve(gfmd_solver *hp, const gfmd_obstacle_t *ob, const gfmd_min_params_t
     if (it >= maxit) break;
     if (!(gg > 0.0)) { status = GFMD_ENONFINITE; err = "the preconditioned gradient is not a descent direction"; break; }
     const double sg = std::sqrt(gg), a = std::min(1.0, delta / sg);
+    if (prm->refine && !refining &&
+        ((a - 0.5 * a * a) * gg <= e_noise * std::fabs(E) || rejects >= 32)) {
+      refining = true;
+      hh = prm->refine;
+      rejects = 0;
+      if ((ce = restart()) != cudaSuccess) break;
+      continue;
+    }
     k_axpby<<<w.nblk, kRedThreads, 0, w.st>>>(w.n, u, h, 1.0, a);
     if ((ce = total_force(w, hh, o, u, fel, f, &E, &fmax, &f2)) != cudaSuccess) break;
     evals++;
@@ -452,7 +464,9 @@ int tr_solve(gfmd_solver *hp, const gfmd_obstacle_t *ob, const gfmd_min_params_t
       k_axpby<<<w.nblk, kRedThreads, 0, w.st>>>(w.n, u, h, 1.0, -a);
       if ((ce = cudaMemcpyAsync(f, g, bytes, cudaMemcpyDeviceToDevice, w.st)) != cudaSuccess) break;
       E = Eprev;
+      rejects++;
     } else {
+      rejects = 0;
       const double fac = 2.0 * std::fabs(E - Eprev) / (std::min(0.5, 1.0 - delta / (2.0 * sg)) * sg);
       delta = std::min(2.0 * delta, std::max(0.5 * delta, fac));
       Eprev = E;
