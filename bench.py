@@ -404,24 +404,39 @@ BATCH_SIZES = (64, 128, 256, 384, 512, 1024)
 E_STAR_FCC111 = 1.54  # contact modulus of this kernel (the reference's Hertz fcc111 test)
 
 
-def batched_solve(g, torch, dev, nsurf=64, seed=20261203, ftol=1e-6):
+def batched_solve(g, torch, dev, nsurf=64, seed=20261203, ftol=1e-6, rank=0, ws=1):
     """64 independent surfaces, sizes drawn from {64..1024}^2, each indented
     by a self-affine rigid surface (H = 0.8, rms slope 0.1, cut-offs 4 a and
     L/2, random phases) under load control p in U[1e-3, 1e-2] E*, exp wall
     (eps = 1, range 0.5 a) on both atoms of the cell; FP32 CG bulk plus FP64
     refinement to max|f| <= 1e-6.  Timed twice: one surface after another,
-    and all surfaces in one batched graph (gfmd_minimize_batch)."""
+    and all surfaces in one batched graph (gfmd_minimize_batch).  With N
+    ranks the surfaces are partitioned (shard.partition, by N ndof^2), each
+    rank solves its share, times are the slowest rank's and the reports are
+    gathered (shard.gather_reports)."""
+    shard = importlib.import_module("user-gfmd_gb300.shard")
+
+    def sync_all():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+
     rng = np.random.default_rng(seed)
-    sizes = [int(x) for x in rng.choice(BATCH_SIZES, nsurf)]
-    loads = rng.uniform(1e-3, 1e-2, nsurf)
+    sizes_all = [int(x) for x in rng.choice(BATCH_SIZES, nsurf)]
+    loads_all = rng.uniform(1e-3, 1e-2, nsurf)
     k = g.StiffnessKernel(BATCH_KERNEL)
     d = k.get_dimension()
+    costs = [shard.surface_cost(n * n, d) for n in sizes_all]
+    parts = shard.partition(costs, ws)
+    mine = parts[rank]
+    sizes = [sizes_all[i] for i in mine]
+    loads = [loads_all[i] for i in mine]
     t0 = time.perf_counter()
     tabs = {n: k.phi_table(n, n, "half") for n in sorted(set(sizes))}
     t_phi = time.perf_counter() - t0
     cell_area = 3.0 ** 0.5  # a x a sqrt(3) rectangular cell, two atoms
     probs = []
-    for i, (n, p) in enumerate(zip(sizes, loads)):
+    for i, n, p in zip(mine, sizes, loads):
         half, linf = tabs[n]
         hs = []
         for prec in ("f32", "f64"):
@@ -434,60 +449,69 @@ def batched_solve(g, torch, dev, nsurf=64, seed=20261203, ftol=1e-6):
         ob = g.map_obstacle(zmap, 1.0, 0.5, z0=-float(zmap.min()), norm=-1, nlayer=2)
         ob.fz_ext = float(p) * E_STAR_FCC111 * cell_area / 2.0
         probs.append((hs[0], hs[1], ob, zmap, n))
-    dofs = sum(d * n * n for n in sizes)
+    dofs = sum(d * n * n for n in sizes_all)
 
     def fresh():
         return [torch.zeros(d, n * n, dtype=torch.float64, device=dev) for *_, n in probs]
 
     # warm-up: module load and first graph instantiation
-    small = next(p for p in probs if p[4] == min(sizes))
-    uw = torch.zeros(d, small[4] ** 2, dtype=torch.float64, device=dev)
-    try:
-        g.minimize_batch([(small[0], uw, small[2], small[1])], ftol=ftol, maxiter=3)
-    except g.GFMDError:
-        pass
+    if probs:
+        small = min(probs, key=lambda p: p[4])
+        uw = torch.zeros(d, small[4] ** 2, dtype=torch.float64, device=dev)
+        try:
+            g.minimize_batch([(small[0], uw, small[2], small[1])], ftol=ftol, maxiter=3)
+        except g.GFMDError:
+            pass
     us = fresh()
-    torch.cuda.synchronize()
+    sync_all()
     t0 = time.perf_counter()
     seq = [s32.minimize(u, ob, "cg", ftol=ftol, maxiter=50000, refine=s64)
            for (s32, s64, ob, _, _), u in zip(probs, us)]
-    torch.cuda.synchronize()
-    t_seq = time.perf_counter() - t0
+    sync_all()
+    t_seq = shard.max_over_ranks(time.perf_counter() - t0)
     ub = fresh()
-    torch.cuda.synchronize()
+    sync_all()
     t0 = time.perf_counter()
     reps = g.minimize_batch([(s32, u, ob, s64) for (s32, s64, ob, _, _), u in zip(probs, ub)],
-                            ftol=ftol, maxiter=50000)
-    torch.cuda.synchronize()
-    t_bat = time.perf_counter() - t0
-    same = all(torch.equal(a, b) for a, b in zip(us, ub))
+                            ftol=ftol, maxiter=50000) if probs else []
+    sync_all()
+    t_bat = shard.max_over_ranks(time.perf_counter() - t0)
+    same_local = all(torch.equal(a, b) for a, b in zip(us, ub))
+    # every rank's reports, in the global surface order
+    reps = list(shard.gather_reports(dict(zip(mine, reps))).values())
+    seq = list(shard.gather_reports(dict(zip(mine, seq))).values())
+    same = all(shard.gather_reports({rank: same_local}).values())
     its = [r["iterations"] for r in reps]
     # the same batch, preconditioned CG (shift 0.01)
     pres = [s32.make_preconditioner(0.01) for (s32, _, _, _, _) in probs]
     up_ = fresh()
-    try:
-        g.minimize_batch([(s32, u, ob, s64, p) for (s32, s64, ob, _, _), u, p in zip(probs, up_, pres)],
-                         ftol=ftol, maxiter=3)
-    except g.GFMDError:
-        pass
+    if probs:
+        try:
+            g.minimize_batch([(s32, u, ob, s64, p) for (s32, s64, ob, _, _), u, p in zip(probs, up_, pres)],
+                             ftol=ftol, maxiter=3)
+        except g.GFMDError:
+            pass
     up_ = fresh()
-    torch.cuda.synchronize()
+    sync_all()
     t0 = time.perf_counter()
     repp = g.minimize_batch([(s32, u, ob, s64, p) for (s32, s64, ob, _, _), u, p in zip(probs, up_, pres)],
-                            ftol=ftol, maxiter=50000)
-    torch.cuda.synchronize()
-    t_pcg = time.perf_counter() - t0
+                            ftol=ftol, maxiter=50000) if probs else []
+    sync_all()
+    t_pcg = shard.max_over_ranks(time.perf_counter() - t0)
+    repp = list(shard.gather_reports(dict(zip(mine, repp))).values())
     return {
         "config": f"{nsurf} x {BATCH_KERNEL}, sizes {BATCH_SIZES} (seeded), rough indenter "
                   "H 0.8 rms slope 0.1 cut-offs 4 a / L/2, load p in U[1e-3, 1e-2] E* "
                   f"(E* = {E_STAR_FCC111}), FP32 CG + FP64 refinement to max|f| <= {ftol}",
-        "sizes": sizes, "dofs_total": dofs,
+        "sizes": sizes_all, "dofs_total": dofs,
+        "shards": {"ranks": ws, "surfaces_per_rank": [len(p) for p in parts],
+                   "cost_per_rank": [sum(costs[i] for i in p) for p in parts]},
         "sequential_seconds": t_seq, "batched_seconds": t_bat, "speedup": t_seq / t_bat,
         "batched_preconditioned_seconds": t_pcg,
         "preconditioned_iterations_total": int(sum(r["iterations"] for r in repp)),
         "preconditioned_all_converged": all(r["status"] == 0 for r in repp),
         "iterations_total": int(sum(its)), "iterations_max": int(max(its)),
-        "dof_iterations_per_s": float(sum(d * n * n * r["iterations"] for n, r in zip(sizes, reps)) / t_bat),
+        "dof_iterations_per_s": float(sum(d * n * n * r["iterations"] for n, r in zip(sizes_all, reps)) / t_bat),
         "max_fmax": float(max(r["fmax"] for r in reps)),
         "all_converged": all(r["status"] == 0 for r in reps) and all(r["status"] == 0 for r in seq),
         "batched_equals_sequential": same,
@@ -635,7 +659,7 @@ def run_gb300(args):
     if not args.no_static:
         extra["static_solve"] = static_solve(g, torch, dev, stream, args.static_n)
     if not args.no_batch:
-        extra["batched_solve"] = batched_solve(g, torch, dev, args.batch_n)
+        extra["batched_solve"] = batched_solve(g, torch, dev, args.batch_n, rank=rank, ws=ws)
     if not args.no_warmstart:
         if args.ws_full:
             extra["warmstart"] = warmstart_run(g, torch, dev, 512, 2000, 10, 4096, 32)
