@@ -123,6 +123,57 @@ bool invert(int n, cplx *A) {
   return true;
 }
 
+// One step of the transfer-matrix recursion for a Hermitian positive definite
+// A (row-major, lower triangle read):  X = -V A^{-1} V^H = -W^H W with
+// A = L L^H (Cholesky) and W = L^{-1} V^H, about a third of the flops of an
+// explicit inverse and two products.  L and W are n*n scratch.  Returns false
+// when a pivot is not safely positive (below 1e-12 of its diagonal entry);
+// the caller then takes the Gauss-Jordan path.
+bool schur_step_chol(int n, const cplx *A, const cplx *V, cplx *X, cplx *L, cplx *W) {
+  for (int j = 0; j < n; j++) {
+    double djj = A[j * n + j].re;
+    for (int k = 0; k < j; k++) djj -= L[j * n + k].re * L[j * n + k].re + L[j * n + k].im * L[j * n + k].im;
+    if (!(djj > 1e-12 * std::fabs(A[j * n + j].re))) return false;
+    const double ljj = std::sqrt(djj), inv = 1.0 / ljj;
+    L[j * n + j] = {ljj, 0.0};
+    for (int i = j + 1; i < n; i++) {
+      double re = A[i * n + j].re, im = A[i * n + j].im;
+      for (int k = 0; k < j; k++) {  // - L[i][k] conj(L[j][k])
+        const cplx a = L[i * n + k], b = L[j * n + k];
+        re -= a.re * b.re + a.im * b.im;
+        im -= a.im * b.re - a.re * b.im;
+      }
+      L[i * n + j] = {re * inv, im * inv};
+    }
+  }
+  // W = L^{-1} V^H, V^H[i][c] = conj(V[c][i])
+  for (int i = 0; i < n; i++) {
+    const double inv = 1.0 / L[i * n + i].re;
+    for (int c = 0; c < n; c++) {
+      double re = V[c * n + i].re, im = -V[c * n + i].im;
+      for (int k = 0; k < i; k++) {
+        const cplx a = L[i * n + k], w = W[k * n + c];
+        re -= a.re * w.re - a.im * w.im;
+        im -= a.re * w.im + a.im * w.re;
+      }
+      W[i * n + c] = {re * inv, im * inv};
+    }
+  }
+  // X = -W^H W (Hermitian: upper triangle, mirrored)
+  for (int i = 0; i < n; i++)
+    for (int j = i; j < n; j++) {
+      double re = 0.0, im = 0.0;
+      for (int k = 0; k < n; k++) {  // conj(W[k][i]) W[k][j]
+        const cplx a = W[k * n + i], b = W[k * n + j];
+        re += a.re * b.re + a.im * b.im;
+        im += a.re * b.im - a.im * b.re;
+      }
+      X[i * n + j] = {-re, i == j ? 0.0 : -im};
+      if (j != i) X[j * n + i] = {-re, im};
+    }
+  return true;
+}
+
 }  // namespace
 
 // ---- crystal surfaces -------------------------------------------------------
@@ -783,6 +834,23 @@ bool StiffnessKernel::stiffness(double qx, double qy, cplx *phi, cplx *work) con
   if (height_ == 0) {
     std::memcpy(phi, U0, sizeof(cplx) * d2);
     return true;
+  }
+  // Cholesky steps while U + X stays safely positive definite (a Schur
+  // complement of the substrate's stiffness matrix); the Gauss-Jordan
+  // iteration of the reference otherwise, and at q = 0, where Phi = U0 + X
+  // cancels to O(1/height) and the reference's own elimination order keeps
+  // the table within 1e-13 of the reference's (Cholesky: 6e-13)
+  if (height_ > 0 && !(qx == 0.0 && qy == 0.0)) {
+    cplx *A = Vd, *L = T, *W = phi;  // scratch (Vd is built below if needed)
+    bool ok = schur_step_chol(d, U, V, X, L, W);
+    for (int it = 0; ok && it < height_ - 1; it++) {
+      for (int i = 0; i < d2; i++) A[i] = {U[i].re + X[i].re, U[i].im + X[i].im};
+      ok = schur_step_chol(d, A, V, X, L, W);
+    }
+    if (ok) {
+      for (int i = 0; i < d2; i++) phi[i] = {U0[i].re + X[i].re, U0[i].im + X[i].im};
+      return true;
+    }
   }
   for (int i = 0; i < d; i++)
     for (int j = 0; j < d; j++) Vd[i * d + j] = {-V[j * d + i].re, V[j * d + i].im};
