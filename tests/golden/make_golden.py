@@ -46,6 +46,8 @@ CASES = [
     ("nonperiodic_nu03_9x7", "nonperiodic 0.3 1.0", 9, 7, True),
     ("nonperiodic_nu025_16x12", "nonperiodic 0.25 2.0", 16, 12, True),
     ("nonperiodic_nu03_63x63", "nonperiodic 0.3 1.0", 63, 63, False),
+    # prime grid sizes: the host transform's generic radix
+    ("nonperiodic_nu03_31x29", "nonperiodic 0.3 1.0", 31, 29, True),
 ]
 
 # kernels that read the box lengths; the fixtures store them as xprd, yprd
