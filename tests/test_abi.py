@@ -42,6 +42,11 @@ def test_argument_errors_return_status_without_gpu():
     assert L.gfmd_post_force(None, None, None, None) == 1
     assert L.gfmd_set_phi(None, None, 0, None) == 1
     assert b"NULL" in L.gfmd_last_error()
+    c = (ctypes.c_double * 9)()
+    assert L.gfmd_prec_gradient(None, c, None, None) == 1
+    assert L.gfmd_prec_gradient_host(None, c, None, None) == 1
+    assert L.gfmd_kernel_set_box(None, 1.0, 1.0) == 1
+    assert L.gfmd_minimize(None, None, None, None, None) == 1
 
 
 def test_solver_factory_names():
