@@ -324,7 +324,8 @@ int gfmd_atoms_to_grid(int natoms, const double *d_x, const double *d_xeq, const
  * force f[3 iu + c][ix ny + iy] of every atom into (accumulate: added to)
  * d_fatoms [natoms][3]; fsum (host, may be NULL) gets the force summed over
  * the atoms (FP64, fixed order).  GFMD_EINVAL for ids outside the grid.
- * Synchronizes the stream. */
+ * Synchronizes the stream.  The fix's `fix_center` option (fix_gfmd.cpp:913-927)
+ * is then the caller's f[i][c] -= fsum[c] / natoms on its total forces. */
 int gfmd_grid_to_atoms(int natoms, const int *d_gid, const double *d_f, int nx, int ny, int ndof,
                        double *d_fatoms, int accumulate, double *fsum, void *cuda_stream);
 
