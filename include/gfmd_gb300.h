@@ -108,7 +108,8 @@ int gfmd_get_u0(gfmd_handle_t h, double *u0);
  * the reference. */
 int gfmd_plan_info(gfmd_handle_t h, int *rows_per_block, int *phi_prefetch);
 
-/* Device bytes held by the handle.
+/* Device bytes held by the handle (with the preconditioner gfmd_prec_gradient
+ * keeps for it, once built).
  * Replaces: GFMDSolver::memory_usage (src/main/gfmd_solver.h:97). */
 int gfmd_memory_usage(gfmd_handle_t h, double *bytes);
 

@@ -338,7 +338,7 @@ int gfmd_solver_info(gfmd_handle_t h, int *launches_per_eval, int *fused) {
 
 int gfmd_memory_usage(gfmd_handle_t h, double *bytes) {
   if (!h || !bytes) return fail(GFMD_EINVAL, "gfmd_memory_usage: NULL argument");
-  *bytes = h->bytes;
+  *bytes = h->bytes + (h->prec_grad ? h->prec_grad->bytes : 0.0);  // + gfmd_prec_gradient's handle
   return GFMD_OK;
 }
 
