@@ -390,3 +390,19 @@ def test_mixed_precision_trust_region_with_fp64_refinement():
     rep = s32.minimize(u, o, "tr", ftol=1e-8, precond=pre, refine=s64)
     assert rep["fmax"] <= 1e-8
     assert rel_l2(u.cpu().numpy(), u_ref) <= 1e-6
+
+
+def test_mixed_precision_fire_with_fp64_refinement():
+    # FP32 FIRE hands over to the FP64 handle at ftol or when its forces stall
+    # at the FP32 noise level; the FP64 phase finishes at the oracle's minimum
+    nx = ny = 32
+    d, half, full, linf, ob = _problem(osv.SPHERE_EXP)
+    el = oracle_elastic(full, linf, nx, ny)
+    u_ref, _ = osv.cg(el, ob, np.zeros((d, nx * ny)), nx, ny, ftol=1e-8)
+    s32 = _solver(nx, ny, d, half, linf, "f32")
+    s64 = _solver(nx, ny, d, half, linf)
+    o, keep = _gpu_obst(ob)
+    u = torch.zeros(d, nx * ny, dtype=torch.float64, device="cuda")
+    rep = s32.minimize(u, o, "fire", ftol=1e-8, maxiter=20000, dtmax=0.2, dt=0.05, refine=s64)
+    assert rep["fmax"] <= 1e-8
+    assert rel_l2(u.cpu().numpy(), u_ref) <= 1e-6

@@ -320,9 +320,19 @@ int fire_solve(gfmd_solver *hp, const gfmd_obstacle_t *ob, const gfmd_min_params
   int evals = 1, it = 0, cut = minsteps, status = GFMD_ENOTCONVERGED;
   double mix = mix_in;
   bool refining = false;
+  // With a refine handle the bulk phase also ends when max|f| has not halved
+  // for 500 steps: forces evaluated in FP32 stall at their noise level, which
+  // can sit above ftol.
+  double best = fmax;
+  int best_it = 0;
   while (ce == cudaSuccess) {
     if (!std::isfinite(fmax)) { status = GFMD_ENONFINITE; break; }
-    if (fmax <= prm->ftol) {
+    if (fmax < 0.5 * best) {
+      best = fmax;
+      best_it = it;
+    }
+    const bool stalled = prm->refine && !refining && it - best_it >= 500;
+    if (fmax <= prm->ftol || stalled) {
       if (prm->refine && !refining) {
         refining = true;
         hh = prm->refine;
