@@ -989,7 +989,7 @@ std::string fill_nonperiodic(const StiffnessKernel &k, int nx, int ny, int layou
       std::memcpy(&g[e * nxy + (size_t)ix * ny], out.data(), sizeof(cplx) * ny);
     }
   });
-  std::atomic<int> singular(0);
+  std::atomic<int> singular(0), nonherm(0);
   const double inv = 1.0 / ((double)nx * (double)ny);
   parallel_for(nyc, nthreads, [&](int iy) {
     std::vector<cplx> col(9 * (size_t)nx);
@@ -998,6 +998,14 @@ std::string fill_nonperiodic(const StiffnessKernel &k, int nx, int ny, int layou
     for (int ix = 0; ix < nx; ix++) {
       for (int e = 0; e < 9; e++) m[e] = col[e * (size_t)nx + ix];
       if (!invert(3, m)) singular.store(1);
+      // fill_phi_buffer's Hermitian check (gfmd_misc.cpp:55-76)
+      const double tr = m[0].re + m[4].re + m[8].re, tri = m[0].im + m[4].im + m[8].im;
+      const double trabs = std::sqrt(tr * tr + tri * tri);
+      for (int a = 0; a < 3; a++)
+        for (int b = a + 1; b < 3; b++) {
+          const double dr = m[3 * a + b].re - m[3 * b + a].re, di = m[3 * a + b].im + m[3 * b + a].im;
+          if (std::sqrt(dr * dr + di * di) > 1e-6 * trabs) nonherm.store(1);
+        }
       double *o = phi + 2 * ((size_t)ix * nyc + iy) * 9;
       for (int e = 0; e < 9; e++) {
         o[2 * e] = m[e].re * inv;
@@ -1006,6 +1014,7 @@ std::string fill_nonperiodic(const StiffnessKernel &k, int nx, int ny, int layou
     }
   });
   if (singular.load()) return "singular matrix while computing the stiffness kernel";
+  if (nonherm.load()) return "kernel is not Hermitian";
   return std::string();
 }
 

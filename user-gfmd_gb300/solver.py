@@ -306,6 +306,8 @@ class GFMDSolverGB300:
         (gfmd_prec_gradient_host); Cavg is a symmetric ndof x ndof matrix
         (GFMDSolverStatic::prec_gradient)."""
         c = np.ascontiguousarray(np.broadcast_to(np.asarray(cavg, np.float64), (self.ndof, self.ndof)))
+        if _is_device(g) != _is_device(gP):
+            raise GFMDError(_lib.GFMD_EINVAL, "prec_gradient: g and gP must both be on the device or both on the host")
         if _is_device(g):
             check(lib().gfmd_prec_gradient(self._handle(), _ptr(c), _ptr(g), _ptr(gP)))
         else:
