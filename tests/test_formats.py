@@ -134,3 +134,31 @@ def test_solver_dump_stiffness_and_greens_function(tmp_path):
         d.mkdir()
         (s.dump_greens_function if greens else s.dump_stiffness)(str(d))
         _check_dump_dir(str(d), c)
+
+
+def test_filter_map_keeps_long_and_removes_short_wavelengths():
+    nx, ny = 48, 40
+    x = np.arange(nx)[:, None]
+    y = np.arange(ny)[None, :]
+    long_ = 0.3 * np.cos(2 * np.pi * 2 * x / nx) + 0.2 * np.sin(2 * np.pi * 3 * y / ny)
+    short = 0.1 * np.cos(2 * np.pi * (9 * x / nx + 7 * y / ny))
+    z = 1.5 + long_ + short
+    # box 2 length units per pixel: mode (2, 0) has |q| = 2/96, mode (9, 7)
+    # sqrt((9/96)^2 + (7/80)^2) = 0.128; cut at wavelength 10 (|q| = 0.1)
+    out = fmt.filter_map(z, 10.0, xprd=2.0 * nx, yprd=2.0 * ny)
+    assert np.abs(out - (1.5 + long_)).max() < 1e-13
+    assert np.abs(fmt.filter_map(z, 1.0, 2.0 * nx, 2.0 * ny) - z).max() < 1e-13  # cut above every mode
+    with pytest.raises(ValueError):
+        fmt.filter_map(z, 0.0)
+
+
+def test_displace_map_alignment_and_statistics():
+    z = np.random.default_rng(5).normal(0.3, 0.2, (16, 16))
+    for align, key in (("bottom", "min"), ("top", "max"), ("average", "mean")):
+        out, info = fmt.displace_map(z, -1.25, align)
+        assert abs(info[key] + 1.25) < 1e-14
+        assert abs(info["rms"] - z.std()) < 1e-14
+        assert np.allclose(out - z, out[0, 0] - z[0, 0])
+    assert abs(fmt.displace_map(z, 0.0, "bottom")[0].min()) < 1e-15
+    with pytest.raises(ValueError):
+        fmt.displace_map(z, 0.0, "middle")

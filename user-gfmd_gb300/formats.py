@@ -16,6 +16,11 @@
   P.q.f<i>.real.out / .imag.out with F(q) = Phi(q) u(q) (the table scaled by
   1/(nx ny)), and P.q.uP.out, .fP.out, .e.out with sum |u|^2, sum |F|^2 and
   Re sum u conj(F) per wavevector; same line layout.
+* Map preprocessing (FixWallMap::filter_map / displace_map,
+  src/extras/fix_wall_map.cpp:1220-1366): a low-pass filter that zeroes every
+  Fourier mode with |q| = sqrt((kx/xprd)^2 + (ky/yprd)^2) > 1/lambda (k the
+  folded mode index, q in cycles per length), and a shift that puts the
+  map's bottom, top or average at z0, reporting min, max, rms height and mean.
 * Stiffness and Green's function dumps (GFMDSolverFFT::dump_stiffness,
   dump_greens_function, src/solvers/gfmd_solver_fft.cpp:294-420): files
   phi<i><j>.real.out / .imag.out (g<i><j>... for the Green's function, the
@@ -110,6 +115,44 @@ def write_q_space_dump(dump_prefix: str, u, phi_full, nx: int, ny: int) -> None:
     _write_grid(f"{dump_prefix}.q.uP.out", (np.abs(uq) ** 2).sum(0), nx, ny)
     _write_grid(f"{dump_prefix}.q.fP.out", (np.abs(Fq) ** 2).sum(0), nx, ny)
     _write_grid(f"{dump_prefix}.q.e.out", (uq * np.conj(Fq)).sum(0).real, nx, ny)
+
+
+def filter_map(zmap, lam: float, xprd: float | None = None, yprd: float | None = None) -> np.ndarray:
+    """FixWallMap::filter_map: remove wavelengths shorter than lam from an
+    nx x ny map (box xprd x yprd, default one length unit per pixel)."""
+    z = np.asarray(zmap, np.float64)
+    nx, ny = z.shape
+    xprd = float(nx if xprd is None else xprd)
+    yprd = float(ny if yprd is None else yprd)
+    if not lam > 0.0:
+        raise ValueError("the cut-off wavelength must be positive")
+    zq = np.fft.fft2(z)  # exp(-i), as FFT3d::compute(+1)
+    kx = np.minimum(np.arange(nx), nx - np.arange(nx)) / xprd
+    ky = np.minimum(np.arange(ny), ny - np.arange(ny)) / yprd
+    r = np.sqrt(kx[:, None] ** 2 + ky[None, :] ** 2)
+    zq[r > 1.0 / lam] = 0.0
+    return np.fft.ifft2(zq).real  # exp(+i) / (nx ny)
+
+
+def displace_map(zmap, z0: float, align: str = "average"):
+    """FixWallMap::displace_map: shift the map so that its bottom, top or
+    average ("bottom", "top", "average") lies at z0.  Returns the shifted map
+    and {"min", "max", "rms", "mean"} of it (rms: the standard deviation)."""
+    z = np.asarray(zmap, np.float64)
+    n = z.size
+    mean = z.sum() / n
+    rms = np.sqrt((z * z).sum() / n - mean * mean)
+    if align == "bottom":
+        shift = z0 - z.min()
+    elif align == "top":
+        shift = z0 - z.max()
+    elif align == "average":
+        shift = z0 - mean
+    else:
+        raise ValueError(f"unknown alignment {align!r}")
+    out = z + shift
+    return out, {"min": float(z.min() + shift), "max": float(z.max() + shift), "rms": float(rms),
+                 "mean": float(mean + shift)}
 
 
 def write_stiffness_dump(directory: str, phi_full, nx: int, ny: int, greens: bool = False) -> None:
