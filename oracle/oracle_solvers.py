@@ -49,6 +49,56 @@ class ObstacleSpec:
             self.offset = epsilon * np.exp(-cutoff / sigma) if cutoff > 0 else 0.0
 
 
+def map_bicubic(zmap, x, y):
+    """The reference's bicubic map table (Table2D with interpolated
+    derivatives, src/mathutils/table2d.cpp, as FixWallMap builds it,
+    src/extras/fix_wall_map.cpp:267), restated in the cubic Hermite basis:
+    on the periodic cell [i, i+1] x [j, j+1] (pixel units) the bicubic that
+    takes the corner values, the central-difference slopes
+    (z[i+1] - z[i-1]) / 2 along each axis and zero cross derivatives
+    (the reference's 16 conditions, solved there by a 16 x 16 inverse).
+    Returns f, df/dx, df/dy, d2f/dx2, d2f/dy2, d2f/dxdy at the points."""
+    z = np.asarray(zmap, float)
+    nx, ny = z.shape
+    x = np.asarray(x, float)
+    y = np.asarray(y, float)
+    i0 = np.floor(x).astype(int)
+    j0 = np.floor(y).astype(int)
+    t, s = x - i0, y - j0
+
+    def zz(di, dj):
+        return z[(i0 + di) % nx, (j0 + dj) % ny]
+
+    # Hermite basis in t (value at 0, value at 1, slope at 0, slope at 1) and
+    # its first and second derivatives
+    def basis(t):
+        h = [2 * t**3 - 3 * t**2 + 1, -2 * t**3 + 3 * t**2, t**3 - 2 * t**2 + t, t**3 - t**2]
+        d1 = [6 * t**2 - 6 * t, -6 * t**2 + 6 * t, 3 * t**2 - 4 * t + 1, 3 * t**2 - 2 * t]
+        d2 = [12 * t - 6, -12 * t + 6, 6 * t - 4, 6 * t - 2]
+        return h, d1, d2
+
+    hx, dx1, dx2 = basis(t)
+    hy, dy1, dy2 = basis(s)
+    out = [np.zeros_like(t) for _ in range(6)]
+    for a in (0, 1):
+        for b in (0, 1):
+            f = zz(a, b)
+            fx = 0.5 * (zz(a + 1, b) - zz(a - 1, b))
+            fy = 0.5 * (zz(a, b + 1) - zz(a, b - 1))
+            # value term H_a(t) H_b(s), slope terms G_a(t) H_b(s) and H_a(t) G_b(s)
+            terms = ((f, hx[a], hy[b], dx1[a], dy1[b], dx2[a], dy2[b]),
+                     (fx, hx[2 + a], hy[b], dx1[2 + a], dy1[b], dx2[2 + a], dy2[b]),
+                     (fy, hx[a], hy[2 + b], dx1[a], dy1[2 + b], dx2[a], dy2[2 + b]))
+            for c, X, Y, Xd, Yd, Xdd, Ydd in terms:
+                out[0] += c * X * Y
+                out[1] += c * Xd * Y
+                out[2] += c * X * Yd
+                out[3] += c * Xdd * Y
+                out[4] += c * X * Ydd
+                out[5] += c * Xd * Yd
+    return out
+
+
 def wall(ob: ObstacleSpec | None, u, nx, ny, direction=None, a=0.0):
     """Obstacle energy E, force f [ndof, N], and along `direction`:
     sum f.dir and sum dir^T H dir at u + a*dir."""

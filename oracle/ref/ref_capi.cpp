@@ -21,6 +21,7 @@
 #include "surface_stiffness.h"
 #include "gfmd_misc.h"
 #include "gfmd_solver_static.h"
+#include "table2d.h"
 
 using namespace LAMMPS_NS;
 
@@ -205,6 +206,32 @@ int gref_dump(const char *args, int nx, int ny, int greens) {
     solver.set_kernel(k.get(), true);
     if (greens) solver.dump_greens_function();
     else solver.dump_stiffness();
+    return 0;
+  } catch (const std::exception &e) {
+    g_last_error = e.what();
+    return -1;
+  }
+}
+
+/* The reference's bicubic map table (Table2D, src/mathutils/table2d.cpp),
+ * as FixWallMap builds it (interpolated derivatives, fix_wall_map.cpp:267):
+ * values [nx][ny]; at n points (x, y) in pixel units, out[6*i ...] = f, df/dx,
+ * df/dy, d2f/dxdx, d2f/dydy, d2f/dxdy. */
+int gref_table2d(int nx, int ny, const double *values, int n, const double *x, const double *y,
+                 double *out) {
+  try {
+    Env env;
+    double **v;
+    env.memory.create(v, nx, ny, "gref:map");
+    std::memcpy(&v[0][0], values, sizeof(double) * (size_t)nx * ny);
+    {
+      Table2D t(nx, ny, v, true, false, &env.error, &env.memory);
+      for (int i = 0; i < n; i++) {
+        double *o = out + 6 * (size_t)i;
+        t.eval(x[i], y[i], o[0], o[1], o[2], o[3], o[4], o[5]);
+      }
+    }
+    env.memory.destroy(v);
     return 0;
   } catch (const std::exception &e) {
     g_last_error = e.what();

@@ -1,8 +1,9 @@
 """Generate the golden fixtures of tests/golden/ from the reference itself.
 
 Runs the reference's own, unmodified ``fill_phi_buffer``,
-``GFMDSolverStatic::post_force``, ``GFMDSolverStatic::prec_gradient`` and the
-``GFMDSolverFFT`` stiffness / Green's function dumps through oracle/_ref/libgfmdref.so (built
+``GFMDSolverStatic::post_force``, ``GFMDSolverStatic::prec_gradient``, the
+``GFMDSolverFFT`` stiffness / Green's function dumps and the ``Table2D`` bicubic
+map table through oracle/_ref/libgfmdref.so (built
 from the reference sources by oracle/ref/Makefile; needs the reference tree,
 so this script runs only where it is present).  Each fixture stores the
 kernel arguments, the grid, seeded displacements, the reference's forces,
@@ -118,6 +119,24 @@ DUMP_CASES = [
 ]
 
 
+# Table2D (bicubic map) fixture (tests/golden/maps/): map, points, reference output
+MAP_CASES = [("table2d_17x13", 17, 13, 400)]
+
+
+def run_map_case(L, nx: int, ny: int, npts: int, seed: int):
+    rng = np.random.default_rng(seed)
+    z = rng.normal(0.0, 1.0, (nx, ny))
+    x = rng.uniform(-2 * nx, 3 * nx, npts)
+    y = rng.uniform(-2 * ny, 3 * ny, npts)
+    x[:8] = np.arange(8) % nx  # grid points
+    y[:8] = (3 * np.arange(8)) % ny
+    out = np.zeros((npts, 6))
+    if L.gref_table2d(nx, ny, z.ctypes.data_as(ctypes.c_void_p), npts, x.ctypes.data_as(ctypes.c_void_p),
+                      y.ctypes.data_as(ctypes.c_void_p), out.ctypes.data_as(ctypes.c_void_p)):
+        raise RuntimeError(L.gref_last_error().decode())
+    return dict(z=z, x=x, y=y, out=out)
+
+
 def run_dump_case(L, args: str, nx: int, ny: int):
     import tempfile
     L.gref_set_box(ctypes.c_double(1.0), ctypes.c_double(1.0))
@@ -139,6 +158,11 @@ def run_dump_case(L, args: str, nx: int, ny: int):
 
 def main() -> int:
     L = load_ref()
+    os.makedirs(os.path.join(HERE, "maps"), exist_ok=True)
+    for i, (name, nx, ny, npts) in enumerate(MAP_CASES):
+        path = os.path.join(HERE, "maps", f"{name}.npz")
+        np.savez_compressed(path, **run_map_case(L, nx, ny, npts, SEED + 200 + i))
+        print(f"{name} -> {os.path.getsize(path)} bytes")
     os.makedirs(os.path.join(HERE, "dumps"), exist_ok=True)
     for name, args, nx, ny in DUMP_CASES:
         path = os.path.join(HERE, "dumps", f"{name}.npz")
