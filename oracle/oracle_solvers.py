@@ -99,6 +99,38 @@ def map_bicubic(zmap, x, y):
     return out
 
 
+def wall_map_bicubic(ob: ObstacleSpec, u, nx, ny):
+    """FixWallMap::pre_force (src/extras/fix_wall_map.cpp:686-817) with the
+    bicubic map table and the exponential wall (eval_exp, :575-582): at each
+    site's displaced position r the map height z(r_x, r_y) and slopes (map
+    pixel = one lattice spacing), dz = norm (r_z - z - map_z0), e = eps
+    exp(-dz/sigma) - offset, f_z = norm eps exp(-dz/sigma)/sigma and the
+    lateral force (f_x, f_y) = -f_z (dz/dx, dz/dy).  Returns (E, f)."""
+    ndof = u.shape[0]
+    f = np.zeros_like(u)
+    nl = ndof // 3
+    nlo = min(nl, ob.nlayer if ob.nlayer > 0 else nl)
+    ix, iy = np.divmod(np.arange(nx * ny), ny)
+    zmap = np.asarray(ob.zmap, float).reshape(nx, ny)
+    E = 0.0
+    for l in range(nlo):
+        off = ob.offsets[l] if l < len(ob.offsets) else (0.0, 0.0, 0.0)
+        rx = ix * ob.ax + off[0] + u[3 * l]
+        ry = iy * ob.ay + off[1] + u[3 * l + 1]
+        rz = off[2] + u[3 * l + 2]
+        z, zx, zy, _, _, _ = map_bicubic(zmap, rx / ob.ax, ry / ob.ay)
+        zx, zy = zx / ob.ax, zy / ob.ay
+        dz = ob.norm * (rz - (z + ob.map_z0))
+        m = np.ones_like(dz, bool) if ob.cutoff <= 0 else dz < ob.cutoff
+        ex = ob.eps * np.exp(-dz / ob.sigma)
+        fz = ob.norm * ex / ob.sigma
+        f[3 * l] = np.where(m, -fz * zx, 0.0)
+        f[3 * l + 1] = np.where(m, -fz * zy, 0.0)
+        f[3 * l + 2] = np.where(m, fz, 0.0)
+        E += np.where(m, ex - ob.offset, 0.0).sum()
+    return E, f
+
+
 def wall(ob: ObstacleSpec | None, u, nx, ny, direction=None, a=0.0):
     """Obstacle energy E, force f [ndof, N], and along `direction`:
     sum f.dir and sum dir^T H dir at u + a*dir."""

@@ -73,3 +73,26 @@ def test_oracle_trust_region_reaches_the_cg_minimum():
         assert np.linalg.norm(u - ucg) <= 1e-5 * np.linalg.norm(ucg)
         assert abs(r["energy"] - rcg["energy"]) <= 1e-9 * abs(rcg["energy"])
     assert rp["iterations"] < rn["iterations"] / 10
+
+
+def test_bicubic_map_wall_forces_are_the_energy_gradient():
+    # the restated FixWallMap force with the bicubic table: the lateral force
+    # -f_z dz/dx is the exact gradient of the energy; at undisplaced sites the
+    # table reproduces the map, so the normal force equals the site-sampled wall's
+    nx, ny = 12, 10
+    rng = np.random.default_rng(8)
+    zmap = 0.2 * rng.normal(0, 1, nx * ny)
+    ob = osv.ObstacleSpec(osv.MAP_EXP, epsilon=0.3, sigma=0.5, zmap=zmap, map_z0=-0.4, norm=1,
+                          layer_offsets=[(0.0, 0.0, 0.0), (0.5, 0.5, 0.7)])
+    u0 = np.zeros((6, nx * ny))
+    E0, f0 = osv.wall_map_bicubic(ob, u0, nx, ny)
+    Es, fs, _, _ = osv.wall(ob, u0, nx, ny)
+    assert np.allclose(f0[2], fs[2], rtol=1e-13)  # layer 0 sits on the map's grid points
+    u = rng.normal(0, 0.05, (6, nx * ny))
+    E, fu = osv.wall_map_bicubic(ob, u, nx, ny)
+    d = rng.normal(0, 1, u.shape)
+    h = 1e-6
+    Ep, _ = osv.wall_map_bicubic(ob, u + h * d, nx, ny)
+    Em, _ = osv.wall_map_bicubic(ob, u - h * d, nx, ny)
+    assert abs(-(Ep - Em) / (2 * h) - (fu * d).sum()) <= 1e-6 * np.abs(fu * d).sum()
+    assert np.abs(fu[:2]).max() > 0.0  # lateral forces present
