@@ -193,9 +193,11 @@ def wall(ob: ObstacleSpec | None, u, nx, ny, direction=None, a=0.0):
     return E, f, fdir, curv
 
 
-def cg(elastic, ob, u, nx, ny, ftol=1e-6, maxiter=100000, recompute=50):
+def cg(elastic, ob, u, nx, ny, ftol=1e-6, maxiter=100000, recompute=50, dmax=None):
     """Polak-Ribiere CG with a Newton line search; elastic(v, with_linf)
-    returns (force, energy).  Returns (u, report)."""
+    returns (force, energy).  dmax: largest displacement of any component in
+    one line search (LAMMPS min_modify dmax, default 0.1 there; None: no
+    cap).  Returns (u, report)."""
     u = u.copy()
     it = evals = 0
 
@@ -219,6 +221,8 @@ def cg(elastic, ob, u, nx, ny, ftol=1e-6, maxiter=100000, recompute=50):
         hKh = (h * Kh).sum()
         felh = (fel * h).sum()
         a, lo, hi = 0.0, 0.0, -1.0
+        if dmax is not None:
+            hi = dmax / np.abs(h).max()  # the step's upper bracket
         for _ in range(16):
             fwh = cw = 0.0
             if ob is not None:
