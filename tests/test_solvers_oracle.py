@@ -96,3 +96,18 @@ def test_bicubic_map_wall_forces_are_the_energy_gradient():
     Em, _ = osv.wall_map_bicubic(ob, u - h * d, nx, ny)
     assert abs(-(Ep - Em) / (2 * h) - (fu * d).sum()) <= 1e-6 * np.abs(fu * d).sum()
     assert np.abs(fu[:2]).max() > 0.0  # lateral forces present
+
+
+@pytest.mark.parametrize("args", [
+    "fcc100 1.0 1",  # tests/TEST_energy_conservation_fcc100 (analytic kernel, no height)
+    "ft fcc100 1.0 2 pair-potential 2 1.0 -0.1 height 10",  # ..._fcc100_pair_potential, ..._two_layers
+])
+def test_oracle_nve_energy_conservation_like_the_reference_tests(args):
+    # 10 x 10, random displacements of 0.1 (seed 12472634), dt = 0.01,
+    # |E - <E>| / <E| < 1e-4; 20 000 of the reference's 100 000 steps
+    nx = ny = 10
+    d, half, full, linf = tables(args, nx, ny)
+    el = oracle_elastic(full, linf, nx, ny)
+    u0 = np.random.default_rng(12472634).uniform(-0.1, 0.1, (d, nx * ny))
+    _, _, e = osv.verlet(el, None, u0, np.zeros_like(u0), nx, ny, 0.01, 0.0, 20000)
+    assert np.abs(e - e.mean()).max() / abs(e.mean()) < 1e-4
