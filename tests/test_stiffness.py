@@ -129,3 +129,18 @@ def test_phi_table_cache_round_trip(tmp_path):
     assert g.PhiTableFile.read(str(files[0]), k.args, 16, 12, "half") is None
     phi3, _ = k.phi_table_cached(16, 12, str(tmp_path))
     assert np.array_equal(phi3, ref)
+
+
+def test_phi_table_cache_keys_on_the_box(tmp_path):
+    # the continuum styles read the box lengths; tables for different boxes
+    # are different cache entries
+    g = gfmd_pkg()
+    a = g.StiffnessKernel("nonperiodic 0.3 1.0")
+    b = g.StiffnessKernel("nonperiodic 0.3 1.0")
+    b.set_box(24.0, 20.0)
+    pa, _ = a.phi_table_cached(12, 10, str(tmp_path))
+    pb, _ = b.phi_table_cached(12, 10, str(tmp_path))
+    assert len(list(tmp_path.iterdir())) == 2
+    assert not np.allclose(pa, pb)
+    ref, _ = b.phi_table(12, 10, "half")
+    assert np.array_equal(b.phi_table_cached(12, 10, str(tmp_path))[0], ref)
