@@ -826,6 +826,89 @@ void StiffnessKernel::dynamical_matrices(double qx, double qy, cplx *U0, cplx *U
 // greens_function_transfer_matrix_stiffness with iterate_Gnn run exactly
 // height-1 times (src/main/surface_stiffness.cpp:811-873, 493-548):
 //   X = -V U^-1 V^+;  repeat: X = -V (U + X)^-1 V^+;  Phi = U0 + X.
+// The recursion X <- -V (U + X)^{-1} V^H on the degrees of freedom V touches.
+// X lives on rows(V) x rows(V); (U + X)^{-1} enters through its cols(V) block.
+// With S = rows(V) u cols(V) and K the rest, that block is the one of
+// (Ut + X)^{-1}, Ut = U_SS - U_SK U_KK^{-1} U_KS the Schur complement of U onto
+// S, formed once per wavevector: the recursion then runs on |S| x |S|
+// matrices (6 instead of 12 for a four-layer fcc(100) cell).  Returns false
+// when S is every degree of freedom or a factorization is not safely
+// positive definite (phi then holds scratch); phi receives U0 + X otherwise.
+// work holds 6 d^2 entries.
+bool StiffnessKernel::reduced_recursion(const cplx *U0, const cplx *U, const cplx *V, cplx *phi,
+                                        cplx *work) const {
+  const int d = dim_;
+  int S[64], K[64], ns = 0, nk = 0;
+  for (int i = 0; i < d; i++) {
+    bool used = false;
+    for (int j = 0; j < d && !used; j++) {
+      const cplx a = V[i * d + j], b = V[j * d + i];
+      used = a.re != 0.0 || a.im != 0.0 || b.re != 0.0 || b.im != 0.0;
+    }
+    if (used) S[ns++] = i;
+    else K[nk++] = i;
+  }
+  if (nk == 0 || ns == 0) return false;
+  cplx *A = work, *Vs = work + d * d, *X = work + 2 * d * d, *L = work + 3 * d * d, *W = work + 4 * d * d,
+       *Y = work + 5 * d * d;
+  // Cholesky of U_KK (lower, in L), Y = L^{-1} U_KS, Ut = U_SS - Y^H Y
+  for (int j = 0; j < nk; j++) {
+    double djj = U[K[j] * d + K[j]].re;
+    for (int m = 0; m < j; m++) djj -= L[j * nk + m].re * L[j * nk + m].re + L[j * nk + m].im * L[j * nk + m].im;
+    if (!(djj > 1e-12 * std::fabs(U[K[j] * d + K[j]].re))) return false;
+    const double ljj = std::sqrt(djj), inv = 1.0 / ljj;
+    L[j * nk + j] = {ljj, 0.0};
+    for (int i = j + 1; i < nk; i++) {
+      double re = U[K[i] * d + K[j]].re, im = U[K[i] * d + K[j]].im;
+      for (int m = 0; m < j; m++) {
+        const cplx a = L[i * nk + m], b = L[j * nk + m];
+        re -= a.re * b.re + a.im * b.im;
+        im -= a.im * b.re - a.re * b.im;
+      }
+      L[i * nk + j] = {re * inv, im * inv};
+    }
+  }
+  for (int i = 0; i < nk; i++) {
+    const double inv = 1.0 / L[i * nk + i].re;
+    for (int c = 0; c < ns; c++) {
+      double re = U[K[i] * d + S[c]].re, im = U[K[i] * d + S[c]].im;
+      for (int m = 0; m < i; m++) {
+        const cplx a = L[i * nk + m], y = Y[m * ns + c];
+        re -= a.re * y.re - a.im * y.im;
+        im -= a.re * y.im + a.im * y.re;
+      }
+      Y[i * ns + c] = {re * inv, im * inv};
+    }
+  }
+  cplx *Ut = phi;  // ns x ns, scratch until the end
+  for (int a = 0; a < ns; a++)
+    for (int b = 0; b < ns; b++) {
+      double re = U[S[a] * d + S[b]].re, im = U[S[a] * d + S[b]].im;
+      for (int m = 0; m < nk; m++) {  // - conj(Y[m][a]) Y[m][b]
+        const cplx p = Y[m * ns + a], q = Y[m * ns + b];
+        re -= p.re * q.re + p.im * q.im;
+        im -= p.re * q.im - p.im * q.re;
+      }
+      Ut[a * ns + b] = {re, im};
+    }
+  for (int a = 0; a < ns; a++)
+    for (int b = 0; b < ns; b++) Vs[a * ns + b] = V[S[a] * d + S[b]];
+  // the recursion on S
+  bool ok = schur_step_chol(ns, Ut, Vs, X, L, W);
+  for (int it = 0; ok && it < height_ - 1; it++) {
+    for (int i = 0; i < ns * ns; i++) A[i] = {Ut[i].re + X[i].re, Ut[i].im + X[i].im};
+    ok = schur_step_chol(ns, A, Vs, X, L, W);
+  }
+  if (!ok) return false;
+  for (int i = 0; i < d * d; i++) phi[i] = U0[i];
+  for (int a = 0; a < ns; a++)
+    for (int b = 0; b < ns; b++) {
+      phi[S[a] * d + S[b]].re += X[a * ns + b].re;
+      phi[S[a] * d + S[b]].im += X[a * ns + b].im;
+    }
+  return true;
+}
+
 bool StiffnessKernel::stiffness(double qx, double qy, cplx *phi, cplx *work) const {
   const int d = dim_, d2 = d * d;
   cplx *U0 = work, *U = work + d2, *V = work + 2 * d2, *Vd = work + 3 * d2, *X = work + 4 * d2,
@@ -840,6 +923,8 @@ bool StiffnessKernel::stiffness(double qx, double qy, cplx *phi, cplx *work) con
   // iteration of the reference otherwise, and at q = 0, where Phi = U0 + X
   // cancels to O(1/height) and the reference's own elimination order keeps
   // the table within 1e-13 of the reference's (Cholesky: 6e-13)
+  if (height_ > 0 && !(qx == 0.0 && qy == 0.0) && reduced_recursion(U0, U, V, phi, work + 6 * d2))
+    return true;
   if (height_ > 0 && !(qx == 0.0 && qy == 0.0)) {
     cplx *A = Vd, *L = T, *W = phi;  // scratch (Vd is built below if needed)
     bool ok = schur_step_chol(d, U, V, X, L, W);
@@ -1034,7 +1119,7 @@ std::string fill_phi_table(const StiffnessKernel &k, int nx, int ny, int layout,
   std::atomic<int> next(0);
   std::atomic<int> bad_ix(-1), bad_herm(-1);
   auto worker = [&]() {
-    std::vector<cplx> work(6 * (size_t)d2), p((size_t)d2);
+    std::vector<cplx> work(12 * (size_t)d2), p((size_t)d2);
     for (;;) {
       int ix = next.fetch_add(1);
       if (ix >= nx) break;

@@ -109,9 +109,10 @@ class StiffnessKernel {
   // U0, U, V at one wavevector (each dim*dim, row-major).
   void dynamical_matrices(double qx, double qy, cplx *U0, cplx *U, cplx *V) const;
   // Phi(q) = U0 + V T_N (zero-force transfer matrix over `height` layers);
-  // work holds at least 6*dim*dim entries.  Returns false if a matrix was
+  // work holds at least 12*dim*dim entries.  Returns false if a matrix was
   // singular.
   bool stiffness(double qx, double qy, cplx *phi, cplx *work) const;
+  bool reduced_recursion(const cplx *U0, const cplx *U, const cplx *V, cplx *phi, cplx *work) const;
 
  private:
   // `ft` (force constants on a crystal surface), the analytic lattice styles,
