@@ -204,9 +204,9 @@ int orc_fft2d(double *data, int nx, int ny, int flag, int nthreads)
  * with GFMDSolverFFT::fft_forward/fft_reverse
  * (src/solvers/gfmd_solver_fft.cpp:96-147, 150-195) inlined, single process.
  */
-double orc_post_force(int nx, int ny, int ndof, const double *phi,
-                      const double *linf, const double *u, double *f,
-                      double *u0, int nthreads)
+static double post_force_impl(int nx, int ny, int ndof, const double *phi, int half,
+                              const double *linf, const double *u, double *f,
+                              double *u0, int nthreads)
 {
     const size_t nxy = (size_t)nx * ny;
     const int nu = ndof / 3;
@@ -243,12 +243,25 @@ double orc_post_force(int nx, int ny, int ndof, const double *phi,
 #pragma omp parallel for num_threads(nthreads) reduction(+ : esum) schedule(static)
     for (long idq = 0; idq < (long)nxy; idq++) {
         double Fr[24], Fi[24];
-        const double *P = phi + 2 * (size_t)idq * ndof * ndof;
+        const double *P;
+        double cj = 1.0; /* -1: conjugate of the mirrored stored entry */
+        if (!half) {
+            P = phi + 2 * (size_t)idq * ndof * ndof;
+        } else {
+            const int nyc = ny / 2 + 1;
+            const int ix = (int)(idq / ny), iy = (int)(idq % ny);
+            if (iy < nyc) {
+                P = phi + 2 * ((size_t)ix * nyc + iy) * ndof * ndof;
+            } else {
+                P = phi + 2 * ((size_t)((nx - ix) % nx) * nyc + (ny - iy)) * ndof * ndof;
+                cj = -1.0;
+            }
+        }
         double *uq = q + 2 * (size_t)idq * ndof;
         for (int i = 0; i < ndof; i++) {
             double sr = 0.0, si = 0.0;
             for (int j = 0; j < ndof; j++) {
-                double pr = P[2 * (i * ndof + j)], pi = P[2 * (i * ndof + j) + 1];
+                double pr = P[2 * (i * ndof + j)], pi = cj * P[2 * (i * ndof + j) + 1];
                 double xr = uq[2 * j], xi = uq[2 * j + 1];
                 sr += pr * xr - pi * xi;
                 si += pr * xi + pi * xr;
@@ -283,6 +296,68 @@ double orc_post_force(int nx, int ny, int ndof, const double *phi,
     free(fft_data);
     free(q);
     return epot;
+}
+
+double orc_post_force(int nx, int ny, int ndof, const double *phi,
+                      const double *linf, const double *u, double *f,
+                      double *u0, int nthreads)
+{
+    return post_force_impl(nx, ny, ndof, phi, 0, linf, u, f, u0, nthreads);
+}
+
+double orc_post_force_half(int nx, int ny, int ndof, const double *phi_half,
+                           const double *linf, const double *u, double *f,
+                           double *u0, int nthreads)
+{
+    return post_force_impl(nx, ny, ndof, phi_half, 1, linf, u, f, u0, nthreads);
+}
+
+/* SplitMix64 finaliser: a counter-based hash, so that every thread fills
+ * its wavevectors independently and the table does not depend on the thread
+ * count. */
+static unsigned long long orc_mix64(unsigned long long z)
+{
+    z += 0x9e3779b97f4a7c15ULL;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+}
+
+static double orc_unit(unsigned long long seed, unsigned long long i)
+{
+    return (double)(orc_mix64(seed ^ orc_mix64(i)) >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+}
+
+void orc_synthetic_phi_full(int nx, int ny, int ndof, unsigned long long seed, double scale,
+                            double *full, int nthreads)
+{
+    const size_t d2 = (size_t)ndof * ndof;
+    if (nthreads <= 0) nthreads = orc_max_threads();
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+    for (int ix = 0; ix < nx; ix++) {
+        for (int iy = 0; iy < ny; iy++) {
+            /* canonical member of the pair (q, -q): the mirror entry is the
+             * complex conjugate, so Phi(-q) = conj Phi(q) holds exactly */
+            const int mx = (nx - ix) % nx, my = (ny - iy) % ny;
+            const long a = (long)ix * ny + iy, b = (long)mx * ny + my;
+            const long c = a < b ? a : b;
+            const double cj = (a <= b) ? 1.0 : -1.0;
+            double *dst = full + 2 * (size_t)a * d2;
+            for (int i = 0; i < ndof; i++) {
+                for (int j = i; j < ndof; j++) {
+                    const unsigned long long k = ((unsigned long long)c * d2 + (size_t)i * ndof + j) * 2;
+                    double re = scale * orc_unit(seed, k);
+                    double im = (i == j) ? 0.0 : cj * scale * orc_unit(seed, k + 1);
+                    if (i == j) re += 2.0 * scale;
+                    if (a == b) im = 0.0; /* self-mirror wavevectors: real */
+                    dst[2 * (i * ndof + j)] = re;
+                    dst[2 * (i * ndof + j) + 1] = im;
+                    dst[2 * (j * ndof + i)] = re;
+                    dst[2 * (j * ndof + i) + 1] = -im;
+                }
+            }
+        }
+    }
 }
 
 void orc_phi_half_to_full(int nx, int ny, int ndof, const double *half, double *full,

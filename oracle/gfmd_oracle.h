@@ -54,6 +54,24 @@ double orc_post_force(int nx, int ny, int ndof, const double *phi,
                       const double *linf, const double *u, double *f,
                       double *u0, int nthreads);
 
+/* The same with the table given on the stored half spectrum
+ * [nx][ny/2+1][ndof][ndof] (the layout the GPU path uploads): entries with
+ * ky > ny/2 are read as conj Phi(-q), the relation fill_phi_buffer's tables
+ * satisfy for the ft kernels.  Identical arithmetic to orc_post_force on the
+ * expanded table, without its nx*ny*ndof^2 complex memory (9.7 GB at 2048^2,
+ * ndof 12). */
+double orc_post_force_half(int nx, int ny, int ndof, const double *phi_half,
+                           const double *linf, const double *u, double *f,
+                           double *u0, int nthreads);
+
+/* Fills a full-grid table [nx*ny][ndof][ndof] with seeded pseudo-random
+ * Hermitian matrices (diagonal 2*scale + U(-scale/2, scale/2), off-diagonal
+ * parts U(-scale/2, scale/2)) that satisfy Phi(-q) = conj Phi(q) exactly.
+ * Timing input only: the operation count of orc_post_force does not depend
+ * on the table's values. */
+void orc_synthetic_phi_full(int nx, int ny, int ndof, unsigned long long seed, double scale,
+                            double *full, int nthreads);
+
 /* Expand a half-spectrum table [nx][ny/2+1][ndof][ndof] to the full grid
  * [nx*ny][ndof][ndof] using Phi(-q) = conj Phi(q) (test and baseline input
  * preparation; the reference itself computes every grid point). */

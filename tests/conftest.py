@@ -40,6 +40,11 @@ def oracle() -> ctypes.CDLL:
         L.orc_post_force.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p] * 5 + [ctypes.c_int]
         L.orc_fft2d.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.orc_fft2d.restype = ctypes.c_int
+        L.orc_post_force_half.restype = ctypes.c_double
+        L.orc_post_force_half.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p] * 5 + [ctypes.c_int]
+        L.orc_synthetic_phi_full.restype = None
+        L.orc_synthetic_phi_full.argtypes = [ctypes.c_int] * 3 + [ctypes.c_ulonglong, ctypes.c_double,
+                                                                  ctypes.c_void_p, ctypes.c_int]
         _oracle = L
     return _oracle
 
@@ -54,6 +59,21 @@ def oracle_post_force(phi_full, linf, u, nx, ny, nthreads=0):
     u0 = np.zeros(d)
     e = oracle().orc_post_force(nx, ny, d, phi_full.ctypes.data, lf.ctypes.data, u.ctypes.data,
                                 f.ctypes.data, u0.ctypes.data, nthreads)
+    return f, e, u0
+
+
+def oracle_post_force_half(phi_half, linf, u, nx, ny, nthreads=0):
+    """Oracle force evaluation from the half-spectrum table
+    [nx, ny//2+1, d, d] (entries with ky > ny/2 read as conj Phi(-q)):
+    returns (f, E, u0)."""
+    d = u.shape[0]
+    phi_half = np.ascontiguousarray(phi_half, np.complex128)
+    u = np.ascontiguousarray(u, np.float64)
+    lf = np.ascontiguousarray(linf if linf is not None else np.zeros(d // 3), np.float64)
+    f = np.zeros_like(u)
+    u0 = np.zeros(d)
+    e = oracle().orc_post_force_half(nx, ny, d, phi_half.ctypes.data, lf.ctypes.data, u.ctypes.data,
+                                     f.ctypes.data, u0.ctypes.data, nthreads)
     return f, e, u0
 
 

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from conftest import (golden_cases, gfmd_pkg, kernel_for, half_to_full, load_golden, oracle,
-                      oracle_post_force, rel_l2)
+                      oracle_post_force, oracle_post_force_half, rel_l2)
 
 
 @pytest.mark.parametrize("nx,ny", [(8, 8), (12, 10), (37, 64), (64, 37), (30, 7), (1, 16), (16, 1)])
@@ -108,3 +108,34 @@ def test_oracle_bicubic_map_matches_reference_table2d():
     assert np.abs((fp - fm)[inside] / (2 * h) - mine[inside, 4]).max() <= 1e-6
     # the table reproduces the map at the grid points
     assert np.abs(mine[:8, 0] - c["z"][c["x"][:8].astype(int), c["y"][:8].astype(int)]).max() <= 1e-14
+
+
+@pytest.mark.parametrize("nx,ny", [(12, 10), (9, 7), (16, 5)])
+def test_oracle_half_table_entry_equals_full_table_entry(nx, ny):
+    # orc_post_force_half reads ky > ny/2 as conj Phi(-q); on the expanded
+    # table orc_post_force must give the same forces, energy and u(q=0)
+    k = gfmd_pkg().StiffnessKernel("ft fcc100 1.0 2 pair-potential 1 1.0 height 64")
+    d = k.get_dimension()
+    half, linf = k.phi_table(nx, ny, "half")
+    u = np.random.default_rng(nx * ny).normal(0.0, 0.01, (d, nx * ny))
+    fa, ea, ua = oracle_post_force(half_to_full(half, nx, ny), linf, u, nx, ny)
+    fb, eb, ub = oracle_post_force_half(half, linf, u, nx, ny)
+    assert rel_l2(fb, fa) <= 1e-14 and abs(ea - eb) <= 1e-14 * abs(ea)
+    assert np.array_equal(ua, ub)
+
+
+def test_oracle_synthetic_table_is_hermitian_and_mirror_conjugate():
+    nx, ny, d = 6, 5, 6
+    full = np.empty((nx * ny, d, d), np.complex128)
+    oracle().orc_synthetic_phi_full(nx, ny, d, 99, 1e-3, full.ctypes.data, 0)
+    again = np.empty_like(full)
+    oracle().orc_synthetic_phi_full(nx, ny, d, 99, 1e-3, again.ctypes.data, 1)
+    assert np.array_equal(full, again)  # independent of the thread count
+    assert np.allclose(full, np.conj(np.transpose(full, (0, 2, 1))), rtol=0, atol=0)
+    t = full.reshape(nx, ny, d, d)
+    mirror = t[(-np.arange(nx)) % nx][:, (-np.arange(ny)) % ny]
+    assert np.array_equal(t, np.conj(mirror))
+    # the forces of a real field are real, as with a physical table
+    u = np.random.default_rng(1).normal(0.0, 0.01, (d, nx * ny))
+    f, e, _ = oracle_post_force(full, None, u, nx, ny)
+    assert np.isfinite(f).all() and e > 0
