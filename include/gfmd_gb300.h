@@ -118,6 +118,24 @@ int gfmd_memory_usage(gfmd_handle_t h, double *bytes);
  * counterpart in the reference (introspection for benchmarks and tests). */
 int gfmd_solver_info(gfmd_handle_t h, int *launches_per_eval, int *fused);
 
+/* Device time of each kernel launch of one force evaluation: records CUDA
+ * events around the launches on the handle's stream, synchronizes, and
+ * writes gfmd_solver_info's launches_per_eval times (milliseconds) to ms
+ * (nmax entries available) and their count to *nk.  u and f are device
+ * buffers of the handle's arithmetic type (double for GFMD_PREC_F64, float
+ * for GFMD_PREC_F32); d_epot receives the energy.  No counterpart in the
+ * reference (measurement). */
+int gfmd_force_kernel_times(gfmd_handle_t h, const void *d_u, void *d_f, double *d_epot, float *ms,
+                            int nmax, int *nk);
+
+/* Kernels of the fused FP32 path: row_warp_tma = 1 when the row transforms
+ * run one warp per row with TMA-staged spectrum tiles (rows of ny = 2048),
+ * col_cluster = blocks per ky of the thread-block-cluster column kernel
+ * (0: the single-block column kernel), phi_vector = the packed stiffness
+ * table's vector width (4: 16-byte vectors).  No counterpart in the
+ * reference (introspection). */
+int gfmd_kernel_plan(gfmd_handle_t h, int *row_warp_tma, int *col_cluster, int *phi_vector);
+
 /* ---- solver loops ----------------------------------------------------- */
 
 /* Obstacles acting on every atom of the grid.  The position of the atom of

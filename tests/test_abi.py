@@ -94,3 +94,27 @@ def test_ctypes_structs_match_the_c_layout(tmp_path):
         assert got[(py, "size")] == ctypes.sizeof(S), py
         for name, _ in S._fields_:
             assert got[(py, name)] == getattr(S, name).offset, (py, name)
+
+
+def test_device_buffer_dtype_is_checked_before_the_c_abi():
+    # a float32 tensor handed to an entry that reads doubles would be read as
+    # the wrong numbers; the Python mirror refuses it (CPU tensors suffice)
+    torch = pytest.importorskip("torch")
+    from importlib import import_module
+
+    chk = import_module("user-gfmd_gb300.solver")._check_device_array
+    chk(torch.zeros(12, dtype=torch.float64), "float64", 12, "u")
+    with pytest.raises(TypeError):
+        chk(torch.zeros(12, dtype=torch.float32), "float64", 12, "u")
+    with pytest.raises(TypeError):
+        chk(torch.zeros(4, 6, dtype=torch.float64).t(), "float64", 12, "u")
+    with pytest.raises(ValueError):
+        chk(torch.zeros(11, dtype=torch.float64), "float64", 12, "u")
+
+
+def test_timing_and_plan_entries_reject_bad_arguments_without_gpu():
+    L = gfmd_pkg().lib()
+    nk = ctypes.c_int()
+    ms = (ctypes.c_float * 4)()
+    assert L.gfmd_force_kernel_times(None, None, None, None, ms, 4, ctypes.byref(nk)) == 1
+    assert L.gfmd_kernel_plan(None, None, None, None) == 1

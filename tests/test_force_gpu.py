@@ -16,7 +16,9 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 F64_TOL = 1e-10
-FP32_TOL = 5e-6
+# FP32 against the reference: measured 0.9e-7 .. 2.2e-7 (forces, rel L2) and
+# <= 5e-8 (energy) over the fixtures, 2.5e-7 at 2048^2 ndof 12
+FP32_TOL = 6e-7
 
 
 def _phi(c, nx, ny):
@@ -128,6 +130,11 @@ def test_errors_are_status_codes_on_gpu():
         ("ft fcc111 1 1.0 pair-potential 1 1.0 height 128", 1024, 64),
         ("ft fcc100 1.0 4 pair-potential 1 1.0 height 64", 2048, 32),
         ("ft sc100 1 1.0 pair-potential 2 1.0 1.0 height 128", 32, 4096),
+        # rows of ny = 2048: warp-per-row TMA row kernels (FP32)
+        ("ft sc100 1 1.0 pair-potential 2 1.0 1.0 height 128", 16, 2048),
+        ("ft fcc100 1.0 4 pair-potential 1 1.0 height 64", 256, 2048),
+        ("ft fcc100 1.0 2 pair-potential 1 1.0 height 64", 1024, 2048),
+        ("ft fcc100 1.0 4 pair-potential 1 1.0 height 64", 4096, 64),
     ],
 )
 def test_fused_path_matches_oracle_and_plain_path(args, nx, ny, monkeypatch):
@@ -147,7 +154,7 @@ def test_fused_path_matches_oracle_and_plain_path(args, nx, ny, monkeypatch):
         assert rel_l2(f, f_ref) <= tol, prec
         assert abs(e - e_ref) <= tol * abs(e_ref), prec
         # u(q=0) is a sum over the grid: FP32 error scales with sum |u|
-        atol = (FP32_TOL if prec == "f32" else 1e-13) * np.abs(u).sum(axis=1).max()
+        atol = (5e-6 if prec == "f32" else 1e-13) * np.abs(u).sum(axis=1).max()
         assert np.allclose(s.get_u0(), u0_ref, rtol=0, atol=atol)
         if prec == "f32":
             assert fused, "power-of-two FP32 grid should take the fused path"
@@ -196,3 +203,40 @@ def test_autotuned_plan_is_valid_and_changes_no_result(monkeypatch):
         e = s.post_force(u, f)
         outs.append((f, e))
     assert np.array_equal(outs[0][0], outs[1][0]) and outs[0][1] == outs[1][1]
+
+
+@pytest.mark.parametrize(
+    "args,nx,ny,rows,cl",
+    [
+        ("ft fcc100 1.0 4 pair-potential 1 1.0 height 64", 2048, 2048, True, 2),
+        ("ft fcc100 1.0 2 pair-potential 1 1.0 height 64", 512, 2048, True, 1),
+        ("ft sc100 1 1.0 pair-potential 2 1.0 1.0 height 128", 256, 256, False, 1),
+        ("ft fcc100 1.0 4 pair-potential 1 1.0 height 64", 4096, 64, False, 4),
+    ],
+)
+def test_fp32_kernel_plan_and_earlier_kernels_agree(args, nx, ny, rows, cl, monkeypatch):
+    # the FP32 plan picks the warp-per-row TMA row kernels for ny = 2048 and
+    # the cluster column kernel with the expected blocks per ky; the earlier
+    # fused kernels (GFMD_FAST_V1=1) give the same forces within FP32 rounding
+    g = gfmd_pkg()
+    k = g.StiffnessKernel(args)
+    d = k.get_dimension()
+    half, linf = k.phi_table(nx, ny, "half")
+    s = _solver(nx, ny, d, "f32", half, "half", linf)
+    info = s.info()
+    assert info["row_warp_tma"] == rows and info["col_cluster"] == cl
+    monkeypatch.setenv("GFMD_FAST_V1", "1")
+    s1 = _solver(nx, ny, d, "f32", half, "half", linf)
+    monkeypatch.delenv("GFMD_FAST_V1")
+    assert not s1.info()["row_warp_tma"] and s1.info()["col_cluster"] == 0
+    u = torch.from_numpy(np.random.default_rng(3).normal(0.0, 0.01, (d, nx * ny))).float().cuda()
+    outs = []
+    for sv in (s, s1):
+        f = torch.empty_like(u)
+        ep = torch.zeros(1, dtype=torch.float64, device="cuda")
+        ms = sv.kernel_times(u, f, ep)
+        assert len(ms) == sv.info()["launches_per_eval"] and all(t > 0 for t in ms)
+        outs.append((f.double(), float(ep)))
+    (fa, ea), (fb, eb) = outs
+    assert float((fa - fb).norm() / fb.norm()) <= FP32_TOL
+    assert abs(ea - eb) <= FP32_TOL * abs(eb)

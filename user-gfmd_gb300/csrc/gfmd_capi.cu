@@ -53,7 +53,7 @@ void release(gfmd_solver *h) {
   if (!h) return;
   void *ptrs[] = {h->d_zero,  h->d_tw_hi, h->d_tw_lo,  h->d_W,     h->d_phi,     h->d_linf,
                   h->d_epart, h->d_scal,   h->d_io,    h->d_ftw,
-                  h->d_counter};
+                  h->d_counter, h->d_tw32, h->d_err};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h->ws) cudaFree(h->ws);
@@ -132,6 +132,83 @@ void push_stage_tables(gfmd::P2Plan &p, std::vector<double> &d, std::vector<floa
   p.tsize = (int)(d.size() / 2 - base);
 }
 
+// Compensated FP32 table entry (c_hi, s_hi, c_lo, s_lo) of exp(-2 pi i e / L).
+void push_c4(std::vector<float> &f, long e, long L) {
+  const double a = -2.0 * kPi * (double)(e % L) / (double)L;
+  const double c = std::cos(a), sn = std::sin(a);
+  const float ch = (float)c, sh = (float)sn;
+  f.push_back(ch);
+  f.push_back(sh);
+  f.push_back((float)(c - (double)ch));
+  f.push_back((float)(sn - (double)sh));
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no
+// link-time dependency on the driver library).
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiled encode_tiled() {
+  static EncodeTiled fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiled>(p);
+  });
+  return fn;
+}
+
+// Column-kernel cluster size for D columns of length nx: the fewest blocks
+// per ky whose share of the columns fits in 100 KB of shared memory (two
+// blocks per SM); 0 if the cluster kernel has no instance for D.
+int pick_col_cluster(int D, int nx) {
+  if (D != 3 && D != 6 && D != 12) return 0;
+  for (int cl : {1, 2, 4})
+    if (D % cl == 0 && (size_t)(D / cl) * nx * 8 <= 100 * 1024 && !(D == 3 && cl > 1)) return cl;
+  return 0;
+}
+
+// FP32 kernels of the fused path: the warp-per-row row kernels with TMA
+// tiles when ny = 2048 (rows of 1024 complex points), and the cluster
+// column kernel.  Tables and the tensor map of W are built here; a grid
+// these kernels do not cover keeps the earlier fused kernels.
+cudaError_t setup_fp32_kernels(gfmd_solver *h) {
+  const gfmd::Geom &g = h->g;
+  cudaError_t e = cudaMalloc((void **)&h->d_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(h->d_err, 0, sizeof(int));
+  if (e != cudaSuccess) return e;
+  const int cl = pick_col_cluster(g.ndof, g.nx);
+  int nepart_needed = g.nyc * std::max(cl, 1);
+  if (cl > 0 && nepart_needed <= h->n_epart) {
+    h->col_cl = cl;
+    h->phi_v = (g.ndof * g.ndof) % 4 == 0 ? 4 : 1;
+  }
+  if (g.ny == 2048 && g.nx % 8 == 0 && encode_tiled() != nullptr) {
+    std::vector<float> f;
+    for (int k1 = 0; k1 < 32; k1++)
+      for (int l = 0; l < 32; l++) push_c4(f, (long)l * k1, 1024);
+    for (int k = 0; k <= 1024; k++) push_c4(f, k, 2048);
+    e = cudaMalloc(&h->d_tw32, f.size() * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_tw32, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return e;
+    const cuuint64_t dims[3] = {(cuuint64_t)2 * g.nxp, (cuuint64_t)g.ndof, (cuuint64_t)g.nyc};
+    const cuuint64_t strides[2] = {(cuuint64_t)2 * g.nxp * 4, (cuuint64_t)g.ndof * 2 * g.nxp * 4};
+    const cuuint32_t box[3] = {16, 1, 128}, estr[3] = {1, 1, 1};
+    CUresult r = encode_tiled()(&h->tm_w, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, h->d_W, dims, strides, box, estr,
+                                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r == CUDA_SUCCESS) {
+      h->rows32 = true;
+      h->bytes += (double)f.size() * sizeof(float);
+    }
+  }
+  return cudaSuccess;
+}
+
 // Sets up the fused power-of-two path when the grid allows it.
 cudaError_t setup_fast(gfmd_solver *h) {
   const gfmd::Geom &g = h->g;
@@ -157,9 +234,15 @@ cudaError_t setup_fast(gfmd_solver *h) {
   pr.tsize += g.ny / 2 + 1;
   const int col_off = pr.tsize;
   push_stage_tables(pc, d, f);
-  // shared-memory budgets (static shared memory of the kernels < 256 bytes)
+  // shared-memory budgets (static shared memory of the kernels < 256 bytes):
+  // the single-block column kernel holds all ndof columns and its twiddles;
+  // the FP32 cluster column kernel spreads the columns over 1-4 blocks
   const size_t slack = 256;
-  if ((size_t)pc.tsize * 16 + (size_t)g.ndof * g.nx * cs + slack > h->smem_optin) return cudaSuccess;
+  const char *v1env = getenv("GFMD_FAST_V1");  // 1: only the earlier fused kernels
+  const bool v1 = v1env && v1env[0] == '1';
+  const bool col_fits = (size_t)pc.tsize * 16 + (size_t)g.ndof * g.nx * cs + slack <= h->smem_optin;
+  const bool cl_fits = h->precision == GFMD_PREC_F32 && !v1 && pick_col_cluster(g.ndof, g.nx) > 0;
+  if (!col_fits && !cl_fits) return cudaSuccess;
   const size_t row_bytes = (size_t)(g.nrow + 1) * cs;
   const size_t row_fixed = (size_t)pr.tsize * 16 + ((size_t)g.nrow * 2 + 15) / 16 * 16;
   int rb = 16;
@@ -181,6 +264,11 @@ cudaError_t setup_fast(gfmd_solver *h) {
   h->fast_rb_max = rb;
   h->bytes += (double)nent * 16 + sizeof(unsigned);
   h->fast = true;
+  if (h->precision == GFMD_PREC_F32 && !v1) {
+    e = setup_fp32_kernels(h);
+    if (e != cudaSuccess) return e;
+  }
+  if (!col_fits && h->col_cl == 0) h->fast = false;  // no column kernel fits: general path
   return cudaSuccess;
 }
 
@@ -189,6 +277,16 @@ cudaError_t setup_fast(gfmd_solver *h) {
 namespace gfmd {
 
 int set_error(int code, const std::string &msg) { return fail(code, msg); }
+
+size_t phi_index(const gfmd_solver *h, int ky, int pos, int e) {
+  const Geom &g = h->g;
+  const size_t D2 = (size_t)g.npk;
+  if (!h->fast) return ((size_t)ky * D2 + e) * g.nxp + pos;  // [ky][e][nxp]
+  const size_t blk = (size_t)ky * (g.nxp / 32) + pos / 32;
+  if (h->col_cl > 0 && h->phi_v == 4)  // [ky][x/32][e/4][32][4]
+    return (blk * (D2 / 4) + e / 4) * 128 + (size_t)(pos % 32) * 4 + e % 4;
+  return (blk * D2 + e) * 32 + pos % 32;  // [ky][x/32][e][32]
+}
 
 FftPlan make_plan(int n, std::vector<double> &tw) {
   FftPlan p{};
@@ -480,16 +578,14 @@ int gfmd_set_phi(gfmd_handle_t h, const double *phi, int layout, const double *l
           eff[2 * e + 1] = pa[2 * e + 1];
         }
       }
-      // plain path: [ky][p][nxp]; fused path: [ky][nxp/32][p][32] over the
-      // digit-reversed position of kx (the order the fused forward FFT leaves)
+      // storage position: the digit-reversed position of kx on the fused
+      // path (the order its forward FFT leaves), kx otherwise
       const int xs = fused ? p2_digit_rev(h->p2_col, kx) : kx;
-      const size_t base = fused ? ((size_t)ky * (g.nxp / 32) + xs / 32) * D2 * 32 + (xs % 32)
-                                : (size_t)ky * D2 * g.nxp + kx;
-      const size_t pstride = fused ? 32 : (size_t)g.nxp;
       auto put = [&](int p, double v) {
         if (!std::isfinite(v)) ok = false;
-        if (f64) packd[base + (size_t)p * pstride] = v;
-        else packf[base + (size_t)p * pstride] = (float)v;
+        const size_t at = gfmd::phi_index(h, ky, xs, p);
+        if (f64) packd[at] = v;
+        else packf[at] = (float)v;
       };
       for (int i = 0; i < D; i++) put(i, eff[2 * (i * D + i)]);
       int p = D;
@@ -548,7 +644,7 @@ static int inverse_table_handle(gfmd_handle_t h, const char *who, double scale, 
   gfmd_handle_t p = nullptr;
   int rc = gfmd_create(g.nx, g.ny, g.ndof, h->precision, &p);
   if (rc != GFMD_OK) return rc;
-  if (p->fast != h->fast) {  // same parameters give the same path
+  if (p->fast != h->fast || p->col_cl != h->col_cl || p->phi_v != h->phi_v) {  // same parameters, same path
     release(p);
     return fail(GFMD_ECUDA, w + ": path mismatch");
   }
@@ -571,21 +667,18 @@ static int inverse_table_handle(gfmd_handle_t h, const char *who, double scale, 
       return cuda_fail(e, (w + ": download").c_str());
     }
   }
-  const bool fused = h->fast;
   std::atomic<bool> ok(true);
   parallel_for((long)nslot, [&](long a, long b) {
     std::vector<std::complex<double>> A(D2), I(D2);
     for (long t = a; t < b; t++) {
       const int ky = (int)(t / g.nxp), xs = (int)(t % g.nxp);
-      const size_t base = fused ? ((size_t)ky * (g.nxp / 32) + xs / 32) * D2 * 32 + (xs % 32)
-                                : (size_t)ky * D2 * g.nxp + xs;
-      const size_t ps = fused ? 32 : (size_t)g.nxp;
+      auto at = [&](int e) { return gfmd::phi_index(h, ky, xs, e); };
       // Hermitian block of the uploaded table
-      for (int i = 0; i < D; i++) A[i * D + i] = tab[base + (size_t)i * ps];
+      for (int i = 0; i < D; i++) A[i * D + i] = tab[at(i)];
       int q = D;
       for (int i = 0; i < D; i++)
         for (int j = i + 1; j < D; j++) {
-          const std::complex<double> v(tab[base + (size_t)q * ps], tab[base + (size_t)(q + 1) * ps]);
+          const std::complex<double> v(tab[at(q)], tab[at(q + 1)]);
           A[i * D + j] = v;
           A[j * D + i] = std::conj(v);
           q += 2;
@@ -616,13 +709,13 @@ static int inverse_table_handle(gfmd_handle_t h, const char *who, double scale, 
         }
       }
       // pack scale * inverse (Hermitian part)
-      for (int i = 0; i < D; i++) tab[base + (size_t)i * ps] = scale * I[i * D + i].real();
+      for (int i = 0; i < D; i++) tab[at(i)] = scale * I[i * D + i].real();
       q = D;
       for (int i = 0; i < D; i++)
         for (int j = i + 1; j < D; j++) {
           const std::complex<double> v = 0.5 * scale * (I[i * D + j] + std::conj(I[j * D + i]));
-          tab[base + (size_t)q * ps] = v.real();
-          tab[base + (size_t)(q + 1) * ps] = v.imag();
+          tab[at(q)] = v.real();
+          tab[at(q + 1)] = v.imag();
           q += 2;
         }
     }
@@ -738,6 +831,17 @@ int gfmd_force_f32(gfmd_handle_t h, const float *d_u, float *d_f, double *d_epot
   return force_common(h, d_u, 1, d_f, 1, d_epot, "gfmd_force_f32");
 }
 
+// After a synchronisation: a bounded device wait that gave up (recorded in
+// the handle's error word by the TMA row kernels) becomes GFMD_ETIMEDOUT.
+static int check_device_error(gfmd_handle_t h, const char *who) {
+  if (!h->d_err) return GFMD_OK;
+  int v = 0;
+  CK(cudaMemcpy(&v, h->d_err, sizeof(int), cudaMemcpyDeviceToHost), who);
+  if (v == 0) return GFMD_OK;
+  CK(cudaMemset(h->d_err, 0, sizeof(int)), who);
+  return fail(GFMD_ETIMEDOUT, std::string(who) + ": a device wait for a tile timed out");
+}
+
 int gfmd_post_force(gfmd_handle_t h, const double *d_u, double *d_f, double *epot) {
   int rc = force_common(h, d_u, 0, d_f, 0, h ? h->d_scal : nullptr, "gfmd_post_force");
   if (rc) return rc;
@@ -745,6 +849,7 @@ int gfmd_post_force(gfmd_handle_t h, const double *d_u, double *d_f, double *epo
   CK(cudaMemcpyAsync(&e, h->d_scal, sizeof(double), cudaMemcpyDeviceToHost, h->stream),
      "gfmd_post_force: energy");
   CK(cudaStreamSynchronize(h->stream), "gfmd_post_force");
+  if ((rc = check_device_error(h, "gfmd_post_force"))) return rc;
   if (!std::isfinite(e)) return fail(GFMD_ENONFINITE, "gfmd_post_force: energy is not finite");
   if (epot) *epot = e;
   return GFMD_OK;
@@ -765,6 +870,7 @@ int gfmd_post_force_host(gfmd_handle_t h, const double *u, double *f, double *ep
   CK(cudaMemcpyAsync(&e, h->d_scal, sizeof(double), cudaMemcpyDeviceToHost, h->stream),
      "gfmd_post_force_host: energy");
   CK(cudaStreamSynchronize(h->stream), "gfmd_post_force_host");
+  if ((rc = check_device_error(h, "gfmd_post_force_host"))) return rc;
   if (!std::isfinite(e)) return fail(GFMD_ENONFINITE, "gfmd_post_force_host: energy is not finite");
   if (epot) *epot = e;
   return GFMD_OK;
@@ -782,6 +888,43 @@ int gfmd_prec_gradient_host(gfmd_handle_t h, const double *cavg, const double *g
   CK(cudaMemcpyAsync(gP, dp, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream),
      "gfmd_prec_gradient_host: copy out");
   CK(cudaStreamSynchronize(h->stream), "gfmd_prec_gradient_host");
+  return GFMD_OK;
+}
+
+int gfmd_force_kernel_times(gfmd_handle_t h, const void *d_u, void *d_f, double *d_epot, float *ms, int nmax,
+                            int *nk) {
+  if (!h || !d_u || !d_f || !d_epot || !ms || !nk)
+    return fail(GFMD_EINVAL, "gfmd_force_kernel_times: NULL argument");
+  if (d_u == d_f) return fail(GFMD_EINVAL, "gfmd_force_kernel_times: u and f must not alias");
+  if (!h->have_phi) return fail(GFMD_ENOPHI, "gfmd_force_kernel_times: no stiffness table uploaded");
+  const int nl = gfmd::force_launches(h);
+  if (nmax < nl) return fail(GFMD_EINVAL, "gfmd_force_kernel_times: ms holds fewer entries than launches");
+  std::vector<cudaEvent_t> ev(nl + 1, nullptr);
+  cudaError_t e = cudaSuccess;
+  for (auto &x : ev)
+    if (e == cudaSuccess) e = cudaEventCreate(&x);
+  if (e == cudaSuccess) {
+    h->mark = ev.data();
+    h->nmark = nl + 1;
+    const int t = h->precision == GFMD_PREC_F64 ? 0 : 1;
+    e = gfmd::enqueue_force(h, d_u, t, d_f, t, d_epot);
+    h->mark = nullptr;
+    h->nmark = 0;
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  for (int i = 0; i < nl && e == cudaSuccess; i++) e = cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]);
+  for (auto &x : ev)
+    if (x) cudaEventDestroy(x);
+  if (e != cudaSuccess) return cuda_fail(e, "gfmd_force_kernel_times");
+  *nk = nl;
+  return check_device_error(h, "gfmd_force_kernel_times");
+}
+
+int gfmd_kernel_plan(gfmd_handle_t h, int *row_warp_tma, int *col_cluster, int *phi_vector) {
+  if (!h) return fail(GFMD_EINVAL, "gfmd_kernel_plan: NULL handle");
+  if (row_warp_tma) *row_warp_tma = h->rows32 ? 1 : 0;
+  if (col_cluster) *col_cluster = h->col_cl;
+  if (phi_vector) *phi_vector = h->phi_v;
   return GFMD_OK;
 }
 

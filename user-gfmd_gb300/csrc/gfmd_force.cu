@@ -22,7 +22,9 @@
 #include "gfmd_fft.cuh"
 #include "gfmd_internal.h"
 #include "gfmd_fast_kernels.cuh"
+#include "gfmd_col_cluster.cuh"
 #include "gfmd_plain_kernels.cuh"
+#include "gfmd_rows_warp.cuh"
 
 namespace gfmd {
 
@@ -63,7 +65,70 @@ void launch_col_fast(gfmd_solver *h, C<T> *W, size_t sm, double *d_epot) {
       h->d_counter, d_epot);
 }
 
-// Fused power-of-two path: three launches.
+// Event i of a timed evaluation (gfmd_force_kernel_times), before launch i.
+inline void mark(gfmd_solver *h, int i) {
+  if (h->mark && i < h->nmark) cudaEventRecord(h->mark[i], h->stream);
+}
+
+// Cluster column kernel: CL blocks per ky (a thread-block cluster).
+template <int D, int CL, int V>
+cudaError_t launch_col_cl(gfmd_solver *h, float2 *W, double *d_epot) {
+  auto kf = k_col_phi_cl<D, CL, V>;
+  const size_t sm = (size_t)(D / CL) * h->g.nx * sizeof(float2);
+  cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(h->g.nyc * CL);
+  cfg.blockDim = dim3(colcl::kThreads);
+  cfg.dynamicSmemBytes = sm;
+  cfg.stream = h->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = CL;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kf, W, reinterpret_cast<const float *>(h->d_phi), h->g, h->p2_col,
+                            reinterpret_cast<const float4 *>(h->d_ftw) + h->ftw_col_off,
+                            (const double *)h->d_linf, h->d_epart, h->d_scal, h->d_counter, d_epot);
+}
+
+cudaError_t enqueue_col_cl(gfmd_solver *h, float2 *W, double *d_epot) {
+  const int D = h->g.ndof, CL = h->col_cl;
+  if (D == 3 && CL == 1) return launch_col_cl<3, 1, 1>(h, W, d_epot);
+  if (D == 6 && CL == 1) return launch_col_cl<6, 1, 4>(h, W, d_epot);
+  if (D == 6 && CL == 2) return launch_col_cl<6, 2, 4>(h, W, d_epot);
+  if (D == 12 && CL == 1) return launch_col_cl<12, 1, 4>(h, W, d_epot);
+  if (D == 12 && CL == 2) return launch_col_cl<12, 2, 4>(h, W, d_epot);
+  if (D == 12 && CL == 4) return launch_col_cl<12, 4, 4>(h, W, d_epot);
+  return cudaErrorInvalidValue;
+}
+
+// Warp-per-row row kernels with TMA tiles (FP32 handles, ny = 2048).
+template <typename Tin> cudaError_t launch_row_fwd32(gfmd_solver *h, const void *d_u) {
+  auto kf = k_row_fwd_w32<Tin>;
+  cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows32::kSmemBytes);
+  if (e != cudaSuccess) return e;
+  const float4 *tw = reinterpret_cast<const float4 *>(h->d_tw32);
+  kf<<<dim3(h->g.nx / rows32::kRB, h->g.ndof), rows32::kThreads, rows32::kSmemBytes, h->stream>>>(
+      reinterpret_cast<const Tin *>(d_u), reinterpret_cast<float2 *>(h->d_W), h->tm_w, h->g, tw, tw + 1024);
+  return cudaSuccess;
+}
+template <typename Tout> cudaError_t launch_row_inv32(gfmd_solver *h, void *d_f) {
+  auto kf = k_row_inv_w32<Tout>;
+  cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows32::kSmemBytes);
+  if (e != cudaSuccess) return e;
+  const float4 *tw = reinterpret_cast<const float4 *>(h->d_tw32);
+  kf<<<dim3(h->g.nx / rows32::kRB, h->g.ndof), rows32::kThreads, rows32::kSmemBytes, h->stream>>>(
+      reinterpret_cast<const float2 *>(h->d_W), h->tm_w, reinterpret_cast<Tout *>(d_f), h->g, tw, tw + 1024,
+      h->d_err);
+  return cudaSuccess;
+}
+
+// Fused power-of-two path: three launches.  FP32 handles use the
+// warp-per-row TMA row kernels where the row length allows (rows32) and the
+// cluster column kernel where it has an instance (col_cl > 0).
 template <typename T>
 cudaError_t enqueue_fast(gfmd_solver *h, const void *d_u, int in_t, void *d_f, int out_t,
                          double *d_epot) {
@@ -75,7 +140,13 @@ cudaError_t enqueue_fast(gfmd_solver *h, const void *d_u, int in_t, void *d_f, i
   const size_t smr = (size_t)h->p2_row.tsize * sizeof(E) + srev_bytes(g.nrow) +
                      (size_t)rb * (g.nrow + 1) * sizeof(C<T>);
   dim3 gridr((g.nx + rb - 1) / rb, g.ndof);
-  if (in_t == 0) {
+  constexpr bool f32 = sizeof(T) == 4;
+  cudaError_t e = cudaSuccess;
+
+  mark(h, 0);
+  if (f32 && h->rows32) {
+    e = in_t == 0 ? launch_row_fwd32<double>(h, d_u) : launch_row_fwd32<float>(h, d_u);
+  } else if (in_t == 0) {
     auto kf = k_row_fwd_fast<T, double>;
     cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr);
     kf<<<gridr, kRowThreads, smr, h->stream>>>(reinterpret_cast<const double *>(d_u), W, g, h->p2_row, tab_row, rb);
@@ -84,19 +155,31 @@ cudaError_t enqueue_fast(gfmd_solver *h, const void *d_u, int in_t, void *d_f, i
     cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr);
     kf<<<gridr, kRowThreads, smr, h->stream>>>(reinterpret_cast<const float *>(d_u), W, g, h->p2_row, tab_row, rb);
   }
-  const size_t smc = (size_t)h->p2_col.tsize * sizeof(E) + (size_t)g.ndof * g.nx * sizeof(C<T>);
-  switch (g.ndof) {
-    case 3: launch_col_fast<T, 3>(h, W, smc, d_epot); break;
-    case 6: launch_col_fast<T, 6>(h, W, smc, d_epot); break;
-    case 9: launch_col_fast<T, 9>(h, W, smc, d_epot); break;
-    case 12: launch_col_fast<T, 12>(h, W, smc, d_epot); break;
-    case 15: launch_col_fast<T, 15>(h, W, smc, d_epot); break;
-    case 18: launch_col_fast<T, 18>(h, W, smc, d_epot); break;
-    case 21: launch_col_fast<T, 21>(h, W, smc, d_epot); break;
-    case 24: launch_col_fast<T, 24>(h, W, smc, d_epot); break;
-    default: return cudaErrorInvalidValue;
+  if (e != cudaSuccess) return e;
+
+  mark(h, 1);
+  if (f32 && h->col_cl > 0) {
+    e = enqueue_col_cl(h, reinterpret_cast<float2 *>(W), d_epot);
+  } else {
+    const size_t smc = (size_t)h->p2_col.tsize * sizeof(E) + (size_t)g.ndof * g.nx * sizeof(C<T>);
+    switch (g.ndof) {
+      case 3: launch_col_fast<T, 3>(h, W, smc, d_epot); break;
+      case 6: launch_col_fast<T, 6>(h, W, smc, d_epot); break;
+      case 9: launch_col_fast<T, 9>(h, W, smc, d_epot); break;
+      case 12: launch_col_fast<T, 12>(h, W, smc, d_epot); break;
+      case 15: launch_col_fast<T, 15>(h, W, smc, d_epot); break;
+      case 18: launch_col_fast<T, 18>(h, W, smc, d_epot); break;
+      case 21: launch_col_fast<T, 21>(h, W, smc, d_epot); break;
+      case 24: launch_col_fast<T, 24>(h, W, smc, d_epot); break;
+      default: return cudaErrorInvalidValue;
+    }
   }
-  if (out_t == 0) {
+  if (e != cudaSuccess) return e;
+
+  mark(h, 2);
+  if (f32 && h->rows32) {
+    e = out_t == 0 ? launch_row_inv32<double>(h, d_f) : launch_row_inv32<float>(h, d_f);
+  } else if (out_t == 0) {
     auto kf = k_row_inv_fast<T, double>;
     cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr);
     kf<<<gridr, kRowThreads, smr, h->stream>>>(W, reinterpret_cast<double *>(d_f), g, h->p2_row, tab_row, rb);
@@ -105,6 +188,8 @@ cudaError_t enqueue_fast(gfmd_solver *h, const void *d_u, int in_t, void *d_f, i
     cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr);
     kf<<<gridr, kRowThreads, smr, h->stream>>>(W, reinterpret_cast<float *>(d_f), g, h->p2_row, tab_row, rb);
   }
+  if (e != cudaSuccess) return e;
+  mark(h, 3);
   return cudaGetLastError();
 }
 
@@ -181,7 +266,9 @@ void force_layout(const Geom &g, int precision, size_t *w_bytes, size_t *phi_byt
   size_t s = precision == GFMD_PREC_F64 ? 8 : 4;
   *w_bytes = (size_t)g.nyc * g.ndof * g.nxp * 2 * s;
   *phi_bytes = (size_t)g.nyc * g.npk * g.nxp * s;
-  *n_epart = ((g.nx + kPhiThreads - 1) / kPhiThreads) * g.nyc;  // >= nyc (fused path)
+  // plain path: one partial per phi_apply block; fused paths: one per
+  // column block (up to 4 per ky for the cluster column kernel)
+  *n_epart = std::max((g.nx + kPhiThreads - 1) / kPhiThreads, 4) * g.nyc;
 }
 
 int force_launches(const gfmd_solver *h) { return h->fast ? 3 : 6; }

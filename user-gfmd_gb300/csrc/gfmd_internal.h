@@ -2,6 +2,7 @@
 #ifndef GFMD_GB300_INTERNAL_H
 #define GFMD_GB300_INTERNAL_H
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <string>
@@ -93,6 +94,16 @@ struct gfmd_solver {
   int fast_rpost = 0;
   double bytes = 0.0;
 
+  // FP32 kernels of the fused path (gfmd_rows_warp.cuh, gfmd_col_cluster.cuh)
+  bool rows32 = false;       // warp-per-row row kernels with TMA tiles (ny = 2048)
+  int col_cl = 0;            // blocks per ky of the cluster column kernel (0: not used)
+  int phi_v = 1;             // packed-Phi vector width of that kernel (1 or 4)
+  void *d_tw32 = nullptr;    // float4: [k1][l] w_1024^(l k1), then e^{-2 pi i k/2048}, k = 0..1024
+  CUtensorMap tm_w;          // W as floats {2 nxp, ndof, nyc}, box {16, 1, 128}
+  int *d_err = nullptr;      // device error word: GFMD_ETIMEDOUT from a bounded wait
+  cudaEvent_t *mark = nullptr;  // when set: events recorded around each launch
+  int nmark = 0;
+
   // solver workspace, kept between solves (gfmd_cg.cu)
   void *ws = nullptr;
   size_t ws_bytes = 0;
@@ -120,6 +131,9 @@ int cg_minimize(gfmd_solver *hp, const gfmd_obstacle_t *ob, const gfmd_min_param
 int set_error(int code, const std::string &msg);
 // Kernel launches one force evaluation makes.
 int force_launches(const gfmd_solver *h);
+// Index (in reals) of packed element e of the wavevector at storage position
+// pos (digit-reversed kx on the fused path, kx otherwise) of row ky.
+size_t phi_index(const gfmd_solver *h, int ky, int pos, int e);
 // Device bytes of the spectrum/Phi arrays and the number of energy partials.
 void force_layout(const Geom &g, int precision, size_t *w_bytes, size_t *phi_bytes, int *n_epart);
 }  // namespace gfmd

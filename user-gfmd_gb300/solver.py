@@ -38,6 +38,29 @@ def _ptr(a) -> int:
     raise TypeError(f"cannot take the address of {type(a)!r}")
 
 
+def _check_device_array(a, dtype: str, count: int, what: str) -> None:
+    """A device buffer passed by address must hold `count` contiguous
+    elements of `dtype` ("float64" or "float32"); anything else would be
+    read as the wrong numbers by the C ABI, so it is refused here."""
+    if hasattr(a, "dtype") and hasattr(a, "is_contiguous"):  # torch tensor
+        got = str(a.dtype).replace("torch.", "")
+        if got != dtype:
+            raise TypeError(f"{what} must be {dtype}, got {got}")
+        if not a.is_contiguous():
+            raise TypeError(f"{what} must be contiguous")
+        if a.numel() < count:
+            raise ValueError(f"{what} holds {a.numel()} elements, needs {count}")
+    elif hasattr(a, "__cuda_array_interface__"):
+        ai = a.__cuda_array_interface__
+        want = {"float64": "<f8", "float32": "<f4"}[dtype]
+        if ai.get("typestr") != want:
+            raise TypeError(f"{what} must be {dtype}, got {ai.get('typestr')}")
+        if ai.get("strides") is not None:
+            raise TypeError(f"{what} must be contiguous")
+        if int(np.prod(ai["shape"])) < count:
+            raise ValueError(f"{what} holds fewer than {count} elements")
+
+
 def _is_device(a) -> bool:
     if hasattr(a, "is_cuda"):
         return bool(a.is_cuda)
@@ -274,6 +297,11 @@ class GFMDSolverGB300:
             formats.write_q_space_dump(dump_prefix, uh, full, self.nx, self.ny)
         e = ctypes.c_double()
         if _is_device(u) and _is_device(f):
+            # the reference's GPU post_force takes double buffers whatever the
+            # arithmetic of the handle (the FP32 handle converts on the fly)
+            n = self.ndof * self.nx * self.ny
+            _check_device_array(u, "float64", n, "u")
+            _check_device_array(f, "float64", n, "f")
             check(lib().gfmd_post_force(self._handle(), _ptr(u), _ptr(f), ctypes.byref(e)))
         elif not _is_device(u) and not _is_device(f):
             uh = np.ascontiguousarray(u, dtype=np.float64)
@@ -288,6 +316,11 @@ class GFMDSolverGB300:
         """Device-resident evaluation without a host sync; epot is a device
         float64 scalar tensor."""
         fn = lib().gfmd_force_f64 if self.precision == "f64" else lib().gfmd_force_f32
+        n = self.ndof * self.nx * self.ny
+        dt = "float64" if self.precision == "f64" else "float32"
+        _check_device_array(u, dt, n, "u")
+        _check_device_array(f, dt, n, "f")
+        _check_device_array(epot, "float64", 1, "epot")
         check(fn(self._handle(), _ptr(u), _ptr(f), _ptr(epot)))
 
     def make_preconditioner(self, shift: float) -> "GFMDSolverGB300":
@@ -365,8 +398,26 @@ class GFMDSolverGB300:
         check(lib().gfmd_solver_info(self._handle(), ctypes.byref(n), ctypes.byref(f)))
         rb, pf = ctypes.c_int(), ctypes.c_int()
         check(lib().gfmd_plan_info(self._handle(), ctypes.byref(rb), ctypes.byref(pf)))
+        rw, cl, pv = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(lib().gfmd_kernel_plan(self._handle(), ctypes.byref(rw), ctypes.byref(cl), ctypes.byref(pv)))
         return {"launches_per_eval": n.value, "fused": bool(f.value),
-                "rows_per_block": rb.value, "phi_prefetch": pf.value}
+                "rows_per_block": rb.value, "phi_prefetch": pf.value,
+                "row_warp_tma": bool(rw.value), "col_cluster": cl.value, "phi_vector": pv.value}
+
+    def kernel_times(self, u, f, epot) -> list:
+        """Device milliseconds of each launch of one evaluation of u (device
+        buffers of the handle's arithmetic type), from CUDA events on the
+        handle's stream."""
+        n = self.ndof * self.nx * self.ny
+        dt = "float64" if self.precision == "f64" else "float32"
+        _check_device_array(u, dt, n, "u")
+        _check_device_array(f, dt, n, "f")
+        _check_device_array(epot, "float64", 1, "epot")
+        ms = (ctypes.c_float * 16)()
+        nk = ctypes.c_int()
+        check(lib().gfmd_force_kernel_times(self._handle(), _ptr(u), _ptr(f), _ptr(epot), ms, 16,
+                                            ctypes.byref(nk)))
+        return [float(ms[i]) for i in range(nk.value)]
 
     def get_nxy_loc(self) -> int:
         return self.nx * self.ny
