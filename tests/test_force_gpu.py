@@ -135,6 +135,11 @@ def test_errors_are_status_codes_on_gpu():
         ("ft fcc100 1.0 4 pair-potential 1 1.0 height 64", 256, 2048),
         ("ft fcc100 1.0 2 pair-potential 1 1.0 height 64", 1024, 2048),
         ("ft fcc100 1.0 4 pair-potential 1 1.0 height 64", 4096, 64),
+        # nx = 1024, 2048: register-transform column kernel (FP32)
+        ("ft sc100 1 1.0 pair-potential 2 1.0 1.0 height 128", 2048, 64),
+        ("ft fcc100 1.0 2 pair-potential 1 1.0 height 64", 2048, 128),
+        ("ft fcc100 1.0 4 pair-potential 1 1.0 height 64", 1024, 32),
+        ("ft sc100 1 1.0 pair-potential 2 1.0 1.0 height 128", 1024, 16),
     ],
 )
 def test_fused_path_matches_oracle_and_plain_path(args, nx, ny, monkeypatch):
@@ -208,7 +213,7 @@ def test_autotuned_plan_is_valid_and_changes_no_result(monkeypatch):
 @pytest.mark.parametrize(
     "args,nx,ny,rows,cl",
     [
-        ("ft fcc100 1.0 4 pair-potential 1 1.0 height 64", 2048, 2048, True, 2),
+        ("ft fcc100 1.0 4 pair-potential 1 1.0 height 64", 2048, 2048, True, 3),
         ("ft fcc100 1.0 2 pair-potential 1 1.0 height 64", 512, 2048, True, 1),
         ("ft sc100 1 1.0 pair-potential 2 1.0 1.0 height 128", 256, 256, False, 1),
         ("ft fcc100 1.0 4 pair-potential 1 1.0 height 64", 4096, 64, False, 4),

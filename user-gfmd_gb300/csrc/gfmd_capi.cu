@@ -53,7 +53,7 @@ void release(gfmd_solver *h) {
   if (!h) return;
   void *ptrs[] = {h->d_zero,  h->d_tw_hi, h->d_tw_lo,  h->d_W,     h->d_phi,     h->d_linf,
                   h->d_epart, h->d_scal,   h->d_io,    h->d_ftw,
-                  h->d_counter, h->d_tw32, h->d_err};
+                  h->d_counter, h->d_tw32, h->d_err, h->d_twc};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h->ws) cudaFree(h->ws);
@@ -181,7 +181,33 @@ cudaError_t setup_fp32_kernels(gfmd_solver *h) {
   cudaError_t e = cudaMalloc((void **)&h->d_err, sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(h->d_err, 0, sizeof(int));
   if (e != cudaSuccess) return e;
-  const int cl = pick_col_cluster(g.ndof, g.nx);
+  const int D = g.ndof;
+  const char *r32env = getenv("GFMD_COL_R32");  // 0: keep the shared-memory-stage column kernel
+  const bool r32_ok = !(r32env && r32env[0] == '0');
+  if (r32_ok && (g.nx == 1024 || g.nx == 2048) && (D == 3 || D == 6 || D == 12)) {
+    // register-transform column kernel: DL = D / CL columns of nx / 32
+    // threads each, at most 256 threads and 100 KB of shared memory a block
+    const int P = g.nx / 32;
+    int cl = 0;
+    for (int c : {1, 2, 3, 4, 6})
+      if (D % c == 0 && (D / c) * P <= 256 && (size_t)(D / c) * g.nx * 8 <= 100 * 1024) {
+        cl = c;
+        break;
+      }
+    if (cl > 0 && g.nyc * cl <= h->n_epart) {
+      std::vector<float> f;
+      for (int k1 = 0; k1 < 32; k1++)
+        for (int t = 0; t < P; t++) push_c4(f, (long)t * k1, g.nx);
+      e = cudaMalloc(&h->d_twc, f.size() * sizeof(float));
+      if (e == cudaSuccess) e = cudaMemcpy(h->d_twc, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) return e;
+      h->col_r32 = true;
+      h->col_cl = cl;
+      h->phi_v = (D * D) % 4 == 0 ? 4 : 1;
+      h->bytes += (double)f.size() * sizeof(float);
+    }
+  }
+  const int cl = h->col_r32 ? 0 : pick_col_cluster(g.ndof, g.nx);
   int nepart_needed = g.nyc * std::max(cl, 1);
   if (cl > 0 && nepart_needed <= h->n_epart) {
     h->col_cl = cl;
@@ -580,7 +606,9 @@ int gfmd_set_phi(gfmd_handle_t h, const double *phi, int layout, const double *l
       }
       // storage position: the digit-reversed position of kx on the fused
       // path (the order its forward FFT leaves), kx otherwise
-      const int xs = fused ? p2_digit_rev(h->p2_col, kx) : kx;
+      const int xs = !fused ? kx
+                     : h->col_r32 ? (g.nx / 32) * (kx & 31) + (kx >> 5)
+                                  : p2_digit_rev(h->p2_col, kx);
       auto put = [&](int p, double v) {
         if (!std::isfinite(v)) ok = false;
         const size_t at = gfmd::phi_index(h, ky, xs, p);
@@ -644,7 +672,8 @@ static int inverse_table_handle(gfmd_handle_t h, const char *who, double scale, 
   gfmd_handle_t p = nullptr;
   int rc = gfmd_create(g.nx, g.ny, g.ndof, h->precision, &p);
   if (rc != GFMD_OK) return rc;
-  if (p->fast != h->fast || p->col_cl != h->col_cl || p->phi_v != h->phi_v) {  // same parameters, same path
+  if (p->fast != h->fast || p->col_cl != h->col_cl || p->phi_v != h->phi_v ||
+      p->col_r32 != h->col_r32) {  // same parameters, same path
     release(p);
     return fail(GFMD_ECUDA, w + ": path mismatch");
   }

@@ -37,6 +37,7 @@
 #include "gfmd_fast_kernels.cuh"
 #include "gfmd_fft.cuh"
 #include "gfmd_internal.h"
+#include "gfmd_rows_warp.cuh"
 
 namespace gfmd {
 
@@ -314,6 +315,206 @@ __global__ void __launch_bounds__(colcl::kThreads, 2)
       double t = 0.0;
       for (int w = 0; w < nwarp; w++) t += red[w];
       *d_epot = 0.5 * t;
+      *counter = 0u;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Register-transform column kernel for nx = 32 P, P in {32, 64} (nx = 1024,
+// 2048).  A column x[t + P m] (t < P, m < 32) is transformed in two passes
+// held in registers:
+//   pass A (thread t of the column): 32-point DFT over m, straight from the
+//     coalesced global loads of W, times the compensated twiddle w_nx^(t k1),
+//     written transposed to shared memory S[k1][t] (XOR-swizzled);
+//   pass B (thread (k1, s), s = t mod 2 for P = 64): 32-point DFT over the
+//     column's t of that parity and, for P = 64, one radix-2 step across the
+//     thread pair by warp shuffles; the spectrum X[k1 + 32 k2] is stored at
+//     position q = P k1 + k2 (swizzled q ^ ((q >> 5) & 15)), the order in
+//     which the stiffness table is packed for this kernel.
+// The backward transform runs the passes in reverse; its pass A stores the
+// column to W with coalesced stores, so the kernel reads and writes W once
+// and stages nothing but the transposes in shared memory.
+namespace colr {
+
+template <int P> __device__ __forceinline__ int swa(int k1) { return P == 64 ? 2 * (k1 & 7) : (k1 & 15); }
+__device__ __forceinline__ int physq(int q) { return q ^ ((q >> 5) & 15); }
+
+// (cos, sin) of 2 pi k / 64, k = 0..31
+__device__ __forceinline__ float2 w64(int k) {
+  const float c[32] = {1.00000000000000000000f, 0.99518472667219692873f, 0.98078528040323043058f, 0.95694033573220882438f, 0.92387953251128673848f, 0.88192126434835504956f, 0.83146961230254523567f, 0.77301045336273699338f, 0.70710678118654757274f, 0.63439328416364548779f, 0.55557023301960228867f, 0.47139673682599780857f, 0.38268343236508983729f, 0.29028467725446233105f, 0.19509032201612833135f, 0.09801714032956077016f, 0.0f, -0.09801714032956064526f, -0.19509032201612819257f, -0.29028467725446216452f, -0.38268343236508972627f, -0.47139673682599769755f, -0.55557023301960195560f, -0.63439328416364537677f, -0.70710678118654746172f, -0.77301045336273699338f, -0.83146961230254534669f, -0.88192126434835493853f, -0.92387953251128673848f, -0.95694033573220882438f, -0.98078528040323043058f, -0.99518472667219681771f};
+  const float sn[32] = {0.00000000000000000000f, 0.09801714032956060363f, 0.19509032201612824808f, 0.29028467725446233105f, 0.38268343236508978178f, 0.47139673682599764204f, 0.55557023301960217765f, 0.63439328416364548779f, 0.70710678118654746172f, 0.77301045336273699338f, 0.83146961230254523567f, 0.88192126434835493853f, 0.92387953251128673848f, 0.95694033573220893540f, 0.98078528040323043058f, 0.99518472667219681771f, 1.00000000000000000000f, 0.99518472667219692873f, 0.98078528040323043058f, 0.95694033573220893540f, 0.92387953251128673848f, 0.88192126434835504956f, 0.83146961230254545772f, 0.77301045336273710440f, 0.70710678118654757274f, 0.63439328416364548779f, 0.55557023301960217765f, 0.47139673682599786408f, 0.38268343236508989280f, 0.29028467725446238656f, 0.19509032201612860891f, 0.09801714032956082567f};
+  return make_float2(c[k], sn[k]);
+}
+
+}  // namespace colr
+
+// One cluster of CL blocks per ky, block rank r owning columns
+// [r DL, (r+1) DL), DL * P threads (thread c P + t: column c, index t).
+// twa: [k1][t] compensated w_nx^(t k1); phi packed [ky][q/32][D*D/4][32][4]
+// (V = 4) or [ky][q/32][D*D][32] (V = 1) over the storage positions q.
+template <int D, int CL, int LGN, int MINB>
+__global__ void __launch_bounds__((D / CL) * (1 << LGN) / 32, MINB)
+    k_col_phi_r32(float2 *__restrict__ W, const float *__restrict__ phi, Geom g, const float4 *__restrict__ twa,
+                  const double *__restrict__ linf, double *__restrict__ epart, double *__restrict__ scal,
+                  unsigned *__restrict__ counter, double *__restrict__ d_epot) {
+  namespace cg = cooperative_groups;
+  constexpr int n = 1 << LGN, P = n / 32, DL = D / CL, NT = DL * P;
+  constexpr int V = (D * D) % 4 == 0 ? 4 : 1;
+  constexpr int kPerPos = D * D;
+  constexpr unsigned kBlk = (unsigned)(kPerPos * 32 * 4);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double red[NT / 32];
+  __shared__ int is_last;
+  float2 *sm = reinterpret_cast<float2 *>(smem_raw);
+  const int rank = (int)(blockIdx.x % CL), ky = (int)(blockIdx.x / CL);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = NT / 32;
+  const int c = threadIdx.x / P, t = threadIdx.x % P;
+  float2 *S = sm + c * n;
+  float2 *colg = W + ((size_t)ky * D + rank * DL + c) * g.nxp;
+  const int nkb = g.nxp >> 5;
+  const float *phik = phi + (size_t)ky * nkb * (kPerPos * 32);
+  constexpr int kbn = n / 32;
+  const int kb0 = (kbn * rank) / CL, kb1 = (kbn * (rank + 1)) / CL;
+  // pass-B roles: k1 and the parity s of t (P = 64)
+  const int k1b = P == 64 ? (t >> 1) : t, sb = P == 64 ? (t & 1) : 0;
+
+  if (lane == 0 && kb0 + warp < kb1) prefetch_l2(phik + (size_t)(kb0 + warp) * (kPerPos * 32), kBlk);
+  float2 x[32];
+  // ---- forward pass A ----
+#pragma unroll
+  for (int m = 0; m < 32; m++) x[m] = __ldcs(colg + t + P * m);
+  rows32::dft32<-1>(x);
+#pragma unroll
+  for (int k1 = 1; k1 < 32; k1++) x[k1] = rows32::twc<-1>(x[k1], __ldg(&twa[k1 * P + t]));
+#pragma unroll
+  for (int k1 = 0; k1 < 32; k1++) S[k1 * P + (t ^ colr::swa<P>(k1))] = x[k1];
+  __syncthreads();
+  // ---- forward pass B ----
+#pragma unroll
+  for (int tp = 0; tp < 32; tp++) {
+    const int tt = P == 64 ? 2 * tp + sb : tp;
+    x[tp] = S[k1b * P + (tt ^ colr::swa<P>(k1b))];
+  }
+  rows32::dft32<-1>(x);
+  if constexpr (P == 64) {
+#pragma unroll
+    for (int k = 0; k < 32; k++) {
+      const float2 own = x[k];
+      const float2 oth = make_float2(__shfl_xor_sync(0xffffffffu, own.x, 1), __shfl_xor_sync(0xffffffffu, own.y, 1));
+      const float2 a = sb ? oth : own, b = sb ? own : oth;  // D_0, D_1
+      const float2 w = colr::w64(k);
+      const float2 wb = make_float2(fmaf(b.x, w.x, b.y * w.y), fmaf(b.y, w.x, -b.x * w.y));  // b e^{-2 pi i k/64}
+      x[k] = sb ? make_float2(a.x - wb.x, a.y - wb.y) : make_float2(a.x + wb.x, a.y + wb.y);
+    }
+  }
+  __syncthreads();  // pass-B reads of S done
+#pragma unroll
+  for (int k = 0; k < 32; k++) S[colr::physq(P * k1b + 32 * sb + k)] = x[k];
+
+  cg::cluster_group cluster = cg::this_cluster();
+  if constexpr (CL > 1) cluster.sync();
+  else __syncthreads();
+  float2 *part[CL];
+#pragma unroll
+  for (int q = 0; q < CL; q++) part[q] = (q == rank) ? sm : cluster.map_shared_rank(sm, q);
+
+  // ---- F = -Phi u over this block's share of the positions ----
+  const bool mirror_self = (ky == 0) || (g.ny_even && ky == g.ny / 2);
+  const double wgt = mirror_self ? 1.0 : 2.0;
+  double e = 0.0;
+  for (int kb = kb0 + warp; kb < kb1; kb += nwarp) {
+    if (lane == 0 && kb + nwarp < kb1) prefetch_l2(phik + (size_t)(kb + nwarp) * (kPerPos * 32), kBlk);
+    const int q = (kb << 5) + lane;
+    const int pos = colr::physq(q);
+    const float *ph = phik + (size_t)kb * (kPerPos * 32) + lane * V;
+    float2 uq[D], F[D];
+#pragma unroll
+    for (int j = 0; j < D; j++) {
+      uq[j] = part[j / DL][(j % DL) * n + pos];
+      F[j] = make_float2(0.0f, 0.0f);
+    }
+    colcl::PhiApply<D, V>::run(ph, uq, F);
+    float es = 0.0f;
+#pragma unroll
+    for (int i = 0; i < D; i++) es = fmaf(F[i].x, uq[i].x, fmaf(F[i].y, uq[i].y, es));
+    e += wgt * (double)es;
+    if (ky == 0 && q == 0) {  // kx = 0 sits at position 0
+#pragma unroll
+      for (int j = 0; j < D; j++) scal[1 + j] = (double)uq[j].x;
+#pragma unroll
+      for (int l = 0; l < D / 3; l++) {
+        e -= 2.0 * linf[l] * (double)uq[3 * l + 2].x;
+        F[3 * l + 2].x -= (float)linf[l];
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < D; i++) part[i / DL][(i % DL) * n + pos] = make_float2(-F[i].x, -F[i].y);
+  }
+  if constexpr (CL > 1) cluster.sync();
+  else __syncthreads();
+
+  // ---- backward pass B ----
+#pragma unroll
+  for (int k = 0; k < 32; k++) x[k] = S[colr::physq(P * k1b + 32 * sb + k)];
+  if constexpr (P == 64) {
+#pragma unroll
+    for (int k = 0; k < 32; k++) {
+      const float2 own = x[k];
+      const float2 oth = make_float2(__shfl_xor_sync(0xffffffffu, own.x, 1), __shfl_xor_sync(0xffffffffu, own.y, 1));
+      if (sb == 0) {
+        x[k] = make_float2(own.x + oth.x, own.y + oth.y);  // X_0 + X_1
+      } else {
+        const float2 d = make_float2(oth.x - own.x, oth.y - own.y);  // X_0 - X_1
+        const float2 w = colr::w64(k);
+        x[k] = make_float2(fmaf(d.x, w.x, -d.y * w.y), fmaf(d.y, w.x, d.x * w.y));  // d e^{+2 pi i k/64}
+      }
+    }
+  }
+  rows32::dft32<+1>(x);
+  __syncthreads();  // reads of the spectrum done
+#pragma unroll
+  for (int tp = 0; tp < 32; tp++) {
+    const int tt = P == 64 ? 2 * tp + sb : tp;
+    S[k1b * P + (tt ^ colr::swa<P>(k1b))] = x[tp];
+  }
+  __syncthreads();
+  // ---- backward pass A ----
+#pragma unroll
+  for (int k1 = 0; k1 < 32; k1++) x[k1] = S[k1 * P + (t ^ colr::swa<P>(k1))];
+#pragma unroll
+  for (int k1 = 1; k1 < 32; k1++) x[k1] = rows32::twc<+1>(x[k1], __ldg(&twa[k1 * P + t]));
+  rows32::dft32<+1>(x);
+#pragma unroll
+  for (int m = 0; m < 32; m++) __stcs(colg + t + P * m, x[m]);
+
+  // energy: block partial, then the last block sums all partials in order
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
+  if (lane == 0) red[warp] = e;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sacc = 0.0;
+    for (int w = 0; w < nwarp; w++) sacc += red[w];
+    epart[blockIdx.x] = sacc;
+    __threadfence();
+    unsigned prev = atomicAdd(counter, 1u);
+    is_last = (prev == gridDim.x - 1) ? 1 : 0;
+  }
+  __syncthreads();
+  if (is_last) {
+    __threadfence();
+    double sacc = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += NT) sacc += ((volatile double *)epart)[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sacc += __shfl_down_sync(0xffffffffu, sacc, o);
+    __syncthreads();
+    if (lane == 0) red[warp] = sacc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double tsum = 0.0;
+      for (int w = 0; w < nwarp; w++) tsum += red[w];
+      *d_epot = 0.5 * tsum;
       *counter = 0u;
     }
   }

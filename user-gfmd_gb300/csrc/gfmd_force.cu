@@ -94,8 +94,44 @@ cudaError_t launch_col_cl(gfmd_solver *h, float2 *W, double *d_epot) {
                             (const double *)h->d_linf, h->d_epart, h->d_scal, h->d_counter, d_epot);
 }
 
+// Register-transform column kernel (nx = 2^LGN in {1024, 2048}).
+template <int D, int CL, int LGN>
+cudaError_t launch_col_r32(gfmd_solver *h, float2 *W, double *d_epot) {
+  constexpr int NT = (D / CL) * (1 << LGN) / 32;
+  constexpr int MINB = NT <= 192 ? 3 : 2;
+  auto kf = k_col_phi_r32<D, CL, LGN, MINB>;
+  const size_t sm = (size_t)(D / CL) * (1 << LGN) * sizeof(float2);
+  cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(h->g.nyc * CL);
+  cfg.blockDim = dim3(NT);
+  cfg.dynamicSmemBytes = sm;
+  cfg.stream = h->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = CL;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kf, W, reinterpret_cast<const float *>(h->d_phi), h->g,
+                            reinterpret_cast<const float4 *>(h->d_twc), (const double *)h->d_linf, h->d_epart,
+                            h->d_scal, h->d_counter, d_epot);
+}
+
 cudaError_t enqueue_col_cl(gfmd_solver *h, float2 *W, double *d_epot) {
   const int D = h->g.ndof, CL = h->col_cl;
+  if (h->col_r32) {
+    const bool n2k = h->g.nx == 2048;
+    if (D == 12 && CL == 3 && n2k) return launch_col_r32<12, 3, 11>(h, W, d_epot);
+    if (D == 12 && CL == 2 && !n2k) return launch_col_r32<12, 2, 10>(h, W, d_epot);
+    if (D == 6 && CL == 2 && n2k) return launch_col_r32<6, 2, 11>(h, W, d_epot);
+    if (D == 6 && CL == 1 && !n2k) return launch_col_r32<6, 1, 10>(h, W, d_epot);
+    if (D == 3 && CL == 1 && n2k) return launch_col_r32<3, 1, 11>(h, W, d_epot);
+    if (D == 3 && CL == 1 && !n2k) return launch_col_r32<3, 1, 10>(h, W, d_epot);
+    return cudaErrorInvalidValue;
+  }
   if (D == 3 && CL == 1) return launch_col_cl<3, 1, 1>(h, W, d_epot);
   if (D == 6 && CL == 1) return launch_col_cl<6, 1, 4>(h, W, d_epot);
   if (D == 6 && CL == 2) return launch_col_cl<6, 2, 4>(h, W, d_epot);
@@ -206,6 +242,7 @@ cudaError_t enqueue_t(gfmd_solver *h, const void *d_u, int in_t, void *d_f, int 
   const size_t smax = h->smem_optin;
 
   // row_fwd
+  mark(h, 0);
   {
     int rb = rows_per_block(g, sizeof(C<T>), smax);
     size_t sm = 2 * (size_t)rb * (g.nrow + 1) * sizeof(C<T>);
@@ -221,12 +258,14 @@ cudaError_t enqueue_t(gfmd_solver *h, const void *d_u, int in_t, void *d_f, int 
     }
   }
   // col_fft forward
+  mark(h, 1);
   int cb = cols_per_block(g, sizeof(C<T>), smax);
   size_t smc = 2 * (size_t)cb * g.nx * sizeof(C<T>);
   dim3 gridc((g.nyc * g.ndof + cb - 1) / cb);
   cudaFuncSetAttribute(k_col_fft<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smc);
   k_col_fft<T><<<gridc, kThreads, smc, h->stream>>>(W, g, h->plan_col, tw, cb, -1);
   // phi
+  mark(h, 2);
   dim3 gridp((g.nx + kPhiThreads - 1) / kPhiThreads, g.nyc);
   switch (g.ndof) {
     case 3: launch_phi<T, 3>(h, gridp, d_epot); break;
@@ -239,10 +278,13 @@ cudaError_t enqueue_t(gfmd_solver *h, const void *d_u, int in_t, void *d_f, int 
     case 24: launch_phi<T, 24>(h, gridp, d_epot); break;
     default: return cudaErrorInvalidValue;
   }
+  mark(h, 3);
   k_reduce<<<1, 256, 0, h->stream>>>(h->d_epart, (int)(gridp.x * gridp.y), d_epot);
   // col_fft backward
+  mark(h, 4);
   k_col_fft<T><<<gridc, kThreads, smc, h->stream>>>(W, g, h->plan_col, tw, cb, +1);
   // row_inv
+  mark(h, 5);
   {
     int rb = rows_per_block(g, sizeof(C<T>), smax);
     size_t sm = 2 * (size_t)rb * (g.nrow + 1) * sizeof(C<T>);
@@ -257,6 +299,7 @@ cudaError_t enqueue_t(gfmd_solver *h, const void *d_u, int in_t, void *d_f, int 
       kf<<<grid, kThreads, sm, h->stream>>>(W, reinterpret_cast<float *>(d_f), g, h->plan_row, tw, rb);
     }
   }
+  mark(h, 6);
   return cudaGetLastError();
 }
 
