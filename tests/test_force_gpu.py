@@ -139,7 +139,7 @@ def test_errors_are_status_codes_on_gpu():
         ("ft sc100 1 1.0 pair-potential 2 1.0 1.0 height 128", 2048, 64),
         ("ft fcc100 1.0 2 pair-potential 1 1.0 height 64", 2048, 128),
         ("ft fcc100 1.0 4 pair-potential 1 1.0 height 64", 1024, 32),
-        ("ft sc100 1 1.0 pair-potential 2 1.0 1.0 height 128", 1024, 16),
+        ("ft sc100 1 1.0 pair-potential 2 1.0 1.0 height 128", 1024, 32),
     ],
 )
 def test_fused_path_matches_oracle_and_plain_path(args, nx, ny, monkeypatch):
