@@ -203,7 +203,7 @@ def test_autotuned_plan_is_valid_and_changes_no_result(monkeypatch):
         monkeypatch.setenv("GFMD_AUTOTUNE", tune)
         s = _solver(nx, ny, d, "f32", half, "half", linf)
         info = s.info()
-        assert info["fused"] and info["rows_per_block"] >= 1 and 0 <= info["phi_prefetch"] <= 2
+        assert info["fused"] and info["rows_per_block"] >= 1 and 0 <= info["phi_prefetch"] <= 3
         f = np.zeros_like(u)
         e = s.post_force(u, f)
         outs.append((f, e))

@@ -472,33 +472,42 @@ int gfmd_memory_usage(gfmd_handle_t h, double *bytes) {
 // i < j in row-major order.  With Phi_eff the half-spectrum real transforms
 // reproduce the real part of the reference's full complex transforms.
 // ---- plan autotuner -----------------------------------------------------
-// The fused path's launch plan has a free parameter that changes no
-// arithmetic: the rows per block of the row kernels (1/4 to 1 of the
-// largest that fits the shared-memory budget).  With the table uploaded, each candidate is timed
-// (CUDA events, best of 3 after a warm-up) on scratch inputs and the fastest
-// is kept; results are cached per (nx, ny, ndof, precision) for the
-// process.  GFMD_AUTOTUNE=0 keeps the rule-based defaults.
+// The fused path's launch plan has free parameters that change no
+// arithmetic: the rows per block of the shared-memory row kernels (1/4 to 1
+// of the largest that fits the shared-memory budget) and, for the
+// register-transform column kernel, the rounds of its Phi stream prefetched
+// into L2 ahead of use (1-3) and the resident blocks per SM it is compiled
+// for (2 or 3, for the 12-column kernel at nx = 2048).  With the table
+// uploaded, each candidate is timed (CUDA events, best of 3 after a warm-up)
+// on scratch inputs and the fastest is kept; results are cached per grid,
+// precision and kernel selection for the process.  GFMD_AUTOTUNE=0 keeps the
+// rule-based defaults.
 namespace {
 struct PlanKey {
-  int nx, ny, ndof, prec;
+  int nx, ny, ndof, prec, kernels;
   bool operator<(const PlanKey &o) const {
-    return std::tie(nx, ny, ndof, prec) < std::tie(o.nx, o.ny, o.ndof, o.prec);
+    return std::tie(nx, ny, ndof, prec, kernels) < std::tie(o.nx, o.ny, o.ndof, o.prec, o.kernels);
   }
 };
+struct Plan {
+  int rb, col_pf, col_minb;
+};
 std::mutex g_plan_mu;
-std::map<PlanKey, std::pair<int, int>> g_plans;
+std::map<PlanKey, Plan> g_plans;
 
 cudaError_t autotune(gfmd_solver *h) {
   if (!h->fast || h->tuned) return cudaSuccess;
   const char *env = getenv("GFMD_AUTOTUNE");
   if (env && env[0] == '0') return cudaSuccess;
-  const PlanKey key{h->g.nx, h->g.ny, h->g.ndof, h->precision};
+  const PlanKey key{h->g.nx, h->g.ny, h->g.ndof, h->precision,
+                    (h->rows32 ? 1 : 0) | (h->col_r32 ? 2 : 0) | (h->col_cl << 2)};
   {
     std::lock_guard<std::mutex> lk(g_plan_mu);
     auto it = g_plans.find(key);
     if (it != g_plans.end()) {
-      h->fast_rb = it->second.first;
-      h->fast_pf = it->second.second;
+      h->fast_rb = it->second.rb;
+      h->col_pf = it->second.col_pf;
+      h->col_minb = it->second.col_minb;
       h->tuned = true;
       return cudaSuccess;
     }
@@ -520,36 +529,51 @@ cudaError_t autotune(gfmd_solver *h) {
   const char *tr = getenv("GFMD_TRACE");
   const bool trace = tr && tr[0] && tr[0] != '0';
   cudaStream_t keep = h->stream;
-  const int rb0 = h->fast_rb, pf0 = h->fast_pf;
-  int best_rb = rb0, best_pf = pf0;
+  const Plan p0{h->fast_rb, h->col_pf, h->col_minb};
+  std::vector<Plan> cand;
+  std::vector<int> rbs, pfs{h->col_pf}, minbs{h->col_minb};
+  if (h->rows32 && h->precision == GFMD_PREC_F32) rbs.push_back(h->fast_rb);  // not used by those kernels
+  else
+    for (int rb = h->fast_rb_max; rb >= 1 && rb * 4 >= h->fast_rb_max; rb /= 2) rbs.push_back(rb);
+  if (h->col_r32) {
+    pfs = {1, 2, 3};
+    if (h->g.ndof == 12 && h->g.nx == 2048) minbs = {2, 3};
+  }
+  for (int rb : rbs)
+    for (int pf : pfs)
+      for (int mb : minbs) cand.push_back({rb, pf, mb});
+  Plan best_p = p0;
   float best = 1e30f;
   h->stream = st;
-  for (int rb = h->fast_rb_max; rb >= 1 && rb * 4 >= h->fast_rb_max && e == cudaSuccess; rb /= 2)
-    for (int pf = 1; pf <= 1 && e == cudaSuccess; pf++) {
-      h->fast_rb = rb;
-      e = gfmd::enqueue_force(h, u, t, f, t, ep);  // warm-up
-      float ms = 1e30f;
-      for (int r = 0; r < 3 && e == cudaSuccess; r++) {
-        e = cudaEventRecord(e0, st);
-        if (e == cudaSuccess) e = gfmd::enqueue_force(h, u, t, f, t, ep);
-        if (e == cudaSuccess) e = cudaEventRecord(e1, st);
-        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-        float x = 0.0f;
-        if (e == cudaSuccess) e = cudaEventElapsedTime(&x, e0, e1);
-        ms = std::min(ms, x);
-      }
-      if (trace)
-        fprintf(stderr, "gfmd autotune %dx%d ndof %d: rows/block %d, Phi prefetch %d: %.4f ms\n", h->g.nx,
-                h->g.ny, h->g.ndof, rb, pf, ms);
-      if (e == cudaSuccess && ms < best) {
-        best = ms;
-        best_rb = rb;
-        best_pf = pf;
-      }
+  for (const Plan &c : cand) {
+    if (e != cudaSuccess) break;
+    h->fast_rb = c.rb;
+    h->col_pf = c.col_pf;
+    h->col_minb = c.col_minb;
+    e = gfmd::enqueue_force(h, u, t, f, t, ep);  // warm-up
+    float ms = 1e30f;
+    for (int r = 0; r < 3 && e == cudaSuccess; r++) {
+      e = cudaEventRecord(e0, st);
+      if (e == cudaSuccess) e = gfmd::enqueue_force(h, u, t, f, t, ep);
+      if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      float x = 0.0f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&x, e0, e1);
+      ms = std::min(ms, x);
     }
+    if (trace)
+      fprintf(stderr, "gfmd autotune %dx%d ndof %d: rows/block %d, column Phi prefetch %d, blocks/SM %d: %.4f ms\n",
+              h->g.nx, h->g.ny, h->g.ndof, c.rb, c.col_pf, c.col_minb, ms);
+    if (e == cudaSuccess && ms < best) {
+      best = ms;
+      best_p = c;
+    }
+  }
   h->stream = keep;
-  h->fast_rb = e == cudaSuccess ? best_rb : rb0;
-  h->fast_pf = e == cudaSuccess ? best_pf : pf0;
+  const Plan &use = e == cudaSuccess ? best_p : p0;
+  h->fast_rb = use.rb;
+  h->col_pf = use.col_pf;
+  h->col_minb = use.col_minb;
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
   if (st) cudaStreamDestroy(st);
@@ -558,7 +582,7 @@ cudaError_t autotune(gfmd_solver *h) {
   if (e != cudaSuccess) return e;
   h->tuned = true;
   std::lock_guard<std::mutex> lk(g_plan_mu);
-  g_plans[key] = {h->fast_rb, h->fast_pf};
+  g_plans[key] = use;
   return cudaSuccess;
 }
 }  // namespace
@@ -644,7 +668,7 @@ int gfmd_set_phi(gfmd_handle_t h, const double *phi, int layout, const double *l
 int gfmd_plan_info(gfmd_handle_t h, int *rows_per_block, int *phi_prefetch) {
   if (!h) return fail(GFMD_EINVAL, "gfmd_plan_info: NULL handle");
   if (rows_per_block) *rows_per_block = h->fast ? h->fast_rb : 0;
-  if (phi_prefetch) *phi_prefetch = h->fast ? h->fast_pf : 0;
+  if (phi_prefetch) *phi_prefetch = h->fast ? (h->col_r32 ? h->col_pf : h->fast_pf) : 0;
   return GFMD_OK;
 }
 

@@ -357,7 +357,7 @@ template <int D, int CL, int LGN, int MINB>
 __global__ void __launch_bounds__((D / CL) * (1 << LGN) / 32, MINB)
     k_col_phi_r32(float2 *__restrict__ W, const float *__restrict__ phi, Geom g, const float4 *__restrict__ twa,
                   const double *__restrict__ linf, double *__restrict__ epart, double *__restrict__ scal,
-                  unsigned *__restrict__ counter, double *__restrict__ d_epot) {
+                  unsigned *__restrict__ counter, double *__restrict__ d_epot, int pf) {
   namespace cg = cooperative_groups;
   constexpr int n = 1 << LGN, P = n / 32, DL = D / CL, NT = DL * P;
   constexpr int V = (D * D) % 4 == 0 ? 4 : 1;
@@ -379,7 +379,12 @@ __global__ void __launch_bounds__((D / CL) * (1 << LGN) / 32, MINB)
   // pass-B roles: k1 and the parity s of t (P = 64)
   const int k1b = P == 64 ? (t >> 1) : t, sb = P == 64 ? (t & 1) : 0;
 
-  if (lane == 0 && kb0 + warp < kb1) prefetch_l2(phik + (size_t)(kb0 + warp) * (kPerPos * 32), kBlk);
+  // the first pf rounds of this block's Phi stream go to L2 during the
+  // forward transform (pf is tuned per grid: deeper rounds of all resident
+  // blocks compete for L2)
+  if (lane == 0)
+    for (int r = 0; r < pf; r++)
+      if (kb0 + warp + r * nwarp < kb1) prefetch_l2(phik + (size_t)(kb0 + warp + r * nwarp) * (kPerPos * 32), kBlk);
   float2 x[32];
   // ---- forward pass A ----
 #pragma unroll
@@ -424,7 +429,7 @@ __global__ void __launch_bounds__((D / CL) * (1 << LGN) / 32, MINB)
   const double wgt = mirror_self ? 1.0 : 2.0;
   double e = 0.0;
   for (int kb = kb0 + warp; kb < kb1; kb += nwarp) {
-    if (lane == 0 && kb + nwarp < kb1) prefetch_l2(phik + (size_t)(kb + nwarp) * (kPerPos * 32), kBlk);
+    if (lane == 0 && kb + pf * nwarp < kb1) prefetch_l2(phik + (size_t)(kb + pf * nwarp) * (kPerPos * 32), kBlk);
     const int q = (kb << 5) + lane;
     const int pos = colr::physq(q);
     const float *ph = phik + (size_t)kb * (kPerPos * 32) + lane * V;

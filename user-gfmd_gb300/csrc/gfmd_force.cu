@@ -95,13 +95,14 @@ cudaError_t launch_col_cl(gfmd_solver *h, float2 *W, double *d_epot) {
 }
 
 // Register-transform column kernel (nx = 2^LGN in {1024, 2048}).
-template <int D, int CL, int LGN>
+template <int D, int CL, int LGN, int MINB>
 cudaError_t launch_col_r32(gfmd_solver *h, float2 *W, double *d_epot) {
   constexpr int NT = (D / CL) * (1 << LGN) / 32;
-  constexpr int MINB = NT <= 192 ? 3 : 2;
   auto kf = k_col_phi_r32<D, CL, LGN, MINB>;
   const size_t sm = (size_t)(D / CL) * (1 << LGN) * sizeof(float2);
   cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(kf, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(h->g.nyc * CL);
@@ -117,19 +118,21 @@ cudaError_t launch_col_r32(gfmd_solver *h, float2 *W, double *d_epot) {
   cfg.numAttrs = 1;
   return cudaLaunchKernelEx(&cfg, kf, W, reinterpret_cast<const float *>(h->d_phi), h->g,
                             reinterpret_cast<const float4 *>(h->d_twc), (const double *)h->d_linf, h->d_epart,
-                            h->d_scal, h->d_counter, d_epot);
+                            h->d_scal, h->d_counter, d_epot, h->col_pf);
 }
 
 cudaError_t enqueue_col_cl(gfmd_solver *h, float2 *W, double *d_epot) {
   const int D = h->g.ndof, CL = h->col_cl;
   if (h->col_r32) {
     const bool n2k = h->g.nx == 2048;
-    if (D == 12 && CL == 3 && n2k) return launch_col_r32<12, 3, 11>(h, W, d_epot);
-    if (D == 12 && CL == 2 && !n2k) return launch_col_r32<12, 2, 10>(h, W, d_epot);
-    if (D == 6 && CL == 2 && n2k) return launch_col_r32<6, 2, 11>(h, W, d_epot);
-    if (D == 6 && CL == 1 && !n2k) return launch_col_r32<6, 1, 10>(h, W, d_epot);
-    if (D == 3 && CL == 1 && n2k) return launch_col_r32<3, 1, 11>(h, W, d_epot);
-    if (D == 3 && CL == 1 && !n2k) return launch_col_r32<3, 1, 10>(h, W, d_epot);
+    const bool m3 = h->col_minb == 3;
+    if (D == 12 && CL == 3 && n2k)
+      return m3 ? launch_col_r32<12, 3, 11, 3>(h, W, d_epot) : launch_col_r32<12, 3, 11, 2>(h, W, d_epot);
+    if (D == 12 && CL == 2 && !n2k) return launch_col_r32<12, 2, 10, 3>(h, W, d_epot);
+    if (D == 6 && CL == 2 && n2k) return launch_col_r32<6, 2, 11, 3>(h, W, d_epot);
+    if (D == 6 && CL == 1 && !n2k) return launch_col_r32<6, 1, 10, 3>(h, W, d_epot);
+    if (D == 3 && CL == 1 && n2k) return launch_col_r32<3, 1, 11, 3>(h, W, d_epot);
+    if (D == 3 && CL == 1 && !n2k) return launch_col_r32<3, 1, 10, 3>(h, W, d_epot);
     return cudaErrorInvalidValue;
   }
   if (D == 3 && CL == 1) return launch_col_cl<3, 1, 1>(h, W, d_epot);
@@ -141,13 +144,20 @@ cudaError_t enqueue_col_cl(gfmd_solver *h, float2 *W, double *d_epot) {
   return cudaErrorInvalidValue;
 }
 
+// Persistent blocks of the warp-per-row kernels: two per SM, at most one
+// per row set.
+inline int row_blocks(const gfmd_solver *h) {
+  const int nsets = h->g.nx / rows32::kRB * h->g.ndof;
+  return std::max(1, std::min(nsets, 2 * std::max(1, h->sm_count)));
+}
+
 // Warp-per-row row kernels with TMA tiles (FP32 handles, ny = 2048).
 template <typename Tin> cudaError_t launch_row_fwd32(gfmd_solver *h, const void *d_u) {
   auto kf = k_row_fwd_w32<Tin>;
   cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows32::kSmemBytes);
   if (e != cudaSuccess) return e;
   const float4 *tw = reinterpret_cast<const float4 *>(h->d_tw32);
-  kf<<<dim3(h->g.nx / rows32::kRB, h->g.ndof), rows32::kThreads, rows32::kSmemBytes, h->stream>>>(
+  kf<<<row_blocks(h), rows32::kThreads, rows32::kSmemBytes, h->stream>>>(
       reinterpret_cast<const Tin *>(d_u), reinterpret_cast<float2 *>(h->d_W), h->tm_w, h->g, tw, tw + 1024);
   return cudaSuccess;
 }
@@ -156,7 +166,7 @@ template <typename Tout> cudaError_t launch_row_inv32(gfmd_solver *h, void *d_f)
   cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows32::kSmemBytes);
   if (e != cudaSuccess) return e;
   const float4 *tw = reinterpret_cast<const float4 *>(h->d_tw32);
-  kf<<<dim3(h->g.nx / rows32::kRB, h->g.ndof), rows32::kThreads, rows32::kSmemBytes, h->stream>>>(
+  kf<<<row_blocks(h), rows32::kThreads, rows32::kSmemBytes, h->stream>>>(
       reinterpret_cast<const float2 *>(h->d_W), h->tm_w, reinterpret_cast<Tout *>(d_f), h->g, tw, tw + 1024,
       h->d_err);
   return cudaSuccess;

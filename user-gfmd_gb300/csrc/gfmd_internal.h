@@ -101,6 +101,8 @@ struct gfmd_solver {
   bool col_r32 = false;      // register-transform column kernel (nx = 1024, 2048): positions
                              // q = (nx/32) (kx mod 32) + kx/32; else digit-reversed kx
   void *d_twc = nullptr;     // float4 [k1][t] w_nx^(t k1) of that kernel
+  int col_pf = 1;            // Phi rounds prefetched into L2 ahead (tuned)
+  int col_minb = 2;          // resident blocks per SM the kernel is compiled for (tuned: 2 or 3)
   void *d_tw32 = nullptr;    // float4: [k1][l] w_1024^(l k1), then e^{-2 pi i k/2048}, k = 0..1024
   CUtensorMap tm_w;          // W as floats {2 nxp, ndof, nyc}, box {16, 1, 128}
   int *d_err = nullptr;      // device error word: GFMD_ETIMEDOUT from a bounded wait

@@ -133,6 +133,12 @@ __device__ __forceinline__ float2 inv_split_one(float2 xk, float2 xm, float4 pk)
   return make_float2(A.x - wB.y, A.y + wB.x);
 }
 
+// Blocks are persistent: block b takes the row sets s = b, b + gridDim.x, ...
+// (set s: dof = s / (nx/8), rows ix0 = 8 (s mod nx/8) .. ix0 + 7).  The
+// global loads (forward) or TMA tile loads (inverse) of the next set are
+// issued before the current set's split or transform, so they are in flight
+// while the block computes.
+
 // Forward: u[dof][x][2n] (Tin) -> W[ky][dof][x] complex FP32, ky = 0..n.
 // tmW: 3-D tensor map of W as floats {2 nxp, ndof, nyc}, box {16, 1, kChunk}.
 // tw: [k1][l] compensated w_n^(l k1); post: e^{-2 pi i k / (2n)}, k = 0..n.
@@ -145,13 +151,14 @@ __global__ void __launch_bounds__(rows32::kThreads, 2)
   float2 *xs = reinterpret_cast<float2 *>(smem_rows + 128);
   float2 *stage = reinterpret_cast<float2 *>(smem_rows + 128 + kRowBytes);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int dof = blockIdx.y, ix0 = blockIdx.x * kRB;
+  const int nxb = g.nx / kRB, nsets = nxb * g.ndof;
   if (threadIdx.x == 0) prefetch_tmap(&tmW);
+  const int r = threadIdx.x & (kRB - 1), j0 = threadIdx.x >> 3;
 
-  // ---- row transform (one warp per row) ----
-  {
+  float2 x[32];
+  auto load_rows = [&](int set) {  // this warp's row of the set, into x
+    const int dof = set / nxb, ix0 = (set % nxb) * kRB;
     const Tin *src = u + ((size_t)dof * g.nx + ix0 + warp) * (size_t)(2 * kN);
-    float2 x[32];
 #pragma unroll
     for (int m = 0; m < 32; m++) {
       if constexpr (sizeof(Tin) == 4) {
@@ -161,51 +168,61 @@ __global__ void __launch_bounds__(rows32::kThreads, 2)
         x[m] = make_float2((float)v.x, (float)v.y);
       }
     }
-    float2 *row = xs + warp * kPitch;
-    row_fft<-1>(x, tw, row, lane);
+  };
+  if ((int)blockIdx.x < nsets) load_rows(blockIdx.x);
+  int cc = 0;  // tiles pairs committed by this block so far (stage buffer parity)
+  for (int set = blockIdx.x; set < nsets; set += gridDim.x) {
+    const int dof = set / nxb, ix0 = (set % nxb) * kRB;
+    // ---- row transform (one warp per row) ----
+    {
+      float2 *row = xs + warp * kPitch;
+      row_fft<-1>(x, tw, row, lane);
 #pragma unroll
-    for (int k2 = 0; k2 < 32; k2++) row[lane + 32 * k2] = x[k2];
-  }
-  __syncthreads();
-
-  // ---- real-to-half-complex split in mirror pairs of tiles ----
-  // thread (r = t % 8, j = t / 8 + 32 i): row r, ky = a + j and n - a - j
-  const int r = threadIdx.x & (kRB - 1), j0 = threadIdx.x >> 3;
-  const float2 *row = xs + r * kPitch;
-  for (int c = 0; c < kNChunk; c++) {
-    float2 *lo = stage + (c & 1) * 2 * kTile, *hi = lo + kTile;
-    if (c >= 2) {
-      if (threadIdx.x == 0) bulk_wait_read<1>();  // the stores of chunk c - 2 have left this buffer
-      __syncthreads();
+      for (int k2 = 0; k2 < 32; k2++) row[lane + 32 * k2] = x[k2];
     }
-    const int a = c * kChunk, hbase = kN - a - kChunk + 1;  // hi tile: ky = hbase .. n - a
-#pragma unroll 4
-    for (int j = j0; j < kChunk; j += rows32::kThreads / kRB) {
-      const int k = a + j;
-      const float2 xk = row[k], xm = row[(kN - k) & (kN - 1)];
-      lo[j * kRB + r] = fwd_split_one(xk, xm, __ldg(&post[k]));
-      hi[(kChunk - 1 - j) * kRB + r] = fwd_split_one(xm, xk, __ldg(&post[kN - k]));
-    }
-    fence_proxy_async_smem();
     __syncthreads();
-    if (threadIdx.x == 0) {
-      tma_store_3d(&tmW, 2 * ix0, dof, a, lo);
-      tma_store_3d(&tmW, 2 * ix0, dof, hbase, hi);
-      bulk_commit();
+    if (set + (int)gridDim.x < nsets) load_rows(set + gridDim.x);  // in flight during the split
+
+    // ---- real-to-half-complex split in mirror pairs of tiles ----
+    // thread (r = t % 8, j = t / 8 + 32 i): row r, ky = a + j and n - a - j
+    const float2 *row = xs + r * kPitch;
+    for (int c = 0; c < kNChunk; c++, cc++) {
+      float2 *lo = stage + (cc & 1) * 2 * kTile, *hi = lo + kTile;
+      if (cc >= 2) {
+        if (threadIdx.x == 0) bulk_wait_read<1>();  // the stores of pair cc - 2 have left this buffer
+        __syncthreads();
+      }
+      const int a = c * kChunk, hbase = kN - a - kChunk + 1;  // hi tile: ky = hbase .. n - a
+#pragma unroll 4
+      for (int j = j0; j < kChunk; j += rows32::kThreads / kRB) {
+        const int k = a + j;
+        const float2 xk = row[k], xm = row[(kN - k) & (kN - 1)];
+        lo[j * kRB + r] = fwd_split_one(xk, xm, __ldg(&post[k]));
+        hi[(kChunk - 1 - j) * kRB + r] = fwd_split_one(xm, xk, __ldg(&post[kN - k]));
+      }
+      fence_proxy_async_smem();
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        tma_store_3d(&tmW, 2 * ix0, dof, a, lo);
+        tma_store_3d(&tmW, 2 * ix0, dof, hbase, hi);
+        bulk_commit();
+      }
     }
-  }
-  // ky = n/2 is its own mirror: plain stores
-  if (threadIdx.x < kRB) {
-    const float2 xk = xs[threadIdx.x * kPitch + kN / 2];
-    W[((size_t)(kN / 2) * g.ndof + dof) * g.nxp + ix0 + threadIdx.x] = fwd_split_one(xk, xk, __ldg(&post[kN / 2]));
+    // ky = n/2 is its own mirror: plain stores
+    if (threadIdx.x < kRB) {
+      const float2 xk = xs[threadIdx.x * kPitch + kN / 2];
+      W[((size_t)(kN / 2) * g.ndof + dof) * g.nxp + ix0 + threadIdx.x] = fwd_split_one(xk, xk, __ldg(&post[kN / 2]));
+    }
+    __syncthreads();  // the split's reads of the row buffer are done before the next transform
   }
   if (threadIdx.x == 0) bulk_wait<0>();
 }
 
 // ---------------------------------------------------------------------------
 // Inverse: W[ky][dof][x] complex FP32 -> f[dof][x][2n] (Tout).  The tiles
-// come in by TMA, two mirror pairs in flight; err receives GFMD_ETIMEDOUT
-// if a tile never arrives (the block then stops without writing f).
+// come in by TMA, two mirror pairs in flight (the first two of the next set
+// load during the current set's transform); err receives GFMD_ETIMEDOUT if a
+// tile never arrives (the block then stops).
 template <typename Tout>
 __global__ void __launch_bounds__(rows32::kThreads, 2)
     k_row_inv_w32(const float2 *__restrict__ W, const __grid_constant__ CUtensorMap tmW, Tout *__restrict__ f,
@@ -216,65 +233,75 @@ __global__ void __launch_bounds__(rows32::kThreads, 2)
   float2 *xs = reinterpret_cast<float2 *>(smem_rows + 128);
   float2 *stage = reinterpret_cast<float2 *>(smem_rows + 128 + kRowBytes);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int dof = blockIdx.y, ix0 = blockIdx.x * kRB;
-  auto issue = [&](int c) {  // thread 0: both tiles of mirror pair c
-    float2 *lo = stage + (c & 1) * 2 * kTile, *hi = lo + kTile;
-    mbar_arrive_tx(&bar[c & 1], 2 * kTile * 8);
-    tma_load_3d(lo, &tmW, 2 * ix0, dof, c * kChunk, &bar[c & 1]);
-    tma_load_3d(hi, &tmW, 2 * ix0, dof, kN - c * kChunk - kChunk + 1, &bar[c & 1]);
+  const int nxb = g.nx / kRB, nsets = nxb * g.ndof;
+  // pair p (global count) of this block: set blockIdx.x + (p / kNChunk) gridDim.x,
+  // chunk p % kNChunk, buffer p & 1, mbarrier phase (p >> 1) & 1
+  const int npairs = ((int)blockIdx.x < nsets ? (nsets - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0) * kNChunk;
+  auto issue = [&](int p) {  // thread 0: both tiles of pair p
+    const int set = blockIdx.x + (p / kNChunk) * gridDim.x, c = p % kNChunk;
+    const int dof = set / nxb, ix0 = (set % nxb) * kRB;
+    float2 *lo = stage + (p & 1) * 2 * kTile, *hi = lo + kTile;
+    mbar_arrive_tx(&bar[p & 1], 2 * kTile * 8);
+    tma_load_3d(lo, &tmW, 2 * ix0, dof, c * kChunk, &bar[p & 1]);
+    tma_load_3d(hi, &tmW, 2 * ix0, dof, kN - c * kChunk - kChunk + 1, &bar[p & 1]);
   };
   if (threadIdx.x == 0) {
     prefetch_tmap(&tmW);
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     fence_mbar_init();
-    issue(0);
-    issue(1);
-  }
-  // ky = n/2 (its own mirror) with plain loads
-  if (threadIdx.x < kRB) {
-    const float2 xk = W[((size_t)(kN / 2) * g.ndof + dof) * g.nxp + ix0 + threadIdx.x];
-    xs[threadIdx.x * kPitch + kN / 2] = inv_split_one(xk, xk, __ldg(&post[kN / 2]));
+    if (npairs > 0) issue(0);
+    if (npairs > 1) issue(1);
   }
   __syncthreads();  // barrier initialisation visible to all threads
   const int r = threadIdx.x & (kRB - 1), j0 = threadIdx.x >> 3;
   float2 *rowr = xs + r * kPitch;
-  for (int c = 0; c < kNChunk; c++) {
-    const float2 *lo = stage + (c & 1) * 2 * kTile, *hi = lo + kTile;
-    const bool ok = mbar_wait(&bar[c & 1], (c >> 1) & 1);
-    if (__syncthreads_or(!ok)) {
-      if (threadIdx.x == 0) report_timeout(err);
-      return;
+  int p = 0;
+  for (int set = blockIdx.x; set < nsets; set += gridDim.x) {
+    const int dof = set / nxb, ix0 = (set % nxb) * kRB;
+    // ky = n/2 (its own mirror) with plain loads
+    if (threadIdx.x < kRB) {
+      const float2 xk = W[((size_t)(kN / 2) * g.ndof + dof) * g.nxp + ix0 + threadIdx.x];
+      xs[threadIdx.x * kPitch + kN / 2] = inv_split_one(xk, xk, __ldg(&post[kN / 2]));
     }
-    const int a = c * kChunk;
-#pragma unroll 4
-    for (int j = j0; j < kChunk; j += rows32::kThreads / kRB) {
-      const int k = a + j;
-      const float2 xk = lo[j * kRB + r], xm = hi[(kChunk - 1 - j) * kRB + r];  // X[k], X[n-k]
-      if (k == 0) {
-        rowr[0] = make_float2(xk.x + xm.x, xk.x - xm.x);  // imaginary parts of X[0], X[n] dropped
-      } else {
-        rowr[k] = inv_split_one(xk, xm, __ldg(&post[k]));
-        rowr[kN - k] = inv_split_one(xm, xk, __ldg(&post[kN - k]));
+    for (int c = 0; c < kNChunk; c++, p++) {
+      const float2 *lo = stage + (p & 1) * 2 * kTile, *hi = lo + kTile;
+      const bool ok = mbar_wait(&bar[p & 1], (p >> 1) & 1);
+      if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) report_timeout(err);
+        return;
       }
+      const int a = c * kChunk;
+#pragma unroll 4
+      for (int j = j0; j < kChunk; j += rows32::kThreads / kRB) {
+        const int k = a + j;
+        const float2 xk = lo[j * kRB + r], xm = hi[(kChunk - 1 - j) * kRB + r];  // X[k], X[n-k]
+        if (k == 0) {
+          rowr[0] = make_float2(xk.x + xm.x, xk.x - xm.x);  // imaginary parts of X[0], X[n] dropped
+        } else {
+          rowr[k] = inv_split_one(xk, xm, __ldg(&post[k]));
+          rowr[kN - k] = inv_split_one(xm, xk, __ldg(&post[kN - k]));
+        }
+      }
+      __syncthreads();  // buffer p & 1 consumed
+      if (threadIdx.x == 0 && p + 2 < npairs) issue(p + 2);
     }
-    __syncthreads();  // buffer c & 1 consumed
-    if (threadIdx.x == 0 && c + 2 < kNChunk) issue(c + 2);
-  }
-  // ---- row transform (one warp per row) ----
-  float2 *row = xs + warp * kPitch;
-  float2 x[32];
+    // ---- row transform (one warp per row) ----
+    float2 *row = xs + warp * kPitch;
+    float2 x[32];
 #pragma unroll
-  for (int m = 0; m < 32; m++) x[m] = row[lane + 32 * m];
-  __syncwarp();
-  row_fft<+1>(x, tw, row, lane);
-  Tout *dst = f + ((size_t)dof * g.nx + ix0 + warp) * (size_t)(2 * kN);
+    for (int m = 0; m < 32; m++) x[m] = row[lane + 32 * m];
+    __syncwarp();
+    row_fft<+1>(x, tw, row, lane);
+    Tout *dst = f + ((size_t)dof * g.nx + ix0 + warp) * (size_t)(2 * kN);
 #pragma unroll
-  for (int k2 = 0; k2 < 32; k2++) {
-    if constexpr (sizeof(Tout) == 4)
-      __stcs(reinterpret_cast<float2 *>(dst) + lane + 32 * k2, x[k2]);
-    else
-      __stcs(reinterpret_cast<double2 *>(dst) + lane + 32 * k2, make_double2((double)x[k2].x, (double)x[k2].y));
+    for (int k2 = 0; k2 < 32; k2++) {
+      if constexpr (sizeof(Tout) == 4)
+        __stcs(reinterpret_cast<float2 *>(dst) + lane + 32 * k2, x[k2]);
+      else
+        __stcs(reinterpret_cast<double2 *>(dst) + lane + 32 * k2, make_double2((double)x[k2].x, (double)x[k2].y));
+    }
+    __syncthreads();  // row buffers free before the next set's pre-split
   }
 }
 
