@@ -213,7 +213,7 @@ cudaError_t setup_fp32_kernels(gfmd_solver *h) {
     h->col_cl = cl;
     h->phi_v = (g.ndof * g.ndof) % 4 == 0 ? 4 : 1;
   }
-  if (g.ny == 2048 && g.nx % 8 == 0 && encode_tiled() != nullptr) {
+  if (g.ny == 2048 && g.nx % 16 == 0 && encode_tiled() != nullptr) {
     std::vector<float> f;
     for (int k1 = 0; k1 < 32; k1++)
       for (int l = 0; l < 32; l++) push_c4(f, (long)l * k1, 1024);
@@ -223,10 +223,14 @@ cudaError_t setup_fp32_kernels(gfmd_solver *h) {
     if (e != cudaSuccess) return e;
     const cuuint64_t dims[3] = {(cuuint64_t)2 * g.nxp, (cuuint64_t)g.ndof, (cuuint64_t)g.nyc};
     const cuuint64_t strides[2] = {(cuuint64_t)2 * g.nxp * 4, (cuuint64_t)g.ndof * 2 * g.nxp * 4};
-    const cuuint32_t box[3] = {16, 1, 128}, estr[3] = {1, 1, 1};
-    CUresult r = encode_tiled()(&h->tm_w, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, h->d_W, dims, strides, box, estr,
-                                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+    const cuuint32_t box8[3] = {16, 1, 128}, box16[3] = {32, 1, 64}, estr[3] = {1, 1, 1};
+    CUresult r = encode_tiled()(&h->tm_w[0], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, h->d_W, dims, strides, box8,
+                                estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                                 CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r == CUDA_SUCCESS)
+      r = encode_tiled()(&h->tm_w[1], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, h->d_W, dims, strides, box16, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r == CUDA_SUCCESS) {
       h->rows32 = true;
       h->bytes += (double)f.size() * sizeof(float);
@@ -490,7 +494,7 @@ struct PlanKey {
   }
 };
 struct Plan {
-  int rb, col_pf, col_minb;
+  int rb, col_pf, col_minb, row_rb;
 };
 std::mutex g_plan_mu;
 std::map<PlanKey, Plan> g_plans;
@@ -508,6 +512,7 @@ cudaError_t autotune(gfmd_solver *h) {
       h->fast_rb = it->second.rb;
       h->col_pf = it->second.col_pf;
       h->col_minb = it->second.col_minb;
+      h->row_rb = it->second.row_rb;
       h->tuned = true;
       return cudaSuccess;
     }
@@ -529,9 +534,10 @@ cudaError_t autotune(gfmd_solver *h) {
   const char *tr = getenv("GFMD_TRACE");
   const bool trace = tr && tr[0] && tr[0] != '0';
   cudaStream_t keep = h->stream;
-  const Plan p0{h->fast_rb, h->col_pf, h->col_minb};
+  const Plan p0{h->fast_rb, h->col_pf, h->col_minb, h->row_rb};
   std::vector<Plan> cand;
-  std::vector<int> rbs, pfs{h->col_pf}, minbs{h->col_minb};
+  std::vector<int> rbs, pfs{h->col_pf}, minbs{h->col_minb}, rrbs{h->row_rb};
+  if (h->rows32) rrbs = {8, 16};
   if (h->rows32 && h->precision == GFMD_PREC_F32) rbs.push_back(h->fast_rb);  // not used by those kernels
   else
     for (int rb = h->fast_rb_max; rb >= 1 && rb * 4 >= h->fast_rb_max; rb /= 2) rbs.push_back(rb);
@@ -541,7 +547,8 @@ cudaError_t autotune(gfmd_solver *h) {
   }
   for (int rb : rbs)
     for (int pf : pfs)
-      for (int mb : minbs) cand.push_back({rb, pf, mb});
+      for (int mb : minbs)
+        for (int rr : rrbs) cand.push_back({rb, pf, mb, rr});
   Plan best_p = p0;
   float best = 1e30f;
   h->stream = st;
@@ -550,6 +557,7 @@ cudaError_t autotune(gfmd_solver *h) {
     h->fast_rb = c.rb;
     h->col_pf = c.col_pf;
     h->col_minb = c.col_minb;
+    h->row_rb = c.row_rb;
     e = gfmd::enqueue_force(h, u, t, f, t, ep);  // warm-up
     float ms = 1e30f;
     for (int r = 0; r < 3 && e == cudaSuccess; r++) {
@@ -562,8 +570,10 @@ cudaError_t autotune(gfmd_solver *h) {
       ms = std::min(ms, x);
     }
     if (trace)
-      fprintf(stderr, "gfmd autotune %dx%d ndof %d: rows/block %d, column Phi prefetch %d, blocks/SM %d: %.4f ms\n",
-              h->g.nx, h->g.ny, h->g.ndof, c.rb, c.col_pf, c.col_minb, ms);
+      fprintf(stderr,
+              "gfmd autotune %dx%d ndof %d: rows/block %d (warp rows %d), column Phi prefetch %d, blocks/SM %d: "
+              "%.4f ms\n",
+              h->g.nx, h->g.ny, h->g.ndof, c.rb, c.row_rb, c.col_pf, c.col_minb, ms);
     if (e == cudaSuccess && ms < best) {
       best = ms;
       best_p = c;
@@ -574,6 +584,7 @@ cudaError_t autotune(gfmd_solver *h) {
   h->fast_rb = use.rb;
   h->col_pf = use.col_pf;
   h->col_minb = use.col_minb;
+  h->row_rb = use.row_rb;
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
   if (st) cudaStreamDestroy(st);

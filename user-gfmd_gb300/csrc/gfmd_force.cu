@@ -101,8 +101,6 @@ cudaError_t launch_col_r32(gfmd_solver *h, float2 *W, double *d_epot) {
   auto kf = k_col_phi_r32<D, CL, LGN, MINB>;
   const size_t sm = (size_t)(D / CL) * (1 << LGN) * sizeof(float2);
   cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(kf, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(h->g.nyc * CL);
@@ -144,32 +142,41 @@ cudaError_t enqueue_col_cl(gfmd_solver *h, float2 *W, double *d_epot) {
   return cudaErrorInvalidValue;
 }
 
-// Persistent blocks of the warp-per-row kernels: two per SM, at most one
-// per row set.
-inline int row_blocks(const gfmd_solver *h) {
-  const int nsets = h->g.nx / rows32::kRB * h->g.ndof;
-  return std::max(1, std::min(nsets, 2 * std::max(1, h->sm_count)));
+// Persistent blocks of the warp-per-row kernels: as many as fit on the GPU
+// (2 per SM with 8-row blocks, 1 with 16-row blocks), at most one per row set.
+inline int row_blocks(const gfmd_solver *h, int rb) {
+  const int nsets = h->g.nx / rb * h->g.ndof;
+  return std::max(1, std::min(nsets, (rb == 8 ? 2 : 1) * std::max(1, h->sm_count)));
 }
 
 // Warp-per-row row kernels with TMA tiles (FP32 handles, ny = 2048).
-template <typename Tin> cudaError_t launch_row_fwd32(gfmd_solver *h, const void *d_u) {
-  auto kf = k_row_fwd_w32<Tin>;
-  cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows32::kSmemBytes);
+template <typename Tin, int RB> cudaError_t launch_row_fwd32(gfmd_solver *h, const void *d_u) {
+  using K = rows32::Cfg<RB>;
+  auto kf = k_row_fwd_w32<Tin, RB>;
+  cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K::kSmemBytes);
   if (e != cudaSuccess) return e;
   const float4 *tw = reinterpret_cast<const float4 *>(h->d_tw32);
-  kf<<<row_blocks(h), rows32::kThreads, rows32::kSmemBytes, h->stream>>>(
-      reinterpret_cast<const Tin *>(d_u), reinterpret_cast<float2 *>(h->d_W), h->tm_w, h->g, tw, tw + 1024);
+  kf<<<row_blocks(h, RB), K::kThreads, K::kSmemBytes, h->stream>>>(
+      reinterpret_cast<const Tin *>(d_u), reinterpret_cast<float2 *>(h->d_W), h->tm_w[RB == 8 ? 0 : 1], h->g, tw,
+      tw + 1024);
   return cudaSuccess;
 }
-template <typename Tout> cudaError_t launch_row_inv32(gfmd_solver *h, void *d_f) {
-  auto kf = k_row_inv_w32<Tout>;
-  cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows32::kSmemBytes);
+template <typename Tout, int RB> cudaError_t launch_row_inv32(gfmd_solver *h, void *d_f) {
+  using K = rows32::Cfg<RB>;
+  auto kf = k_row_inv_w32<Tout, RB>;
+  cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K::kSmemBytes);
   if (e != cudaSuccess) return e;
   const float4 *tw = reinterpret_cast<const float4 *>(h->d_tw32);
-  kf<<<row_blocks(h), rows32::kThreads, rows32::kSmemBytes, h->stream>>>(
-      reinterpret_cast<const float2 *>(h->d_W), h->tm_w, reinterpret_cast<Tout *>(d_f), h->g, tw, tw + 1024,
-      h->d_err);
+  kf<<<row_blocks(h, RB), K::kThreads, K::kSmemBytes, h->stream>>>(
+      reinterpret_cast<const float2 *>(h->d_W), h->tm_w[RB == 8 ? 0 : 1], reinterpret_cast<Tout *>(d_f), h->g, tw,
+      tw + 1024, h->d_err);
   return cudaSuccess;
+}
+template <int RB> cudaError_t row_fwd32(gfmd_solver *h, const void *d_u, int in_t) {
+  return in_t == 0 ? launch_row_fwd32<double, RB>(h, d_u) : launch_row_fwd32<float, RB>(h, d_u);
+}
+template <int RB> cudaError_t row_inv32(gfmd_solver *h, void *d_f, int out_t) {
+  return out_t == 0 ? launch_row_inv32<double, RB>(h, d_f) : launch_row_inv32<float, RB>(h, d_f);
 }
 
 // Fused power-of-two path: three launches.  FP32 handles use the
@@ -191,7 +198,7 @@ cudaError_t enqueue_fast(gfmd_solver *h, const void *d_u, int in_t, void *d_f, i
 
   mark(h, 0);
   if (f32 && h->rows32) {
-    e = in_t == 0 ? launch_row_fwd32<double>(h, d_u) : launch_row_fwd32<float>(h, d_u);
+    e = h->row_rb == 16 ? row_fwd32<16>(h, d_u, in_t) : row_fwd32<8>(h, d_u, in_t);
   } else if (in_t == 0) {
     auto kf = k_row_fwd_fast<T, double>;
     cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr);
@@ -224,7 +231,7 @@ cudaError_t enqueue_fast(gfmd_solver *h, const void *d_u, int in_t, void *d_f, i
 
   mark(h, 2);
   if (f32 && h->rows32) {
-    e = out_t == 0 ? launch_row_inv32<double>(h, d_f) : launch_row_inv32<float>(h, d_f);
+    e = h->row_rb == 16 ? row_inv32<16>(h, d_f, out_t) : row_inv32<8>(h, d_f, out_t);
   } else if (out_t == 0) {
     auto kf = k_row_inv_fast<T, double>;
     cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr);

@@ -35,16 +35,23 @@ namespace gfmd {
 
 namespace rows32 {
 
-constexpr int kN = 1024;             // complex points per row
-constexpr int kRB = 8;               // rows per block (one warp each)
-constexpr int kThreads = 32 * kRB;   // 256
-constexpr int kPitch = kN + 2;       // row pitch of the row buffer (complex)
-constexpr int kChunk = 128;          // ky per tile
-constexpr int kNChunk = kN / 2 / kChunk;  // 4 mirror pairs of tiles
-constexpr int kTile = kChunk * kRB;       // complex per tile
-constexpr size_t kRowBytes = (size_t)kRB * kPitch * 8;
-constexpr size_t kStageBytes = (size_t)2 * 2 * kTile * 8;  // 2 buffers x (lo, hi)
-constexpr size_t kSmemBytes = 128 + kRowBytes + kStageBytes;  // + mbarriers
+constexpr int kN = 1024;  // complex points per row
+
+// Block shape: RB rows (one warp each) and tiles of C ky x RB x, i.e. RB * 8
+// contiguous bytes of W per ky (64 bytes at RB = 8, 128 bytes at RB = 16).
+// The row buffer pitch keeps the split's (row, ky) accesses conflict-free.
+template <int RB> struct Cfg {
+  static constexpr int kRB = RB;
+  static constexpr int kThreads = 32 * RB;
+  static constexpr int kPitch = RB == 8 ? kN + 2 : kN + 1;
+  static constexpr int kChunk = RB == 8 ? 128 : 64;
+  static constexpr int kNChunk = kN / 2 / kChunk;
+  static constexpr int kTile = kChunk * RB;  // complex per tile
+  static constexpr size_t kRowBytes = (size_t)RB * kPitch * 8;
+  static constexpr size_t kStageOff = (128 + kRowBytes + 127) / 128 * 128;
+  static constexpr size_t kStageBytes = (size_t)2 * 2 * kTile * 8;  // 2 buffers x (lo, hi)
+  static constexpr size_t kSmemBytes = kStageOff + kStageBytes;     // + mbarriers at 0
+};
 
 // 32-point DFT in registers, natural order in and out:
 // X[k] = sum_m x[m] exp(sign 2 pi i m k / 32).  Decimation in time:
@@ -134,26 +141,28 @@ __device__ __forceinline__ float2 inv_split_one(float2 xk, float2 xm, float4 pk)
 }
 
 // Blocks are persistent: block b takes the row sets s = b, b + gridDim.x, ...
-// (set s: dof = s / (nx/8), rows ix0 = 8 (s mod nx/8) .. ix0 + 7).  The
+// (set s: dof = s / (nx/RB), rows ix0 = RB (s mod nx/RB) .. ix0 + RB - 1).  The
 // global loads (forward) or TMA tile loads (inverse) of the next set are
 // issued before the current set's split or transform, so they are in flight
 // while the block computes.
 
 // Forward: u[dof][x][2n] (Tin) -> W[ky][dof][x] complex FP32, ky = 0..n.
-// tmW: 3-D tensor map of W as floats {2 nxp, ndof, nyc}, box {16, 1, kChunk}.
+// tmW: 3-D tensor map of W as floats {2 nxp, ndof, nyc}, box {2 RB, 1, C}.
 // tw: [k1][l] compensated w_n^(l k1); post: e^{-2 pi i k / (2n)}, k = 0..n.
-template <typename Tin>
-__global__ void __launch_bounds__(rows32::kThreads, 2)
+template <typename Tin, int RB>
+__global__ void __launch_bounds__(32 * RB, RB == 8 ? 2 : 1)
     k_row_fwd_w32(const Tin *__restrict__ u, float2 *__restrict__ W, const __grid_constant__ CUtensorMap tmW,
                   Geom g, const float4 *__restrict__ tw, const float4 *__restrict__ post) {
   using namespace rows32;
+  using K = Cfg<RB>;
+  constexpr int kRB = K::kRB, kPitch = K::kPitch, kChunk = K::kChunk, kNChunk = K::kNChunk, kTile = K::kTile;
   extern __shared__ __align__(128) unsigned char smem_rows[];
   float2 *xs = reinterpret_cast<float2 *>(smem_rows + 128);
-  float2 *stage = reinterpret_cast<float2 *>(smem_rows + 128 + kRowBytes);
+  float2 *stage = reinterpret_cast<float2 *>(smem_rows + K::kStageOff);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nxb = g.nx / kRB, nsets = nxb * g.ndof;
   if (threadIdx.x == 0) prefetch_tmap(&tmW);
-  const int r = threadIdx.x & (kRB - 1), j0 = threadIdx.x >> 3;
+  const int r = threadIdx.x & (kRB - 1), j0 = threadIdx.x / kRB;
 
   float2 x[32];
   auto load_rows = [&](int set) {  // this warp's row of the set, into x
@@ -194,7 +203,7 @@ __global__ void __launch_bounds__(rows32::kThreads, 2)
       }
       const int a = c * kChunk, hbase = kN - a - kChunk + 1;  // hi tile: ky = hbase .. n - a
 #pragma unroll 4
-      for (int j = j0; j < kChunk; j += rows32::kThreads / kRB) {
+      for (int j = j0; j < kChunk; j += K::kThreads / kRB) {
         const int k = a + j;
         const float2 xk = row[k], xm = row[(kN - k) & (kN - 1)];
         lo[j * kRB + r] = fwd_split_one(xk, xm, __ldg(&post[k]));
@@ -223,15 +232,17 @@ __global__ void __launch_bounds__(rows32::kThreads, 2)
 // come in by TMA, two mirror pairs in flight (the first two of the next set
 // load during the current set's transform); err receives GFMD_ETIMEDOUT if a
 // tile never arrives (the block then stops).
-template <typename Tout>
-__global__ void __launch_bounds__(rows32::kThreads, 2)
+template <typename Tout, int RB>
+__global__ void __launch_bounds__(32 * RB, RB == 8 ? 2 : 1)
     k_row_inv_w32(const float2 *__restrict__ W, const __grid_constant__ CUtensorMap tmW, Tout *__restrict__ f,
                   Geom g, const float4 *__restrict__ tw, const float4 *__restrict__ post, int *err) {
   using namespace rows32;
+  using K = Cfg<RB>;
+  constexpr int kRB = K::kRB, kPitch = K::kPitch, kChunk = K::kChunk, kNChunk = K::kNChunk, kTile = K::kTile;
   extern __shared__ __align__(128) unsigned char smem_rows[];
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem_rows);
   float2 *xs = reinterpret_cast<float2 *>(smem_rows + 128);
-  float2 *stage = reinterpret_cast<float2 *>(smem_rows + 128 + kRowBytes);
+  float2 *stage = reinterpret_cast<float2 *>(smem_rows + K::kStageOff);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nxb = g.nx / kRB, nsets = nxb * g.ndof;
   // pair p (global count) of this block: set blockIdx.x + (p / kNChunk) gridDim.x,
@@ -254,7 +265,7 @@ __global__ void __launch_bounds__(rows32::kThreads, 2)
     if (npairs > 1) issue(1);
   }
   __syncthreads();  // barrier initialisation visible to all threads
-  const int r = threadIdx.x & (kRB - 1), j0 = threadIdx.x >> 3;
+  const int r = threadIdx.x & (kRB - 1), j0 = threadIdx.x / kRB;
   float2 *rowr = xs + r * kPitch;
   int p = 0;
   for (int set = blockIdx.x; set < nsets; set += gridDim.x) {
@@ -273,7 +284,7 @@ __global__ void __launch_bounds__(rows32::kThreads, 2)
       }
       const int a = c * kChunk;
 #pragma unroll 4
-      for (int j = j0; j < kChunk; j += rows32::kThreads / kRB) {
+      for (int j = j0; j < kChunk; j += K::kThreads / kRB) {
         const int k = a + j;
         const float2 xk = lo[j * kRB + r], xm = hi[(kChunk - 1 - j) * kRB + r];  // X[k], X[n-k]
         if (k == 0) {
