@@ -287,7 +287,10 @@ int gfmd_run_dynamics(gfmd_handle_t h, const gfmd_obstacle_t *obst, double dt, d
  * process exits; grids that need more (e.g. beyond 512 x 512 at ndof 6) are
  * rejected with GFMD_EINVAL.  Calls share that array: calls that overlap on
  * the GPU race.  The first call on each device looks up the array's address;
- * make it before any stream capture.  Asynchronous on cuda_stream. */
+ * make it before any stream capture (later calls on a stream that is not
+ * capturing look it up again, so a device reset does not leave it stale).
+ * Buffers that the device cannot reach (plain host memory) are refused with
+ * GFMD_EINVAL.  Asynchronous on cuda_stream. */
 int gfmd_post_force_noalloc(int nx, int ny, int ndof, const double *d_phi_half,
                             const double *d_linf, const double *d_u, double *d_f,
                             double *d_epot, void *cuda_stream);

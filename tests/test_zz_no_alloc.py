@@ -70,3 +70,18 @@ def test_noalloc_rejects_grids_beyond_its_scratch():
     assert rc == 1
     msg = L.gfmd_last_error().decode()
     assert "scratch" in msg and "16 MiB" in msg
+
+
+def test_noalloc_refuses_host_memory():
+    # a plain host array handed as u is refused before any launch
+    L = gfmd_pkg().lib()
+    nx = ny = 16
+    d = 3
+    phi = torch.zeros(nx * (ny // 2 + 1) * d * d * 2, dtype=torch.float64, device="cuda")
+    u_host = np.zeros(d * nx * ny)
+    f = torch.zeros(d * nx * ny, dtype=torch.float64, device="cuda")
+    ep = torch.zeros(1, dtype=torch.float64, device="cuda")
+    rc = L.gfmd_post_force_noalloc(nx, ny, d, phi.data_ptr(), None, u_host.ctypes.data, f.data_ptr(),
+                                   ep.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    assert rc == 1
+    assert "device-accessible" in L.gfmd_last_error().decode()

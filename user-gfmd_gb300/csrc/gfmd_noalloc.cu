@@ -25,7 +25,14 @@
 // with cudaGetSymbolAddress, with that device current, and caches it; host
 // code never passes the array's own name to a kernel (on the host that name
 // is only a stand-in, not a device address).  Make the first call on each
-// device before any stream capture begins.
+// device before any stream capture begins.  Later calls on a stream that is
+// not capturing look the address up again (no allocation, no sync), so the
+// cache cannot go stale after a cudaDeviceReset reloads the module; a call
+// on a capturing stream uses the cached address.
+//
+// Arguments: every buffer must be reachable from the device (device or
+// managed memory, or host memory mapped into the device's address space);
+// plain host memory is refused with GFMD_EINVAL before any launch.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -181,6 +188,19 @@ __global__ void __launch_bounds__(kPhiThreads)
 
 int noalloc_fail(int code, const std::string &msg) { return set_error(code, msg); }
 
+// True when the device can dereference p (device, managed, or mapped host
+// memory).  cudaPointerGetAttributes allocates nothing.
+bool device_reachable(const void *p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // clear the sticky-free error of an unknown pointer
+    return false;
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return true;
+  if (a.type == cudaMemoryTypeHost) return a.devicePointer != nullptr;
+  return false;
+}
+
 }  // namespace
 
 }  // namespace gfmd
@@ -223,6 +243,14 @@ extern "C" int gfmd_post_force_noalloc(int nx, int ny, int ndof, const double *d
     return noalloc_fail(GFMD_EINVAL, std::string(who) + ": NULL argument");
   if ((const void *)d_u == (const void *)d_f)
     return noalloc_fail(GFMD_EINVAL, std::string(who) + ": u and f must not alias");
+  {
+    const void *bufs[] = {d_phi_half, d_u, d_f, d_epot, d_linf};
+    const char *names[] = {"phi", "u", "f", "epot", "linf"};
+    for (int i = 0; i < 5; i++)
+      if (bufs[i] && !device_reachable(bufs[i]))
+        return noalloc_fail(GFMD_EINVAL, std::string(who) + ": " + names[i] +
+                                             " is not device-accessible memory");
+  }
 
   // per-device set-up: device address of the scratch array, shared-memory limit
   int dev = 0;
@@ -233,8 +261,23 @@ extern "C" int gfmd_post_force_noalloc(int nx, int ny, int ndof, const double *d
     return noalloc_fail(GFMD_EINVAL, std::string(who) + ": device index out of range");
   void *base = nullptr;
   int smem = 0;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  ce = cudaStreamIsCapturing(reinterpret_cast<cudaStream_t>(cuda_stream), &cap);
+  if (ce != cudaSuccess)
+    return noalloc_fail(GFMD_ECUDA, std::string(who) + ": cudaStreamIsCapturing: " + cudaGetErrorString(ce));
   {
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev] && cap != cudaStreamCaptureStatusNone)
+      return noalloc_fail(GFMD_EINVAL, std::string(who) +
+                                           ": the first call on a device must come before stream capture");
+    if (g_noalloc_ptr[dev] && cap == cudaStreamCaptureStatusNone) {
+      void *p = nullptr;  // refresh: the module may have been reloaded by a device reset
+      ce = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (ce != cudaSuccess || !p)
+        return noalloc_fail(GFMD_ECUDA, std::string(who) + ": cudaGetSymbolAddress: " +
+                                            cudaGetErrorString(ce));
+      g_noalloc_ptr[dev] = p;
+    }
     if (!g_noalloc_ptr[dev]) {
       void *p = nullptr;
       ce = cudaGetSymbolAddress(&p, g_noalloc_scratch);
