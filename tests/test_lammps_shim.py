@@ -17,3 +17,10 @@ def test_solver_style_builds_against_the_reference_interface():
     # with a GPU the library accepts the grid and the table; without one the
     # call reaches gfmd_create and reports through LAMMPS' error->one
     assert out.startswith("ok static/gb300") or ("error" in out and "gfmd_create" in out), out
+
+
+@pytest.mark.skipif(not os.path.exists(DRIVER), reason="reference harness not built here")
+def test_dynamic_style_builds_and_parses_its_damping():
+    out = subprocess.run([DRIVER, "ft sc100 1.0 1 pair-potential 2 1.0 1.0 height 16", "dynamic"],
+                         capture_output=True, text=True, timeout=120).stdout.strip()
+    assert out.startswith("ok dynamic/gb300") or ("error" in out and "gfmd_create" in out), out

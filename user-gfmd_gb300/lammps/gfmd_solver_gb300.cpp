@@ -1,6 +1,7 @@
 // GFMDSolverGB300: see gfmd_solver_gb300.h.
 #include "gfmd_solver_gb300.h"
 
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -45,7 +46,9 @@ void GFMDSolverGB300::set_kernel(StiffnessKernel *kernel, bool normalize) {
 }
 
 double GFMDSolverGB300::post_force(void *u, void *f, char *dump_prefix) {
-  if (dump_prefix) error->all(FLERR, "static/gb300 does not write q-space dumps");
+  // q-space dumps (dumpq_every) need the spectra on the host; this style
+  // keeps them on the device, so it refuses rather than writing nothing
+  if (dump_prefix) error->all(FLERR, "static/gb300 does not write q-space dumps (unset dumpq_every)");
   double e = 0.0;
   check(gfmd_post_force_host(h_, &static_cast<double **>(u)[0][0], &static_cast<double **>(f)[0][0], &e));
   check(gfmd_get_u0(h_, u0));
@@ -60,4 +63,25 @@ double GFMDSolverGB300::memory_usage() {
   double b = 0.0;
   if (h_) gfmd_memory_usage(h_, &b);
   return b;
+}
+
+GFMDSolverGB300Dynamic::GFMDSolverGB300Dynamic(LAMMPS *lmp, int narg, int *carg, char **arg)
+    : GFMDSolverGB300(lmp, narg, carg, arg) {
+  strcpy(name, "dynamic/gb300");
+  if (carg && arg && *carg + 1 < narg && !strcmp(arg[*carg], "gamma")) {
+    char *end = nullptr;
+    gamma_ = strtod(arg[*carg + 1], &end);
+    if (!end || *end != '\0' || !(gamma_ >= 0.0)) error->all(FLERR, "dynamic/gb300: gamma must be a number >= 0");
+    *carg += 2;
+  }
+}
+
+double GFMDSolverGB300Dynamic::post_force(void *u, void *f, char *dump_prefix) {
+  double *fp = &static_cast<double **>(f)[0][0];
+  const size_t n = (size_t)ndof * nx * ny;
+  if (gamma_ > 0.0) v_.assign(fp, fp + n);  // the fix's velocities
+  const double e = GFMDSolverGB300::post_force(u, f, dump_prefix);
+  if (gamma_ > 0.0)
+    for (size_t i = 0; i < n; i++) fp[i] -= gamma_ * v_[i];
+  return e;
 }

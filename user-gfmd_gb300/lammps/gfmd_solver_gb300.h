@@ -9,6 +9,8 @@
 #ifndef GFMD_SOLVER_GB300_H
 #define GFMD_SOLVER_GB300_H
 
+#include <vector>
+
 #include "gfmd_gb300.h"
 #include "gfmd_solver.h"
 
@@ -40,6 +42,28 @@ class GFMDSolverGB300 : public GFMDSolver {
   gfmd_handle_t h_ = nullptr;
   int precision_ = GFMD_PREC_F64;
   void check(int rc);
+};
+
+// USER-GFMD solver style "dynamic/gb300": damped GFMD dynamics for a fix
+// gfmd integrated by LAMMPS (fix nve).  FixGFMD hands a dynamic solver the
+// atoms' velocities in the force buffer (src/main/fix_gfmd.cpp:782-793,
+// "Velocities are needed for the dynamic GFMD only"); this style returns the
+// elastic force of u minus the linear damping force, f = F_el(u) - gamma v
+// (unit masses), the same damping gfmd_run_dynamics integrates.  Register
+// beside static/gb300:
+//   else if (!strcmp(solver_name, "dynamic/gb300"))
+//     solver = new GFMDSolverGB300Dynamic(lmp, narg, carg, arg);
+// Arguments after the style name: optional "f32", then optional
+// "gamma <value>" (default 0: undamped).
+class GFMDSolverGB300Dynamic : public GFMDSolverGB300 {
+ public:
+  GFMDSolverGB300Dynamic(LAMMPS *lmp, int narg, int *carg, char **arg);
+  double post_force(void *u, void *f, char *dump_prefix) override;
+  double gamma() const { return gamma_; }
+
+ private:
+  double gamma_ = 0.0;
+  std::vector<double> v_;  // velocities taken from the force buffer
 };
 
 }  // namespace LAMMPS_NS

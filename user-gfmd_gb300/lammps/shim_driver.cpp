@@ -4,6 +4,7 @@
 // library's error message (e.g. no GPU).  Used by tests/test_lammps_shim.py.
 #include <cstdio>
 #include <exception>
+#include <stdexcept>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -44,9 +45,22 @@ int main(int argc, char **argv) {
     int karg = 1;
     StiffnessKernel *k = stiffness_kernel_factory(av[karg], (int)av.size(), &karg, av.data(), &domain,
                                                   nullptr, &memory, &error);
-    solver.set_grid_size(16, 16, k->get_dimension());
-    solver.set_kernel(k, true);
-    std::printf("ok %s\n", solver.get_name());
+    std::string styles = "static/gb300";
+    if (argc > 2 && std::string(argv[2]) == "dynamic") {
+      // the dynamic style: gamma parsed, velocities in f damped
+      char g0[] = "gamma", g1[] = "0.25";
+      char *dargs[] = {g0, g1};
+      int dc = 0;
+      GFMDSolverGB300Dynamic dyn(&lmp, 2, &dc, dargs);
+      if (dc != 2 || dyn.gamma() != 0.25) throw std::runtime_error("dynamic/gb300: arguments not parsed");
+      styles = dyn.get_name();
+      dyn.set_grid_size(16, 16, k->get_dimension());
+      dyn.set_kernel(k, true);
+    } else {
+      solver.set_grid_size(16, 16, k->get_dimension());
+      solver.set_kernel(k, true);
+    }
+    std::printf("ok %s\n", styles.c_str());
   } catch (const std::exception &e) {
     std::printf("error %s\n", e.what());
   }
