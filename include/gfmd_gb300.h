@@ -195,6 +195,10 @@ typedef struct {
   /* TR parameters (<= 0: defaults): largest trust radius (LAMMPS min_modify
      dmax, default 0.1) and the acceptance ratio (0.01, min_tr_gfmd.cpp:76) */
   double tr_dmax, tr_rho_tol;
+  /* CG: largest move of any displacement component in one line-search step
+     (LAMMPS min_modify dmax, which the reference's Hertz inputs leave at its
+     default 0.1); <= 0: no cap */
+  double dmax;
 } gfmd_min_params_t;
 
 typedef struct {

@@ -74,6 +74,7 @@ class MinParams(ctypes.Structure):
         ("precond", ctypes.c_void_p),
         ("tr_dmax", ctypes.c_double),
         ("tr_rho_tol", ctypes.c_double),
+        ("dmax", ctypes.c_double),
     ]
 
 

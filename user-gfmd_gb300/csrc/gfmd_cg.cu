@@ -79,6 +79,8 @@ struct CgCtl {
   double ftol;              // tolerance of the running phase
   double ftol_req;          // requested tolerance
   double fmax_restart;      // max |g_i| at the last restart
+  double dmax;              // largest move of a component per line-search step (<= 0: none)
+  double amax;              // step cap of this line search: dmax / max|h_i|
   int bulk;                 // FP32 phase: tolerance floored at the FP32 noise level
   int parked;               // phase finished: the branch skips its restart and loop
   int it, since, maxit, recompute;
@@ -219,6 +221,7 @@ __global__ void __launch_bounds__(kT) k_dirforce(Obst o, Geom gm, const Tx *__re
   const int nl = gm.ndof / 3;
   Dot<Tv> hkh, gh;
   double cw = 0.0, fw0h = 0.0;
+  Tv hmx = (Tv)0;
 #pragma unroll 2
   for (int s = blockIdx.x * kT + threadIdx.x; s < N; s += gridDim.x * kT) {
     for (int l = 0; l < nl; l++) {
@@ -228,6 +231,7 @@ __global__ void __launch_bounds__(kT) k_dirforce(Obst o, Geom gm, const Tx *__re
         const Tv hv = h[idx];
         hkh.add(hv, fKh[idx]);
         gh.add(g[idx], hv);
+        hmx = fmax(hmx, fabs(hv));
       }
     }
     if (map_in_f32<Tx>(o)) {
@@ -253,21 +257,25 @@ __global__ void __launch_bounds__(kT) k_dirforce(Obst o, Geom gm, const Tx *__re
       }
     }
   }
-  const double acc[4] = {-hkh.get(), gh.get(), cw, fw0h};
-  __shared__ double res[4];
-  if (!reduce_last<4, 0>(acc, part, &ctl->counter, res)) return;
+  const double acc[5] = {-hkh.get(), gh.get(), cw, fw0h, (double)hmx};
+  __shared__ double res[5];
+  if (!reduce_last<4, 1>(acc, part, &ctl->counter, res)) return;
   if (threadIdx.x == 0) {
     const double hKh = res[0], ghv = res[1], curv = res[0] + res[2];
+    // LAMMPS min_modify dmax: no component moves more than dmax in one step
+    ctl->amax = (ctl->dmax > 0.0 && res[4] > 0.0) ? ctl->dmax / res[4] : 1e300;
     ctl->hKh = hKh;
     ctl->gh = ghv;
     ctl->fw0h = res[3];
     ctl->lo = 0.0;
-    ctl->hi = -1.0;
     ctl->ls_it = 0;
+    // with the cap, amax is the upper bracket of the step from the start
+    ctl->hi = ctl->amax < 1e300 ? ctl->amax : -1.0;
     // Newton step from a = 0 on phi'(a) = -(g.h - a hKh + dF_w(a).h)
     double a;
     if (curv > 0.0 && ghv > 0.0) a = ghv / curv;
     else a = ghv > 0.0 ? 1e-3 : 0.0;
+    if (ghv > 0.0 && ctl->hi >= 0.0 && a >= ctl->hi) a = 0.5 * ctl->hi;  // bisect the bracket
     ctl->a = a;
     ctl->ls_done = (o.kind == GFMD_OBST_NONE || ghv <= 0.0) ? 1 : 0;
   }
@@ -938,6 +946,7 @@ int item_init(Item &it, gfmd_solver *hp, gfmd_solver *hr64, gfmd_solver *hpre, c
   CgCtl c{};
   c.ftol = prm->ftol;
   c.ftol_req = prm->ftol;
+  c.dmax = prm->dmax > 0.0 && std::isfinite(prm->dmax) ? prm->dmax : 0.0;
   c.bulk = it.mixed ? 1 : 0;
   c.maxit = prm->maxiter > 0 ? prm->maxiter : 100000;
   c.recompute = std::min(10000, prm->recompute > 0 ? prm->recompute : 50);

@@ -348,10 +348,12 @@ class GFMDSolverGB300:
 
     def minimize(self, u, obstacle=None, method: str = "cg", ftol: float = 1e-6,
                  maxiter: int = 0, refine: "GFMDSolverGB300 | None" = None,
-                 precond: "GFMDSolverGB300 | None" = None, **fire) -> dict:
+                 precond: "GFMDSolverGB300 | None" = None, dmax: float = 0.0, **fire) -> dict:
         """Static minimization from the displacements in u (CUDA float64
-        tensor [ndof, nx*ny], updated in place); returns the report.  Raises
-        GFMDError on failure (e.g. ENOTCONVERGED)."""
+        tensor [ndof, nx*ny], updated in place); returns the report.  ``dmax``
+        caps the CG's move of any component per line-search step (LAMMPS
+        min_modify dmax; 0: no cap).  Raises GFMDError on failure (e.g.
+        ENOTCONVERGED)."""
         p = _lib.MinParams()
         methods = {"cg": _lib.GFMD_MIN_CG, "fire": _lib.GFMD_MIN_FIRE, "tr": _lib.GFMD_MIN_TR}
         if method not in methods:
@@ -361,6 +363,7 @@ class GFMDSolverGB300:
         p.maxiter = maxiter
         p.refine = refine._handle().value if refine is not None else None
         p.precond = precond._handle().value if precond is not None else None
+        p.dmax = dmax
         for k, v in fire.items():  # FIRE parameters by name; TR ones as tr_dmax, tr_rho_tol
             setattr(p, k if k.startswith("tr_") else "fire_" + k, v)
         rep = _lib.MinReport()
