@@ -40,6 +40,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -60,6 +61,9 @@ using red::kQ;
 using red::Dot;
 using red::reduce_last;
 constexpr int kLsMax = 8;   // Newton probes per line search
+
+// Grids whose site count allows the 4-site vector kernels.
+inline bool nsite4(const Geom &g) { return ((size_t)g.nx * g.ny) % 4 == 0; }
 
 #define RT_CHECK(call)                \
   do {                                \
@@ -499,6 +503,239 @@ __global__ void __launch_bounds__(kT) k_dir(size_t n, Tv *__restrict__ h, const 
     h[i] = g[i] + beta * h[i];
 }
 
+// ---- 4-site vector forms of the streaming kernels ---------------------------
+// The per-element work of k_update, k_dirforce and k_dir is a few operations
+// on 4-6 streamed arrays: they are bound by how many loads each thread keeps
+// in flight.  The V = 4 forms take 4 consecutive sites per thread with 16-byte
+// loads (two for FP64), for grids with nx*ny divisible by 4 (all power-of-two
+// grids); the scalar forms above handle the rest.  Same arithmetic per site.
+template <typename T> struct Vec4;
+template <> struct Vec4<float> {
+  static __device__ __forceinline__ void ld(const float *p, float o[4]) {
+    const float4 v = *reinterpret_cast<const float4 *>(p);
+    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+  }
+  static __device__ __forceinline__ void st(float *p, const float o[4]) {
+    *reinterpret_cast<float4 *>(p) = make_float4(o[0], o[1], o[2], o[3]);
+  }
+};
+template <> struct Vec4<double> {
+  static __device__ __forceinline__ void ld(const double *p, double o[4]) {
+    const double2 a = *reinterpret_cast<const double2 *>(p), b = *reinterpret_cast<const double2 *>(p + 2);
+    o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+  }
+  static __device__ __forceinline__ void st(double *p, const double o[4]) {
+    *reinterpret_cast<double2 *>(p) = make_double2(o[0], o[1]);
+    *reinterpret_cast<double2 *>(p + 2) = make_double2(o[2], o[3]);
+  }
+};
+
+template <typename Tx, typename Tv>
+__global__ void __launch_bounds__(kT, 2) k_update4(Obst o, Geom gm, Tx *__restrict__ x,
+                                                    const Tv *__restrict__ h, const Tv *__restrict__ fKh,
+                                                    Tv *__restrict__ g, Tv *__restrict__ gp,
+                                                    unsigned char *__restrict__ active,
+                                                    double *__restrict__ part, CgCtl *ctl,
+                                                    cudaGraphConditionalHandle hc, int use_hc) {
+  const double ad = ctl->a;
+  const Tx a = (Tx)ad;
+  const Tv av = (Tv)ad;
+  const int N = gm.nx * gm.ny;
+  const int nl = gm.ndof / 3;
+  const bool obst = o.kind != GFMD_OBST_NONE;
+  Dot<Tv> gg, ggo, hg;
+  double ew = 0.0;
+  float fmx = 0.0f;
+  double fmx_d = 0.0;
+  for (int s0 = 4 * (blockIdx.x * kT + threadIdx.x); s0 < N; s0 += 4 * gridDim.x * kT) {
+    bool nearflag[4] = {false, false, false, false};
+    for (int l = 0; l < nl; l++) {
+      Tx xv[3][4], xn[3][4];
+      Tv hv[3][4], fk[3][4], go[3][4], gn[3][4];
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const size_t idx = (size_t)(3 * l + c) * N + s0;
+        Vec4<Tx>::ld(x + idx, xv[c]);
+        Vec4<Tv>::ld(h + idx, hv[c]);
+        Vec4<Tv>::ld(fKh + idx, fk[c]);
+        Vec4<Tv>::ld(g + idx, go[c]);
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          xn[c][j] = xv[c][j] + a * (Tx)hv[c][j];
+          gn[c][j] = go[c][j] + av * fk[c][j];
+        }
+      }
+      if (obst && l < o.nlayer) {
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const int s = s0 + j;
+          if (map_in_f32<Tx>(o)) {
+            float e1, f1, e0, f0;
+            map_wall_f(o, s, (float)xn[2][j] + o.foff[l][2], e1, f1);
+            map_wall_f(o, s, (float)xv[2][j] + o.foff[l][2], e0, f0);
+            nearflag[j] = true;
+            ew += e1;
+            gn[2][j] = gn[2][j] + (Tv)(f1 - f0);
+          } else {
+            const int ix = s / gm.ny, iy = s - ix * gm.ny;
+            const Tx xo3[3] = {xv[0][j], xv[1][j], xv[2][j]}, xn3[3] = {xn[0][j], xn[1][j], xn[2][j]};
+            const float ge_new = gap_reg(o, ix, iy, l, s, xn3);
+            const float ge_old = gap_reg(o, ix, iy, l, s, xo3);
+            if (ge_new < o.fgate_active) nearflag[j] = true;
+            if (ge_new < o.fgate_wall || ge_old < o.fgate_wall) {
+              const WallDelta<Tv> wd = wall_delta<Tx, Tv>(o, ix, iy, l, s, V3<Tx>{{xo3[0], xo3[1], xo3[2]}},
+                                                          V3<Tx>{{xn3[0], xn3[1], xn3[2]}},
+                                                          V3<Tv>{{go[0][j], go[1][j], go[2][j]}},
+                                                          V3<Tv>{{fk[0][j], fk[1][j], fk[2][j]}}, ad);
+              ew += wd.e;
+              gn[0][j] = wd.g[0];
+              gn[1][j] = wd.g[1];
+              gn[2][j] = wd.g[2];
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const size_t idx = (size_t)(3 * l + c) * N + s0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          gg.add(gn[c][j], gn[c][j]);
+          ggo.add(gn[c][j], go[c][j]);
+          hg.add(hv[c][j], gn[c][j]);
+          if constexpr (sizeof(Tv) == 4) fmx = fmaxf(fmx, fabsf(gn[c][j]));
+          else fmx_d = fmax(fmx_d, fabs(gn[c][j]));
+        }
+        Vec4<Tx>::st(x + idx, xn[c]);
+        Vec4<Tv>::st(g + idx, gn[c]);
+        if (gp) Vec4<Tv>::st(gp + idx, go[c]);  // previous gradient (preconditioned Polak-Ribiere)
+      }
+    }
+    *reinterpret_cast<uchar4 *>(active + s0) =
+        make_uchar4(nearflag[0] ? 1 : 0, nearflag[1] ? 1 : 0, nearflag[2] ? 1 : 0, nearflag[3] ? 1 : 0);
+  }
+  const double acc[5] = {gg.get(), ggo.get(), hg.get(), ew, sizeof(Tv) == 4 ? (double)fmx : fmx_d};
+  __shared__ double res[5];
+  if (!reduce_last<4, 1>(acc, part, &ctl->counter, res)) return;
+  if (threadIdx.x == 0) {
+    const double gg_new = res[0], g_gold = res[1], h_g = res[2];
+    if (!gp) {
+      const double gg_old = ctl->gg;
+      double beta = gg_old > 0.0 ? (gg_new - g_gold) / gg_old : 0.0;  // Polak-Ribiere
+      if (beta < 0.0) beta = 0.0;
+      if (!(gg_new + beta * h_g > 0.0)) beta = 0.0;
+      ctl->beta = beta;
+      ctl->gg = gg_new;
+    } else {
+      ctl->hg = h_g;
+    }
+    ctl->ew = res[3];
+    ctl->fmax = res[4];
+    ctl->it += 1;
+    ctl->since += 1;
+    if (!isfinite(gg_new)) ctl->done = 3;
+    else if (res[4] <= ctl->ftol) ctl->done = 1;
+    else if (ctl->it >= ctl->maxit) ctl->done = 2;
+    const bool go_on = ctl->done == 0 && ctl->since < ctl->recompute;
+    set_loop(hc, use_hc, go_on ? 1u : 0u);
+  }
+}
+
+template <typename Tx, typename Tv>
+__global__ void __launch_bounds__(kT, 2) k_dirforce4(Obst o, Geom gm, const Tx *__restrict__ x,
+                                                      const Tv *__restrict__ fKh, const Tv *__restrict__ h,
+                                                      const Tv *__restrict__ g,
+                                                      const unsigned char *__restrict__ active,
+                                                      double *__restrict__ part, CgCtl *ctl) {
+  const int N = gm.nx * gm.ny;
+  const int nl = gm.ndof / 3;
+  Dot<Tv> hkh, gh;
+  double cw = 0.0, fw0h = 0.0;
+  Tv hmx = (Tv)0;
+  for (int s0 = 4 * (blockIdx.x * kT + threadIdx.x); s0 < N; s0 += 4 * gridDim.x * kT) {
+    for (int l = 0; l < nl; l++) {
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const size_t idx = (size_t)(3 * l + c) * N + s0;
+        Tv hv[4], fk[4], gv[4];
+        Vec4<Tv>::ld(h + idx, hv);
+        Vec4<Tv>::ld(fKh + idx, fk);
+        Vec4<Tv>::ld(g + idx, gv);
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          hkh.add(hv[j], fk[j]);
+          gh.add(gv[j], hv[j]);
+          hmx = fmax(hmx, fabs(hv[j]));
+        }
+      }
+    }
+    if (o.kind == GFMD_OBST_NONE) continue;
+    const uchar4 act = map_in_f32<Tx>(o) ? make_uchar4(1, 1, 1, 1) : *reinterpret_cast<const uchar4 *>(active + s0);
+    const unsigned char av[4] = {act.x, act.y, act.z, act.w};
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      if (!av[j]) continue;
+      const int s = s0 + j;
+      if (map_in_f32<Tx>(o)) {
+        float cwf = 0.0f, fhf = 0.0f;
+        for (int l = 0; l < o.nlayer; l++) {
+          const size_t iz = (size_t)(3 * l + 2) * N + s;
+          float e, fz;
+          map_wall_f(o, s, (float)x[iz] + o.foff[l][2], e, fz);
+          const float hz = (float)h[iz];
+          cwf += fz * o.fnorm * o.finv_sigma * hz * hz;  // d2E/dz2 = F / sigma
+          fhf += fz * hz;
+        }
+        cw += cwf;
+        fw0h += fhf;
+      } else {
+        const int ix = s / gm.ny, iy = s - ix * gm.ny;
+        for (int l = 0; l < o.nlayer; l++) {
+          double r[3], d[3];
+          atom_pos<Tx, Tv>(o, ix, iy, l, x, h, N, s, 0.0, r, d);
+          const WallOut w = wall_eval(o, ix, iy, s, r, d);
+          cw += w.curv;
+          fw0h += w.f[0] * d[0] + w.f[1] * d[1] + w.f[2] * d[2];
+        }
+      }
+    }
+  }
+  const double acc[5] = {-hkh.get(), gh.get(), cw, fw0h, (double)hmx};
+  __shared__ double res[5];
+  if (!reduce_last<4, 1>(acc, part, &ctl->counter, res)) return;
+  if (threadIdx.x == 0) {
+    const double hKh = res[0], ghv = res[1], curv = res[0] + res[2];
+    ctl->amax = (ctl->dmax > 0.0 && res[4] > 0.0) ? ctl->dmax / res[4] : 1e300;
+    ctl->hKh = hKh;
+    ctl->gh = ghv;
+    ctl->fw0h = res[3];
+    ctl->lo = 0.0;
+    ctl->ls_it = 0;
+    ctl->hi = ctl->amax < 1e300 ? ctl->amax : -1.0;
+    double a;
+    if (curv > 0.0 && ghv > 0.0) a = ghv / curv;
+    else a = ghv > 0.0 ? 1e-3 : 0.0;
+    if (ghv > 0.0 && ctl->hi >= 0.0 && a >= ctl->hi) a = 0.5 * ctl->hi;
+    ctl->a = a;
+    ctl->ls_done = (o.kind == GFMD_OBST_NONE || ghv <= 0.0) ? 1 : 0;
+  }
+}
+
+// h = g + beta h, 4 elements per thread
+template <typename Tv>
+__global__ void __launch_bounds__(kT) k_dir4(size_t n, Tv *__restrict__ h, const Tv *__restrict__ g,
+                                              const CgCtl *ctl) {
+  const Tv beta = (Tv)ctl->beta;
+  for (size_t i = 4 * (blockIdx.x * (size_t)kT + threadIdx.x); i < n; i += 4 * (size_t)gridDim.x * kT) {
+    Tv hv[4], gv[4];
+    Vec4<Tv>::ld(h + i, hv);
+    Vec4<Tv>::ld(g + i, gv);
+#pragma unroll
+    for (int j = 0; j < 4; j++) hv[j] = gv[j] + beta * hv[j];
+    Vec4<Tv>::st(h + i, hv);
+  }
+}
+
 // Preconditioned CG.  The preconditioner handle's force evaluation of g
 // returns mz = -z, z = (Phi + c)^{-1} g.
 // Restart: h = z; g.z.
@@ -763,18 +1000,23 @@ cudaError_t enqueue_iteration(Item &it, cudaStream_t st, cudaGraphConditionalHan
   Tx *x = phase_x<Tx>(it);
   Tv *g = reinterpret_cast<Tv *>(b.g), *h = reinterpret_cast<Tv *>(b.h), *fKh = reinterpret_cast<Tv *>(b.fKh);
   RT_CHECK(eval_on(hd, st, h, io_type<Tv>(), fKh, io_type<Tv>(), b.d_e, false));
-  k_dirforce<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, gm, x, fKh, h, g, b.active, b.part, b.ctl);
+  auto al16 = [](const void *p) { return p == nullptr || ((uintptr_t)p & 15) == 0; };
+  Tv *gp = it.hpre ? reinterpret_cast<Tv *>(b.gp) : nullptr;
+  const bool v4 = nsite4(gm) && al16(x) && al16(h) && al16(fKh) && al16(g) && al16(gp);
+  if (v4) k_dirforce4<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, gm, x, fKh, h, g, b.active, b.part, b.ctl);
+  else k_dirforce<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, gm, x, fKh, h, g, b.active, b.part, b.ctl);
   if (it.o.kind != GFMD_OBST_NONE)
     for (int p = 0; p < kLsMax; p++) k_probe<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, gm, x, h, b.active, b.part, b.ctl);
-  Tv *gp = it.hpre ? reinterpret_cast<Tv *>(b.gp) : nullptr;
-  k_update<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, gm, x, h, fKh, g, gp, b.active, b.part, b.ctl, hwh, use_hc);
+  if (v4) k_update4<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, gm, x, h, fKh, g, gp, b.active, b.part, b.ctl, hwh, use_hc);
+  else k_update<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, gm, x, h, fKh, g, gp, b.active, b.part, b.ctl, hwh, use_hc);
   if (it.hpre) {
     Tv *mz = reinterpret_cast<Tv *>(b.mz);
     RT_CHECK(eval_on(it.hpre, st, g, io_type<Tv>(), mz, io_type<Tv>(), b.d_e, false));
     k_pcg_beta<Tv><<<b.nblk, kT, 0, st>>>(b.n, g, gp, mz, b.part, b.ctl);
     k_dir_pcg<Tv><<<b.nblk * 4, kT, 0, st>>>(b.n, h, mz, b.ctl);
   } else {
-    k_dir<Tv><<<b.nblk * 4, kT, 0, st>>>(b.n, h, g, b.ctl);
+    if (v4) k_dir4<Tv><<<b.nblk * 2, kT, 0, st>>>(b.n, h, g, b.ctl);
+    else k_dir<Tv><<<b.nblk * 4, kT, 0, st>>>(b.n, h, g, b.ctl);
   }
   return cudaGetLastError();
 }
