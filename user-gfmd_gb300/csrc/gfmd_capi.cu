@@ -482,8 +482,8 @@ int gfmd_memory_usage(gfmd_handle_t h, double *bytes) {
 // register-transform column kernel, the rounds of its Phi stream prefetched
 // into L2 ahead of use (1-3) and the resident blocks per SM it is compiled
 // for (2 or 3, for the 12-column kernel at nx = 2048).  With the table
-// uploaded, each candidate is timed (CUDA events, best of 3 after a warm-up)
-// on scratch inputs and the fastest is kept; results are cached per grid,
+// uploaded, each candidate is timed (CUDA events, best of 3 runs of 4
+// evaluations after a warm-up) on scratch inputs and the fastest is kept; results are cached per grid,
 // precision and kernel selection for the process.  GFMD_AUTOTUNE=0 keeps the
 // rule-based defaults.
 namespace {
@@ -562,7 +562,7 @@ cudaError_t autotune(gfmd_solver *h) {
     float ms = 1e30f;
     for (int r = 0; r < 3 && e == cudaSuccess; r++) {
       e = cudaEventRecord(e0, st);
-      if (e == cudaSuccess) e = gfmd::enqueue_force(h, u, t, f, t, ep);
+      for (int k = 0; k < 4 && e == cudaSuccess; k++) e = gfmd::enqueue_force(h, u, t, f, t, ep);
       if (e == cudaSuccess) e = cudaEventRecord(e1, st);
       if (e == cudaSuccess) e = cudaEventSynchronize(e1);
       float x = 0.0f;

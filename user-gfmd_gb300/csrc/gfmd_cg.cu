@@ -65,6 +65,20 @@ constexpr int kLsMax = 8;   // Newton probes per line search
 // Grids whose site count allows the 4-site vector kernels.
 inline bool nsite4(const Geom &g) { return ((size_t)g.nx * g.ny) % 4 == 0; }
 
+// Blocks of a grid-stride kernel: the resident blocks of the whole GPU (a
+// grid of several partial waves leaves SMs idle at its end), at most one per
+// `per_block` elements of work.
+template <typename K> int grid_for(K kernel, int sms, size_t work, size_t per_block) {
+  static int resident = 0;  // per kernel instance
+  if (resident == 0) {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kT, 0) != cudaSuccess || nb < 1) nb = 1;
+    resident = nb;
+  }
+  const size_t need = (work + per_block - 1) / per_block;
+  return (int)std::max<size_t>(1, std::min<size_t>((size_t)resident * sms, need));
+}
+
 #define RT_CHECK(call)                \
   do {                                \
     cudaError_t e_ = (call);          \
@@ -285,6 +299,29 @@ __global__ void __launch_bounds__(kT) k_dirforce(Obst o, Geom gm, const Tx *__re
   }
 }
 
+// The Newton step of a probe from the reduced F_w(u + a h).h and curvature.
+__device__ __forceinline__ void probe_step(CgCtl *ctl, double a, double dfh, double cwall) {
+  {
+    const double gdir = ctl->gh - a * ctl->hKh + (dfh - ctl->fw0h);
+    const double curv = ctl->hKh + cwall;
+    double lo = ctl->lo, hi = ctl->hi;
+    if (gdir > 0.0) lo = a;
+    else hi = a;
+    double an = (curv > 0.0) ? a + gdir / curv : -1.0;
+    if (hi >= 0.0 && (an <= lo || an >= hi || an < 0.0)) an = 0.5 * (lo + hi);
+    else if (an < 0.0) an = lo > 0.0 ? 2.0 * lo : 1e-3;
+    const double step = fabs(an - a);
+    ctl->lo = lo;
+    ctl->hi = hi;
+    ctl->a = an;
+    ctl->ls_it += 1;
+    // an exact line minimum is not needed: Polak-Ribiere with restarts
+    // converges from a step within 1e-6 of it
+    if (step <= 1e-6 * fabs(an) || ctl->ls_it >= kLsMax || !isfinite(an)) ctl->ls_done = 1;
+    if (!isfinite(an)) ctl->a = 0.0;
+  }
+}
+
 // ---- one Newton probe of the line search at u + a h ------------------------
 // gdir(a) = g.h - a hKh + sum F_w(u + a h).h - F_w(u).h   (= -phi'(a))
 // curv(a) = hKh + sum h^T H_w(u + a h) h                   (=  phi''(a))
@@ -325,25 +362,7 @@ __global__ void __launch_bounds__(kT) k_probe(Obst o, Geom gm, const Tx *__restr
   const double acc[2] = {dfh, cw};
   __shared__ double res[2];
   if (!reduce_last<2, 0>(acc, part, &ctl->counter, res)) return;
-  if (threadIdx.x == 0) {
-    const double gdir = ctl->gh - a * ctl->hKh + (res[0] - ctl->fw0h);
-    const double curv = ctl->hKh + res[1];
-    double lo = ctl->lo, hi = ctl->hi;
-    if (gdir > 0.0) lo = a;
-    else hi = a;
-    double an = (curv > 0.0) ? a + gdir / curv : -1.0;
-    if (hi >= 0.0 && (an <= lo || an >= hi || an < 0.0)) an = 0.5 * (lo + hi);
-    else if (an < 0.0) an = lo > 0.0 ? 2.0 * lo : 1e-3;
-    const double step = fabs(an - a);
-    ctl->lo = lo;
-    ctl->hi = hi;
-    ctl->a = an;
-    ctl->ls_it += 1;
-    // an exact line minimum is not needed: Polak-Ribiere with restarts
-    // converges from a step within 1e-6 of it
-    if (step <= 1e-6 * fabs(an) || ctl->ls_it >= kLsMax || !isfinite(an)) ctl->ls_done = 1;
-    if (!isfinite(an)) ctl->a = 0.0;
-  }
+  if (threadIdx.x == 0) probe_step(ctl, a, res[0], res[1]);
 }
 
 // ---- update after the line search ------------------------------------------
@@ -370,7 +389,7 @@ template <typename T> struct V3 { T v[3]; };
 template <typename Tv> struct WallDelta { double e; Tv g[3]; };
 
 template <typename Tx, typename Tv>
-__device__ __forceinline__ WallDelta<Tv> wall_delta(const Obst &o, int ix, int iy, int l, int s, V3<Tx> xv,
+__device__ __noinline__ WallDelta<Tv> wall_delta(const Obst &o, int ix, int iy, int l, int s, V3<Tx> xv,
                                                  V3<Tx> xn, V3<Tv> go, V3<Tv> fk, double a) {
   WallOut w1, w0;
   wall_at<Tx, Tv>(o, ix, iy, l, s, xn.v, w1);
@@ -543,7 +562,7 @@ __global__ void __launch_bounds__(kT, 2) k_update4(Obst o, Geom gm, Tx *__restri
   const int N = gm.nx * gm.ny;
   const int nl = gm.ndof / 3;
   const bool obst = o.kind != GFMD_OBST_NONE;
-  Dot<Tv> gg, ggo, hg;
+  Dot<Tv> gg[2], ggo[2], hg[2];  // two chains each: sites j even / odd
   double ew = 0.0;
   float fmx = 0.0f;
   double fmx_d = 0.0;
@@ -600,9 +619,9 @@ __global__ void __launch_bounds__(kT, 2) k_update4(Obst o, Geom gm, Tx *__restri
         const size_t idx = (size_t)(3 * l + c) * N + s0;
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-          gg.add(gn[c][j], gn[c][j]);
-          ggo.add(gn[c][j], go[c][j]);
-          hg.add(hv[c][j], gn[c][j]);
+          gg[j & 1].add(gn[c][j], gn[c][j]);
+          ggo[j & 1].add(gn[c][j], go[c][j]);
+          hg[j & 1].add(hv[c][j], gn[c][j]);
           if constexpr (sizeof(Tv) == 4) fmx = fmaxf(fmx, fabsf(gn[c][j]));
           else fmx_d = fmax(fmx_d, fabs(gn[c][j]));
         }
@@ -614,7 +633,8 @@ __global__ void __launch_bounds__(kT, 2) k_update4(Obst o, Geom gm, Tx *__restri
     *reinterpret_cast<uchar4 *>(active + s0) =
         make_uchar4(nearflag[0] ? 1 : 0, nearflag[1] ? 1 : 0, nearflag[2] ? 1 : 0, nearflag[3] ? 1 : 0);
   }
-  const double acc[5] = {gg.get(), ggo.get(), hg.get(), ew, sizeof(Tv) == 4 ? (double)fmx : fmx_d};
+  const double acc[5] = {gg[0].get() + gg[1].get(), ggo[0].get() + ggo[1].get(), hg[0].get() + hg[1].get(), ew,
+                         sizeof(Tv) == 4 ? (double)fmx : fmx_d};
   __shared__ double res[5];
   if (!reduce_last<4, 1>(acc, part, &ctl->counter, res)) return;
   if (threadIdx.x == 0) {
@@ -641,15 +661,34 @@ __global__ void __launch_bounds__(kT, 2) k_update4(Obst o, Geom gm, Tx *__restri
   }
 }
 
+// Wall curvature along h and F_w.h of one site at a = 0 (out of line: only
+// sites near the obstacle take it, and its FP64 registers stay out of the
+// streaming loop).
 template <typename Tx, typename Tv>
-__global__ void __launch_bounds__(kT, 2) k_dirforce4(Obst o, Geom gm, const Tx *__restrict__ x,
+__device__ __noinline__ double2 wall_dir_site(Obst o, Geom gm, const Tx *__restrict__ x, const Tv *__restrict__ h,
+                                              int s) {
+  const int N = gm.nx * gm.ny;
+  const int ix = s / gm.ny, iy = s - ix * gm.ny;
+  double cw = 0.0, fh = 0.0;
+  for (int l = 0; l < o.nlayer; l++) {
+    double r[3], d[3];
+    atom_pos<Tx, Tv>(o, ix, iy, l, x, h, N, s, 0.0, r, d);
+    const WallOut w = wall_eval(o, ix, iy, s, r, d);
+    cw += w.curv;
+    fh += w.f[0] * d[0] + w.f[1] * d[1] + w.f[2] * d[2];
+  }
+  return make_double2(cw, fh);
+}
+
+template <typename Tx, typename Tv>
+__global__ void __launch_bounds__(kT, 4) k_dirforce4(Obst o, Geom gm, const Tx *__restrict__ x,
                                                       const Tv *__restrict__ fKh, const Tv *__restrict__ h,
                                                       const Tv *__restrict__ g,
                                                       const unsigned char *__restrict__ active,
                                                       double *__restrict__ part, CgCtl *ctl) {
   const int N = gm.nx * gm.ny;
   const int nl = gm.ndof / 3;
-  Dot<Tv> hkh, gh;
+  Dot<Tv> hkh[2], gh[2];  // two chains each: sites j even / odd
   double cw = 0.0, fw0h = 0.0;
   Tv hmx = (Tv)0;
   for (int s0 = 4 * (blockIdx.x * kT + threadIdx.x); s0 < N; s0 += 4 * gridDim.x * kT) {
@@ -663,8 +702,8 @@ __global__ void __launch_bounds__(kT, 2) k_dirforce4(Obst o, Geom gm, const Tx *
         Vec4<Tv>::ld(g + idx, gv);
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-          hkh.add(hv[j], fk[j]);
-          gh.add(gv[j], hv[j]);
+          hkh[j & 1].add(hv[j], fk[j]);
+          gh[j & 1].add(gv[j], hv[j]);
           hmx = fmax(hmx, fabs(hv[j]));
         }
       }
@@ -689,18 +728,13 @@ __global__ void __launch_bounds__(kT, 2) k_dirforce4(Obst o, Geom gm, const Tx *
         cw += cwf;
         fw0h += fhf;
       } else {
-        const int ix = s / gm.ny, iy = s - ix * gm.ny;
-        for (int l = 0; l < o.nlayer; l++) {
-          double r[3], d[3];
-          atom_pos<Tx, Tv>(o, ix, iy, l, x, h, N, s, 0.0, r, d);
-          const WallOut w = wall_eval(o, ix, iy, s, r, d);
-          cw += w.curv;
-          fw0h += w.f[0] * d[0] + w.f[1] * d[1] + w.f[2] * d[2];
-        }
+        const double2 w = wall_dir_site<Tx, Tv>(o, gm, x, h, s);
+        cw += w.x;
+        fw0h += w.y;
       }
     }
   }
-  const double acc[5] = {-hkh.get(), gh.get(), cw, fw0h, (double)hmx};
+  const double acc[5] = {-(hkh[0].get() + hkh[1].get()), gh[0].get() + gh[1].get(), cw, fw0h, (double)hmx};
   __shared__ double res[5];
   if (!reduce_last<4, 1>(acc, part, &ctl->counter, res)) return;
   if (threadIdx.x == 0) {
@@ -888,7 +922,9 @@ cudaError_t bufs_init(CgBufs &b, gfmd_solver *h, bool mixed, bool map, bool pcg)
   const size_t vb = up(sizeof(double) * b.n);
   size_t off[12], tot = 0;
   const size_t sz[12] = {vb, vb, vb, vb, mixed ? up(sizeof(float) * b.n) : 0, map ? up(sizeof(float) * nsite) : 0,
-                         up(nsite), up(sizeof(double) * kQ * b.nblk), up(sizeof(double) * 4), up(sizeof(CgCtl)),
+                         // partials: room for the most resident 256-thread blocks (8 per SM)
+                         up(nsite), up(sizeof(double) * kQ * std::max<size_t>(b.nblk, (size_t)h->sm_count * 8)),
+                         up(sizeof(double) * 4), up(sizeof(CgCtl)),
                          pcg ? vb : 0, pcg ? vb : 0};
   for (int k = 0; k < 12; k++) {
     off[k] = tot;
@@ -1003,11 +1039,17 @@ cudaError_t enqueue_iteration(Item &it, cudaStream_t st, cudaGraphConditionalHan
   auto al16 = [](const void *p) { return p == nullptr || ((uintptr_t)p & 15) == 0; };
   Tv *gp = it.hpre ? reinterpret_cast<Tv *>(b.gp) : nullptr;
   const bool v4 = nsite4(gm) && al16(x) && al16(h) && al16(fKh) && al16(g) && al16(gp);
-  if (v4) k_dirforce4<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, gm, x, fKh, h, g, b.active, b.part, b.ctl);
+  const size_t nsite = (size_t)gm.nx * gm.ny;
+  const int sms = it.hp->sm_count;
+  if (v4)
+    k_dirforce4<Tx, Tv><<<grid_for(k_dirforce4<Tx, Tv>, sms, nsite, 4 * kT), kT, 0, st>>>(it.o, gm, x, fKh, h, g,
+                                                                                           b.active, b.part, b.ctl);
   else k_dirforce<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, gm, x, fKh, h, g, b.active, b.part, b.ctl);
   if (it.o.kind != GFMD_OBST_NONE)
     for (int p = 0; p < kLsMax; p++) k_probe<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, gm, x, h, b.active, b.part, b.ctl);
-  if (v4) k_update4<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, gm, x, h, fKh, g, gp, b.active, b.part, b.ctl, hwh, use_hc);
+  if (v4)
+    k_update4<Tx, Tv><<<grid_for(k_update4<Tx, Tv>, sms, nsite, 4 * kT), kT, 0, st>>>(
+        it.o, gm, x, h, fKh, g, gp, b.active, b.part, b.ctl, hwh, use_hc);
   else k_update<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, gm, x, h, fKh, g, gp, b.active, b.part, b.ctl, hwh, use_hc);
   if (it.hpre) {
     Tv *mz = reinterpret_cast<Tv *>(b.mz);
@@ -1015,7 +1057,7 @@ cudaError_t enqueue_iteration(Item &it, cudaStream_t st, cudaGraphConditionalHan
     k_pcg_beta<Tv><<<b.nblk, kT, 0, st>>>(b.n, g, gp, mz, b.part, b.ctl);
     k_dir_pcg<Tv><<<b.nblk * 4, kT, 0, st>>>(b.n, h, mz, b.ctl);
   } else {
-    if (v4) k_dir4<Tv><<<b.nblk * 2, kT, 0, st>>>(b.n, h, g, b.ctl);
+    if (v4) k_dir4<Tv><<<grid_for(k_dir4<Tv>, sms, b.n, 4 * kT), kT, 0, st>>>(b.n, h, g, b.ctl);
     else k_dir<Tv><<<b.nblk * 4, kT, 0, st>>>(b.n, h, g, b.ctl);
   }
   return cudaGetLastError();
