@@ -149,8 +149,16 @@ int gfmd_kernel_plan(gfmd_handle_t h, int *row_warp_tma, int *col_cluster, int *
 #define GFMD_OBST_SPHERE_LJ 2  /* LJ 12-6 on the gap, shifted at cutoff
                                   (FixContactSphere, src/extras/fix_contact_sphere.cpp:207-264) */
 #define GFMD_OBST_MAP_EXP 3    /* exponential wall on dz = norm (z - (map + map_z0)),
-                                  normal force only (FixWallMap::pre_force,
-                                  src/extras/fix_wall_map.cpp:686-817) */
+                                  map height at the grid site, normal force only
+                                  (FixWallMap::pre_force, src/extras/fix_wall_map.cpp:686-817,
+                                  for small lateral displacements and slopes) */
+#define GFMD_OBST_MAP_BICUBIC 4 /* the same wall with FixWallMap's bicubic map table
+                                  (corner values, central-difference slopes, zero cross
+                                  derivatives; src/mathutils/table2d.cpp:176-260)
+                                  evaluated at the atom's displaced (x, y) (map pixel
+                                  (i, j) at (i lattice[0], j lattice[1])), and the
+                                  lateral force -f_z dz/dx, -f_z dz/dy
+                                  (fix_wall_map.cpp:686-817, 1381) */
 
 typedef struct {
   int kind;
@@ -273,6 +281,17 @@ int gfmd_minimize_batch(int n, gfmd_batch_item_t *items, const gfmd_min_params_t
 int gfmd_run_dynamics(gfmd_handle_t h, const gfmd_obstacle_t *obst, double dt, double gamma,
                       int nsteps, double *d_u, double *d_v, double *energies,
                       gfmd_min_report_t *report);
+
+/* Force of an obstacle on every atom of the grid at displacements d_u
+ * (device, FP64 [ndof][nx*ny]) into d_f (same layout; zero on layers the
+ * obstacle does not act on) and its energy into *d_energy (device, one
+ * double), summed in a fixed order.  Synchronizes cuda_stream.
+ * Replaces: the per-atom evaluations of FixWallMap::pre_force
+ * (src/extras/fix_wall_map.cpp:686-817) and FixContactSphere::post_force
+ * (src/extras/fix_contact_sphere.cpp:207-264) for a fix that keeps its
+ * atoms on the device as a grid. */
+int gfmd_obstacle_force(int nx, int ny, int ndof, const gfmd_obstacle_t *ob, const double *d_u,
+                        double *d_f, double *d_energy, void *cuda_stream);
 
 /* ---- allocation-free force evaluation ------------------------------------- */
 

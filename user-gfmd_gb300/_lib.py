@@ -29,6 +29,7 @@ GFMD_OBST_NONE = 0
 GFMD_OBST_SPHERE_EXP = 1
 GFMD_OBST_SPHERE_LJ = 2
 GFMD_OBST_MAP_EXP = 3
+GFMD_OBST_MAP_BICUBIC = 4
 GFMD_MIN_CG = 0
 GFMD_MIN_FIRE = 1
 GFMD_MIN_TR = 2
@@ -164,6 +165,7 @@ SIGNATURES = {
     "gfmd_minimize_batch": [_c_int, ctypes.POINTER(BatchItem), ctypes.POINTER(MinParams)],
     "gfmd_run_dynamics": [_vp, ctypes.POINTER(Obstacle), _c_dbl, _c_dbl, _c_int, _vp, _vp, _vp,
                           ctypes.POINTER(MinReport)],
+    "gfmd_obstacle_force": [_c_int, _c_int, _c_int, ctypes.POINTER(Obstacle), _vp, _vp, _vp, _vp],
     "gfmd_post_force_noalloc": [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp],
     "gfmd_atoms_to_grid": [_c_int, _vp, _vp, _vp, _vp, _c_int, _c_int, _c_int, _c_dbl, _c_dbl, _c_int,
                            _c_int, _vp, _vp, _vp, _pi, _vp],

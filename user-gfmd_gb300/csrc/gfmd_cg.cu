@@ -1399,9 +1399,9 @@ extern "C" int gfmd_minimize_batch(int n, gfmd_batch_item_t *items, const gfmd_m
     if ((b.precond != nullptr) != (items[0].precond != nullptr))
       return set_error(GFMD_EINVAL, "gfmd_minimize_batch: items must share preconditioning");
     const gfmd_obstacle_t *ob = b.obstacle;
-    if (ob && (ob->kind < GFMD_OBST_NONE || ob->kind > GFMD_OBST_MAP_EXP))
+    if (ob && (ob->kind < GFMD_OBST_NONE || ob->kind > GFMD_OBST_MAP_BICUBIC))
       return set_error(GFMD_EINVAL, "gfmd_minimize_batch: unknown obstacle kind");
-    if (ob && ob->kind == GFMD_OBST_MAP_EXP && !ob->d_map)
+    if (ob && (ob->kind == GFMD_OBST_MAP_EXP || ob->kind == GFMD_OBST_MAP_BICUBIC) && !ob->d_map)
       return set_error(GFMD_EINVAL, "gfmd_minimize_batch: map obstacle without a map");
   }
   const auto t0 = std::chrono::steady_clock::now();

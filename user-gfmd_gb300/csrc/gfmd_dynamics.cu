@@ -307,9 +307,9 @@ extern "C" int gfmd_run_dynamics(gfmd_handle_t h, const gfmd_obstacle_t *obst, d
   if (!h || !d_u || !d_v || nsteps < 0 || !(dt > 0.0) || gamma < 0.0)
     return set_error(GFMD_EINVAL, "gfmd_run_dynamics: bad argument");
   if (!h->have_phi) return set_error(GFMD_ENOPHI, "gfmd_run_dynamics: no stiffness table uploaded");
-  if (obst && obst->kind == GFMD_OBST_MAP_EXP && !obst->d_map)
+  if (obst && (obst->kind == GFMD_OBST_MAP_EXP || obst->kind == GFMD_OBST_MAP_BICUBIC) && !obst->d_map)
     return set_error(GFMD_EINVAL, "gfmd_run_dynamics: map obstacle without a map");
-  if (obst && (obst->kind < GFMD_OBST_NONE || obst->kind > GFMD_OBST_MAP_EXP))
+  if (obst && (obst->kind < GFMD_OBST_NONE || obst->kind > GFMD_OBST_MAP_BICUBIC))
     return set_error(GFMD_EINVAL, "gfmd_run_dynamics: unknown obstacle kind");
   const auto t0 = std::chrono::steady_clock::now();
   const Obst o = make_obst(obst, h->g);

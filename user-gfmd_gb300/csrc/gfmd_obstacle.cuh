@@ -5,7 +5,11 @@
 //   sphere, Lennard-Jones 12-6 on the gap, shifted at the cutoff
 //                              (FixContactSphere::post_force, src/extras/fix_contact_sphere.cpp:207-264);
 //   rigid map, exponential wall on dz = r_z - z_map (normal force only;
-//                              FixWallMap::pre_force, src/extras/fix_wall_map.cpp:686-817).
+//                              FixWallMap::pre_force, src/extras/fix_wall_map.cpp:686-817);
+//   rigid map, exponential wall with FixWallMap's bicubic map table evaluated
+//                              at the atom's displaced (x, y) and the lateral
+//                              force -f_z dz/dx, -f_z dz/dy (fix_wall_map.cpp:686-817,
+//                              src/mathutils/table2d.cpp:176-260).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -21,6 +25,7 @@ struct Obst {
   double cx, cy, cz, R, eps, sigma, cutoff, offset;
   double c1, c2, c3, c4;  // LJ coefficients
   const double *map;
+  int mnx, mny;    // map size (the grid's)
   double map_z0;
   int norm;
   double ax, ay, lx, ly;  // lattice spacing, box
@@ -51,6 +56,76 @@ __device__ __forceinline__ void map_wall_f(const Obst &o, size_t s, float rz, fl
   const float ex = o.feps * expf(-dz * o.finv_sigma);
   e = ex - o.foffset;
   fz = o.fnorm * ex * o.finv_sigma;
+}
+
+// FixWallMap's bicubic map table (Table2D with interpolated derivatives,
+// src/mathutils/table2d.cpp): on the periodic pixel cell [i, i+1] x [j, j+1]
+// the bicubic with the corner values, central-difference slopes
+// (z[i+1] - z[i-1]) / 2 along each axis and zero cross derivatives, written in
+// the cubic Hermite basis.  (x, y) in pixel units; outputs z and its first and
+// second derivatives in pixel units.
+struct MapBicubic {
+  double z, zx, zy, zxx, zyy, zxy;
+};
+template <typename T>
+__device__ __forceinline__ T map_at(const T *m, int nx, int ny, int i, int j) {
+  i %= nx;
+  if (i < 0) i += nx;
+  j %= ny;
+  if (j < 0) j += ny;
+  return m[(size_t)i * ny + j];
+}
+__device__ __forceinline__ MapBicubic map_bicubic(const double *m, int nx, int ny, double x, double y) {
+  const double fx = floor(x), fy = floor(y);
+  const int i0 = (int)fx, j0 = (int)fy;
+  const double t = x - fx, u = y - fy;
+  // Hermite basis H0, H1 (values at 0, 1), G0, G1 (slopes at 0, 1) and derivatives
+  const double t2 = t * t, t3 = t2 * t, u2 = u * u, u3 = u2 * u;
+  const double hx[4] = {2 * t3 - 3 * t2 + 1, -2 * t3 + 3 * t2, t3 - 2 * t2 + t, t3 - t2};
+  const double dx1[4] = {6 * t2 - 6 * t, -6 * t2 + 6 * t, 3 * t2 - 4 * t + 1, 3 * t2 - 2 * t};
+  const double dx2[4] = {12 * t - 6, -12 * t + 6, 6 * t - 4, 6 * t - 2};
+  const double hy[4] = {2 * u3 - 3 * u2 + 1, -2 * u3 + 3 * u2, u3 - 2 * u2 + u, u3 - u2};
+  const double dy1[4] = {6 * u2 - 6 * u, -6 * u2 + 6 * u, 3 * u2 - 4 * u + 1, 3 * u2 - 2 * u};
+  const double dy2[4] = {12 * u - 6, -12 * u + 6, 6 * u - 4, 6 * u - 2};
+  MapBicubic r{0, 0, 0, 0, 0, 0};
+#pragma unroll
+  for (int a = 0; a < 2; a++)
+#pragma unroll
+    for (int b = 0; b < 2; b++) {
+      const double f = map_at(m, nx, ny, i0 + a, j0 + b);
+      const double fxs = 0.5 * (map_at(m, nx, ny, i0 + a + 1, j0 + b) - map_at(m, nx, ny, i0 + a - 1, j0 + b));
+      const double fys = 0.5 * (map_at(m, nx, ny, i0 + a, j0 + b + 1) - map_at(m, nx, ny, i0 + a, j0 + b - 1));
+      // value term H_a(t) H_b(u), slope terms G_a(t) H_b(u) and H_a(t) G_b(u)
+      r.z += f * hx[a] * hy[b] + fxs * hx[2 + a] * hy[b] + fys * hx[a] * hy[2 + b];
+      r.zx += f * dx1[a] * hy[b] + fxs * dx1[2 + a] * hy[b] + fys * dx1[a] * hy[2 + b];
+      r.zy += f * hx[a] * dy1[b] + fxs * hx[2 + a] * dy1[b] + fys * hx[a] * dy1[2 + b];
+      r.zxx += f * dx2[a] * hy[b] + fxs * dx2[2 + a] * hy[b] + fys * dx2[a] * hy[2 + b];
+      r.zyy += f * hx[a] * dy2[b] + fxs * hx[2 + a] * dy2[b] + fys * hx[a] * dy2[2 + b];
+      r.zxy += f * dx1[a] * dy1[b] + fxs * dx1[2 + a] * dy1[b] + fys * dx1[a] * dy1[2 + b];
+    }
+  return r;
+}
+// Value only, FP32 (gating estimates).
+__device__ __forceinline__ float map_bicubic_f(const double *m, int nx, int ny, float x, float y) {
+  const float fx = floorf(x), fy = floorf(y);
+  const int i0 = (int)fx, j0 = (int)fy;
+  const float t = x - fx, u = y - fy;
+  const float t2 = t * t, t3 = t2 * t, u2 = u * u, u3 = u2 * u;
+  const float hx[4] = {2 * t3 - 3 * t2 + 1, -2 * t3 + 3 * t2, t3 - 2 * t2 + t, t3 - t2};
+  const float hy[4] = {2 * u3 - 3 * u2 + 1, -2 * u3 + 3 * u2, u3 - 2 * u2 + u, u3 - u2};
+  float z = 0.0f;
+#pragma unroll
+  for (int a = 0; a < 2; a++)
+#pragma unroll
+    for (int b = 0; b < 2; b++) {
+      const float f = (float)map_at(m, nx, ny, i0 + a, j0 + b);
+      const float fxs =
+          0.5f * (float)(map_at(m, nx, ny, i0 + a + 1, j0 + b) - map_at(m, nx, ny, i0 + a - 1, j0 + b));
+      const float fys =
+          0.5f * (float)(map_at(m, nx, ny, i0 + a, j0 + b + 1) - map_at(m, nx, ny, i0 + a, j0 + b - 1));
+      z += f * hx[a] * hy[b] + fxs * hx[2 + a] * hy[b] + fys * hx[a] * hy[2 + b];
+    }
+  return z;
 }
 
 struct WallOut {
@@ -101,6 +176,24 @@ __device__ __forceinline__ WallOut wall_eval(const Obst &o, int s_ix, int s_iy, 
     w.e = ex - o.offset;
     w.f[2] = o.norm * ex / o.sigma;
     w.curv = ex / (o.sigma * o.sigma) * dir[2] * dir[2];
+  } else if (o.kind == GFMD_OBST_MAP_BICUBIC) {
+    // map pixel (i, j) sits at (i ax, j ay): evaluate at the displaced position
+    const MapBicubic mb = map_bicubic(o.map, o.mnx, o.mny, r[0] / o.ax, r[1] / o.ay);
+    const double zx = mb.zx / o.ax, zy = mb.zy / o.ay;
+    const double zxx = mb.zxx / (o.ax * o.ax), zyy = mb.zyy / (o.ay * o.ay), zxy = mb.zxy / (o.ax * o.ay);
+    const double dz = o.norm * (r[2] - (mb.z + o.map_z0));
+    if (dz >= o.gcut) return w;
+    const double ex = o.eps * exp(-dz / o.sigma);
+    const double fz = o.norm * ex / o.sigma;
+    w.e = ex - o.offset;
+    w.f[0] = -fz * zx;
+    w.f[1] = -fz * zy;
+    w.f[2] = fz;
+    // E = eps exp(-dz/sigma), grad dz = norm (-zx, -zy, 1):
+    // d^T H d = E/sigma^2 (grad dz . d)^2 + E/sigma norm (zxx dx^2 + 2 zxy dx dy + zyy dy^2)
+    const double gd = o.norm * (dir[2] - zx * dir[0] - zy * dir[1]);
+    w.curv = ex / (o.sigma * o.sigma) * gd * gd +
+             ex / o.sigma * o.norm * (zxx * dir[0] * dir[0] + 2.0 * zxy * dir[0] * dir[1] + zyy * dir[1] * dir[1]);
   }
   return w;
 }
@@ -110,6 +203,10 @@ __device__ __forceinline__ WallOut wall_eval(const Obst &o, int s_ix, int s_iy, 
 __device__ __forceinline__ float gap_estimate(const Obst &o, size_t site, const double r[3]) {
   if (o.kind == GFMD_OBST_MAP_EXP) {
     return (float)o.norm * ((float)r[2] - (float)(o.map[site] + o.map_z0));
+  }
+  if (o.kind == GFMD_OBST_MAP_BICUBIC) {
+    const float zm = map_bicubic_f(o.map, o.mnx, o.mny, (float)(r[0] / o.ax), (float)(r[1] / o.ay));
+    return o.fnorm * ((float)r[2] - (zm + o.fz0));
   }
   float dx = (float)(r[0] - o.cx), dy = (float)(r[1] - o.cy), dz = (float)(r[2] - o.cz);
   const float lx = (float)o.lx, ly = (float)o.ly;
@@ -122,6 +219,10 @@ __device__ __forceinline__ float gap_estimate(const Obst &o, size_t site, const 
 __device__ __forceinline__ float gap_estimate_f(const Obst &o, size_t site, const float r[3]) {
   if (o.kind == GFMD_OBST_MAP_EXP) {
     const float zm = o.mapf ? o.mapf[site] : (float)o.map[site];
+    return o.fnorm * (r[2] - (zm + o.fz0));
+  }
+  if (o.kind == GFMD_OBST_MAP_BICUBIC) {
+    const float zm = map_bicubic_f(o.map, o.mnx, o.mny, r[0] / o.fax, r[1] / o.fay);
     return o.fnorm * (r[2] - (zm + o.fz0));
   }
   float dx = r[0] - o.fcx, dy = r[1] - o.fcy, dz = r[2] - o.fcz;
@@ -142,6 +243,8 @@ inline Obst make_obst(const gfmd_obstacle_t *ob, const Geom &g) {
   o.sigma = ob->sigma;
   o.cutoff = ob->cutoff;
   o.map = ob->d_map;
+  o.mnx = g.nx;
+  o.mny = g.ny;
   o.map_z0 = ob->map_z0;
   o.norm = ob->norm == 0 ? 1 : ob->norm;
   o.fz_ext = ob->fz_ext;

@@ -526,9 +526,9 @@ int gfmd_minimize(gfmd_handle_t h, const gfmd_obstacle_t *obst, const gfmd_min_p
         prm->precond->precision != h->precision || prm->precond == h || prm->precond == prm->refine)
       return gfmd::set_error(GFMD_EINVAL, "gfmd_minimize: preconditioner does not match");
   }
-  if (obst && obst->kind == GFMD_OBST_MAP_EXP && !obst->d_map)
+  if (obst && (obst->kind == GFMD_OBST_MAP_EXP || obst->kind == GFMD_OBST_MAP_BICUBIC) && !obst->d_map)
     return gfmd::set_error(GFMD_EINVAL, "gfmd_minimize: map obstacle without a map");
-  if (obst && (obst->kind < GFMD_OBST_NONE || obst->kind > GFMD_OBST_MAP_EXP))
+  if (obst && (obst->kind < GFMD_OBST_NONE || obst->kind > GFMD_OBST_MAP_BICUBIC))
     return gfmd::set_error(GFMD_EINVAL, "gfmd_minimize: unknown obstacle kind");
   std::string err;
   auto t0 = std::chrono::steady_clock::now();
