@@ -18,6 +18,7 @@
 
 #include "gfmd_internal.h"
 #include "gfmd_obstacle.cuh"
+#include "gfmd_reduce.cuh"
 
 namespace gfmd {
 
@@ -138,59 +139,6 @@ __global__ void __launch_bounds__(kRedThreads) k_total_force(Obst o, Geom g, con
   block_reduce(acc, 2, true, part);
 }
 
-// FIRE, first half (FixFIRE::initial_integrate): v += dtf f, |v| per atom
-// limited to vlimit, u += dt v.
-__global__ void k_fire_first(Geom g, double *__restrict__ x, double *__restrict__ v,
-                             const double *__restrict__ f, double dt, double dtf, double vlimsq) {
-  const size_t N = (size_t)g.nx * g.ny;
-  const int nl = g.ndof / 3;
-  for (size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x; s < N; s += (size_t)gridDim.x * blockDim.x)
-    for (int l = 0; l < nl; l++) {
-      double vv[3], vsq = 0.0;
-      for (int c = 0; c < 3; c++) {
-        const size_t idx = (size_t)(3 * l + c) * N + s;
-        vv[c] = v[idx] + dtf * f[idx];
-        vsq += vv[c] * vv[c];
-      }
-      const double sc = (vlimsq > 0.0 && vsq > vlimsq) ? sqrt(vlimsq / vsq) : 1.0;
-      for (int c = 0; c < 3; c++) {
-        const size_t idx = (size_t)(3 * l + c) * N + s;
-        v[idx] = vv[c] * sc;
-        x[idx] += dt * v[idx];
-      }
-    }
-}
-
-// FIRE, second half (FixFIRE::final_integrate): v += dtf f, limit; sums
-// v.f, v.v, f.f.
-__global__ void __launch_bounds__(kRedThreads) k_fire_second(Geom g, double *__restrict__ v,
-                                                             const double *__restrict__ f,
-                                                             double dtf, double vlimsq,
-                                                             double *__restrict__ part) {
-  const size_t N = (size_t)g.nx * g.ny;
-  const int nl = g.ndof / 3;
-  double acc[3] = {0.0, 0.0, 0.0};
-  for (size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x; s < N; s += (size_t)gridDim.x * blockDim.x)
-    for (int l = 0; l < nl; l++) {
-      double vv[3], vsq = 0.0;
-      for (int c = 0; c < 3; c++) {
-        const size_t idx = (size_t)(3 * l + c) * N + s;
-        vv[c] = v[idx] + dtf * f[idx];
-        vsq += vv[c] * vv[c];
-      }
-      const double sc = (vlimsq > 0.0 && vsq > vlimsq) ? sqrt(vlimsq / vsq) : 1.0;
-      for (int c = 0; c < 3; c++) {
-        const size_t idx = (size_t)(3 * l + c) * N + s;
-        const double vn = vv[c] * sc;
-        v[idx] = vn;
-        acc[0] += vn * f[idx];
-        acc[1] += vn * vn;
-        acc[2] += f[idx] * f[idx];
-      }
-    }
-  block_reduce(acc, 3, false, part);
-}
-
 // v = a v + b f
 __global__ void k_axpby(size_t n, double *__restrict__ v, const double *__restrict__ f, double a,
                         double b) {
@@ -296,6 +244,264 @@ cudaError_t total_force(Work &w, gfmd_solver *hh, const Obst &o, const double *u
 }
 
 // ---- static: FIRE -----------------------------------------------------------
+// FixFIRE (src/cuda/fix_fire.cpp:117-297) with its scalar logic on the
+// device: one CUDA graph per phase, a prologue (v = 0 on the first phase,
+// the total force) and a WHILE loop whose body is
+//   k_fire_first   v += dt/2 f (|v| per atom limited), u += dt v
+//   F_el(u)        the handle's force evaluation
+//   k_fire_total   f = F_el + F_w, E_w, |f|^2, max|f_i| (last block)
+//   k_fire_second  v += dt/2 f (limited), v.f, v.v, f.f; the last block takes
+//                  FIRE's decision (P = v.f < 0: stop, dt *= decfac, mixing
+//                  reset; else mix v with f, and after minsteps positive steps
+//                  dt = min(incfac dt, dtmax), mixing *= mixdec), counts the
+//                  iteration and sets the loop condition
+//   k_fire_mix     v = 0, or v = (1 - mix) v + mix |v|/|f| f
+// No scalar returns to the host until the phase ends.  With a refine
+// handle, the FP32 phase also ends when max|f| has not halved for 500 steps
+// (FP32 forces stall at their noise level), and the FP64 phase continues
+// with the same velocities, step and mixing.
+namespace fire {
+
+using red::reduce_last;
+constexpr int kT = red::kT;
+
+struct Ctl {
+  double dt, mix, amix, help;  // step, mixing; mixing and |v|/|f| factor of this step
+  double fmax, f2, ew, best;   // max|f_i|, |f|^2, wall energy, last halving of max|f|
+  int cut, it, best_it;
+  int done;    // 0 running, 1 converged, 2 iteration cap, 3 non-finite, 4 stalled
+  int zero_v;  // this step's decision: stop (v = 0)
+  int evals;
+  unsigned int counter;
+};
+
+struct Par {
+  int minsteps, maxit, stall_check;
+  double incfac, decfac, mix_in, mixdec, max_dt, xlimit, ftol;
+};
+
+__device__ __forceinline__ double vlimsq(const Par &p, double dt) {
+  return p.xlimit > 0.0 ? (p.xlimit / dt) * (p.xlimit / dt) : 0.0;
+}
+
+__global__ void __launch_bounds__(kT) k_fire_first(Geom g, double *__restrict__ x, double *__restrict__ v,
+                                                    const double *__restrict__ f, Par p, const Ctl *ctl) {
+  const double dt = ctl->dt, dtf = 0.5 * dt, vl = vlimsq(p, dt);
+  const size_t N = (size_t)g.nx * g.ny;
+  const int nl = g.ndof / 3;
+  for (size_t s = blockIdx.x * (size_t)kT + threadIdx.x; s < N; s += (size_t)gridDim.x * kT)
+    for (int l = 0; l < nl; l++) {
+      double vv[3], vsq = 0.0;
+      for (int c = 0; c < 3; c++) {
+        const size_t idx = (size_t)(3 * l + c) * N + s;
+        vv[c] = v[idx] + dtf * f[idx];
+        vsq += vv[c] * vv[c];
+      }
+      const double sc = (vl > 0.0 && vsq > vl) ? sqrt(vl / vsq) : 1.0;
+      for (int c = 0; c < 3; c++) {
+        const size_t idx = (size_t)(3 * l + c) * N + s;
+        v[idx] = vv[c] * sc;
+        x[idx] += dt * v[idx];
+      }
+    }
+}
+
+// f = F_el + F_w (+ external load); with `check` (the prologue) the last
+// block also tests convergence and arms the loop.
+__global__ void __launch_bounds__(kT) k_fire_total(Obst o, Geom g, const double *__restrict__ x,
+                                                    const double *__restrict__ fel, double *__restrict__ ftot,
+                                                    double *__restrict__ part, Ctl *ctl, Par p, int check,
+                                                    cudaGraphConditionalHandle hc) {
+  const size_t N = (size_t)g.nx * g.ny;
+  const int nl = g.ndof / 3;
+  double ew = 0.0, f2 = 0.0, fm = 0.0;
+  for (size_t s = blockIdx.x * (size_t)kT + threadIdx.x; s < N; s += (size_t)gridDim.x * kT) {
+    for (int l = 0; l < nl; l++) {
+      double fw[3] = {0.0, 0.0, 0.0};
+      if (l < o.nlayer && o.kind != GFMD_OBST_NONE) {
+        double r[3], dir[3];
+        site_pos(o, g, s, l, x, N, 0.0, nullptr, r, dir);
+        const float ge = gap_estimate(o, s, r);
+        if (ge < (float)o.gcut + 0.01f * (float)o.gcut + 1e-3f) {
+          const WallOut w = wall_eval(o, (int)(s / g.ny), (int)(s % g.ny), s, r, dir);
+          fw[0] = w.f[0];
+          fw[1] = w.f[1];
+          fw[2] = w.f[2];
+          ew += w.e;
+        }
+      }
+      if (l < o.nlayer && o.fz_ext != 0.0) {
+        fw[2] += o.fz_ext;
+        ew -= o.fz_ext * x[(size_t)(3 * l + 2) * N + s];
+      }
+      for (int c = 0; c < 3; c++) {
+        const size_t idx = (size_t)(3 * l + c) * N + s;
+        const double f = fel[idx] + fw[c];
+        ftot[idx] = f;
+        f2 += f * f;
+        fm = fmax(fm, fabs(f));
+      }
+    }
+  }
+  const double acc[3] = {ew, f2, fm};
+  __shared__ double res[3];
+  if (!reduce_last<2, 1>(acc, part, &ctl->counter, res)) return;
+  if (threadIdx.x == 0) {
+    ctl->ew = res[0];
+    ctl->f2 = res[1];
+    ctl->fmax = res[2];
+    ctl->evals += 1;
+    if (check) {
+      ctl->best = res[2];
+      ctl->best_it = ctl->it;
+      if (!isfinite(res[2])) ctl->done = 3;
+      else if (res[2] <= p.ftol) ctl->done = 1;
+      else if (ctl->it >= p.maxit) ctl->done = 2;
+      else ctl->done = 0;
+      cudaGraphSetConditional(hc, ctl->done == 0 ? 1u : 0u);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kT) k_fire_second(Geom g, double *__restrict__ v, const double *__restrict__ f,
+                                                     double *__restrict__ part, Ctl *ctl, Par p,
+                                                     cudaGraphConditionalHandle hc) {
+  const double dt = ctl->dt, dtf = 0.5 * dt, vl = vlimsq(p, dt);
+  const size_t N = (size_t)g.nx * g.ny;
+  const int nl = g.ndof / 3;
+  double vf = 0.0, vv2 = 0.0, ff = 0.0;
+  for (size_t s = blockIdx.x * (size_t)kT + threadIdx.x; s < N; s += (size_t)gridDim.x * kT)
+    for (int l = 0; l < nl; l++) {
+      double vv[3], vsq = 0.0;
+      for (int c = 0; c < 3; c++) {
+        const size_t idx = (size_t)(3 * l + c) * N + s;
+        vv[c] = v[idx] + dtf * f[idx];
+        vsq += vv[c] * vv[c];
+      }
+      const double sc = (vl > 0.0 && vsq > vl) ? sqrt(vl / vsq) : 1.0;
+      for (int c = 0; c < 3; c++) {
+        const size_t idx = (size_t)(3 * l + c) * N + s;
+        const double vn = vv[c] * sc;
+        v[idx] = vn;
+        vf += vn * f[idx];
+        vv2 += vn * vn;
+        ff += f[idx] * f[idx];
+      }
+    }
+  const double acc[3] = {vf, vv2, ff};
+  __shared__ double res[3];
+  if (!reduce_last<3, 0>(acc, part, &ctl->counter, res)) return;
+  if (threadIdx.x == 0) {
+    const double P = res[0], vvs = res[1], ffs = res[2];
+    ctl->help = ffs > 0.0 ? ctl->mix * sqrt(vvs / ffs) : 0.0;
+    ctl->amix = ctl->mix;
+    if (P < 0.0) {
+      ctl->zero_v = 1;
+      ctl->cut = p.minsteps;
+      ctl->dt *= p.decfac;
+      ctl->mix = p.mix_in;
+    } else {
+      ctl->zero_v = 0;
+      if (ctl->cut < 0) {
+        ctl->dt = fmin(ctl->dt * p.incfac, p.max_dt);
+        ctl->mix *= p.mixdec;
+      } else {
+        ctl->cut -= 1;
+      }
+    }
+    ctl->it += 1;
+    const double fm = ctl->fmax;
+    if (fm < 0.5 * ctl->best) {
+      ctl->best = fm;
+      ctl->best_it = ctl->it;
+    }
+    if (!isfinite(fm)) ctl->done = 3;
+    else if (fm <= p.ftol) ctl->done = 1;
+    else if (p.stall_check && ctl->it - ctl->best_it >= 500) ctl->done = 4;
+    else if (ctl->it >= p.maxit) ctl->done = 2;
+    cudaGraphSetConditional(hc, ctl->done == 0 ? 1u : 0u);
+  }
+}
+
+__global__ void __launch_bounds__(kT) k_fire_mix(size_t n, double *__restrict__ v, const double *__restrict__ f,
+                                                  const Ctl *ctl) {
+  const bool stop = ctl->zero_v != 0;
+  const double a = 1.0 - ctl->amix, b = ctl->help;
+  for (size_t i = blockIdx.x * (size_t)kT + threadIdx.x; i < n; i += (size_t)gridDim.x * kT)
+    v[i] = stop ? 0.0 : a * v[i] + b * f[i];
+}
+
+}  // namespace fire
+
+// One FIRE phase on handle hh as a graph: prologue (total force, convergence
+// test) and WHILE(running) { FIRE step }.  Synchronizes its stream.
+cudaError_t fire_phase(gfmd_solver *hh, cudaStream_t st, const Obst &o, const fire::Par &p, double *u, double *v,
+                       double *fel, double *f, double *part, double *d_e, fire::Ctl *ctl, int nblk) {
+  using namespace fire;
+  const Geom &g = hh->g;
+  const size_t n = (size_t)g.ndof * g.nx * g.ny;
+  cudaGraph_t graph = nullptr, body = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraphConditionalHandle hc;
+  cudaError_t e = cudaGraphCreate(&graph, 0);
+  if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hc, graph, 0, cudaGraphCondAssignDefault);
+  auto eval = [&](cudaStream_t cs) {
+    cudaStream_t keep = hh->stream;
+    hh->stream = cs;
+    cudaError_t ee = enqueue_force_opts(hh, u, 0, fel, 0, d_e, true);
+    hh->stream = keep;
+    return ee;
+  };
+  if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(st, graph, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+  if (e == cudaSuccess) {
+    cudaError_t ec = eval(st);
+    if (ec == cudaSuccess) {
+      k_fire_total<<<nblk, kT, 0, st>>>(o, g, u, fel, f, part, ctl, p, 1, hc);
+      ec = cudaGetLastError();
+    }
+    cudaStreamCaptureStatus cs;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t nd = 0;
+    if (ec == cudaSuccess) ec = cudaStreamGetCaptureInfo(st, &cs, nullptr, nullptr, &deps, nullptr, &nd);
+    cudaGraphNodeParams cp = {};
+    cudaGraphNode_t node = nullptr;
+    if (ec == cudaSuccess) {
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = hc;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      ec = cudaGraphAddNode(&node, graph, deps, nullptr, nd, &cp);
+    }
+    if (ec == cudaSuccess) {
+      body = cp.conditional.phGraph_out[0];
+      ec = cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    }
+    cudaGraph_t got = nullptr;
+    e = cudaStreamEndCapture(st, &got);
+    if (ec != cudaSuccess) e = ec;
+  }
+  if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+  if (e == cudaSuccess) {
+    k_fire_first<<<nblk, kT, 0, st>>>(g, u, v, f, p, ctl);
+    cudaError_t ec = eval(st);
+    if (ec == cudaSuccess) {
+      k_fire_total<<<nblk, kT, 0, st>>>(o, g, u, fel, f, part, ctl, p, 0, hc);
+      k_fire_second<<<nblk, kT, 0, st>>>(g, v, f, part, ctl, p, hc);
+      k_fire_mix<<<nblk * 4, kT, 0, st>>>(n, v, f, ctl);
+      ec = cudaGetLastError();
+    }
+    cudaGraph_t got = nullptr;
+    e = cudaStreamEndCapture(st, &got);
+    if (ec != cudaSuccess) e = ec;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+  if (e == cudaSuccess) e = cudaGraphLaunch(exec, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  return e;
+}
+
 int fire_solve(gfmd_solver *hp, const gfmd_obstacle_t *ob, const gfmd_min_params_t *prm,
                double *u, gfmd_min_report_t *rep, std::string &err) {
   Work w;
@@ -304,79 +510,52 @@ int fire_solve(gfmd_solver *hp, const gfmd_obstacle_t *ob, const gfmd_min_params
   double *fel = w.bufs[0], *f = w.bufs[1], *v = w.bufs[2];
   const Obst o = make_obst(ob, hp->g);
   // FixFIRE defaults (src/cuda/fix_fire.cpp:63-69)
-  const int minsteps = prm->fire_minsteps > 0 ? prm->fire_minsteps : 10;
-  const double incfac = prm->fire_incfac > 0 ? prm->fire_incfac : 1.2;
-  const double decfac = prm->fire_decfac > 0 ? prm->fire_decfac : 0.5;
-  const double mix_in = prm->fire_mix > 0 ? prm->fire_mix : 0.1;
-  const double mixdec = prm->fire_mixdec > 0 ? prm->fire_mixdec : 0.99;
-  const double max_dt = prm->fire_dtmax > 0 ? prm->fire_dtmax : 0.001;
-  double dt = prm->fire_dt > 0 ? prm->fire_dt : max_dt;
-  const double xlimit = prm->fire_xlimit;
-  const int maxit = prm->maxiter > 0 ? prm->maxiter : 100000;
-  gfmd_solver *hh = hp;
-  ce = cudaMemsetAsync(v, 0, sizeof(double) * w.n, w.st);
-  double E = 0.0, fmax = 0.0, f2 = 0.0;
-  if (ce == cudaSuccess) ce = total_force(w, hh, o, u, fel, f, &E, &fmax, &f2);
-  int evals = 1, it = 0, cut = minsteps, status = GFMD_ENOTCONVERGED;
-  double mix = mix_in;
-  bool refining = false;
-  // With a refine handle the bulk phase also ends when max|f| has not halved
-  // for 500 steps: forces evaluated in FP32 stall at their noise level, which
-  // can sit above ftol.
-  double best = fmax;
-  int best_it = 0;
-  while (ce == cudaSuccess) {
-    if (!std::isfinite(fmax)) { status = GFMD_ENONFINITE; break; }
-    if (fmax < 0.5 * best) {
-      best = fmax;
-      best_it = it;
-    }
-    const bool stalled = prm->refine && !refining && it - best_it >= 500;
-    if (fmax <= prm->ftol || stalled) {
-      if (prm->refine && !refining) {
-        refining = true;
-        hh = prm->refine;
-        ce = total_force(w, hh, o, u, fel, f, &E, &fmax, &f2);
-        evals++;
-        if (ce != cudaSuccess || fmax <= prm->ftol) { status = GFMD_OK; break; }
-        continue;
-      }
-      status = GFMD_OK;
-      break;
-    }
-    if (it >= maxit) break;
-    const double dtf = 0.5 * dt;
-    const double vlimsq = xlimit > 0.0 ? (xlimit / dt) * (xlimit / dt) : 0.0;
-    k_fire_first<<<w.nblk, kRedThreads, 0, w.st>>>(hh->g, u, v, f, dt, dtf, vlimsq);
-    if ((ce = total_force(w, hh, o, u, fel, f, &E, &fmax, &f2)) != cudaSuccess) break;
-    evals++;
-    k_fire_second<<<w.nblk, kRedThreads, 0, w.st>>>(hh->g, v, f, dtf, vlimsq, w.part);
-    if ((ce = fetch(w, 3, false)) != cudaSuccess) break;
-    const double vf = w.hres[0], vv = w.hres[1], ff = w.hres[2];
-    const double help = ff > 0.0 ? mix * std::sqrt(vv / ff) : 0.0;
-    if (vf < 0.0) {
-      ce = cudaMemsetAsync(v, 0, sizeof(double) * w.n, w.st);
-      cut = minsteps;
-      dt *= decfac;
-      mix = mix_in;
-    } else {
-      k_axpby<<<w.nblk, kRedThreads, 0, w.st>>>(w.n, v, f, 1.0 - mix, help);
-      if (cut < 0) {
-        dt = std::min(dt * incfac, max_dt);
-        mix *= mixdec;
-      } else {
-        cut--;
-      }
-    }
-    it++;
+  fire::Par p{};
+  p.minsteps = prm->fire_minsteps > 0 ? prm->fire_minsteps : 10;
+  p.incfac = prm->fire_incfac > 0 ? prm->fire_incfac : 1.2;
+  p.decfac = prm->fire_decfac > 0 ? prm->fire_decfac : 0.5;
+  p.mix_in = prm->fire_mix > 0 ? prm->fire_mix : 0.1;
+  p.mixdec = prm->fire_mixdec > 0 ? prm->fire_mixdec : 0.99;
+  p.max_dt = prm->fire_dtmax > 0 ? prm->fire_dtmax : 0.001;
+  p.xlimit = prm->fire_xlimit;
+  p.maxit = prm->maxiter > 0 ? prm->maxiter : 100000;
+  p.ftol = prm->ftol;
+  p.stall_check = prm->refine ? 1 : 0;
+  fire::Ctl c{};
+  c.dt = prm->fire_dt > 0 ? prm->fire_dt : p.max_dt;
+  c.mix = p.mix_in;
+  c.cut = p.minsteps;
+  fire::Ctl *ctl = nullptr;
+  // control block and its last-block partials: after the Work's own
+  double *part = nullptr;
+  if (ce == cudaSuccess) ce = cudaMalloc((void **)&ctl, sizeof(fire::Ctl));
+  if (ce == cudaSuccess) ce = cudaMalloc((void **)&part, sizeof(double) * red::kQ * w.nblk);
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(ctl, &c, sizeof(c), cudaMemcpyHostToDevice, w.st);
+  if (ce == cudaSuccess) ce = cudaMemsetAsync(v, 0, sizeof(double) * w.n, w.st);
+  int status = GFMD_ENOTCONVERGED;
+  if (ce == cudaSuccess) ce = fire_phase(hp, w.st, o, p, u, v, fel, f, part, w.d_e, ctl, w.nblk);
+  if (ce == cudaSuccess) ce = cudaMemcpy(&c, ctl, sizeof(c), cudaMemcpyDeviceToHost);
+  if (ce == cudaSuccess && prm->refine && (c.done == 1 || c.done == 4)) {
+    // FP64 phase: same velocities, step and mixing
+    p.stall_check = 0;
+    c.done = 0;
+    ce = cudaMemcpyAsync(ctl, &c, sizeof(c), cudaMemcpyHostToDevice, w.st);
+    if (ce == cudaSuccess) ce = fire_phase(prm->refine, w.st, o, p, u, v, fel, f, part, w.d_e, ctl, w.nblk);
+    if (ce == cudaSuccess) ce = cudaMemcpy(&c, ctl, sizeof(c), cudaMemcpyDeviceToHost);
   }
+  double eel = 0.0;
+  if (ce == cudaSuccess) ce = cudaMemcpy(&eel, w.d_e, sizeof(double), cudaMemcpyDeviceToHost);
+  if (part) cudaFree(part);
+  if (ctl) cudaFree(ctl);
   if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return GFMD_ECUDA; }
+  if (c.done == 1) status = GFMD_OK;
+  else if (c.done == 3) status = GFMD_ENONFINITE;
   if (rep) {
-    rep->iterations = it;
-    rep->force_evals = evals;
-    rep->energy = E;
-    rep->fmax = fmax;
-    rep->fnorm = std::sqrt(f2);
+    rep->iterations = c.it;
+    rep->force_evals = c.evals;
+    rep->energy = eel + c.ew;
+    rep->fmax = c.fmax;
+    rep->fnorm = std::sqrt(c.f2);
   }
   if (status == GFMD_ENOTCONVERGED) err = "FIRE reached the iteration cap before max|f| <= ftol";
   if (status == GFMD_ENONFINITE) err = "non-finite force during FIRE";
