@@ -526,8 +526,16 @@ int fire_solve(gfmd_solver *hp, const gfmd_obstacle_t *ob, const gfmd_min_params
   c.mix = p.mix_in;
   c.cut = p.minsteps;
   fire::Ctl *ctl = nullptr;
-  // control block and its last-block partials: after the Work's own
-  double *part = nullptr;
+  double *part = nullptr;  // last-block partials
+  // the phases are captured on a stream of their own (the handle's may be
+  // the legacy default stream, which cannot be captured), ordered after it
+  cudaStream_t gs = nullptr;
+  cudaEvent_t ev = nullptr;
+  if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&gs, cudaStreamNonBlocking);
+  if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+  if (ce == cudaSuccess) ce = cudaEventRecord(ev, w.st);
+  if (ce == cudaSuccess) ce = cudaStreamWaitEvent(gs, ev, 0);
+  w.st = gs;
   if (ce == cudaSuccess) ce = cudaMalloc((void **)&ctl, sizeof(fire::Ctl));
   if (ce == cudaSuccess) ce = cudaMalloc((void **)&part, sizeof(double) * red::kQ * w.nblk);
   if (ce == cudaSuccess) ce = cudaMemcpyAsync(ctl, &c, sizeof(c), cudaMemcpyHostToDevice, w.st);
@@ -545,8 +553,11 @@ int fire_solve(gfmd_solver *hp, const gfmd_obstacle_t *ob, const gfmd_min_params
   }
   double eel = 0.0;
   if (ce == cudaSuccess) ce = cudaMemcpy(&eel, w.d_e, sizeof(double), cudaMemcpyDeviceToHost);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(gs);
   if (part) cudaFree(part);
   if (ctl) cudaFree(ctl);
+  if (ev) cudaEventDestroy(ev);
+  if (gs) cudaStreamDestroy(gs);
   if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return GFMD_ECUDA; }
   if (c.done == 1) status = GFMD_OK;
   else if (c.done == 3) status = GFMD_ENONFINITE;
