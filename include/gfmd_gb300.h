@@ -158,7 +158,8 @@ int gfmd_kernel_plan(gfmd_handle_t h, int *row_warp_tma, int *col_cluster, int *
                                   evaluated at the atom's displaced (x, y) (map pixel
                                   (i, j) at (i lattice[0], j lattice[1])), and the
                                   lateral force -f_z dz/dx, -f_z dz/dy
-                                  (fix_wall_map.cpp:686-817, 1381) */
+                                  (fix_wall_map.cpp:686-817, 1381); with GFMD_MIN_CG
+                                  and gfmd_obstacle_force */
 
 typedef struct {
   int kind;

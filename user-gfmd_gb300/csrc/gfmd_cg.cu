@@ -147,7 +147,7 @@ __device__ __forceinline__ void set_loop(cudaGraphConditionalHandle hc, int use,
 }
 
 // ---- restart: g = f_el + F_w(u), h = g; arms the loop ---------------------
-template <typename Tx, typename Tv>
+template <typename Tx, typename Tv, bool BIC = false>
 __global__ void __launch_bounds__(kT, 4) k_restart(Obst o, Geom gm, const Tx *__restrict__ x,
                                                  const Tx *__restrict__ fel, Tv *__restrict__ g,
                                                  Tv *__restrict__ h, unsigned char *__restrict__ active,
@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(kT, 4) k_restart(Obst o, Geom gm, const Tx *__
         if (wall_near(o, ge)) {
           double r[3], d[3];
           atom_pos<Tx, Tv>(o, ix, iy, l, x, nullptr, N, s, 0.0, r, d);
-          const WallOut w = wall_eval(o, ix, iy, s, r, d);
+          const WallOut w = wall_eval<BIC>(o, ix, iy, s, r, d);
           fw[0] = w.f[0];
           fw[1] = w.f[1];
           fw[2] = w.f[2];
@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(kT, 4) k_restart(Obst o, Geom gm, const Tx *__
 }
 
 // ---- along the direction: h.K.h, g.h, wall curvature, first Newton step ----
-template <typename Tx, typename Tv>
+template <typename Tx, typename Tv, bool BIC = false>
 __global__ void __launch_bounds__(kT) k_dirforce(Obst o, Geom gm, const Tx *__restrict__ x,
                                                   const Tv *__restrict__ fKh, const Tv *__restrict__ h,
                                                   const Tv *__restrict__ g,
@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(kT) k_dirforce(Obst o, Geom gm, const Tx *__re
       for (int l = 0; l < o.nlayer; l++) {
         double r[3], d[3];
         atom_pos<Tx, Tv>(o, ix, iy, l, x, h, N, s, 0.0, r, d);
-        const WallOut w = wall_eval(o, ix, iy, s, r, d);
+        const WallOut w = wall_eval<BIC>(o, ix, iy, s, r, d);
         cw += w.curv;
         fw0h += w.f[0] * d[0] + w.f[1] * d[1] + w.f[2] * d[2];
       }
@@ -325,7 +325,7 @@ __device__ __forceinline__ void probe_step(CgCtl *ctl, double a, double dfh, dou
 // ---- one Newton probe of the line search at u + a h ------------------------
 // gdir(a) = g.h - a hKh + sum F_w(u + a h).h - F_w(u).h   (= -phi'(a))
 // curv(a) = hKh + sum h^T H_w(u + a h) h                   (=  phi''(a))
-template <typename Tx, typename Tv>
+template <typename Tx, typename Tv, bool BIC = false>
 __global__ void __launch_bounds__(kT) k_probe(Obst o, Geom gm, const Tx *__restrict__ x,
                                                const Tv *__restrict__ h,
                                                const unsigned char *__restrict__ active,
@@ -354,7 +354,7 @@ __global__ void __launch_bounds__(kT) k_probe(Obst o, Geom gm, const Tx *__restr
     for (int l = 0; l < o.nlayer; l++) {
       double r[3], d[3];
       atom_pos<Tx, Tv>(o, ix, iy, l, x, h, N, s, a, r, d);
-      const WallOut w1 = wall_eval(o, ix, iy, s, r, d);
+      const WallOut w1 = wall_eval<BIC>(o, ix, iy, s, r, d);
       dfh += w1.f[0] * d[0] + w1.f[1] * d[1] + w1.f[2] * d[2];
       cw += w1.curv;
     }
@@ -370,7 +370,7 @@ __global__ void __launch_bounds__(kT) k_probe(Obst o, Geom gm, const Tx *__restr
 // updated through the linearity of F_el, so f_el itself is not stored, and
 // the rounding of the FP32 state is relative to the (small) gradient rather
 // than to the elastic force.
-template <typename Tx, typename Tv>
+template <typename Tx, typename Tv, bool BIC = false>
 __device__ __forceinline__ void wall_at(const Obst &o, int ix, int iy, int l, size_t s, const Tx xv[3],
                                         WallOut &w) {
   const double zero[3] = {0.0, 0.0, 0.0};
@@ -379,7 +379,7 @@ __device__ __forceinline__ void wall_at(const Obst &o, int ix, int iy, int l, si
   for (int c = 0; c < 3; c++) r[c] = (double)xv[c] + o.off[l][c];
   r[0] += ix * o.ax;
   r[1] += iy * o.ay;
-  w = wall_eval(o, ix, iy, s, r, zero);
+  w = wall_eval<BIC>(o, ix, iy, s, r, zero);
 }
 
 // Near the obstacle: g_new = g_old + a fKh + F_w(x_new) - F_w(x_old) in FP64,
@@ -388,12 +388,12 @@ __device__ __forceinline__ void wall_at(const Obst &o, int ix, int iy, int l, si
 template <typename T> struct V3 { T v[3]; };
 template <typename Tv> struct WallDelta { double e; Tv g[3]; };
 
-template <typename Tx, typename Tv>
+template <typename Tx, typename Tv, bool BIC = false>
 __device__ __noinline__ WallDelta<Tv> wall_delta(const Obst &o, int ix, int iy, int l, int s, V3<Tx> xv,
                                                  V3<Tx> xn, V3<Tv> go, V3<Tv> fk, double a) {
   WallOut w1, w0;
-  wall_at<Tx, Tv>(o, ix, iy, l, s, xn.v, w1);
-  wall_at<Tx, Tv>(o, ix, iy, l, s, xv.v, w0);
+  wall_at<Tx, Tv, BIC>(o, ix, iy, l, s, xn.v, w1);
+  wall_at<Tx, Tv, BIC>(o, ix, iy, l, s, xv.v, w0);
   WallDelta<Tv> r;
   r.e = w1.e;
   for (int c = 0; c < 3; c++) r.g[c] = (Tv)((double)go.v[c] + a * (double)fk.v[c] + (w1.f[c] - w0.f[c]));
@@ -410,7 +410,7 @@ __device__ __forceinline__ float gap_reg(const Obst &o, int ix, int iy, int l, s
   return gap_estimate_f(o, s, r);
 }
 
-template <typename Tx, typename Tv>
+template <typename Tx, typename Tv, bool BIC = false>
 __global__ void __launch_bounds__(kT, 4) k_update(Obst o, Geom gm, Tx *__restrict__ x,
                                                    const Tv *__restrict__ h, const Tv *__restrict__ fKh,
                                                    Tv *__restrict__ g, Tv *__restrict__ gp,
@@ -460,7 +460,7 @@ __global__ void __launch_bounds__(kT, 4) k_update(Obst o, Geom gm, Tx *__restric
         const float ge_old = gap_reg(o, ix, iy, l, s, xv);
         if (ge_new < o.fgate_active) nearflag = true;
         if (ge_new < o.fgate_wall || ge_old < o.fgate_wall) {
-          const WallDelta<Tv> wd = wall_delta<Tx, Tv>(o, ix, iy, l, s, V3<Tx>{{xv[0], xv[1], xv[2]}},
+          const WallDelta<Tv> wd = wall_delta<Tx, Tv, BIC>(o, ix, iy, l, s, V3<Tx>{{xv[0], xv[1], xv[2]}},
                                                       V3<Tx>{{xn[0], xn[1], xn[2]}},
                                                       V3<Tv>{{go[0], go[1], go[2]}},
                                                       V3<Tv>{{fk[0], fk[1], fk[2]}}, ad);
@@ -549,7 +549,7 @@ template <> struct Vec4<double> {
   }
 };
 
-template <typename Tx, typename Tv>
+template <typename Tx, typename Tv, bool BIC = false>
 __global__ void __launch_bounds__(kT, 2) k_update4(Obst o, Geom gm, Tx *__restrict__ x,
                                                     const Tv *__restrict__ h, const Tv *__restrict__ fKh,
                                                     Tv *__restrict__ g, Tv *__restrict__ gp,
@@ -602,7 +602,7 @@ __global__ void __launch_bounds__(kT, 2) k_update4(Obst o, Geom gm, Tx *__restri
             const float ge_old = gap_reg(o, ix, iy, l, s, xo3);
             if (ge_new < o.fgate_active) nearflag[j] = true;
             if (ge_new < o.fgate_wall || ge_old < o.fgate_wall) {
-              const WallDelta<Tv> wd = wall_delta<Tx, Tv>(o, ix, iy, l, s, V3<Tx>{{xo3[0], xo3[1], xo3[2]}},
+              const WallDelta<Tv> wd = wall_delta<Tx, Tv, BIC>(o, ix, iy, l, s, V3<Tx>{{xo3[0], xo3[1], xo3[2]}},
                                                           V3<Tx>{{xn3[0], xn3[1], xn3[2]}},
                                                           V3<Tv>{{go[0][j], go[1][j], go[2][j]}},
                                                           V3<Tv>{{fk[0][j], fk[1][j], fk[2][j]}}, ad);
@@ -664,7 +664,7 @@ __global__ void __launch_bounds__(kT, 2) k_update4(Obst o, Geom gm, Tx *__restri
 // Wall curvature along h and F_w.h of one site at a = 0 (out of line: only
 // sites near the obstacle take it, and its FP64 registers stay out of the
 // streaming loop).
-template <typename Tx, typename Tv>
+template <typename Tx, typename Tv, bool BIC = false>
 __device__ __noinline__ double2 wall_dir_site(Obst o, Geom gm, const Tx *__restrict__ x, const Tv *__restrict__ h,
                                               int s) {
   const int N = gm.nx * gm.ny;
@@ -673,14 +673,14 @@ __device__ __noinline__ double2 wall_dir_site(Obst o, Geom gm, const Tx *__restr
   for (int l = 0; l < o.nlayer; l++) {
     double r[3], d[3];
     atom_pos<Tx, Tv>(o, ix, iy, l, x, h, N, s, 0.0, r, d);
-    const WallOut w = wall_eval(o, ix, iy, s, r, d);
+    const WallOut w = wall_eval<BIC>(o, ix, iy, s, r, d);
     cw += w.curv;
     fh += w.f[0] * d[0] + w.f[1] * d[1] + w.f[2] * d[2];
   }
   return make_double2(cw, fh);
 }
 
-template <typename Tx, typename Tv>
+template <typename Tx, typename Tv, bool BIC = false>
 __global__ void __launch_bounds__(kT, 4) k_dirforce4(Obst o, Geom gm, const Tx *__restrict__ x,
                                                       const Tv *__restrict__ fKh, const Tv *__restrict__ h,
                                                       const Tv *__restrict__ g,
@@ -728,7 +728,7 @@ __global__ void __launch_bounds__(kT, 4) k_dirforce4(Obst o, Geom gm, const Tx *
         cw += cwf;
         fw0h += fhf;
       } else {
-        const double2 w = wall_dir_site<Tx, Tv>(o, gm, x, h, s);
+        const double2 w = wall_dir_site<Tx, Tv, BIC>(o, gm, x, h, s);
         cw += w.x;
         fw0h += w.y;
       }
@@ -838,6 +838,7 @@ __global__ void k_gate(const CgCtl *ctl, cudaGraphConditionalHandle hif) {
 
 // Final report from FP64 elastic forces fel of u: total force
 // f = fel + F_w(u) + external; sums: E_w + E_ext, |f|^2; max |f_i|.
+template <bool BIC = false>
 __global__ void __launch_bounds__(kT) k_report(Obst o, Geom gm, const double *__restrict__ x,
                                                 const double *__restrict__ fel, double *__restrict__ part,
                                                 CgCtl *ctl, double *__restrict__ out) {
@@ -853,7 +854,7 @@ __global__ void __launch_bounds__(kT) k_report(Obst o, Geom gm, const double *__
             (o.kind != GFMD_OBST_NONE && wall_near(o, gap_of(o, ix, iy, l, x, N, s)))) {
           double r[3], d[3];
           atom_pos<double, double>(o, ix, iy, l, x, nullptr, N, s, 0.0, r, d);
-          const WallOut w = wall_eval(o, ix, iy, s, r, d);
+          const WallOut w = wall_eval<BIC>(o, ix, iy, s, r, d);
           fw[0] = w.f[0];
           fw[1] = w.f[1];
           fw[2] = w.f[2];
@@ -1009,7 +1010,7 @@ cudaError_t add_cond(cudaStream_t st, cudaGraph_t top, cudaGraphConditionalHandl
 
 // Restart of one item on stream st: fresh F_el(u), g = f_el + F_w + f_ext,
 // h = g; arms the item's loop through hwh when use_hc.
-template <typename Tx, typename Tv>
+template <typename Tx, typename Tv, bool BIC = false>
 cudaError_t enqueue_restart(Item &it, bool refine, cudaStream_t st, cudaGraphConditionalHandle hwh, int use_hc) {
   CgBufs &b = it.b;
   gfmd_solver *hr = refine ? it.hr64 : it.hp;
@@ -1018,7 +1019,7 @@ cudaError_t enqueue_restart(Item &it, bool refine, cudaStream_t st, cudaGraphCon
   Tv *g = reinterpret_cast<Tv *>(b.g), *h = reinterpret_cast<Tv *>(b.h);
   RT_CHECK(cudaMemsetAsync(&b.ctl->counter, 0, sizeof(unsigned int), st));
   RT_CHECK(eval_on(hr, st, x, io_type<Tx>(), fel, io_type<Tx>(), b.d_e, true));
-  k_restart<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, it.hp->g, x, fel, g, h, b.active, b.part, b.ctl, hwh, use_hc);
+  k_restart<Tx, Tv, BIC><<<b.nblk, kT, 0, st>>>(it.o, it.hp->g, x, fel, g, h, b.active, b.part, b.ctl, hwh, use_hc);
   if (it.hpre) {
     Tv *mz = reinterpret_cast<Tv *>(b.mz);
     RT_CHECK(eval_on(it.hpre, st, g, io_type<Tv>(), mz, io_type<Tv>(), b.d_e, false));
@@ -1028,7 +1029,7 @@ cudaError_t enqueue_restart(Item &it, bool refine, cudaStream_t st, cudaGraphCon
 }
 
 // One CG iteration of one item on stream st.
-template <typename Tx, typename Tv>
+template <typename Tx, typename Tv, bool BIC = false>
 cudaError_t enqueue_iteration(Item &it, cudaStream_t st, cudaGraphConditionalHandle hwh, int use_hc) {
   CgBufs &b = it.b;
   gfmd_solver *hd = it.hp;
@@ -1042,15 +1043,15 @@ cudaError_t enqueue_iteration(Item &it, cudaStream_t st, cudaGraphConditionalHan
   const size_t nsite = (size_t)gm.nx * gm.ny;
   const int sms = it.hp->sm_count;
   if (v4)
-    k_dirforce4<Tx, Tv><<<grid_for(k_dirforce4<Tx, Tv>, sms, nsite, 4 * kT), kT, 0, st>>>(it.o, gm, x, fKh, h, g,
+    k_dirforce4<Tx, Tv, BIC><<<grid_for(k_dirforce4<Tx, Tv, BIC>, sms, nsite, 4 * kT), kT, 0, st>>>(it.o, gm, x, fKh, h, g,
                                                                                            b.active, b.part, b.ctl);
-  else k_dirforce<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, gm, x, fKh, h, g, b.active, b.part, b.ctl);
+  else k_dirforce<Tx, Tv, BIC><<<b.nblk, kT, 0, st>>>(it.o, gm, x, fKh, h, g, b.active, b.part, b.ctl);
   if (it.o.kind != GFMD_OBST_NONE)
-    for (int p = 0; p < kLsMax; p++) k_probe<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, gm, x, h, b.active, b.part, b.ctl);
+    for (int p = 0; p < kLsMax; p++) k_probe<Tx, Tv, BIC><<<b.nblk, kT, 0, st>>>(it.o, gm, x, h, b.active, b.part, b.ctl);
   if (v4)
-    k_update4<Tx, Tv><<<grid_for(k_update4<Tx, Tv>, sms, nsite, 4 * kT), kT, 0, st>>>(
+    k_update4<Tx, Tv, BIC><<<grid_for(k_update4<Tx, Tv, BIC>, sms, nsite, 4 * kT), kT, 0, st>>>(
         it.o, gm, x, h, fKh, g, gp, b.active, b.part, b.ctl, hwh, use_hc);
-  else k_update<Tx, Tv><<<b.nblk, kT, 0, st>>>(it.o, gm, x, h, fKh, g, gp, b.active, b.part, b.ctl, hwh, use_hc);
+  else k_update<Tx, Tv, BIC><<<b.nblk, kT, 0, st>>>(it.o, gm, x, h, fKh, g, gp, b.active, b.part, b.ctl, hwh, use_hc);
   if (it.hpre) {
     Tv *mz = reinterpret_cast<Tv *>(b.mz);
     RT_CHECK(eval_on(it.hpre, st, g, io_type<Tv>(), mz, io_type<Tv>(), b.d_e, false));
@@ -1100,12 +1101,14 @@ cudaError_t build_phase(std::vector<Item *> &its, bool refine, cudaStream_t ms, 
   for (size_t i = 0; i < n; i++) {
     cudaStream_t st = its[i]->b.cs;
     RT_CHECK(cudaStreamBeginCaptureToGraph(st, bif[i], nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-    e = enqueue_restart<Tx, Tv>(*its[i], refine, st, hwh[i], 1);
+    e = its[i]->o.kind == GFMD_OBST_MAP_BICUBIC ? enqueue_restart<Tx, Tv, true>(*its[i], refine, st, hwh[i], 1)
+                                                : enqueue_restart<Tx, Tv>(*its[i], refine, st, hwh[i], 1);
     e2 = cudaStreamEndCapture(st, &got);
     if (e == cudaSuccess) e = e2;
     if (e != cudaSuccess) return e;
     RT_CHECK(cudaStreamBeginCaptureToGraph(st, bwh[i], nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-    e = enqueue_iteration<Tx, Tv>(*its[i], st, hwh[i], 1);
+    e = its[i]->o.kind == GFMD_OBST_MAP_BICUBIC ? enqueue_iteration<Tx, Tv, true>(*its[i], st, hwh[i], 1)
+                                                : enqueue_iteration<Tx, Tv>(*its[i], st, hwh[i], 1);
     e2 = cudaStreamEndCapture(st, &got);
     if (e == cudaSuccess) e = e2;
     if (e != cudaSuccess) return e;
@@ -1134,11 +1137,13 @@ cudaError_t run_launch_direct(std::vector<Item *> &its, bool refine, cudaStream_
     RT_CHECK(cudaMemcpyAsync(&c, it->b.ctl, sizeof(CgCtl), cudaMemcpyDeviceToHost, ms));
     RT_CHECK(cudaStreamSynchronize(ms));
     if (c.parked) continue;
-    RT_CHECK((enqueue_restart<Tx, Tv>(*it, refine, ms, none, 0)));
+    RT_CHECK((it->o.kind == GFMD_OBST_MAP_BICUBIC ? enqueue_restart<Tx, Tv, true>(*it, refine, ms, none, 0)
+                                                  : enqueue_restart<Tx, Tv>(*it, refine, ms, none, 0)));
     RT_CHECK(cudaMemcpyAsync(&c, it->b.ctl, sizeof(CgCtl), cudaMemcpyDeviceToHost, ms));
     RT_CHECK(cudaStreamSynchronize(ms));
     while (c.done == 0 && c.since < c.recompute) {
-      RT_CHECK((enqueue_iteration<Tx, Tv>(*it, ms, none, 0)));
+      RT_CHECK((it->o.kind == GFMD_OBST_MAP_BICUBIC ? enqueue_iteration<Tx, Tv, true>(*it, ms, none, 0)
+                                                    : enqueue_iteration<Tx, Tv>(*it, ms, none, 0)));
       RT_CHECK(cudaMemcpyAsync(&c, it->b.ctl, sizeof(CgCtl), cudaMemcpyDeviceToHost, ms));
       RT_CHECK(cudaStreamSynchronize(ms));
     }
@@ -1300,7 +1305,10 @@ int solve_batch(std::vector<Item *> &its, const gfmd_min_params_t *prm, cudaStre
     ce = cudaMemsetAsync(&it->b.ctl->counter, 0, sizeof(unsigned int), ms);
     if (ce == cudaSuccess) ce = eval_on(hh, ms, it->u, 0, fel, 0, it->b.d_e, true);
     if (ce == cudaSuccess) {
-      k_report<<<it->b.nblk, kT, 0, ms>>>(it->o, hh->g, it->u, fel, it->b.part, it->b.ctl, it->b.d_e + 1);
+      if (it->o.kind == GFMD_OBST_MAP_BICUBIC)
+        k_report<true><<<it->b.nblk, kT, 0, ms>>>(it->o, hh->g, it->u, fel, it->b.part, it->b.ctl, it->b.d_e + 1);
+      else
+        k_report<<<it->b.nblk, kT, 0, ms>>>(it->o, hh->g, it->u, fel, it->b.part, it->b.ctl, it->b.d_e + 1);
       ce = cudaGetLastError();
     }
   }

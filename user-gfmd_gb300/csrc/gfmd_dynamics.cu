@@ -311,6 +311,9 @@ extern "C" int gfmd_run_dynamics(gfmd_handle_t h, const gfmd_obstacle_t *obst, d
     return set_error(GFMD_EINVAL, "gfmd_run_dynamics: map obstacle without a map");
   if (obst && (obst->kind < GFMD_OBST_NONE || obst->kind > GFMD_OBST_MAP_BICUBIC))
     return set_error(GFMD_EINVAL, "gfmd_run_dynamics: unknown obstacle kind");
+  if (obst && obst->kind == GFMD_OBST_MAP_BICUBIC)
+    return set_error(GFMD_EINVAL, "gfmd_run_dynamics: the bicubic map wall is offered by gfmd_minimize (CG) "
+                                  "and gfmd_obstacle_force; use GFMD_OBST_MAP_EXP here");
   const auto t0 = std::chrono::steady_clock::now();
   const Obst o = make_obst(obst, h->g);
   double last[5] = {0, 0, 0, 0, 0};

@@ -105,36 +105,17 @@ __device__ __forceinline__ MapBicubic map_bicubic(const double *m, int nx, int n
     }
   return r;
 }
-// Value only, FP32 (gating estimates).
-__device__ __forceinline__ float map_bicubic_f(const double *m, int nx, int ny, float x, float y) {
-  const float fx = floorf(x), fy = floorf(y);
-  const int i0 = (int)fx, j0 = (int)fy;
-  const float t = x - fx, u = y - fy;
-  const float t2 = t * t, t3 = t2 * t, u2 = u * u, u3 = u2 * u;
-  const float hx[4] = {2 * t3 - 3 * t2 + 1, -2 * t3 + 3 * t2, t3 - 2 * t2 + t, t3 - t2};
-  const float hy[4] = {2 * u3 - 3 * u2 + 1, -2 * u3 + 3 * u2, u3 - 2 * u2 + u, u3 - u2};
-  float z = 0.0f;
-#pragma unroll
-  for (int a = 0; a < 2; a++)
-#pragma unroll
-    for (int b = 0; b < 2; b++) {
-      const float f = (float)map_at(m, nx, ny, i0 + a, j0 + b);
-      const float fxs =
-          0.5f * (float)(map_at(m, nx, ny, i0 + a + 1, j0 + b) - map_at(m, nx, ny, i0 + a - 1, j0 + b));
-      const float fys =
-          0.5f * (float)(map_at(m, nx, ny, i0 + a, j0 + b + 1) - map_at(m, nx, ny, i0 + a, j0 + b - 1));
-      z += f * hx[a] * hy[b] + fxs * hx[2 + a] * hy[b] + fys * hx[a] * hy[2 + b];
-    }
-  return z;
-}
-
 struct WallOut {
   double e;        // energy
   double f[3];     // force on the atom
   double curv;     // h^T (d2E/dr2) h for the given direction
 };
 
-// Obstacle energy, force and curvature along dir at position r.
+// Obstacle energy, force and curvature along dir at position r.  The
+// bicubic map wall is compiled in only with BIC = true: its code would raise
+// the register count of every kernel that evaluates walls, so only the
+// kernels of the paths that offer it (CG, gfmd_obstacle_force) carry it.
+template <bool BIC = false>
 __device__ __forceinline__ WallOut wall_eval(const Obst &o, int s_ix, int s_iy, size_t site,
                                              const double r[3], const double dir[3]) {
   WallOut w{0.0, {0.0, 0.0, 0.0}, 0.0};
@@ -176,7 +157,7 @@ __device__ __forceinline__ WallOut wall_eval(const Obst &o, int s_ix, int s_iy, 
     w.e = ex - o.offset;
     w.f[2] = o.norm * ex / o.sigma;
     w.curv = ex / (o.sigma * o.sigma) * dir[2] * dir[2];
-  } else if (o.kind == GFMD_OBST_MAP_BICUBIC) {
+  } else if (BIC && o.kind == GFMD_OBST_MAP_BICUBIC) {
     // map pixel (i, j) sits at (i ax, j ay): evaluate at the displaced position
     const MapBicubic mb = map_bicubic(o.map, o.mnx, o.mny, r[0] / o.ax, r[1] / o.ay);
     const double zx = mb.zx / o.ax, zy = mb.zy / o.ay;
@@ -204,10 +185,7 @@ __device__ __forceinline__ float gap_estimate(const Obst &o, size_t site, const 
   if (o.kind == GFMD_OBST_MAP_EXP) {
     return (float)o.norm * ((float)r[2] - (float)(o.map[site] + o.map_z0));
   }
-  if (o.kind == GFMD_OBST_MAP_BICUBIC) {
-    const float zm = map_bicubic_f(o.map, o.mnx, o.mny, (float)(r[0] / o.ax), (float)(r[1] / o.ay));
-    return o.fnorm * ((float)r[2] - (zm + o.fz0));
-  }
+  if (o.kind == GFMD_OBST_MAP_BICUBIC) return -1e30f;  // no gating: every site is evaluated
   float dx = (float)(r[0] - o.cx), dy = (float)(r[1] - o.cy), dz = (float)(r[2] - o.cz);
   const float lx = (float)o.lx, ly = (float)o.ly;
   dx -= lx * rintf(dx / lx);
@@ -221,10 +199,7 @@ __device__ __forceinline__ float gap_estimate_f(const Obst &o, size_t site, cons
     const float zm = o.mapf ? o.mapf[site] : (float)o.map[site];
     return o.fnorm * (r[2] - (zm + o.fz0));
   }
-  if (o.kind == GFMD_OBST_MAP_BICUBIC) {
-    const float zm = map_bicubic_f(o.map, o.mnx, o.mny, r[0] / o.fax, r[1] / o.fay);
-    return o.fnorm * (r[2] - (zm + o.fz0));
-  }
+  if (o.kind == GFMD_OBST_MAP_BICUBIC) return -1e30f;  // no gating: every site is evaluated
   float dx = r[0] - o.fcx, dy = r[1] - o.fcy, dz = r[2] - o.fcz;
   dx -= o.flx * rintf(dx / o.flx);
   dy -= o.fly * rintf(dy / o.fly);

@@ -720,6 +720,8 @@ int gfmd_minimize(gfmd_handle_t h, const gfmd_obstacle_t *obst, const gfmd_min_p
     return gfmd::set_error(GFMD_EINVAL, "gfmd_minimize: map obstacle without a map");
   if (obst && (obst->kind < GFMD_OBST_NONE || obst->kind > GFMD_OBST_MAP_BICUBIC))
     return gfmd::set_error(GFMD_EINVAL, "gfmd_minimize: unknown obstacle kind");
+  if (obst && obst->kind == GFMD_OBST_MAP_BICUBIC && prm && prm->method != GFMD_MIN_CG)
+    return gfmd::set_error(GFMD_EINVAL, "gfmd_minimize: the bicubic map wall runs with GFMD_MIN_CG");
   std::string err;
   auto t0 = std::chrono::steady_clock::now();
   int rc;

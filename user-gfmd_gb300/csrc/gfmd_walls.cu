@@ -37,7 +37,7 @@ __global__ void __launch_bounds__(kT) k_obstacle_force(Obst o, Geom g, const dou
         for (int c = 0; c < 3; c++) r[c] = u[(size_t)(3 * l + c) * N + s] + o.off[l][c];
         r[0] += ix * o.ax;
         r[1] += iy * o.ay;
-        const WallOut w = wall_eval(o, ix, iy, s, r, zero);
+        const WallOut w = wall_eval<true>(o, ix, iy, s, r, zero);
         e += w.e;
         for (int c = 0; c < 3; c++) fw[c] = w.f[c];
       }
