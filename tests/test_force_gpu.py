@@ -245,3 +245,38 @@ def test_fp32_kernel_plan_and_earlier_kernels_agree(args, nx, ny, rows, cl, monk
     (fa, ea), (fb, eb) = outs
     assert float((fa - fb).norm() / fb.norm()) <= FP32_TOL
     assert abs(ea - eb) <= FP32_TOL * abs(eb)
+
+
+@pytest.mark.parametrize(
+    "args,nx,ny,plain",
+    [
+        ("ft fcc100 1.0 1 pair-potential 1 1.0 height 128", 2048, 2048, False),
+        ("ft fcc100 1.0 2 pair-potential 1 1.0 height 64", 256, 256, False),
+        ("ft sc100 1 1.0 pair-potential 2 1.0 1.0 height 128", 48, 40, False),
+        ("ft fcc100 1.0 2 pair-potential 1 1.0 height 64", 128, 64, True),
+    ],
+)
+def test_energy_of_a_direction_is_half_its_stiffness_product(args, nx, ny, plain, monkeypatch):
+    """The CG line search takes h.K.h = 2 E(h) from the energy of the
+    direction's force evaluation (gamma-point force off): E(h) must equal
+    -h.F(h) / 2 in both precisions and on every evaluation path."""
+    g = gfmd_pkg()
+    k = g.StiffnessKernel(args)
+    d = k.get_dimension()
+    half, linf = k.phi_table(nx, ny, "half")
+    zero = np.zeros_like(np.asarray(linf, dtype=np.float64))
+    rng = np.random.default_rng(nx * 7 + ny)
+    h = rng.normal(0.0, 0.3, (d, nx * ny))
+    if plain:
+        monkeypatch.setenv("GFMD_PLAIN_PATH", "1")
+    for prec, tol in (("f64", 1e-12), ("f32", 2e-6)):
+        s = _solver(nx, ny, d, prec, half, "half", zero)
+        dt = torch.float64 if prec == "f64" else torch.float32
+        hd = torch.from_numpy(h).to(dt).cuda()
+        f = torch.empty_like(hd)
+        ep = torch.zeros(1, dtype=torch.float64, device="cuda")
+        s.force_async(hd, f, ep)
+        torch.cuda.synchronize()
+        hkh = -float((hd.double() * f.double()).sum())
+        assert hkh > 0
+        assert abs(2.0 * float(ep) - hkh) <= tol * hkh, (prec, 2.0 * float(ep), hkh)

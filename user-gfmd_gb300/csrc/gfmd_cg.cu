@@ -9,20 +9,24 @@
 // Layout of one CG iteration (all on one stream, no host round trip):
 //   fKh = F_el(h)                  force evaluation of the direction (no
 //                                  gamma-point term); F_el is linear, so
-//                                  F_el(u + a h) = F_el(u) + a fKh exactly
-//   k_dirforce                     h.K.h, g.h, wall curvature along h at a = 0,
-//                                  first Newton step
-//   k_probe x kLsMax               Newton steps on the line derivative,
-//                                  each a no-op once the step has converged
+//                                  F_el(u + a h) = F_el(u) + a fKh exactly,
+//                                  and its energy is h.K.h / 2
+//   k_lsinit                       wall curvature and F_w.h along h at a = 0
+//                                  over the line-search set, first Newton step
+//   k_probe x kLsMax               Newton steps on the line derivative over the
+//                                  set, each a no-op once the step has converged
 //   k_update                       u += a h, g += a fKh + F_w(u_new) - F_w(u_old),
 //                                  Polak-Ribiere beta with the descent check,
-//                                  convergence test, loop condition
-//   k_dir                          h = g + beta h
+//                                  the next line-search set (sites near the
+//                                  obstacle) and its bounding box, convergence
+//                                  test, loop condition
+//   k_dir                          h = g + beta h, max|h|, g.h
 // The iteration is the body of a CUDA graph WHILE node; the loop condition is
 // set by the last block of k_update, which counts the iterations, so every
 // launch of the graph runs at most `recompute` iterations.  Each launch
 // starts from a fresh evaluation of F_el(u) (the drift of the incremental
-// update is reset) and steepest descent.
+// update is reset) and steepest descent.  Only k_update and k_dir stream the
+// vectors; the line-search kernels visit the box of the set.
 //
 // Precision: the state is held in two types, Tx for u (the quantity that
 // accumulates) and Tv for g, h and fKh.  Plain FP64 runs
@@ -31,12 +35,13 @@
 // restarts use the FP64 force evaluation while the direction forces stay
 // FP32 (their error is relative to |h|, which shrinks as the solve
 // converges).  Dot products are FP64 (plain) or compensated FP32
-// (TwoProd/TwoSum error-free transformations, Ogita, Rump and Oishi 2005),
-// which carries about 48 significant bits on the FP32 pipes: on this GPU the
-// FP64 ALU rate is below the rate at which HBM streams operands, so FP64
-// arithmetic per element would bound these kernels.  Per-block partials are
-// combined in FP64 in a fixed order by the last block, so results are
-// bit-reproducible.
+// (TwoProd/TwoSum error-free transformations, Ogita, Rump and Oishi 2005; the
+// streaming kernels compensate per loop trip rather than per term): on this
+// GPU the FP64 ALU rate is below the rate at which HBM streams operands, so
+// FP64 arithmetic per element would bound these kernels.  For the same
+// reason the FP32 phase evaluates sphere and map walls in FP32.  Per-block
+// partials are combined in FP64 in a fixed order by the last block, so
+// results are bit-reproducible.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -87,22 +92,24 @@ template <typename K> int grid_for(K kernel, int sms, size_t work, size_t per_bl
 
 struct CgCtl {
   double a, lo, hi;         // line search: step and bracket
-  double gh, hKh;           // g.h and h.K.h at the start of the line search
+  double gh, hKh;           // g.h of the direction (set with it) and its h.K.h
   double fw0h;              // F_w(u).h over the line-search set
   double gg;                // g.g of the current gradient
   double fmax;              // max |g_i|
   double ew;                // obstacle energy at the last update
   double beta;              // next direction: h = g + beta h (h = z + beta h with a preconditioner)
-  double hg;                // h_old . g_new (descent check of the preconditioned direction)
+  double hg;                // h_old . g_new (descent check; g.h of the next direction)
   double ftol;              // tolerance of the running phase
   double ftol_req;          // requested tolerance
   double fmax_restart;      // max |g_i| at the last restart
   double dmax;              // largest move of a component per line-search step (<= 0: none)
   double amax;              // step cap of this line search: dmax / max|h_i|
+  double hmax;              // max |h_i| of the direction (set with it)
   int bulk;                 // FP32 phase: tolerance floored at the FP32 noise level
   int parked;               // phase finished: the branch skips its restart and loop
   int it, since, maxit, recompute;
   int ls_it, ls_done;
+  int bx0, bx1, by0, by1;   // box of sites (inclusive) holding the line-search set
   int done;                 // 0 running, 1 converged, 2 iteration cap, 3 non-finite
   int obst;
   unsigned int counter;     // last-block detection
@@ -146,44 +153,177 @@ __device__ __forceinline__ void set_loop(cudaGraphConditionalHandle hc, int use,
   if (use) cudaGraphSetConditional(hc, v);
 }
 
+// ---- per-site pieces ----------------------------------------------------------
+// Sphere walls in the FP32 phase are evaluated in FP32 (sphere_off keeps the
+// gap's rounding relative to the gap; FP64 exponentials and divisions on the
+// sites near the obstacle would bound the phase at this GPU's FP64 rate); the
+// FP64 phases evaluate them in FP64.
+template <typename Tx> __device__ __forceinline__ bool sphere_f32(const Obst &o) {
+  return sizeof(Tx) == 4 && (o.kind == GFMD_OBST_SPHERE_EXP || o.kind == GFMD_OBST_SPHERE_LJ);
+}
+
+template <typename Tx>
+__device__ __forceinline__ float gap_reg(const Obst &o, int ix, int iy, int l, size_t s, const Tx xv[3]) {
+  float r[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) r[c] = (float)xv[c] + o.foff[l][c];
+  r[0] += (float)ix * o.fax;
+  r[1] += (float)iy * o.fay;
+  return gap_estimate_f(o, s, r);
+}
+
+// Gate value of an atom displaced by xd, compared with o.gw (evaluate the
+// wall) and o.ga (keep the site in the line-search set): for a sphere
+// |d|^2 - R^2 in FP32, for a map the gap estimate (bicubic maps: -1e30).
+template <typename Tx>
+__device__ __forceinline__ float cg_gate(const Obst &o, const Geom &gm, int ix, int iy, int l, size_t s,
+                                         const Tx xd[3]) {
+  if (o.kind == GFMD_OBST_SPHERE_EXP || o.kind == GFMD_OBST_SPHERE_LJ)
+    return sphere_off(o, gm.nx, gm.ny, ix, iy, l, (float)xd[0], (float)xd[1], (float)xd[2]).s;
+  return gap_reg(o, ix, iy, l, s, xd);
+}
+
+// Wall on the atom of layer l at site s displaced by xd, with its curvature
+// along dir: FP32 in the FP32 phase for spheres and height maps, else FP64.
+template <typename Tx, bool BIC>
+__device__ __forceinline__ WallOut site_wall(const Obst &o, const Geom &gm, int ix, int iy, int l, size_t s,
+                                             const Tx xd[3], const double dir[3]) {
+  WallOut w{0.0, {0.0, 0.0, 0.0}, 0.0};
+  if (sphere_f32<Tx>(o)) {
+    const SphereOff q = sphere_off(o, gm.nx, gm.ny, ix, iy, l, (float)xd[0], (float)xd[1], (float)xd[2]);
+    const float df[3] = {(float)dir[0], (float)dir[1], (float)dir[2]};
+    float e, f[3], cv;
+    if (sphere_wall_f(o, q, df, e, f, cv)) {
+      w.e = e;
+      w.f[0] = f[0];
+      w.f[1] = f[1];
+      w.f[2] = f[2];
+      w.curv = cv;
+    }
+    return w;
+  }
+  if (map_in_f32<Tx>(o)) {
+    float e, fz;
+    map_wall_f(o, s, (float)xd[2] + o.foff[l][2], e, fz);
+    w.e = e;
+    w.f[2] = fz;
+    w.curv = (double)(fz * o.fnorm * o.finv_sigma) * dir[2] * dir[2];  // d2E/dz2 = F / sigma
+    return w;
+  }
+  double r[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) r[c] = (double)xd[c] + o.off[l][c];
+  r[0] += ix * o.ax;
+  r[1] += iy * o.ay;
+  return wall_eval<BIC>(o, ix, iy, s, r, dir);
+}
+
+// Box of sites [bx0, bx1] x [by0, by1] holding the line-search set, reduced
+// as the maxima of (ix + 1, nx - ix, iy + 1, ny - iy) over its sites (all
+// zero: empty box).
+struct BoxAcc {
+  int a = 0, b = 0, c = 0, d = 0;
+  __device__ __forceinline__ void add(int ix, int iy, const Geom &gm) {
+    a = max(a, ix + 1);
+    b = max(b, gm.nx - ix);
+    c = max(c, iy + 1);
+    d = max(d, gm.ny - iy);
+  }
+};
+__device__ __forceinline__ void set_box(CgCtl *ctl, const double *r, const Geom &gm, bool full) {
+  ctl->bx1 = full ? gm.nx - 1 : (int)r[0] - 1;
+  ctl->bx0 = full ? 0 : gm.nx - (int)r[1];
+  ctl->by1 = full ? gm.ny - 1 : (int)r[2] - 1;
+  ctl->by0 = full ? 0 : gm.ny - (int)r[3];
+}
+
+// Sums of the line search over the sites of the box that are in the set, at
+// x + a h: F_w(x + a h).h and h^T H_w h.  A set smaller than the grid of
+// threads takes one site per thread, consecutive sites on consecutive blocks
+// (the wall work then lands on every SM); a larger one is walked in
+// coalesced order.
+template <typename Tx, typename Tv, bool BIC>
+__device__ __forceinline__ void line_walls(const Obst &o, const Geom &gm, const Tx *__restrict__ x,
+                                           const Tv *__restrict__ h, const unsigned char *__restrict__ active,
+                                           const CgCtl *ctl, double a, double &fh, double &cw) {
+  const int N = gm.nx * gm.ny;
+  const int w = ctl->by1 - ctl->by0 + 1, ht = ctl->bx1 - ctl->bx0 + 1;
+  const int nb = (w > 0 && ht > 0) ? w * ht : 0;
+  const int x0 = ctl->bx0, y0 = ctl->by0;
+  const int nthr = gridDim.x * kT;
+  const Tx at = (Tx)a;
+  for (int i = nb <= nthr ? threadIdx.x * gridDim.x + blockIdx.x : blockIdx.x * kT + threadIdx.x; i < nb;
+       i += nthr) {
+    const int r = i / w;
+    const int ix = x0 + r, iy = y0 + (i - r * w);
+    const int s = ix * gm.ny + iy;
+    if (map_in_f32<Tx>(o)) {
+      float fhf = 0.0f, cwf = 0.0f;
+      for (int l = 0; l < o.nlayer; l++) {
+        const size_t iz = (size_t)(3 * l + 2) * N + s;
+        const float hz = (float)h[iz];
+        float e, fz;
+        map_wall_f(o, s, (float)x[iz] + (float)a * hz + o.foff[l][2], e, fz);
+        fhf += fz * hz;
+        cwf += fz * o.fnorm * o.finv_sigma * hz * hz;  // d2E/dz2 = F / sigma
+      }
+      fh += fhf;
+      cw += cwf;
+      continue;
+    }
+    if (!active[s]) continue;
+    for (int l = 0; l < o.nlayer; l++) {
+      Tx xd[3];
+      double d[3];
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const size_t idx = (size_t)(3 * l + c) * N + s;
+        const Tv hv = h[idx];
+        d[c] = (double)hv;
+        xd[c] = x[idx] + at * (Tx)hv;
+      }
+      const WallOut wo = site_wall<Tx, BIC>(o, gm, ix, iy, l, s, xd, d);
+      fh += wo.f[0] * d[0] + wo.f[1] * d[1] + wo.f[2] * d[2];
+      cw += wo.curv;
+    }
+  }
+}
+
 // ---- restart: g = f_el + F_w(u), h = g; arms the loop ---------------------
 template <typename Tx, typename Tv, bool BIC = false>
-__global__ void __launch_bounds__(kT, 4) k_restart(Obst o, Geom gm, const Tx *__restrict__ x,
+__global__ void __launch_bounds__(kT, 4) k_restart(const __grid_constant__ Obst o, Geom gm, const Tx *__restrict__ x,
                                                  const Tx *__restrict__ fel, Tv *__restrict__ g,
                                                  Tv *__restrict__ h, unsigned char *__restrict__ active,
                                                  double *__restrict__ part, CgCtl *ctl,
                                                  cudaGraphConditionalHandle hc, int use_hc) {
   const int N = gm.nx * gm.ny;
   const int nl = gm.ndof / 3;
+  const bool obst = o.kind != GFMD_OBST_NONE, all = map_in_f32<Tx>(o);
   Dot<Tv> gg;
   double ew = 0.0;
   float fmx = 0.0f, femx = 0.0f;
   const bool has_ext = o.fz_ext != 0.0;
   double fmx_d = 0.0;
+  BoxAcc box;
   for (int s = blockIdx.x * kT + threadIdx.x; s < N; s += gridDim.x * kT) {
     const int ix = s / gm.ny, iy = s - ix * gm.ny;
     bool nearflag = false;
     for (int l = 0; l < nl; l++) {
+      Tx xd[3];
 #pragma unroll
-      for (int c = 0; c < 3; c++) femx = fmaxf(femx, fabsf((float)fel[(size_t)(3 * l + c) * N + s]));
-      double fw[3];
+      for (int c = 0; c < 3; c++) {
+        const size_t idx = (size_t)(3 * l + c) * N + s;
+        femx = fmaxf(femx, fabsf((float)fel[idx]));
+        xd[c] = x[idx];
+      }
+      double fw[3] = {0.0, 0.0, 0.0};
       bool hit = false;
-      if (l < o.nlayer && map_in_f32<Tx>(o)) {
-        float e, fz;
-        map_wall_f(o, s, (float)x[(size_t)(3 * l + 2) * N + s] + o.foff[l][2], e, fz);
-        nearflag = true;
-        ew += e;
-        fw[0] = 0.0;
-        fw[1] = 0.0;
-        fw[2] = fz;
-        hit = true;
-      } else if (l < o.nlayer && o.kind != GFMD_OBST_NONE) {
-        const float ge = gap_of(o, ix, iy, l, x, N, s);
-        if (ge < o.fgate_active) nearflag = true;
-        if (wall_near(o, ge)) {
-          double r[3], d[3];
-          atom_pos<Tx, Tv>(o, ix, iy, l, x, nullptr, N, s, 0.0, r, d);
-          const WallOut w = wall_eval<BIC>(o, ix, iy, s, r, d);
+      if (obst && l < o.nlayer) {
+        const float ge = all ? -1e30f : cg_gate(o, gm, ix, iy, l, s, xd);
+        if (ge < o.ga) nearflag = true;
+        if (ge < o.gw) {
+          const double zero[3] = {0.0, 0.0, 0.0};
+          const WallOut w = site_wall<Tx, BIC>(o, gm, ix, iy, l, s, xd, zero);
           fw[0] = w.f[0];
           fw[1] = w.f[1];
           fw[2] = w.f[2];
@@ -205,18 +345,25 @@ __global__ void __launch_bounds__(kT, 4) k_restart(Obst o, Geom gm, const Tx *__
         else fmx_d = fmax(fmx_d, fabs(gv));
       }
     }
-    active[s] = nearflag ? 1 : 0;
+    if (obst) {
+      active[s] = nearflag ? 1 : 0;
+      if (nearflag && !all) box.add(ix, iy, gm);
+    }
   }
-  const double acc[4] = {gg.get(), ew, sizeof(Tv) == 4 ? (double)fmx : fmx_d, (double)femx};
-  __shared__ double res[4];
-  if (!reduce_last<2, 2>(acc, part, &ctl->counter, res)) return;
+  const double acc[8] = {gg.get(), ew, sizeof(Tv) == 4 ? (double)fmx : fmx_d, (double)femx,
+                         (double)box.a, (double)box.b, (double)box.c, (double)box.d};
+  __shared__ double res[8];
+  if (!reduce_last<2, 6>(acc, part, &ctl->counter, res)) return;
   if (threadIdx.x == 0) {
     ctl->gg = res[0];
+    ctl->gh = res[0];  // h = g
+    ctl->hmax = res[2];
     ctl->ew = res[1];
     ctl->fmax = res[2];
     ctl->fmax_restart = res[2];
     ctl->since = 0;
     ctl->beta = 0.0;
+    set_box(ctl, res + 4, gm, all);
     // FP32 state resolves g = f_el + F_w to about eps32 |f_el|: the FP32
     // phase stops at 64 eps32 max|f_el| if that is above the request
     ctl->ftol = ctl->bulk ? fmax(ctl->ftol_req, 64.0 * 5.960464477539063e-8 * res[3]) : ctl->ftol_req;
@@ -228,63 +375,28 @@ __global__ void __launch_bounds__(kT, 4) k_restart(Obst o, Geom gm, const Tx *__
   }
 }
 
-// ---- along the direction: h.K.h, g.h, wall curvature, first Newton step ----
+// ---- start of the line search: h.K.h from the energy of the direction's
+// force evaluation (E(h) = h.K.h / 2 with the gamma-point force off), g.h and
+// max|h| from the kernel that formed h, wall terms at a = 0 over the set;
+// first Newton step -------------------------------------------------------------
 template <typename Tx, typename Tv, bool BIC = false>
-__global__ void __launch_bounds__(kT) k_dirforce(Obst o, Geom gm, const Tx *__restrict__ x,
-                                                  const Tv *__restrict__ fKh, const Tv *__restrict__ h,
-                                                  const Tv *__restrict__ g,
-                                                  const unsigned char *__restrict__ active,
-                                                  double *__restrict__ part, CgCtl *ctl) {
-  const int N = gm.nx * gm.ny;
-  const int nl = gm.ndof / 3;
-  Dot<Tv> hkh, gh;
-  double cw = 0.0, fw0h = 0.0;
-  Tv hmx = (Tv)0;
-#pragma unroll 2
-  for (int s = blockIdx.x * kT + threadIdx.x; s < N; s += gridDim.x * kT) {
-    for (int l = 0; l < nl; l++) {
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-        const size_t idx = (size_t)(3 * l + c) * N + s;
-        const Tv hv = h[idx];
-        hkh.add(hv, fKh[idx]);
-        gh.add(g[idx], hv);
-        hmx = fmax(hmx, fabs(hv));
-      }
-    }
-    if (map_in_f32<Tx>(o)) {
-      float cwf = 0.0f, fhf = 0.0f;
-      for (int l = 0; l < o.nlayer; l++) {
-        const size_t iz = (size_t)(3 * l + 2) * N + s;
-        float e, fz;
-        map_wall_f(o, s, (float)x[iz] + o.foff[l][2], e, fz);
-        const float hz = (float)h[iz];
-        cwf += fz * o.fnorm * o.finv_sigma * hz * hz;  // d2E/dz2 = F / sigma
-        fhf += fz * hz;
-      }
-      cw += cwf;
-      fw0h += fhf;
-    } else if (o.kind != GFMD_OBST_NONE && active[s]) {
-      const int ix = s / gm.ny, iy = s - ix * gm.ny;
-      for (int l = 0; l < o.nlayer; l++) {
-        double r[3], d[3];
-        atom_pos<Tx, Tv>(o, ix, iy, l, x, h, N, s, 0.0, r, d);
-        const WallOut w = wall_eval<BIC>(o, ix, iy, s, r, d);
-        cw += w.curv;
-        fw0h += w.f[0] * d[0] + w.f[1] * d[1] + w.f[2] * d[2];
-      }
-    }
-  }
-  const double acc[5] = {-hkh.get(), gh.get(), cw, fw0h, (double)hmx};
-  __shared__ double res[5];
-  if (!reduce_last<4, 1>(acc, part, &ctl->counter, res)) return;
+__global__ void __launch_bounds__(kT) k_lsinit(const __grid_constant__ Obst o, Geom gm, const Tx *__restrict__ x,
+                                                const Tv *__restrict__ h,
+                                                const unsigned char *__restrict__ active,
+                                                const double *__restrict__ eh, double *__restrict__ part,
+                                                CgCtl *ctl) {
+  double fh = 0.0, cw = 0.0;
+  if (o.kind != GFMD_OBST_NONE) line_walls<Tx, Tv, BIC>(o, gm, x, h, active, ctl, 0.0, fh, cw);
+  const double acc[2] = {fh, cw};
+  __shared__ double res[2];
+  if (!reduce_last<2, 0>(acc, part, &ctl->counter, res)) return;
   if (threadIdx.x == 0) {
-    const double hKh = res[0], ghv = res[1], curv = res[0] + res[2];
+    const double hKh = 2.0 * (*eh);
+    const double ghv = ctl->gh, curv = hKh + res[1];
     // LAMMPS min_modify dmax: no component moves more than dmax in one step
-    ctl->amax = (ctl->dmax > 0.0 && res[4] > 0.0) ? ctl->dmax / res[4] : 1e300;
+    ctl->amax = (ctl->dmax > 0.0 && ctl->hmax > 0.0) ? ctl->dmax / ctl->hmax : 1e300;
     ctl->hKh = hKh;
-    ctl->gh = ghv;
-    ctl->fw0h = res[3];
+    ctl->fw0h = res[0];
     ctl->lo = 0.0;
     ctl->ls_it = 0;
     // with the cap, amax is the upper bracket of the step from the start
@@ -301,64 +413,37 @@ __global__ void __launch_bounds__(kT) k_dirforce(Obst o, Geom gm, const Tx *__re
 
 // The Newton step of a probe from the reduced F_w(u + a h).h and curvature.
 __device__ __forceinline__ void probe_step(CgCtl *ctl, double a, double dfh, double cwall) {
-  {
-    const double gdir = ctl->gh - a * ctl->hKh + (dfh - ctl->fw0h);
-    const double curv = ctl->hKh + cwall;
-    double lo = ctl->lo, hi = ctl->hi;
-    if (gdir > 0.0) lo = a;
-    else hi = a;
-    double an = (curv > 0.0) ? a + gdir / curv : -1.0;
-    if (hi >= 0.0 && (an <= lo || an >= hi || an < 0.0)) an = 0.5 * (lo + hi);
-    else if (an < 0.0) an = lo > 0.0 ? 2.0 * lo : 1e-3;
-    const double step = fabs(an - a);
-    ctl->lo = lo;
-    ctl->hi = hi;
-    ctl->a = an;
-    ctl->ls_it += 1;
-    // an exact line minimum is not needed: Polak-Ribiere with restarts
-    // converges from a step within 1e-6 of it
-    if (step <= 1e-6 * fabs(an) || ctl->ls_it >= kLsMax || !isfinite(an)) ctl->ls_done = 1;
-    if (!isfinite(an)) ctl->a = 0.0;
-  }
+  const double gdir = ctl->gh - a * ctl->hKh + (dfh - ctl->fw0h);
+  const double curv = ctl->hKh + cwall;
+  double lo = ctl->lo, hi = ctl->hi;
+  if (gdir > 0.0) lo = a;
+  else hi = a;
+  double an = (curv > 0.0) ? a + gdir / curv : -1.0;
+  if (hi >= 0.0 && (an <= lo || an >= hi || an < 0.0)) an = 0.5 * (lo + hi);
+  else if (an < 0.0) an = lo > 0.0 ? 2.0 * lo : 1e-3;
+  const double step = fabs(an - a);
+  ctl->lo = lo;
+  ctl->hi = hi;
+  ctl->a = an;
+  ctl->ls_it += 1;
+  // an exact line minimum is not needed: Polak-Ribiere with restarts
+  // converges from a step within 1e-6 of it
+  if (step <= 1e-6 * fabs(an) || ctl->ls_it >= kLsMax || !isfinite(an)) ctl->ls_done = 1;
+  if (!isfinite(an)) ctl->a = 0.0;
 }
 
 // ---- one Newton probe of the line search at u + a h ------------------------
 // gdir(a) = g.h - a hKh + sum F_w(u + a h).h - F_w(u).h   (= -phi'(a))
 // curv(a) = hKh + sum h^T H_w(u + a h) h                   (=  phi''(a))
 template <typename Tx, typename Tv, bool BIC = false>
-__global__ void __launch_bounds__(kT) k_probe(Obst o, Geom gm, const Tx *__restrict__ x,
+__global__ void __launch_bounds__(kT) k_probe(const __grid_constant__ Obst o, Geom gm, const Tx *__restrict__ x,
                                                const Tv *__restrict__ h,
                                                const unsigned char *__restrict__ active,
                                                double *__restrict__ part, CgCtl *ctl) {
   if (ctl->ls_done) return;  // uniform over the grid
   const double a = ctl->a;
-  const int N = gm.nx * gm.ny;
   double dfh = 0.0, cw = 0.0;
-  for (int s = blockIdx.x * kT + threadIdx.x; s < N; s += gridDim.x * kT) {
-    if (map_in_f32<Tx>(o)) {
-      float dfh_f = 0.0f, cw_f = 0.0f;
-      for (int l = 0; l < o.nlayer; l++) {
-        const size_t iz = (size_t)(3 * l + 2) * N + s;
-        const float hz = (float)h[iz];
-        float e, fz;
-        map_wall_f(o, s, (float)x[iz] + (float)a * hz + o.foff[l][2], e, fz);
-        dfh_f += fz * hz;
-        cw_f += fz * o.fnorm * o.finv_sigma * hz * hz;
-      }
-      dfh += dfh_f;
-      cw += cw_f;
-      continue;
-    }
-    if (!active[s]) continue;
-    const int ix = s / gm.ny, iy = s - ix * gm.ny;
-    for (int l = 0; l < o.nlayer; l++) {
-      double r[3], d[3];
-      atom_pos<Tx, Tv>(o, ix, iy, l, x, h, N, s, a, r, d);
-      const WallOut w1 = wall_eval<BIC>(o, ix, iy, s, r, d);
-      dfh += w1.f[0] * d[0] + w1.f[1] * d[1] + w1.f[2] * d[2];
-      cw += w1.curv;
-    }
-  }
+  line_walls<Tx, Tv, BIC>(o, gm, x, h, active, ctl, a, dfh, cw);
   const double acc[2] = {dfh, cw};
   __shared__ double res[2];
   if (!reduce_last<2, 0>(acc, part, &ctl->counter, res)) return;
@@ -370,166 +455,33 @@ __global__ void __launch_bounds__(kT) k_probe(Obst o, Geom gm, const Tx *__restr
 // updated through the linearity of F_el, so f_el itself is not stored, and
 // the rounding of the FP32 state is relative to the (small) gradient rather
 // than to the elastic force.
-template <typename Tx, typename Tv, bool BIC = false>
-__device__ __forceinline__ void wall_at(const Obst &o, int ix, int iy, int l, size_t s, const Tx xv[3],
-                                        WallOut &w) {
-  const double zero[3] = {0.0, 0.0, 0.0};
-  double r[3];
-#pragma unroll
-  for (int c = 0; c < 3; c++) r[c] = (double)xv[c] + o.off[l][c];
-  r[0] += ix * o.ax;
-  r[1] += iy * o.ay;
-  w = wall_eval<BIC>(o, ix, iy, s, r, zero);
-}
-
-// Near the obstacle: g_new = g_old + a fKh + F_w(x_new) - F_w(x_old) in FP64,
-// with E_w(x_new).  Kept out of line (arguments by value, so the caller's
-// arrays stay in registers) so the far-field loop stays small.
 template <typename T> struct V3 { T v[3]; };
 template <typename Tv> struct WallDelta { double e; Tv g[3]; };
 
+// Near the obstacle: g_new = g_old + a fKh + F_w(x_new) - F_w(x_old), with
+// E_w(x_new).  Kept out of line (arguments by value, so the caller's arrays
+// stay in registers) so the far-field loop stays small.
 template <typename Tx, typename Tv, bool BIC = false>
-__device__ __noinline__ WallDelta<Tv> wall_delta(const Obst &o, int ix, int iy, int l, int s, V3<Tx> xv,
-                                                 V3<Tx> xn, V3<Tv> go, V3<Tv> fk, double a) {
-  WallOut w1, w0;
-  wall_at<Tx, Tv, BIC>(o, ix, iy, l, s, xn.v, w1);
-  wall_at<Tx, Tv, BIC>(o, ix, iy, l, s, xv.v, w0);
+__device__ __noinline__ WallDelta<Tv> wall_delta(const Obst &o, const Geom &gm, int ix, int iy, int l, int s,
+                                                 V3<Tx> xv, V3<Tx> xn, V3<Tv> go, V3<Tv> fk, double a) {
+  const double zero[3] = {0.0, 0.0, 0.0};
+  const WallOut w1 = site_wall<Tx, BIC>(o, gm, ix, iy, l, s, xn.v, zero);
+  const WallOut w0 = site_wall<Tx, BIC>(o, gm, ix, iy, l, s, xv.v, zero);
   WallDelta<Tv> r;
   r.e = w1.e;
   for (int c = 0; c < 3; c++) r.g[c] = (Tv)((double)go.v[c] + a * (double)fk.v[c] + (w1.f[c] - w0.f[c]));
   return r;
 }
 
-template <typename Tx>
-__device__ __forceinline__ float gap_reg(const Obst &o, int ix, int iy, int l, size_t s, const Tx xv[3]) {
-  float r[3];
-#pragma unroll
-  for (int c = 0; c < 3; c++) r[c] = (float)xv[c] + o.foff[l][c];
-  r[0] += (float)ix * o.fax;
-  r[1] += (float)iy * o.fay;
-  return gap_estimate_f(o, s, r);
-}
-
-template <typename Tx, typename Tv, bool BIC = false>
-__global__ void __launch_bounds__(kT, 4) k_update(Obst o, Geom gm, Tx *__restrict__ x,
-                                                   const Tv *__restrict__ h, const Tv *__restrict__ fKh,
-                                                   Tv *__restrict__ g, Tv *__restrict__ gp,
-                                                   unsigned char *__restrict__ active,
-                                                   double *__restrict__ part, CgCtl *ctl,
-                                                   cudaGraphConditionalHandle hc, int use_hc) {
-  const double ad = ctl->a;
-  const Tx a = (Tx)ad;
-  const Tv av = (Tv)ad;
-  const int N = gm.nx * gm.ny;
-  const int nl = gm.ndof / 3;
-  const bool obst = o.kind != GFMD_OBST_NONE;
-  Dot<Tv> gg, ggo, hg;
-  double ew = 0.0;
-  float fmx = 0.0f;
-  double fmx_d = 0.0;
-  for (int s = blockIdx.x * kT + threadIdx.x; s < N; s += gridDim.x * kT) {
-    const int ix = s / gm.ny, iy = s - ix * gm.ny;
-    bool nearflag = false;
-    for (int l = 0; l < nl; l++) {
-      Tx xv[3];
-      Tv hv[3], fk[3], go[3];
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-        const size_t idx = (size_t)(3 * l + c) * N + s;
-        xv[c] = x[idx];
-        hv[c] = h[idx];
-        fk[c] = fKh[idx];
-        go[c] = g[idx];
-      }
-      Tx xn[3];
-      Tv gn[3];
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-        xn[c] = xv[c] + a * (Tx)hv[c];
-        gn[c] = go[c] + av * fk[c];
-      }
-      if (obst && l < o.nlayer && map_in_f32<Tx>(o)) {
-        float e1, f1, e0, f0;
-        map_wall_f(o, s, (float)xn[2] + o.foff[l][2], e1, f1);
-        map_wall_f(o, s, (float)xv[2] + o.foff[l][2], e0, f0);
-        nearflag = true;
-        ew += e1;
-        gn[2] = gn[2] + (Tv)(f1 - f0);
-      } else if (obst && l < o.nlayer) {
-        const float ge_new = gap_reg(o, ix, iy, l, s, xn);
-        const float ge_old = gap_reg(o, ix, iy, l, s, xv);
-        if (ge_new < o.fgate_active) nearflag = true;
-        if (ge_new < o.fgate_wall || ge_old < o.fgate_wall) {
-          const WallDelta<Tv> wd = wall_delta<Tx, Tv, BIC>(o, ix, iy, l, s, V3<Tx>{{xv[0], xv[1], xv[2]}},
-                                                      V3<Tx>{{xn[0], xn[1], xn[2]}},
-                                                      V3<Tv>{{go[0], go[1], go[2]}},
-                                                      V3<Tv>{{fk[0], fk[1], fk[2]}}, ad);
-          ew += wd.e;
-          gn[0] = wd.g[0];
-          gn[1] = wd.g[1];
-          gn[2] = wd.g[2];
-        }
-      }
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-        const size_t idx = (size_t)(3 * l + c) * N + s;
-        gg.add(gn[c], gn[c]);
-        ggo.add(gn[c], go[c]);
-        hg.add(hv[c], gn[c]);
-        if constexpr (sizeof(Tv) == 4) fmx = fmaxf(fmx, fabsf(gn[c]));
-        else fmx_d = fmax(fmx_d, fabs(gn[c]));
-        x[idx] = xn[c];
-        g[idx] = gn[c];
-        if (gp) gp[idx] = go[c];  // previous gradient (preconditioned Polak-Ribiere)
-      }
-    }
-    active[s] = nearflag ? 1 : 0;
-  }
-  const double acc[5] = {gg.get(), ggo.get(), hg.get(), ew, sizeof(Tv) == 4 ? (double)fmx : fmx_d};
-  __shared__ double res[5];
-  if (!reduce_last<4, 1>(acc, part, &ctl->counter, res)) return;
-  if (threadIdx.x == 0) {
-    const double gg_new = res[0], g_gold = res[1], h_g = res[2];
-    if (!gp) {
-      const double gg_old = ctl->gg;
-      double beta = gg_old > 0.0 ? (gg_new - g_gold) / gg_old : 0.0;  // Polak-Ribiere
-      if (beta < 0.0) beta = 0.0;
-      // new direction h' = g + beta h must descend: h'.g = gg_new + beta h.g > 0
-      if (!(gg_new + beta * h_g > 0.0)) beta = 0.0;
-      ctl->beta = beta;
-      ctl->gg = gg_new;
-    } else {
-      ctl->hg = h_g;  // beta follows from the preconditioned gradient (k_pcg_beta)
-    }
-    ctl->ew = res[3];
-    ctl->fmax = res[4];
-    ctl->it += 1;
-    ctl->since += 1;
-    if (!isfinite(gg_new)) ctl->done = 3;
-    else if (res[4] <= ctl->ftol) ctl->done = 1;
-    else if (ctl->it >= ctl->maxit) ctl->done = 2;
-    const bool go_on = ctl->done == 0 && ctl->since < ctl->recompute;
-    set_loop(hc, use_hc, go_on ? 1u : 0u);
-  }
-}
-
-// h = g + beta h
-template <typename Tv>
-__global__ void __launch_bounds__(kT) k_dir(size_t n, Tv *__restrict__ h, const Tv *__restrict__ g,
-                                             const CgCtl *ctl) {
-  const Tv beta = (Tv)ctl->beta;
-  for (size_t i = blockIdx.x * (size_t)kT + threadIdx.x; i < n; i += (size_t)gridDim.x * kT)
-    h[i] = g[i] + beta * h[i];
-}
-
-// ---- 4-site vector forms of the streaming kernels ---------------------------
-// The per-element work of k_update, k_dirforce and k_dir is a few operations
-// on 4-6 streamed arrays: they are bound by how many loads each thread keeps
-// in flight.  The V = 4 forms take 4 consecutive sites per thread with 16-byte
-// loads (two for FP64), for grids with nx*ny divisible by 4 (all power-of-two
-// grids); the scalar forms above handle the rest.  Same arithmetic per site.
-template <typename T> struct Vec4;
-template <> struct Vec4<float> {
+// V consecutive sites per thread: V = 4 with 16-byte loads (two for FP64)
+// for grids with nx*ny divisible by 4 (all power-of-two grids), V = 1 else.
+// The streaming kernels are bound by the loads each thread keeps in flight.
+template <typename T, int V> struct VecN;
+template <typename T> struct VecN<T, 1> {
+  static __device__ __forceinline__ void ld(const T *p, T o[1]) { o[0] = *p; }
+  static __device__ __forceinline__ void st(T *p, const T o[1]) { *p = o[0]; }
+};
+template <> struct VecN<float, 4> {
   static __device__ __forceinline__ void ld(const float *p, float o[4]) {
     const float4 v = *reinterpret_cast<const float4 *>(p);
     o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
@@ -538,7 +490,7 @@ template <> struct Vec4<float> {
     *reinterpret_cast<float4 *>(p) = make_float4(o[0], o[1], o[2], o[3]);
   }
 };
-template <> struct Vec4<double> {
+template <> struct VecN<double, 4> {
   static __device__ __forceinline__ void ld(const double *p, double o[4]) {
     const double2 a = *reinterpret_cast<const double2 *>(p), b = *reinterpret_cast<const double2 *>(p + 2);
     o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
@@ -549,46 +501,55 @@ template <> struct Vec4<double> {
   }
 };
 
-template <typename Tx, typename Tv, bool BIC = false>
-__global__ void __launch_bounds__(kT, 2) k_update4(Obst o, Geom gm, Tx *__restrict__ x,
-                                                    const Tv *__restrict__ h, const Tv *__restrict__ fKh,
-                                                    Tv *__restrict__ g, Tv *__restrict__ gp,
-                                                    unsigned char *__restrict__ active,
-                                                    double *__restrict__ part, CgCtl *ctl,
-                                                    cudaGraphConditionalHandle hc, int use_hc) {
+// Dot products of the streaming kernels: the terms of one loop trip (at most
+// V x ndof) are summed in the vector type, each trip sum then enters the
+// thread's Dot (FP64, or a compensated FP32 pair): FP32 trip sums round at
+// eps32 relative to themselves, below what Polak-Ribiere and the line search
+// resolve, at a fraction of the instructions of compensating every term.
+template <typename Tx, typename Tv, bool BIC = false, int V = 4>
+__global__ void __launch_bounds__(kT, V == 4 ? 2 : 4) k_update(const __grid_constant__ Obst o, Geom gm,
+                                                               Tx *__restrict__ x, const Tv *__restrict__ h,
+                                                               const Tv *__restrict__ fKh, Tv *__restrict__ g,
+                                                               Tv *__restrict__ gp,
+                                                               unsigned char *__restrict__ active,
+                                                               double *__restrict__ part, CgCtl *ctl,
+                                                               cudaGraphConditionalHandle hc, int use_hc) {
   const double ad = ctl->a;
   const Tx a = (Tx)ad;
   const Tv av = (Tv)ad;
   const int N = gm.nx * gm.ny;
   const int nl = gm.ndof / 3;
-  const bool obst = o.kind != GFMD_OBST_NONE;
-  Dot<Tv> gg[2], ggo[2], hg[2];  // two chains each: sites j even / odd
+  const bool obst = o.kind != GFMD_OBST_NONE, all = map_in_f32<Tx>(o);
+  Dot<Tv> gg, ggo, hg;
   double ew = 0.0;
-  float fmx = 0.0f;
-  double fmx_d = 0.0;
-  for (int s0 = 4 * (blockIdx.x * kT + threadIdx.x); s0 < N; s0 += 4 * gridDim.x * kT) {
-    bool nearflag[4] = {false, false, false, false};
+  Tv fmx = (Tv)0;
+  BoxAcc box;
+  for (int s0 = V * (blockIdx.x * kT + threadIdx.x); s0 < N; s0 += V * gridDim.x * kT) {
+    bool nearflag[V];
+#pragma unroll
+    for (int j = 0; j < V; j++) nearflag[j] = false;
+    Tv sgg = (Tv)0, sggo = (Tv)0, shg = (Tv)0;
     for (int l = 0; l < nl; l++) {
-      Tx xv[3][4], xn[3][4];
-      Tv hv[3][4], fk[3][4], go[3][4], gn[3][4];
+      Tx xv[3][V], xn[3][V];
+      Tv hv[3][V], fk[3][V], go[3][V], gn[3][V];
 #pragma unroll
       for (int c = 0; c < 3; c++) {
         const size_t idx = (size_t)(3 * l + c) * N + s0;
-        Vec4<Tx>::ld(x + idx, xv[c]);
-        Vec4<Tv>::ld(h + idx, hv[c]);
-        Vec4<Tv>::ld(fKh + idx, fk[c]);
-        Vec4<Tv>::ld(g + idx, go[c]);
+        VecN<Tx, V>::ld(x + idx, xv[c]);
+        VecN<Tv, V>::ld(h + idx, hv[c]);
+        VecN<Tv, V>::ld(fKh + idx, fk[c]);
+        VecN<Tv, V>::ld(g + idx, go[c]);
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
+        for (int j = 0; j < V; j++) {
           xn[c][j] = xv[c][j] + a * (Tx)hv[c][j];
           gn[c][j] = go[c][j] + av * fk[c][j];
         }
       }
       if (obst && l < o.nlayer) {
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
+        for (int j = 0; j < V; j++) {
           const int s = s0 + j;
-          if (map_in_f32<Tx>(o)) {
+          if (all) {
             float e1, f1, e0, f0;
             map_wall_f(o, s, (float)xn[2][j] + o.foff[l][2], e1, f1);
             map_wall_f(o, s, (float)xv[2][j] + o.foff[l][2], e0, f0);
@@ -598,14 +559,13 @@ __global__ void __launch_bounds__(kT, 2) k_update4(Obst o, Geom gm, Tx *__restri
           } else {
             const int ix = s / gm.ny, iy = s - ix * gm.ny;
             const Tx xo3[3] = {xv[0][j], xv[1][j], xv[2][j]}, xn3[3] = {xn[0][j], xn[1][j], xn[2][j]};
-            const float ge_new = gap_reg(o, ix, iy, l, s, xn3);
-            const float ge_old = gap_reg(o, ix, iy, l, s, xo3);
-            if (ge_new < o.fgate_active) nearflag[j] = true;
-            if (ge_new < o.fgate_wall || ge_old < o.fgate_wall) {
-              const WallDelta<Tv> wd = wall_delta<Tx, Tv, BIC>(o, ix, iy, l, s, V3<Tx>{{xo3[0], xo3[1], xo3[2]}},
-                                                          V3<Tx>{{xn3[0], xn3[1], xn3[2]}},
-                                                          V3<Tv>{{go[0][j], go[1][j], go[2][j]}},
-                                                          V3<Tv>{{fk[0][j], fk[1][j], fk[2][j]}}, ad);
+            const float ge_new = cg_gate(o, gm, ix, iy, l, s, xn3);
+            const float ge_old = cg_gate(o, gm, ix, iy, l, s, xo3);
+            if (ge_new < o.ga) nearflag[j] = true;
+            if (ge_new < o.gw || ge_old < o.gw) {
+              const WallDelta<Tv> wd = wall_delta<Tx, Tv, BIC>(
+                  o, gm, ix, iy, l, s, V3<Tx>{{xo3[0], xo3[1], xo3[2]}}, V3<Tx>{{xn3[0], xn3[1], xn3[2]}},
+                  V3<Tv>{{go[0][j], go[1][j], go[2][j]}}, V3<Tv>{{fk[0][j], fk[1][j], fk[2][j]}}, ad);
               ew += wd.e;
               gn[0][j] = wd.g[0];
               gn[1][j] = wd.g[1];
@@ -618,39 +578,50 @@ __global__ void __launch_bounds__(kT, 2) k_update4(Obst o, Geom gm, Tx *__restri
       for (int c = 0; c < 3; c++) {
         const size_t idx = (size_t)(3 * l + c) * N + s0;
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-          gg[j & 1].add(gn[c][j], gn[c][j]);
-          ggo[j & 1].add(gn[c][j], go[c][j]);
-          hg[j & 1].add(hv[c][j], gn[c][j]);
-          if constexpr (sizeof(Tv) == 4) fmx = fmaxf(fmx, fabsf(gn[c][j]));
-          else fmx_d = fmax(fmx_d, fabs(gn[c][j]));
+        for (int j = 0; j < V; j++) {
+          sgg = fma(gn[c][j], gn[c][j], sgg);
+          sggo = fma(gn[c][j], go[c][j], sggo);
+          shg = fma(hv[c][j], gn[c][j], shg);
+          fmx = fmax(fmx, fabs(gn[c][j]));
         }
-        Vec4<Tx>::st(x + idx, xn[c]);
-        Vec4<Tv>::st(g + idx, gn[c]);
-        if (gp) Vec4<Tv>::st(gp + idx, go[c]);  // previous gradient (preconditioned Polak-Ribiere)
+        VecN<Tx, V>::st(x + idx, xn[c]);
+        VecN<Tv, V>::st(g + idx, gn[c]);
+        if (gp) VecN<Tv, V>::st(gp + idx, go[c]);  // previous gradient (preconditioned Polak-Ribiere)
       }
     }
-    *reinterpret_cast<uchar4 *>(active + s0) =
-        make_uchar4(nearflag[0] ? 1 : 0, nearflag[1] ? 1 : 0, nearflag[2] ? 1 : 0, nearflag[3] ? 1 : 0);
+    gg.addsum(sgg);
+    ggo.addsum(sggo);
+    hg.addsum(shg);
+    if (obst) {
+#pragma unroll
+      for (int j = 0; j < V; j++) {
+        active[s0 + j] = nearflag[j] ? 1 : 0;
+        if (nearflag[j] && !all) {
+          const int ix = (s0 + j) / gm.ny;
+          box.add(ix, s0 + j - ix * gm.ny, gm);
+        }
+      }
+    }
   }
-  const double acc[5] = {gg[0].get() + gg[1].get(), ggo[0].get() + ggo[1].get(), hg[0].get() + hg[1].get(), ew,
-                         sizeof(Tv) == 4 ? (double)fmx : fmx_d};
-  __shared__ double res[5];
-  if (!reduce_last<4, 1>(acc, part, &ctl->counter, res)) return;
+  const double acc[9] = {gg.get(), ggo.get(), hg.get(), ew, (double)fmx,
+                         (double)box.a, (double)box.b, (double)box.c, (double)box.d};
+  __shared__ double res[9];
+  if (!reduce_last<4, 5>(acc, part, &ctl->counter, res)) return;
   if (threadIdx.x == 0) {
     const double gg_new = res[0], g_gold = res[1], h_g = res[2];
     if (!gp) {
       const double gg_old = ctl->gg;
       double beta = gg_old > 0.0 ? (gg_new - g_gold) / gg_old : 0.0;  // Polak-Ribiere
       if (beta < 0.0) beta = 0.0;
+      // new direction h' = g + beta h must descend: h'.g = gg_new + beta h.g > 0
       if (!(gg_new + beta * h_g > 0.0)) beta = 0.0;
       ctl->beta = beta;
       ctl->gg = gg_new;
-    } else {
-      ctl->hg = h_g;
-    }
+    }  // preconditioned: beta follows from the preconditioned gradient (k_pcg_beta)
+    ctl->hg = h_g;
     ctl->ew = res[3];
     ctl->fmax = res[4];
+    set_box(ctl, res + 5, gm, all);
     ctl->it += 1;
     ctl->since += 1;
     if (!isfinite(gg_new)) ctl->done = 3;
@@ -661,131 +632,56 @@ __global__ void __launch_bounds__(kT, 2) k_update4(Obst o, Geom gm, Tx *__restri
   }
 }
 
-// Wall curvature along h and F_w.h of one site at a = 0 (out of line: only
-// sites near the obstacle take it, and its FP64 registers stay out of the
-// streaming loop).
-template <typename Tx, typename Tv, bool BIC = false>
-__device__ __noinline__ double2 wall_dir_site(Obst o, Geom gm, const Tx *__restrict__ x, const Tv *__restrict__ h,
-                                              int s) {
-  const int N = gm.nx * gm.ny;
-  const int ix = s / gm.ny, iy = s - ix * gm.ny;
-  double cw = 0.0, fh = 0.0;
-  for (int l = 0; l < o.nlayer; l++) {
-    double r[3], d[3];
-    atom_pos<Tx, Tv>(o, ix, iy, l, x, h, N, s, 0.0, r, d);
-    const WallOut w = wall_eval<BIC>(o, ix, iy, s, r, d);
-    cw += w.curv;
-    fh += w.f[0] * d[0] + w.f[1] * d[1] + w.f[2] * d[2];
-  }
-  return make_double2(cw, fh);
-}
-
-template <typename Tx, typename Tv, bool BIC = false>
-__global__ void __launch_bounds__(kT, 4) k_dirforce4(Obst o, Geom gm, const Tx *__restrict__ x,
-                                                      const Tv *__restrict__ fKh, const Tv *__restrict__ h,
-                                                      const Tv *__restrict__ g,
-                                                      const unsigned char *__restrict__ active,
-                                                      double *__restrict__ part, CgCtl *ctl) {
-  const int N = gm.nx * gm.ny;
-  const int nl = gm.ndof / 3;
-  Dot<Tv> hkh[2], gh[2];  // two chains each: sites j even / odd
-  double cw = 0.0, fw0h = 0.0;
-  Tv hmx = (Tv)0;
-  for (int s0 = 4 * (blockIdx.x * kT + threadIdx.x); s0 < N; s0 += 4 * gridDim.x * kT) {
-    for (int l = 0; l < nl; l++) {
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-        const size_t idx = (size_t)(3 * l + c) * N + s0;
-        Tv hv[4], fk[4], gv[4];
-        Vec4<Tv>::ld(h + idx, hv);
-        Vec4<Tv>::ld(fKh + idx, fk);
-        Vec4<Tv>::ld(g + idx, gv);
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-          hkh[j & 1].add(hv[j], fk[j]);
-          gh[j & 1].add(gv[j], hv[j]);
-          hmx = fmax(hmx, fabs(hv[j]));
-        }
-      }
-    }
-    if (o.kind == GFMD_OBST_NONE) continue;
-    const uchar4 act = map_in_f32<Tx>(o) ? make_uchar4(1, 1, 1, 1) : *reinterpret_cast<const uchar4 *>(active + s0);
-    const unsigned char av[4] = {act.x, act.y, act.z, act.w};
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-      if (!av[j]) continue;
-      const int s = s0 + j;
-      if (map_in_f32<Tx>(o)) {
-        float cwf = 0.0f, fhf = 0.0f;
-        for (int l = 0; l < o.nlayer; l++) {
-          const size_t iz = (size_t)(3 * l + 2) * N + s;
-          float e, fz;
-          map_wall_f(o, s, (float)x[iz] + o.foff[l][2], e, fz);
-          const float hz = (float)h[iz];
-          cwf += fz * o.fnorm * o.finv_sigma * hz * hz;  // d2E/dz2 = F / sigma
-          fhf += fz * hz;
-        }
-        cw += cwf;
-        fw0h += fhf;
-      } else {
-        const double2 w = wall_dir_site<Tx, Tv, BIC>(o, gm, x, h, s);
-        cw += w.x;
-        fw0h += w.y;
-      }
-    }
-  }
-  const double acc[5] = {-(hkh[0].get() + hkh[1].get()), gh[0].get() + gh[1].get(), cw, fw0h, (double)hmx};
-  __shared__ double res[5];
-  if (!reduce_last<4, 1>(acc, part, &ctl->counter, res)) return;
-  if (threadIdx.x == 0) {
-    const double hKh = res[0], ghv = res[1], curv = res[0] + res[2];
-    ctl->amax = (ctl->dmax > 0.0 && res[4] > 0.0) ? ctl->dmax / res[4] : 1e300;
-    ctl->hKh = hKh;
-    ctl->gh = ghv;
-    ctl->fw0h = res[3];
-    ctl->lo = 0.0;
-    ctl->ls_it = 0;
-    ctl->hi = ctl->amax < 1e300 ? ctl->amax : -1.0;
-    double a;
-    if (curv > 0.0 && ghv > 0.0) a = ghv / curv;
-    else a = ghv > 0.0 ? 1e-3 : 0.0;
-    if (ghv > 0.0 && ctl->hi >= 0.0 && a >= ctl->hi) a = 0.5 * ctl->hi;
-    ctl->a = a;
-    ctl->ls_done = (o.kind == GFMD_OBST_NONE || ghv <= 0.0) ? 1 : 0;
-  }
-}
-
-// h = g + beta h, 4 elements per thread
-template <typename Tv>
-__global__ void __launch_bounds__(kT) k_dir4(size_t n, Tv *__restrict__ h, const Tv *__restrict__ g,
-                                              const CgCtl *ctl) {
+// Direction after an update: h = g + beta h (h = z + beta h with a
+// preconditioner, z = -mz), with max|h| for the step cap and
+// g.h = g.g + beta h_old.g (g.z + beta h_old.g).
+template <typename Tv, int V = 4>
+__global__ void __launch_bounds__(kT) k_dir(size_t n, Tv *__restrict__ h, const Tv *__restrict__ g,
+                                             const Tv *__restrict__ mz, double *__restrict__ part, CgCtl *ctl) {
   const Tv beta = (Tv)ctl->beta;
-  for (size_t i = 4 * (blockIdx.x * (size_t)kT + threadIdx.x); i < n; i += 4 * (size_t)gridDim.x * kT) {
-    Tv hv[4], gv[4];
-    Vec4<Tv>::ld(h + i, hv);
-    Vec4<Tv>::ld(g + i, gv);
+  Tv hm = (Tv)0;
+  for (size_t i = V * (blockIdx.x * (size_t)kT + threadIdx.x); i < n; i += V * (size_t)gridDim.x * kT) {
+    Tv hv[V], gv[V];
+    VecN<Tv, V>::ld(h + i, hv);
+    VecN<Tv, V>::ld(mz ? mz + i : g + i, gv);
 #pragma unroll
-    for (int j = 0; j < 4; j++) hv[j] = gv[j] + beta * hv[j];
-    Vec4<Tv>::st(h + i, hv);
+    for (int j = 0; j < V; j++) {
+      hv[j] = mz ? beta * hv[j] - gv[j] : gv[j] + beta * hv[j];
+      hm = fmax(hm, fabs(hv[j]));
+    }
+    VecN<Tv, V>::st(h + i, hv);
+  }
+  const double acc[1] = {(double)hm};
+  __shared__ double res[1];
+  if (!reduce_last<0, 1>(acc, part, &ctl->counter, res)) return;
+  if (threadIdx.x == 0) {
+    ctl->hmax = res[0];
+    ctl->gh = ctl->gg + ctl->beta * ctl->hg;
   }
 }
 
 // Preconditioned CG.  The preconditioner handle's force evaluation of g
 // returns mz = -z, z = (Phi + c)^{-1} g.
-// Restart: h = z; g.z.
+// Restart: h = z; g.z, max|z|.
 template <typename Tv>
 __global__ void __launch_bounds__(kT) k_pcg_init(size_t n, const Tv *__restrict__ g, const Tv *__restrict__ mz,
                                                   Tv *__restrict__ h, double *__restrict__ part, CgCtl *ctl) {
   Dot<Tv> gz;
+  Tv zm = (Tv)0;
   for (size_t i = blockIdx.x * (size_t)kT + threadIdx.x; i < n; i += (size_t)gridDim.x * kT) {
     const Tv z = -mz[i];
     h[i] = z;
     gz.add(g[i], z);
+    zm = fmax(zm, fabs(z));
   }
-  const double acc[1] = {gz.get()};
-  __shared__ double res[1];
-  if (!reduce_last<1, 0>(acc, part, &ctl->counter, res)) return;
-  if (threadIdx.x == 0) ctl->gg = res[0];
+  const double acc[2] = {gz.get(), (double)zm};
+  __shared__ double res[2];
+  if (!reduce_last<1, 1>(acc, part, &ctl->counter, res)) return;
+  if (threadIdx.x == 0) {
+    ctl->gg = res[0];
+    ctl->gh = res[0];
+    ctl->hmax = res[1];
+  }
 }
 
 // After the update: beta = max(0, z.(g - g_old) / (g_old.z_old)) with the
@@ -811,15 +707,6 @@ __global__ void __launch_bounds__(kT) k_pcg_beta(size_t n, const Tv *__restrict_
     ctl->beta = beta;
     ctl->gg = res[0];
   }
-}
-
-// h = z + beta h
-template <typename Tv>
-__global__ void __launch_bounds__(kT) k_dir_pcg(size_t n, Tv *__restrict__ h, const Tv *__restrict__ mz,
-                                                 const CgCtl *ctl) {
-  const Tv beta = (Tv)ctl->beta;
-  for (size_t i = blockIdx.x * (size_t)kT + threadIdx.x; i < n; i += (size_t)gridDim.x * kT)
-    h[i] = beta * h[i] - mz[i];
 }
 
 __global__ void k_f2d(size_t n, const float *__restrict__ a, double *__restrict__ b) {
@@ -1039,28 +926,26 @@ cudaError_t enqueue_iteration(Item &it, cudaStream_t st, cudaGraphConditionalHan
   RT_CHECK(eval_on(hd, st, h, io_type<Tv>(), fKh, io_type<Tv>(), b.d_e, false));
   auto al16 = [](const void *p) { return p == nullptr || ((uintptr_t)p & 15) == 0; };
   Tv *gp = it.hpre ? reinterpret_cast<Tv *>(b.gp) : nullptr;
-  const bool v4 = nsite4(gm) && al16(x) && al16(h) && al16(fKh) && al16(g) && al16(gp);
+  Tv *mz = it.hpre ? reinterpret_cast<Tv *>(b.mz) : nullptr;
+  const bool v4 = nsite4(gm) && al16(x) && al16(h) && al16(fKh) && al16(g) && al16(gp) && al16(mz);
   const size_t nsite = (size_t)gm.nx * gm.ny;
   const int sms = it.hp->sm_count;
-  if (v4)
-    k_dirforce4<Tx, Tv, BIC><<<grid_for(k_dirforce4<Tx, Tv, BIC>, sms, nsite, 4 * kT), kT, 0, st>>>(it.o, gm, x, fKh, h, g,
-                                                                                           b.active, b.part, b.ctl);
-  else k_dirforce<Tx, Tv, BIC><<<b.nblk, kT, 0, st>>>(it.o, gm, x, fKh, h, g, b.active, b.part, b.ctl);
-  if (it.o.kind != GFMD_OBST_NONE)
+  const bool obst = it.o.kind != GFMD_OBST_NONE;
+  k_lsinit<Tx, Tv, BIC><<<obst ? b.nblk : 1, kT, 0, st>>>(it.o, gm, x, h, b.active, b.d_e, b.part, b.ctl);
+  if (obst)
     for (int p = 0; p < kLsMax; p++) k_probe<Tx, Tv, BIC><<<b.nblk, kT, 0, st>>>(it.o, gm, x, h, b.active, b.part, b.ctl);
   if (v4)
-    k_update4<Tx, Tv, BIC><<<grid_for(k_update4<Tx, Tv, BIC>, sms, nsite, 4 * kT), kT, 0, st>>>(
+    k_update<Tx, Tv, BIC, 4><<<grid_for(k_update<Tx, Tv, BIC, 4>, sms, nsite, 4 * kT), kT, 0, st>>>(
         it.o, gm, x, h, fKh, g, gp, b.active, b.part, b.ctl, hwh, use_hc);
-  else k_update<Tx, Tv, BIC><<<b.nblk, kT, 0, st>>>(it.o, gm, x, h, fKh, g, gp, b.active, b.part, b.ctl, hwh, use_hc);
+  else
+    k_update<Tx, Tv, BIC, 1><<<grid_for(k_update<Tx, Tv, BIC, 1>, sms, nsite, kT), kT, 0, st>>>(
+        it.o, gm, x, h, fKh, g, gp, b.active, b.part, b.ctl, hwh, use_hc);
   if (it.hpre) {
-    Tv *mz = reinterpret_cast<Tv *>(b.mz);
     RT_CHECK(eval_on(it.hpre, st, g, io_type<Tv>(), mz, io_type<Tv>(), b.d_e, false));
     k_pcg_beta<Tv><<<b.nblk, kT, 0, st>>>(b.n, g, gp, mz, b.part, b.ctl);
-    k_dir_pcg<Tv><<<b.nblk * 4, kT, 0, st>>>(b.n, h, mz, b.ctl);
-  } else {
-    if (v4) k_dir4<Tv><<<grid_for(k_dir4<Tv>, sms, b.n, 4 * kT), kT, 0, st>>>(b.n, h, g, b.ctl);
-    else k_dir<Tv><<<b.nblk * 4, kT, 0, st>>>(b.n, h, g, b.ctl);
   }
+  if (v4) k_dir<Tv, 4><<<grid_for(k_dir<Tv, 4>, sms, b.n, 4 * kT), kT, 0, st>>>(b.n, h, g, mz, b.part, b.ctl);
+  else k_dir<Tv, 1><<<grid_for(k_dir<Tv, 1>, sms, b.n, kT), kT, 0, st>>>(b.n, h, g, mz, b.part, b.ctl);
   return cudaGetLastError();
 }
 

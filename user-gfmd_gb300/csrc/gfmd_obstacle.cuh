@@ -42,6 +42,16 @@ struct Obst {
   float foff[8][3];
   float feps, finv_sigma, foffset, fgcut;  // map wall in FP32
   const float *mapf;   // FP32 copy of the map (may be NULL: then map is read)
+  // FP32 sphere walls and gating (sphere_off): the centre's nearest site
+  // (icx, icy) in [0, nx) x [0, ny), per layer the residual offsets
+  // (icx ax + off_x - cx, icy ay + off_y - cy) and off_z - cz + R
+  int icx, icy;
+  float fres[8][3];
+  float fc1, fc2, fc3, fc4;  // LJ coefficients in FP32
+  // gates of the CG kernels on cg_gate's value: evaluate the wall below gw,
+  // keep the site in the line-search set below ga (spheres: G (2R + G) for
+  // the gap ranges G, as |d|^2 - R^2 < G (2R + G) <=> gap < G; maps: gaps)
+  float gw, ga;
 };
 
 // Exponential map wall in FP32 on atom height rz at site s: energy and z force.
@@ -56,6 +66,63 @@ __device__ __forceinline__ void map_wall_f(const Obst &o, size_t s, float rz, fl
   const float ex = o.feps * expf(-dz * o.finv_sigma);
   e = ex - o.foffset;
   fz = o.fnorm * ex * o.finv_sigma;
+}
+
+// Offset of the atom of layer l at site (ix, iy), displaced by (ux, uy, uz),
+// from a sphere's centre, in FP32: dx, dy, the height w above the sphere's
+// lowest point and s = |d|^2 - R^2 = dx^2 + dy^2 + w (w - 2R).  The lateral
+// offsets start from the integer distance to the centre's nearest site
+// (minimum image in integers), so their rounding is relative to the offset
+// itself and not to the box; s has no cancellation against R^2, so the gap
+// s / (|d| + R) keeps FP32 precision relative to the gap.
+struct SphereOff {
+  float dx, dy, w, s;
+};
+__device__ __forceinline__ SphereOff sphere_off(const Obst &o, int nx, int ny, int ix, int iy, int l, float ux,
+                                                float uy, float uz) {
+  int jx = ix - o.icx, jy = iy - o.icy;
+  if (2 * jx >= nx) jx -= nx;
+  else if (2 * jx < -nx) jx += nx;
+  if (2 * jy >= ny) jy -= ny;
+  else if (2 * jy < -ny) jy += ny;
+  SphereOff q;
+  q.dx = fmaf((float)jx, o.fax, o.fres[l][0]) + ux;
+  q.dy = fmaf((float)jy, o.fay, o.fres[l][1]) + uy;
+  q.w = o.fres[l][2] + uz;
+  q.s = fmaf(q.dx, q.dx, fmaf(q.dy, q.dy, q.w * (q.w - 2.0f * o.fR)));
+  return q;
+}
+
+// Sphere wall (exponential or Lennard-Jones on the gap) in FP32 at offset q:
+// energy, force and the curvature dir^T H dir; false beyond the range.
+__device__ __forceinline__ bool sphere_wall_f(const Obst &o, const SphereOff &q, const float dir[3], float &e,
+                                              float f[3], float &curv) {
+  const float dz = q.w - o.fR;
+  const float rho2 = fmaf(q.dx, q.dx, fmaf(q.dy, q.dy, dz * dz));
+  const float ir = rsqrtf(rho2);
+  const float g = q.s / fmaf(rho2, ir, o.fR);
+  if (!(g < o.fgcut)) return false;
+  float F, E2;  // F = -dE/dg, E2 = d2E/dg2
+  if (o.kind == GFMD_OBST_SPHERE_EXP) {
+    const float ex = o.feps * expf(-g * o.finv_sigma);
+    e = ex - o.foffset;
+    F = ex * o.finv_sigma;
+    E2 = F * o.finv_sigma;
+  } else {
+    const float gi = 1.0f / g, g2 = gi * gi, g6 = g2 * g2 * g2;
+    e = g6 * (o.fc3 * g6 - o.fc4) - o.foffset;
+    F = g6 * (o.fc1 * g6 - o.fc2) * gi;
+    E2 = g6 * g2 * (13.0f * o.fc1 * g6 - 7.0f * o.fc2);
+  }
+  const float n0 = q.dx * ir, n1 = q.dy * ir, n2 = dz * ir;
+  f[0] = F * n0;
+  f[1] = F * n1;
+  f[2] = F * n2;
+  const float dn = dir[0] * n0 + dir[1] * n1 + dir[2] * n2;
+  const float dd = dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2];
+  // Hessian of E(|r-c|): E'' n n^T + (E'/rho)(1 - n n^T), E' = -F
+  curv = E2 * dn * dn - F * ir * (dd - dn * dn);
+  return true;
 }
 
 // FixWallMap's bicubic map table (Table2D with interpolated derivatives,
@@ -260,6 +327,26 @@ inline Obst make_obst(const gfmd_obstacle_t *ob, const Geom &g) {
   o.fgate_active = (float)(o.gcut + o.margin);
   for (int l = 0; l < 8; l++)
     for (int c = 0; c < 3; c++) o.foff[l][c] = (float)o.off[l][c];
+  if (o.kind == GFMD_OBST_SPHERE_EXP || o.kind == GFMD_OBST_SPHERE_LJ) {
+    const double kx = std::nearbyint(o.cx / o.ax), ky = std::nearbyint(o.cy / o.ay);
+    o.icx = (int)(((long long)kx % g.nx + g.nx) % g.nx);
+    o.icy = (int)(((long long)ky % g.ny + g.ny) % g.ny);
+    for (int l = 0; l < 8; l++) {
+      o.fres[l][0] = (float)(kx * o.ax + o.off[l][0] - o.cx);
+      o.fres[l][1] = (float)(ky * o.ay + o.off[l][1] - o.cy);
+      o.fres[l][2] = (float)(o.off[l][2] - o.cz + o.R);
+    }
+    const double gw = o.fgate_wall, ga = o.fgate_active;
+    o.gw = (float)(gw * (2.0 * o.R + gw));
+    o.ga = (float)(ga * (2.0 * o.R + ga));
+  } else {
+    o.gw = o.fgate_wall;
+    o.ga = o.fgate_active;
+  }
+  o.fc1 = (float)o.c1;
+  o.fc2 = (float)o.c2;
+  o.fc3 = (float)o.c3;
+  o.fc4 = (float)o.c4;
   o.mapf = nullptr;
   o.feps = (float)o.eps;
   o.finv_sigma = o.sigma > 0.0 ? (float)(1.0 / o.sigma) : 0.0f;

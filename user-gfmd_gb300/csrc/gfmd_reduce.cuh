@@ -9,12 +9,13 @@ namespace gfmd {
 namespace red {
 
 constexpr int kT = 256;  // threads per block of the reducing kernels
-constexpr int kQ = 8;    // partial slots per block
+constexpr int kQ = 10;   // partial slots per block
 
 template <typename T> struct Dot;
 template <> struct Dot<double> {
   double s = 0.0;
   __device__ __forceinline__ void add(double a, double b) { s = fma(a, b, s); }
+  __device__ __forceinline__ void addsum(double p) { s += p; }
   __device__ __forceinline__ double get() const { return s; }
 };
 // Compensated FP32 dot product: TwoProd via fmaf, TwoSum on the running sum.
@@ -28,6 +29,14 @@ template <> struct Dot<float> {
     const float se = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
     hi = s;
     lo = __fadd_rn(lo, __fadd_rn(se, pe));
+  }
+  // adds a partial sum (TwoSum only)
+  __device__ __forceinline__ void addsum(float p) {
+    const float s = __fadd_rn(hi, p);
+    const float bb = __fsub_rn(s, hi);
+    const float se = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    hi = s;
+    lo = __fadd_rn(lo, se);
   }
   __device__ __forceinline__ double get() const { return (double)hi + (double)lo; }
 };
