@@ -375,6 +375,64 @@ __global__ void __launch_bounds__(kT, 4) k_restart(const __grid_constant__ Obst 
   }
 }
 
+// Line-search state: step a and its bracket [lo, hi] (hi < 0: none yet).
+struct LineState {
+  double a, lo, hi, gh, hKh, fw0h, amax;
+  int it, done;
+};
+
+// Start from the sums at a = 0 (F_w(u).h and the wall curvature along h):
+// first Newton step on phi'(a) = -(g.h - a hKh + dF_w(a).h).
+__device__ __forceinline__ void ls_init(LineState &L, double fw0h, double cw0, double gh, double hKh, double hmax,
+                                        double dmax, bool obst) {
+  L.gh = gh;
+  L.hKh = hKh;
+  L.fw0h = fw0h;
+  // LAMMPS min_modify dmax: no component moves more than dmax in one step
+  L.amax = (dmax > 0.0 && hmax > 0.0) ? dmax / hmax : 1e300;
+  L.lo = 0.0;
+  L.it = 0;
+  // with the cap, amax is the upper bracket of the step from the start
+  L.hi = L.amax < 1e300 ? L.amax : -1.0;
+  const double curv = hKh + cw0;
+  double a;
+  if (curv > 0.0 && gh > 0.0) a = gh / curv;
+  else a = gh > 0.0 ? 1e-3 : 0.0;
+  if (gh > 0.0 && L.hi >= 0.0 && a >= L.hi) a = 0.5 * L.hi;  // bisect the bracket
+  L.a = a;
+  L.done = (!obst || gh <= 0.0) ? 1 : 0;
+}
+
+// The Newton step of a probe from the reduced F_w(u + a h).h and curvature.
+__device__ __forceinline__ void ls_step(LineState &L, double dfh, double cwall) {
+  const double a = L.a;
+  const double gdir = L.gh - a * L.hKh + (dfh - L.fw0h);
+  const double curv = L.hKh + cwall;
+  if (gdir > 0.0) L.lo = a;
+  else L.hi = a;
+  double an = (curv > 0.0) ? a + gdir / curv : -1.0;
+  if (L.hi >= 0.0 && (an <= L.lo || an >= L.hi || an < 0.0)) an = 0.5 * (L.lo + L.hi);
+  else if (an < 0.0) an = L.lo > 0.0 ? 2.0 * L.lo : 1e-3;
+  const double step = fabs(an - a);
+  L.a = an;
+  L.it += 1;
+  // an exact line minimum is not needed: Polak-Ribiere with restarts
+  // converges from a step within 1e-6 of it
+  if (step <= 1e-6 * fabs(an) || L.it >= kLsMax || !isfinite(an)) L.done = 1;
+  if (!isfinite(an)) L.a = 0.0;
+}
+
+__device__ __forceinline__ LineState ls_load(const CgCtl *c) {
+  LineState L;
+  L.a = c->a; L.lo = c->lo; L.hi = c->hi; L.gh = c->gh; L.hKh = c->hKh; L.fw0h = c->fw0h; L.amax = c->amax;
+  L.it = c->ls_it; L.done = c->ls_done;
+  return L;
+}
+__device__ __forceinline__ void ls_store(CgCtl *c, const LineState &L) {
+  c->a = L.a; c->lo = L.lo; c->hi = L.hi; c->gh = L.gh; c->hKh = L.hKh; c->fw0h = L.fw0h; c->amax = L.amax;
+  c->ls_it = L.it; c->ls_done = L.done;
+}
+
 // ---- start of the line search: h.K.h from the energy of the direction's
 // force evaluation (E(h) = h.K.h / 2 with the gamma-point force off), g.h and
 // max|h| from the kernel that formed h, wall terms at a = 0 over the set;
@@ -391,45 +449,10 @@ __global__ void __launch_bounds__(kT) k_lsinit(const __grid_constant__ Obst o, G
   __shared__ double res[2];
   if (!reduce_last<2, 0>(acc, part, &ctl->counter, res)) return;
   if (threadIdx.x == 0) {
-    const double hKh = 2.0 * (*eh);
-    const double ghv = ctl->gh, curv = hKh + res[1];
-    // LAMMPS min_modify dmax: no component moves more than dmax in one step
-    ctl->amax = (ctl->dmax > 0.0 && ctl->hmax > 0.0) ? ctl->dmax / ctl->hmax : 1e300;
-    ctl->hKh = hKh;
-    ctl->fw0h = res[0];
-    ctl->lo = 0.0;
-    ctl->ls_it = 0;
-    // with the cap, amax is the upper bracket of the step from the start
-    ctl->hi = ctl->amax < 1e300 ? ctl->amax : -1.0;
-    // Newton step from a = 0 on phi'(a) = -(g.h - a hKh + dF_w(a).h)
-    double a;
-    if (curv > 0.0 && ghv > 0.0) a = ghv / curv;
-    else a = ghv > 0.0 ? 1e-3 : 0.0;
-    if (ghv > 0.0 && ctl->hi >= 0.0 && a >= ctl->hi) a = 0.5 * ctl->hi;  // bisect the bracket
-    ctl->a = a;
-    ctl->ls_done = (o.kind == GFMD_OBST_NONE || ghv <= 0.0) ? 1 : 0;
+    LineState L;
+    ls_init(L, res[0], res[1], ctl->gh, 2.0 * (*eh), ctl->hmax, ctl->dmax, o.kind != GFMD_OBST_NONE);
+    ls_store(ctl, L);
   }
-}
-
-// The Newton step of a probe from the reduced F_w(u + a h).h and curvature.
-__device__ __forceinline__ void probe_step(CgCtl *ctl, double a, double dfh, double cwall) {
-  const double gdir = ctl->gh - a * ctl->hKh + (dfh - ctl->fw0h);
-  const double curv = ctl->hKh + cwall;
-  double lo = ctl->lo, hi = ctl->hi;
-  if (gdir > 0.0) lo = a;
-  else hi = a;
-  double an = (curv > 0.0) ? a + gdir / curv : -1.0;
-  if (hi >= 0.0 && (an <= lo || an >= hi || an < 0.0)) an = 0.5 * (lo + hi);
-  else if (an < 0.0) an = lo > 0.0 ? 2.0 * lo : 1e-3;
-  const double step = fabs(an - a);
-  ctl->lo = lo;
-  ctl->hi = hi;
-  ctl->a = an;
-  ctl->ls_it += 1;
-  // an exact line minimum is not needed: Polak-Ribiere with restarts
-  // converges from a step within 1e-6 of it
-  if (step <= 1e-6 * fabs(an) || ctl->ls_it >= kLsMax || !isfinite(an)) ctl->ls_done = 1;
-  if (!isfinite(an)) ctl->a = 0.0;
 }
 
 // ---- one Newton probe of the line search at u + a h ------------------------
@@ -447,7 +470,11 @@ __global__ void __launch_bounds__(kT) k_probe(const __grid_constant__ Obst o, Ge
   const double acc[2] = {dfh, cw};
   __shared__ double res[2];
   if (!reduce_last<2, 0>(acc, part, &ctl->counter, res)) return;
-  if (threadIdx.x == 0) probe_step(ctl, a, res[0], res[1]);
+  if (threadIdx.x == 0) {
+    LineState L = ls_load(ctl);
+    ls_step(L, res[0], res[1]);
+    ls_store(ctl, L);
+  }
 }
 
 // ---- update after the line search ------------------------------------------
