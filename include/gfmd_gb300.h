@@ -136,6 +136,17 @@ int gfmd_force_kernel_times(gfmd_handle_t h, const void *d_u, void *d_f, double 
  * reference (introspection). */
 int gfmd_kernel_plan(gfmd_handle_t h, int *row_warp_tma, int *col_cluster, int *phi_vector);
 
+/* Storage pattern of the uploaded table, chosen by gfmd_set_phi from the
+ * pairs that are exactly zero at every wavevector: 0 every pair; 1
+ * layer-tridiagonal (3x3 blocks of layers two or more apart are zero); 2 as 1
+ * with the blocks of all layers but the last diagonal (a slab with
+ * nearest-neighbour interactions).  Used by the register-transform column
+ * kernel at ndof 12; reals_per_wavevector = reals streamed per wavevector.
+ * Forces are the same with every pattern (the skipped products are zero and
+ * the kept ones are summed in the same order).  No counterpart in the
+ * reference (introspection). */
+int gfmd_phi_pattern(gfmd_handle_t h, int *pattern, int *reals_per_wavevector);
+
 /* ---- solver loops ----------------------------------------------------- */
 
 /* Obstacles acting on every atom of the grid.  The position of the atom of

@@ -280,3 +280,44 @@ def test_energy_of_a_direction_is_half_its_stiffness_product(args, nx, ny, plain
         hkh = -float((hd.double() * f.double()).sum())
         assert hkh > 0
         assert abs(2.0 * float(ep) - hkh) <= tol * hkh, (prec, 2.0 * float(ep), hkh)
+
+
+@pytest.mark.parametrize(
+    "args,nx,ny,pattern",
+    [
+        ("ft fcc100 1.0 4 pair-potential 1 1.0 height 64", 2048, 32, 2),
+        ("ft fcc100 1.0 4 pair-potential 1 1.0 height 64", 1024, 64, 2),
+    ],
+)
+def test_structured_table_is_bit_identical_to_dense(args, nx, ny, pattern, monkeypatch):
+    """A layer-tridiagonal table is stored without its zero pairs; the column
+    kernel then sums the same nonzero terms in the same order, so forces and
+    energy equal those of the dense storage bit for bit, and the oracle's to
+    the FP32 tolerance."""
+    g = gfmd_pkg()
+    k = g.StiffnessKernel(args)
+    d = k.get_dimension()
+    half, linf = k.phi_table(nx, ny, "half")
+    u = np.random.default_rng(nx + ny).normal(0.0, 0.01, (d, nx * ny))
+    s = _solver(nx, ny, d, "f32", half, "half", linf)
+    info = s.info()
+    assert info["phi_pattern"] == pattern
+    assert info["phi_reals_per_wavevector"] < d * d
+    monkeypatch.setenv("GFMD_PHI_DENSE", "1")
+    sd = _solver(nx, ny, d, "f32", half, "half", linf)
+    monkeypatch.delenv("GFMD_PHI_DENSE")
+    assert sd.info()["phi_pattern"] == 0
+    f, fd = np.zeros_like(u), np.zeros_like(u)
+    e, ed = s.post_force(u, f), sd.post_force(u, fd)
+    assert np.array_equal(f, fd) and e == ed
+    f_ref, e_ref, _ = oracle_post_force(half_to_full(half, nx, ny), linf, u, nx, ny)
+    assert rel_l2(f, f_ref) <= FP32_TOL
+    assert abs(e - e_ref) <= FP32_TOL * abs(e_ref)
+    # the inverse-table handle reads the structured table back
+    p = s.make_preconditioner(1.0) if hasattr(s, "make_preconditioner") else None
+    if p is not None:
+        pd = sd.make_preconditioner(1.0)
+        fp, fpd = np.zeros_like(u), np.zeros_like(u)
+        p.post_force(u, fp)
+        pd.post_force(u, fpd)
+        assert np.array_equal(fp, fpd)

@@ -157,6 +157,7 @@ SIGNATURES = {
     "gfmd_plan_info": [_vp, _pi, _pi],
     "gfmd_force_kernel_times": [_vp, _vp, _vp, _vp, ctypes.POINTER(ctypes.c_float), _c_int, _pi],
     "gfmd_kernel_plan": [_vp, _pi, _pi, _pi],
+    "gfmd_phi_pattern": [_vp, _pi, _pi],
     "gfmd_minimize": [_vp, ctypes.POINTER(Obstacle), ctypes.POINTER(MinParams), _vp,
                       ctypes.POINTER(MinReport)],
     "gfmd_make_preconditioner": [_vp, _c_dbl, ctypes.POINTER(_vp)],

@@ -54,7 +54,7 @@ def build(verbose_ptxas: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     extra = ["-Xptxas", "-v"] if verbose_ptxas else []
     srcs = sources()
-    with ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+    with ThreadPoolExecutor(max_workers=min(max(os.cpu_count() or 1, 1), len(srcs))) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra), srcs))
     newest = max(os.path.getmtime(o) for o in objs)
     if not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:

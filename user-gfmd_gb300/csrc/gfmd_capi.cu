@@ -310,11 +310,17 @@ int set_error(int code, const std::string &msg) { return fail(code, msg); }
 
 size_t phi_index(const gfmd_solver *h, int ky, int pos, int e) {
   const Geom &g = h->g;
-  const size_t D2 = (size_t)g.npk;
+  size_t D2 = (size_t)g.npk;
   if (!h->fast) return ((size_t)ky * D2 + e) * g.nxp + pos;  // [ky][e][nxp]
   const size_t blk = (size_t)ky * (g.nxp / 32) + pos / 32;
-  if (h->col_cl > 0 && h->phi_v == 4)  // [ky][x/32][e/4][32][4]
+  if (h->col_cl > 0 && h->phi_v == 4) {  // [ky][x/32][e/4][32][4]
+    if (h->phi_pat != 0) {  // elements of the storage pattern only
+      if (h->phi_slot[e] < 0) return kPhiAbsent;
+      e = h->phi_slot[e];
+      D2 = (size_t)pat_floats(g.ndof, h->phi_pat);
+    }
     return (blk * (D2 / 4) + e / 4) * 128 + (size_t)(pos % 32) * 4 + e % 4;
+  }
   return (blk * D2 + e) * 32 + pos % 32;  // [ky][x/32][e][32]
 }
 
@@ -505,7 +511,7 @@ cudaError_t autotune(gfmd_solver *h) {
   const char *env = getenv("GFMD_AUTOTUNE");
   if (env && env[0] == '0') return cudaSuccess;
   const PlanKey key{h->g.nx, h->g.ny, h->g.ndof, h->precision,
-                    (h->rows32 ? 1 : 0) | (h->col_r32 ? 2 : 0) | (h->col_cl << 2)};
+                    (h->rows32 ? 1 : 0) | (h->col_r32 ? 2 : 0) | (h->col_cl << 2) | (h->phi_pat << 8)};
   {
     std::lock_guard<std::mutex> lk(g_plan_mu);
     auto it = g_plans.find(key);
@@ -634,6 +640,50 @@ int gfmd_set_phi(gfmd_handle_t h, const double *phi, int layout, const double *l
     if (layout == GFMD_PHI_FULL) return phi + 2 * ((size_t)kx * g.ny + ky) * D2;
     return phi + 2 * ((size_t)kx * g.nyc + ky) * D2;
   };
+  // storage pattern: the register-transform column kernel at ndof 12 skips
+  // the pairs that are exactly zero at every wavevector of the table
+  // (GFMD_PHI_DENSE=1: always every pair)
+  const int old_pat = h->phi_pat;
+  h->phi_pat = 0;
+  h->phi_slot.clear();
+  const char *dense_env = getenv("GFMD_PHI_DENSE");
+  if (h->col_r32 && !f64 && D == 12 && h->phi_v == 4 && !(dense_env && dense_env[0] == '1')) {
+    const size_t nsrc = layout == GFMD_PHI_FULL ? (size_t)g.nx * g.ny : (size_t)g.nx * g.nyc;
+    std::mutex mu;
+    std::vector<char> nz(D2, 0);
+    parallel_for((long)nsrc, [&](long a, long b) {
+      std::vector<char> loc(D2, 0);
+      for (long t = a; t < b; t++) {
+        const double *pe = phi + 2 * (size_t)t * D2;
+        for (int e = 0; e < D2; e++) loc[e] |= (pe[2 * e] != 0.0 || pe[2 * e + 1] != 0.0) ? 1 : 0;
+      }
+      std::lock_guard<std::mutex> lk(mu);
+      for (int e = 0; e < D2; e++) nz[e] |= loc[e];
+    });
+    for (int pat : {2, 1}) {
+      bool fits = true;
+      for (int i = 0; i < D && fits; i++)
+        for (int j = i + 1; j < D; j++)
+          if (!gfmd::pat_keeps(D, pat, i, j) && (nz[i * D + j] || nz[j * D + i])) {
+            fits = false;
+            break;
+          }
+      if (!fits) continue;
+      h->phi_pat = pat;
+      h->phi_slot.assign(D2, -1);
+      for (int i = 0; i < D; i++) h->phi_slot[i] = i;
+      int pd = D, ps = D;  // dense and pattern positions, pairs in row-major order
+      for (int i = 0; i < D; i++)
+        for (int j = i + 1; j < D; j++, pd += 2)
+          if (gfmd::pat_keeps(D, pat, i, j)) {
+            h->phi_slot[pd] = ps;
+            h->phi_slot[pd + 1] = ps + 1;
+            ps += 2;
+          }
+      break;
+    }
+  }
+  if (h->phi_pat != old_pat) h->tuned = false;  // another column kernel: plan it again
   parallel_for((long)g.nyc * g.nx, [&](long a, long b) {
     std::vector<double> eff(2 * D2);
     bool ok = true;
@@ -661,6 +711,7 @@ int gfmd_set_phi(gfmd_handle_t h, const double *phi, int layout, const double *l
       auto put = [&](int p, double v) {
         if (!std::isfinite(v)) ok = false;
         const size_t at = gfmd::phi_index(h, ky, xs, p);
+        if (at == gfmd::kPhiAbsent) return;  // zero at every wavevector
         if (f64) packd[at] = v;
         else packf[at] = (float)v;
       };
@@ -678,7 +729,8 @@ int gfmd_set_phi(gfmd_handle_t h, const double *phi, int layout, const double *l
   });
   if (!finite) return fail(GFMD_ENONFINITE, "gfmd_set_phi: table holds NaN or Inf");
   const void *hp = f64 ? (const void *)packd.data() : (const void *)packf.data();
-  size_t bytes = nq * D2 * (f64 ? 8 : 4);
+  const size_t per_q = h->phi_pat ? (size_t)gfmd::pat_floats(D, h->phi_pat) : (size_t)D2;
+  size_t bytes = nq * per_q * (f64 ? 8 : 4);
   CK(cudaMemcpy(h->d_phi, hp, bytes, cudaMemcpyHostToDevice), "gfmd_set_phi: upload");
   std::vector<double> lf(D / 3, 0.0);
   if (linf)
@@ -745,18 +797,24 @@ static int inverse_table_handle(gfmd_handle_t h, const char *who, double scale, 
       return cuda_fail(e, (w + ": download").c_str());
     }
   }
+  std::vector<double> inv(nel, 0.0);  // p's table (every pair: the inverse is dense)
   std::atomic<bool> ok(true);
   parallel_for((long)nslot, [&](long a, long b) {
     std::vector<std::complex<double>> A(D2), I(D2);
     for (long t = a; t < b; t++) {
       const int ky = (int)(t / g.nxp), xs = (int)(t % g.nxp);
-      auto at = [&](int e) { return gfmd::phi_index(h, ky, xs, e); };
+      // h's table (pairs outside its storage pattern are zero); p's table
+      auto rd = [&](int e) {
+        const size_t i = gfmd::phi_index(h, ky, xs, e);
+        return i == gfmd::kPhiAbsent ? 0.0 : tab[i];
+      };
+      auto at = [&](int e) { return gfmd::phi_index(p, ky, xs, e); };
       // Hermitian block of the uploaded table
-      for (int i = 0; i < D; i++) A[i * D + i] = tab[at(i)];
+      for (int i = 0; i < D; i++) A[i * D + i] = rd(i);
       int q = D;
       for (int i = 0; i < D; i++)
         for (int j = i + 1; j < D; j++) {
-          const std::complex<double> v(tab[at(q)], tab[at(q + 1)]);
+          const std::complex<double> v(rd(q), rd(q + 1));
           A[i * D + j] = v;
           A[j * D + i] = std::conj(v);
           q += 2;
@@ -787,13 +845,13 @@ static int inverse_table_handle(gfmd_handle_t h, const char *who, double scale, 
         }
       }
       // pack scale * inverse (Hermitian part)
-      for (int i = 0; i < D; i++) tab[at(i)] = scale * I[i * D + i].real();
+      for (int i = 0; i < D; i++) inv[at(i)] = scale * I[i * D + i].real();
       q = D;
       for (int i = 0; i < D; i++)
         for (int j = i + 1; j < D; j++) {
           const std::complex<double> v = 0.5 * scale * (I[i * D + j] + std::conj(I[j * D + i]));
-          tab[at(q)] = v.real();
-          tab[at(q + 1)] = v.imag();
+          inv[at(q)] = v.real();
+          inv[at(q + 1)] = v.imag();
           q += 2;
         }
     }
@@ -804,10 +862,10 @@ static int inverse_table_handle(gfmd_handle_t h, const char *who, double scale, 
   }
   cudaError_t e;
   if (f64) {
-    e = cudaMemcpy(p->d_phi, tab.data(), nel * 8, cudaMemcpyHostToDevice);
+    e = cudaMemcpy(p->d_phi, inv.data(), nel * 8, cudaMemcpyHostToDevice);
   } else {
     std::vector<float> tf(nel);
-    for (size_t i = 0; i < nel; i++) tf[i] = (float)tab[i];
+    for (size_t i = 0; i < nel; i++) tf[i] = (float)inv[i];
     e = cudaMemcpy(p->d_phi, tf.data(), nel * 4, cudaMemcpyHostToDevice);
   }
   if (e != cudaSuccess) {
@@ -1003,6 +1061,14 @@ int gfmd_kernel_plan(gfmd_handle_t h, int *row_warp_tma, int *col_cluster, int *
   if (row_warp_tma) *row_warp_tma = h->rows32 ? 1 : 0;
   if (col_cluster) *col_cluster = h->col_cl;
   if (phi_vector) *phi_vector = h->phi_v;
+  return GFMD_OK;
+}
+
+int gfmd_phi_pattern(gfmd_handle_t h, int *pattern, int *reals_per_wavevector) {
+  if (!h) return fail(GFMD_EINVAL, "gfmd_phi_pattern: NULL handle");
+  if (pattern) *pattern = h->phi_pat;
+  if (reals_per_wavevector)
+    *reals_per_wavevector = h->phi_pat ? gfmd::pat_floats(h->g.ndof, h->phi_pat) : h->g.npk;
   return GFMD_OK;
 }
 

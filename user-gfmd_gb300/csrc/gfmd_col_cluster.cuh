@@ -76,7 +76,7 @@ __device__ __forceinline__ void dit_task_g(float2 *col, int base, int S, int j, 
 // Forward transform of nb columns of length p.n (stride cs) in place,
 // natural -> digit-reversed; tab: stage tables (global).  Ends with a
 // block barrier.
-__device__ void fft_dif_g(float2 *buf, int nb, int cs, const P2Plan &p, const float4 *__restrict__ tab) {
+inline __device__ void fft_dif_g(float2 *buf, int nb, int cs, const P2Plan &p, const float4 *__restrict__ tab) {
   int lgL = p.lgn;
 #pragma unroll
   for (int s = 0; s < kP2MaxStages; s++) {
@@ -103,7 +103,7 @@ __device__ void fft_dif_g(float2 *buf, int nb, int cs, const P2Plan &p, const fl
 }
 
 // Backward transform in place, digit-reversed -> natural (unscaled).
-__device__ void fft_dit_g(float2 *buf, int nb, int cs, const P2Plan &p, const float4 *__restrict__ tab) {
+inline __device__ void fft_dit_g(float2 *buf, int nb, int cs, const P2Plan &p, const float4 *__restrict__ tab) {
 #pragma unroll
   for (int s = kP2MaxStages - 1; s >= 0; s--) {
     if (s >= p.nst) continue;
@@ -154,7 +154,8 @@ constexpr int pair_col(int D, int p) {
 // elements come as float4 vectors at ph[g * 32] (g = element / 4); V = 1:
 // scalars at ph[e * 32].  D even with V = 4 keeps every (Re, Im) pair
 // inside one vector.
-template <int D, int V> struct PhiApply {
+template <int D, int V, int PAT = 0> struct PhiApply {
+  static_assert(PAT == 0 || V == 4, "table patterns use the vector layout");
   template <int E>
   static __device__ __forceinline__ void item(float h0, float h1, const float2 *uq, float2 *F) {
     if constexpr (E < D) {  // two diagonal entries (E, E + 1) or one
@@ -164,8 +165,8 @@ template <int D, int V> struct PhiApply {
         F[E + 1].x = fmaf(h1, uq[E + 1].x, F[E + 1].x);
         F[E + 1].y = fmaf(h1, uq[E + 1].y, F[E + 1].y);
       }
-    } else {
-      constexpr int P = (E - D) / 2, I = pair_row(D, P), J = pair_col(D, P);
+    } else if constexpr ((E - D) / 2 < pat_pairs(D, PAT)) {  // else: padding
+      constexpr int P = (E - D) / 2, I = pat_pair(D, PAT, P, 0), J = pat_pair(D, PAT, P, 1);
       const float hr = h0, hi = h1;
       F[I].x = fmaf(hr, uq[J].x, fmaf(-hi, uq[J].y, F[I].x));
       F[I].y = fmaf(hr, uq[J].y, fmaf(hi, uq[J].x, F[I].y));
@@ -198,8 +199,8 @@ template <int D, int V> struct PhiApply {
                                              std::integer_sequence<int, Gs...>) {
     (group<Gs>(ph, uq, F), ...);
   }
-  // number of groups: D*D/4 vectors, or D diagonals + D(D-1)/2 pairs
-  static constexpr int kGroups = V == 4 ? D * D / 4 : D + D * (D - 1) / 2;
+  // number of groups: float4 vectors of the pattern, or D diagonals + D(D-1)/2 pairs
+  static constexpr int kGroups = V == 4 ? pat_floats(D, PAT) / 4 : D + D * (D - 1) / 2;
   static __device__ __forceinline__ void run(const float *__restrict__ ph, const float2 *uq, float2 *F) {
     all(ph, uq, F, std::make_integer_sequence<int, kGroups>{});
   }
@@ -353,7 +354,7 @@ __device__ __forceinline__ float2 w64(int k) {
 // [r DL, (r+1) DL), DL * P threads (thread c P + t: column c, index t).
 // twa: [k1][t] compensated w_nx^(t k1); phi packed [ky][q/32][D*D/4][32][4]
 // (V = 4) or [ky][q/32][D*D][32] (V = 1) over the storage positions q.
-template <int D, int CL, int LGN, int MINB>
+template <int D, int CL, int LGN, int MINB, int PAT = 0>
 __global__ void __launch_bounds__((D / CL) * (1 << LGN) / 32, MINB)
     k_col_phi_r32(float2 *__restrict__ W, const float *__restrict__ phi, Geom g, const float4 *__restrict__ twa,
                   const double *__restrict__ linf, double *__restrict__ epart, double *__restrict__ scal,
@@ -361,7 +362,7 @@ __global__ void __launch_bounds__((D / CL) * (1 << LGN) / 32, MINB)
   namespace cg = cooperative_groups;
   constexpr int n = 1 << LGN, P = n / 32, DL = D / CL, NT = DL * P;
   constexpr int V = (D * D) % 4 == 0 ? 4 : 1;
-  constexpr int kPerPos = D * D;
+  constexpr int kPerPos = V == 4 ? pat_floats(D, PAT) : D * D;  // floats per wavevector
   constexpr unsigned kBlk = (unsigned)(kPerPos * 32 * 4);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red[NT / 32];
@@ -439,7 +440,7 @@ __global__ void __launch_bounds__((D / CL) * (1 << LGN) / 32, MINB)
       uq[j] = part[j / DL][(j % DL) * n + pos];
       F[j] = make_float2(0.0f, 0.0f);
     }
-    colcl::PhiApply<D, V>::run(ph, uq, F);
+    colcl::PhiApply<D, V, PAT>::run(ph, uq, F);
     float es = 0.0f;
 #pragma unroll
     for (int i = 0; i < D; i++) es = fmaf(F[i].x, uq[i].x, fmaf(F[i].y, uq[i].y, es));
@@ -523,6 +524,32 @@ __global__ void __launch_bounds__((D / CL) * (1 << LGN) / 32, MINB)
       *counter = 0u;
     }
   }
+}
+
+// Register-transform column kernel (nx = 2^LGN in {1024, 2048}): one
+// cluster of CL blocks per ky, launched with its cluster dimension.
+template <int D, int CL, int LGN, int MINB, int PAT = 0>
+cudaError_t launch_col_r32(gfmd_solver *h, float2 *W, double *d_epot) {
+  constexpr int NT = (D / CL) * (1 << LGN) / 32;
+  auto kf = k_col_phi_r32<D, CL, LGN, MINB, PAT>;
+  const size_t sm = (size_t)(D / CL) * (1 << LGN) * sizeof(float2);
+  cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(h->g.nyc * CL);
+  cfg.blockDim = dim3(NT);
+  cfg.dynamicSmemBytes = sm;
+  cfg.stream = h->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = CL;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kf, W, reinterpret_cast<const float *>(h->d_phi), h->g,
+                            reinterpret_cast<const float4 *>(h->d_twc), (const double *)h->d_linf, h->d_epart,
+                            h->d_scal, h->d_counter, d_epot, h->col_pf);
 }
 
 }  // namespace gfmd

@@ -98,6 +98,8 @@ struct gfmd_solver {
   bool rows32 = false;       // warp-per-row row kernels with TMA tiles (ny = 2048)
   int col_cl = 0;            // blocks per ky of the cluster column kernel (0: not used)
   int phi_v = 1;             // packed-Phi vector width of that kernel (1 or 4)
+  int phi_pat = 0;           // storage pattern of the packed table (pat_keeps), chosen at upload
+  std::vector<int> phi_slot; // pattern != 0: float slot of each dense element (-1: structural zero)
   bool col_r32 = false;      // register-transform column kernel (nx = 1024, 2048): positions
                              // q = (nx/32) (kx mod 32) + kx/32; else digit-reversed kx
   void *d_twc = nullptr;     // float4 [k1][t] w_nx^(t k1) of that kernel
@@ -122,6 +124,42 @@ struct gfmd_solver {
 };
 
 namespace gfmd {
+// Storage patterns of the packed table (register-transform column kernel).
+// PAT 0: every pair.  PAT 1 (layer-tridiagonal): the pairs inside a layer's
+// 3x3 block and between adjacent layers; blocks of layers two or more apart
+// are zero.  PAT 2: as 1, and the 3x3 blocks of all layers but the last are
+// diagonal (the table of a slab with nearest-neighbour interactions whose
+// last layer carries the substrate below).  The kept pairs stay in row-major
+// order, so every force component sums the same nonzero terms in the same
+// order as with PAT 0; an element of a pattern is D diagonal reals followed
+// by the (Re, Im) of the kept pairs, padded to a multiple of 4 floats.
+constexpr bool pat_keeps(int D, int PAT, int i, int j) {
+  const int li = i / 3, lj = j / 3;
+  if (PAT == 0) return true;
+  if (lj - li >= 2) return false;
+  if (PAT == 2 && li == lj && li < D / 3 - 1) return false;
+  return true;
+}
+constexpr int pat_pairs(int D, int PAT) {
+  int n = 0;
+  for (int i = 0; i < D; i++)
+    for (int j = i + 1; j < D; j++) n += pat_keeps(D, PAT, i, j) ? 1 : 0;
+  return n;
+}
+// row (which = 0) or column (1) of the p-th kept pair
+constexpr int pat_pair(int D, int PAT, int p, int which) {
+  for (int i = 0; i < D; i++)
+    for (int j = i + 1; j < D; j++)
+      if (pat_keeps(D, PAT, i, j)) {
+        if (p == 0) return which == 0 ? i : j;
+        p--;
+      }
+  return -1;
+}
+constexpr int pat_floats(int D, int PAT) { return (D + 2 * pat_pairs(D, PAT) + 3) / 4 * 4; }
+// phi_index of an element outside the handle's storage pattern
+constexpr size_t kPhiAbsent = ~(size_t)0;
+
 // Enqueue one force evaluation.  u/f are [ndof][nx*ny] of type in_t/out_t
 // (0 = double, 1 = float); energy -> d_epot (device double).
 cudaError_t enqueue_force(gfmd_solver *h, const void *d_u, int in_t, void *d_f, int out_t,
@@ -135,6 +173,23 @@ int cg_minimize(gfmd_solver *hp, const gfmd_obstacle_t *ob, const gfmd_min_param
                 gfmd_min_report_t *rep, std::string &err);
 // Records msg as the calling thread's gfmd_last_error() and returns code.
 int set_error(int code, const std::string &msg);
+// The register-transform column kernel of h on W (gfmd_col_r32.cu), and its
+// instances for structured ndof-12 tables (gfmd_col_r32_pat.cu).
+cudaError_t enqueue_col_r32(gfmd_solver *h, float2 *W, double *d_epot);
+cudaError_t enqueue_col_r32_pat(gfmd_solver *h, float2 *W, double *d_epot);
+// The fused shared-memory column kernel of h on W (C<float> / C<double>)
+// with dynamic shared memory smem (gfmd_col_fast_f32.cu, gfmd_col_fast_f64.cu).
+cudaError_t enqueue_col_fast_f32(gfmd_solver *h, void *W, size_t smem, double *d_epot);
+cudaError_t enqueue_col_fast_f64(gfmd_solver *h, void *W, size_t smem, double *d_epot);
+// The thread-block-cluster column kernel of h on W (gfmd_col_cl.cu).
+cudaError_t enqueue_col_cl(gfmd_solver *h, float2 *W, double *d_epot);
+// Warp-per-row TMA row transforms: u (in_t) -> W, W -> f (out_t) (gfmd_rows32.cu).
+cudaError_t enqueue_row_fwd32(gfmd_solver *h, const void *d_u, int in_t);
+cudaError_t enqueue_row_inv32(gfmd_solver *h, void *d_f, int out_t);
+// Phi application of the general-size path on the grid `grid` of
+// wavevector blocks (gfmd_phi_plain_f32.cu, gfmd_phi_plain_f64.cu).
+cudaError_t enqueue_phi_plain_f32(gfmd_solver *h, dim3 grid);
+cudaError_t enqueue_phi_plain_f64(gfmd_solver *h, dim3 grid);
 // Kernel launches one force evaluation makes.
 int force_launches(const gfmd_solver *h);
 // Index (in reals) of packed element e of the wavevector at storage position

@@ -1,0 +1,40 @@
+// Launches of the per-wavevector Phi application of the general-size path
+// (k_phi_apply, gfmd_plain_kernels.cuh) for FP64 handles, one instance per
+// ndof, in a translation unit of their own so the build compiles them beside
+// the other kernels.
+#include <cuda_runtime.h>
+
+#include "gfmd_internal.h"
+#include "gfmd_fft.cuh"
+#include "gfmd_plain_kernels.cuh"
+
+namespace gfmd {
+
+namespace {
+
+template <typename T, int D> cudaError_t launch_phi(gfmd_solver *h, dim3 grid) {
+  k_phi_apply<T, D><<<grid, kPhiThreads, 0, h->stream>>>(reinterpret_cast<C<T> *>(h->d_W),
+                                                         reinterpret_cast<const T *>(h->d_phi), h->g, h->d_linf,
+                                                         h->d_epart, h->d_scal);
+  return cudaGetLastError();
+}
+
+template <typename T> cudaError_t phi_t(gfmd_solver *h, dim3 grid) {
+  switch (h->g.ndof) {
+    case 3: return launch_phi<T, 3>(h, grid);
+    case 6: return launch_phi<T, 6>(h, grid);
+    case 9: return launch_phi<T, 9>(h, grid);
+    case 12: return launch_phi<T, 12>(h, grid);
+    case 15: return launch_phi<T, 15>(h, grid);
+    case 18: return launch_phi<T, 18>(h, grid);
+    case 21: return launch_phi<T, 21>(h, grid);
+    case 24: return launch_phi<T, 24>(h, grid);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace
+
+cudaError_t enqueue_phi_plain_f64(gfmd_solver *h, dim3 grid) { return phi_t<double>(h, grid); }
+
+}  // namespace gfmd

@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(kPhiThreads) k_phi_apply(C<T> *__restrict__ W,
 }
 
 // Fixed-order sum of the energy partials; E = 0.5 * sum (:236).
-__global__ void __launch_bounds__(256) k_reduce(const double *__restrict__ epart, int n,
+static __global__ void __launch_bounds__(256) k_reduce(const double *__restrict__ epart, int n,
                                                 double *__restrict__ out) {
   __shared__ double red[256];
   double s = 0.0;

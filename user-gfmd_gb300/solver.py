@@ -403,9 +403,12 @@ class GFMDSolverGB300:
         check(lib().gfmd_plan_info(self._handle(), ctypes.byref(rb), ctypes.byref(pf)))
         rw, cl, pv = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         check(lib().gfmd_kernel_plan(self._handle(), ctypes.byref(rw), ctypes.byref(cl), ctypes.byref(pv)))
+        pat, npq = ctypes.c_int(), ctypes.c_int()
+        check(lib().gfmd_phi_pattern(self._handle(), ctypes.byref(pat), ctypes.byref(npq)))
         return {"launches_per_eval": n.value, "fused": bool(f.value),
                 "rows_per_block": rb.value, "phi_prefetch": pf.value,
-                "row_warp_tma": bool(rw.value), "col_cluster": cl.value, "phi_vector": pv.value}
+                "row_warp_tma": bool(rw.value), "col_cluster": cl.value, "phi_vector": pv.value,
+                "phi_pattern": pat.value, "phi_reals_per_wavevector": npq.value}
 
     def kernel_times(self, u, f, epot) -> list:
         """Device milliseconds of each launch of one evaluation of u (device
