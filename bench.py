@@ -78,10 +78,11 @@ def dist_env():
     return ws, rank, local
 
 
-def algorithmic_bytes(nx, ny, d, s):
+def algorithmic_bytes(nx, ny, d, s, phi_reals=None):
     """Bytes of one force evaluation: read u, write f, read the
-    Hermitian-packed half-spectrum Phi (ndof^2 reals per stored wavevector)."""
-    return 2 * nx * ny * d * s + nx * (ny // 2 + 1) * d * d * s
+    Hermitian-packed half-spectrum Phi (ndof^2 reals per stored wavevector,
+    or the reals of the table's storage pattern when it has one)."""
+    return 2 * nx * ny * d * s + nx * (ny // 2 + 1) * (phi_reals or d * d) * s
 
 
 def measured_peaks():
@@ -797,12 +798,16 @@ def run_gb300(args):
 
     peak, peak_kind = measured_peaks()
     sz = 4 if args.precision == "f32" else 8
-    bts = algorithmic_bytes(nx, ny, d, sz)
+    info = s.info()
+    phi_reals = info.get("phi_reals_per_wavevector") or d * d
+    bts = algorithmic_bytes(nx, ny, d, sz, phi_reals)
     achieved = bts / (ms * 1e-3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": profile_traffic(),
                 "kernel": "one force evaluation (all launches of the evaluation)",
-                "algorithmic_bytes": bts, "peak_kind": peak_kind}
+                "algorithmic_bytes": bts, "peak_kind": peak_kind,
+                "phi_reals_per_wavevector": phi_reals,
+                "phi_pattern": info.get("phi_pattern", 0)}
     if kernel_ms:
         roofline["kernel_ms"] = kernel_ms
 
