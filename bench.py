@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-f64", action="store_true")
     ap.add_argument("--no-static", action="store_true")
+    ap.add_argument("--no-static-small", action="store_true", help="skip the 128^2 sc100 static solve")
     ap.add_argument("--static-n", type=int, default=2048)
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-dynamics", action="store_true")
@@ -873,12 +874,13 @@ def run_gb300(args):
             extra["warmstart"] = warmstart_run(g, torch, dev)
     if not args.no_c2 and rank == 0:
         extra["c2_repeated_fp32"] = c2_run(g, torch, dev, stream, args.c2_reps)
-    if not args.no_static:
+    if not args.no_static and not args.no_static_small:
         # the 128^2 sc(100) contact: L2-resident, latency-bound (time per iteration)
         try:
             extra["static_solve_128_sc100"] = static_solve(g, torch, dev, stream, 128, kernel=C1_KERNEL)
         except Exception as ex:  # recorded, the headline numbers stand
             extra["static_solve_128_sc100"] = {"error": f"{type(ex).__name__}: {ex}"}
+    if not args.no_static:
         extra["static_solve"] = static_solve(g, torch, dev, stream, args.static_n)
 
     # CPU baseline on the same input; its oracle output judges the GPU results
