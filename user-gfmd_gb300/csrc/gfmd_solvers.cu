@@ -139,27 +139,8 @@ __global__ void __launch_bounds__(kRedThreads) k_total_force(Obst o, Geom g, con
   block_reduce(acc, 2, true, part);
 }
 
-// v = a v + b f
-__global__ void k_axpby(size_t n, double *__restrict__ v, const double *__restrict__ f, double a,
-                        double b) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    v[i] = a * v[i] + b * f[i];
-}
 
-// dst = s * src
-__global__ void k_scale(size_t n, double *__restrict__ dst, const double *__restrict__ src, double s) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    dst[i] = s * src[i];
-}
 
-// partials of sum a.b
-__global__ void __launch_bounds__(kRedThreads) k_dot(size_t n, const double *__restrict__ a,
-                                                     const double *__restrict__ b, double *__restrict__ part) {
-  double acc[1] = {0.0};
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    acc[0] += a[i] * b[i];
-  block_reduce(acc, 1, false, part);
-}
 
 // ---------------------------------------------------------------------------
 // Host-side driver state.
@@ -585,106 +566,334 @@ int fire_solve(gfmd_solver *hp, const gfmd_obstacle_t *ob, const gfmd_min_params
 // the other methods (the reference's loop tests |f|_2 against LAMMPS' ftol,
 // and has an energy criterion that the reference's tests switch off with
 // etol = 0).
+//
+// The scalar logic runs on the device: one CUDA graph per phase, a prologue
+// (total force, preconditioned direction, radius) and a WHILE loop whose body
+// is
+//   k_tr_step     u += a h
+//   F_el(u)       the handle's force evaluation (with its energy)
+//   k_tr_total    f = F_el + F_w, E, max|f_i|; the last block accepts or
+//                 rejects the step (rho) and updates the radius
+//   k_tr_undo     on a rejection: u -= a h, f = g (the old gradient)
+//   P f           the preconditioner's evaluation, every step: after a
+//                 rejection it recomputes the same h from the restored f
+//   k_tr_dir      h = P f, g = f, g.h; the last block makes the checks that
+//                 open the next step (iteration cap, descent, the FP32
+//                 phase's hand-over) and sets the loop condition
+// With a refine handle the FP32 phase ends when max|f| <= ftol, or when its
+// energies can no longer rank a step (the model decrease below 64 FP32 ulp
+// of |E|, or 32 rejections in a row); the FP64 handle then restarts.
+namespace tr {
+
+using red::reduce_last;
+constexpr int kT = red::kT;
+
+struct Ctl {
+  double E, Eprev, fmax, f2, ew, gg, delta, a;
+  int it, evals, rejects, accept;
+  int done;  // 0 running, 1 converged, 2 iteration cap, 3 non-finite, 4 hand over, 5 no descent
+  unsigned int counter;
+};
+
+struct Par {
+  double dmax, rho_tol, ftol, e_noise;
+  int maxit, handover;
+};
+
+// f = F_el + F_w (+ external load), E_w, |f|^2, max|f_i|; the last block sets
+// E = E_el + E_w and, after a step (restart = 0), accepts or rejects it.
+__global__ void __launch_bounds__(kT) k_tr_total(Obst o, Geom g, const double *__restrict__ x,
+                                                  const double *__restrict__ fel, double *__restrict__ ftot,
+                                                  const double *__restrict__ eel, double *__restrict__ part,
+                                                  Ctl *ctl, Par p, int restart) {
+  const size_t N = (size_t)g.nx * g.ny;
+  const int nl = g.ndof / 3;
+  double ew = 0.0, f2 = 0.0, fm = 0.0;
+  for (size_t s = blockIdx.x * (size_t)kT + threadIdx.x; s < N; s += (size_t)gridDim.x * kT) {
+    for (int l = 0; l < nl; l++) {
+      double fw[3] = {0.0, 0.0, 0.0};
+      if (l < o.nlayer && o.kind != GFMD_OBST_NONE) {
+        double r[3], dir[3];
+        site_pos(o, g, s, l, x, N, 0.0, nullptr, r, dir);
+        const float ge = gap_estimate(o, s, r);
+        if (ge < (float)o.gcut + 0.01f * (float)o.gcut + 1e-3f) {
+          const WallOut w = wall_eval(o, (int)(s / g.ny), (int)(s % g.ny), s, r, dir);
+          fw[0] = w.f[0];
+          fw[1] = w.f[1];
+          fw[2] = w.f[2];
+          ew += w.e;
+        }
+      }
+      if (l < o.nlayer && o.fz_ext != 0.0) {
+        fw[2] += o.fz_ext;
+        ew -= o.fz_ext * x[(size_t)(3 * l + 2) * N + s];
+      }
+      for (int c = 0; c < 3; c++) {
+        const size_t idx = (size_t)(3 * l + c) * N + s;
+        const double f = fel[idx] + fw[c];
+        ftot[idx] = f;
+        f2 += f * f;
+        fm = fmax(fm, fabs(f));
+      }
+    }
+  }
+  const double acc[3] = {ew, f2, fm};
+  __shared__ double res[3];
+  if (!reduce_last<2, 1>(acc, part, &ctl->counter, res)) return;
+  if (threadIdx.x == 0) {
+    const double E = *eel + res[0];
+    ctl->ew = res[0];
+    ctl->f2 = res[1];
+    ctl->fmax = res[2];
+    ctl->E = E;
+    ctl->evals += 1;
+    ctl->accept = 1;
+    if (restart) {
+      ctl->Eprev = E;
+      if (!isfinite(res[2]) || !isfinite(E)) ctl->done = 3;
+      else if (res[2] <= p.ftol) ctl->done = 1;
+      return;
+    }
+    ctl->it += 1;
+    if (!isfinite(res[2])) {  // (a non-finite E alone fails rho and is declined)
+      ctl->done = 3;
+      return;
+    }
+    if (res[2] <= p.ftol) {  // converged at the new point
+      ctl->done = 1;
+      return;
+    }
+    const double a = ctl->a, gg = ctl->gg, sg = sqrt(gg), delta = ctl->delta;
+    const double rho = (ctl->Eprev - E) / ((a - 0.5 * a * a) * gg);
+    if (!(rho >= p.rho_tol)) {
+      // declined: the step is undone (k_tr_undo), the old gradient kept
+      ctl->delta = 0.5 * a * sg;
+      ctl->E = ctl->Eprev;
+      ctl->rejects += 1;
+      ctl->accept = 0;
+    } else {
+      ctl->rejects = 0;
+      const double fac = 2.0 * fabs(E - ctl->Eprev) / (fmin(0.5, 1.0 - delta / (2.0 * sg)) * sg);
+      ctl->delta = fmin(2.0 * delta, fmax(0.5 * delta, fac));
+      ctl->Eprev = E;
+    }
+  }
+}
+
+// u += a h
+__global__ void __launch_bounds__(kT) k_tr_step(size_t n, double *__restrict__ u, const double *__restrict__ h,
+                                                 const Ctl *ctl) {
+  const double a = ctl->a;
+  for (size_t i = blockIdx.x * (size_t)kT + threadIdx.x; i < n; i += (size_t)gridDim.x * kT)
+    u[i] = 1.0 * u[i] + a * h[i];
+}
+
+// after a rejected step: u -= a h, f = g
+__global__ void __launch_bounds__(kT) k_tr_undo(size_t n, double *__restrict__ u, double *__restrict__ f,
+                                                 const double *__restrict__ g, const double *__restrict__ h,
+                                                 const Ctl *ctl) {
+  if (ctl->accept || ctl->done) return;  // uniform over the grid
+  const double a = -ctl->a;
+  for (size_t i = blockIdx.x * (size_t)kT + threadIdx.x; i < n; i += (size_t)gridDim.x * kT) {
+    u[i] = 1.0 * u[i] + a * h[i];
+    f[i] = g[i];
+  }
+}
+
+// h = P f (-pf with a preconditioner, else f), g = f, g.h; the last block
+// opens the next step or ends the phase.
+__global__ void __launch_bounds__(kT) k_tr_dir(size_t n, const double *__restrict__ f,
+                                                const double *__restrict__ pf, double *__restrict__ g,
+                                                double *__restrict__ h, double *__restrict__ part, Ctl *ctl,
+                                                Par p, int restart, cudaGraphConditionalHandle hc) {
+  double gh = 0.0;
+  for (size_t i = blockIdx.x * (size_t)kT + threadIdx.x; i < n; i += (size_t)gridDim.x * kT) {
+    const double fv = f[i], hv = pf ? -pf[i] : fv;
+    g[i] = fv;
+    h[i] = hv;
+    gh += fv * hv;
+  }
+  const double acc[1] = {gh};
+  __shared__ double res[1];
+  if (!reduce_last<1, 0>(acc, part, &ctl->counter, res)) return;
+  if (threadIdx.x == 0) {
+    const double gg = res[0];
+    ctl->gg = gg;
+    // preconditioner applications that the step needed (after a restart or
+    // an accepted step of an unfinished phase)
+    if (pf && ctl->done == 0 && ctl->accept) ctl->evals += 1;
+    if (restart && ctl->done == 0) ctl->delta = fmin(p.dmax, sqrt(gg));
+    if (ctl->done == 0) {
+      if (ctl->it >= p.maxit) ctl->done = 2;
+      else if (!(gg > 0.0)) ctl->done = 5;
+      else {
+        const double a = fmin(1.0, ctl->delta / sqrt(gg));
+        ctl->a = a;
+        if (p.handover && ((a - 0.5 * a * a) * gg <= p.e_noise * fabs(ctl->E) || ctl->rejects >= 32))
+          ctl->done = 4;
+      }
+    }
+    if (hc) cudaGraphSetConditional(hc, ctl->done == 0 ? 1u : 0u);
+  }
+}
+
+}  // namespace tr
+
+// One trust-region phase on handle hh as a graph: the prologue (restart) and
+// WHILE(running) { step }.  Synchronizes its stream.
+cudaError_t tr_phase(gfmd_solver *hh, gfmd_solver *pre, cudaStream_t st, const Obst &o, const tr::Par &p,
+                     double *u, double *fel, double *f, double *gv, double *h, double *pf, double *part,
+                     double *d_e, double *d_e_pre, tr::Ctl *ctl, int nblk) {
+  using namespace tr;
+  const Geom &g = hh->g;
+  const size_t n = (size_t)g.ndof * g.nx * g.ny;
+  cudaGraph_t graph = nullptr, body = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraphConditionalHandle hc;
+  cudaError_t e = cudaGraphCreate(&graph, 0);
+  if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hc, graph, 0, cudaGraphCondAssignDefault);
+  auto eval = [&](gfmd_solver *hx, cudaStream_t cs, const double *in, double *out, double *de, bool linf) {
+    cudaStream_t keep = hx->stream;
+    hx->stream = cs;
+    cudaError_t ee = enqueue_force_opts(hx, in, 0, out, 0, de, linf);
+    hx->stream = keep;
+    return ee;
+  };
+  // total force of u, the preconditioned direction and its checks
+  auto tail = [&](cudaStream_t cs, int restart, cudaGraphConditionalHandle hset) {
+    cudaError_t ee = cudaSuccess;
+    if (pre) ee = eval(pre, cs, f, pf, d_e_pre, false);
+    if (ee == cudaSuccess) {
+      k_tr_dir<<<nblk, kT, 0, cs>>>(n, f, pre ? pf : nullptr, gv, h, part, ctl, p, restart, hset);
+      ee = cudaGetLastError();
+    }
+    return ee;
+  };
+  if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(st, graph, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+  if (e == cudaSuccess) {
+    cudaError_t ec = eval(hh, st, u, fel, d_e, true);
+    if (ec == cudaSuccess) {
+      k_tr_total<<<nblk, kT, 0, st>>>(o, g, u, fel, f, d_e, part, ctl, p, 1);
+      ec = cudaGetLastError();
+    }
+    if (ec == cudaSuccess) ec = tail(st, 1, hc);
+    cudaStreamCaptureStatus cs;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t nd = 0;
+    if (ec == cudaSuccess) ec = cudaStreamGetCaptureInfo(st, &cs, nullptr, nullptr, &deps, nullptr, &nd);
+    cudaGraphNodeParams cp = {};
+    cudaGraphNode_t node = nullptr;
+    if (ec == cudaSuccess) {
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = hc;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      ec = cudaGraphAddNode(&node, graph, deps, nullptr, nd, &cp);
+    }
+    if (ec == cudaSuccess) {
+      body = cp.conditional.phGraph_out[0];
+      ec = cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    }
+    cudaGraph_t got = nullptr;
+    e = cudaStreamEndCapture(st, &got);
+    if (ec != cudaSuccess) e = ec;
+  }
+  if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+  if (e == cudaSuccess) {
+    k_tr_step<<<nblk * 4, kT, 0, st>>>(n, u, h, ctl);
+    cudaError_t ec = cudaGetLastError();
+    if (ec == cudaSuccess) ec = eval(hh, st, u, fel, d_e, true);
+    if (ec == cudaSuccess) {
+      k_tr_total<<<nblk, kT, 0, st>>>(o, g, u, fel, f, d_e, part, ctl, p, 0);
+      k_tr_undo<<<nblk * 4, kT, 0, st>>>(n, u, f, gv, h, ctl);
+      ec = cudaGetLastError();
+    }
+    if (ec == cudaSuccess) ec = tail(st, 0, hc);
+    cudaGraph_t got = nullptr;
+    e = cudaStreamEndCapture(st, &got);
+    if (ec != cudaSuccess) e = ec;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+  if (e == cudaSuccess) e = cudaGraphLaunch(exec, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  return e;
+}
+
 int tr_solve(gfmd_solver *hp, const gfmd_obstacle_t *ob, const gfmd_min_params_t *prm,
              double *u, gfmd_min_report_t *rep, std::string &err) {
   Work w;
   cudaError_t ce = work_init(w, hp, 5);  // fel, f, g, h, Pf
   if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return ce == cudaErrorMemoryAllocation ? GFMD_ENOMEM : GFMD_ECUDA; }
-  double *fel = w.bufs[0], *f = w.bufs[1], *g = w.bufs[2], *h = w.bufs[3], *pf = w.bufs[4];
+  double *fel = w.bufs[0], *f = w.bufs[1], *gv = w.bufs[2], *h = w.bufs[3], *pf = w.bufs[4];
   const Obst o = make_obst(ob, hp->g);
-  const double dmax = prm->tr_dmax > 0 ? prm->tr_dmax : 0.1;
-  const double rho_tol = prm->tr_rho_tol > 0 ? prm->tr_rho_tol : 0.01;
-  const int maxit = prm->maxiter > 0 ? prm->maxiter : 100000;
-  const size_t bytes = sizeof(double) * w.n;
+  tr::Par p{};
+  p.dmax = prm->tr_dmax > 0 ? prm->tr_dmax : 0.1;
+  p.rho_tol = prm->tr_rho_tol > 0 ? prm->tr_rho_tol : 0.01;
+  p.maxit = prm->maxiter > 0 ? prm->maxiter : 100000;
+  p.ftol = prm->ftol;
+  p.handover = prm->refine ? 1 : 0;
+  p.e_noise = hp->precision == GFMD_PREC_F32 ? 64.0 * 5.960464477539063e-8 : 0.0;
+  tr::Ctl c{};
+  tr::Ctl *ctl = nullptr;
+  double *part = nullptr, *d_e_pre = nullptr;
+  // phases captured on a stream of their own, ordered after the handle's
+  cudaStream_t gs = nullptr;
+  cudaEvent_t ev = nullptr;
+  if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&gs, cudaStreamNonBlocking);
+  if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+  if (ce == cudaSuccess) ce = cudaEventRecord(ev, w.st);
+  if (ce == cudaSuccess) ce = cudaStreamWaitEvent(gs, ev, 0);
+  w.st = gs;
+  if (ce == cudaSuccess) ce = cudaMalloc((void **)&ctl, sizeof(tr::Ctl));
+  if (ce == cudaSuccess) ce = cudaMalloc((void **)&d_e_pre, sizeof(double));
+  if (ce == cudaSuccess) ce = cudaMalloc((void **)&part, sizeof(double) * red::kQ * w.nblk);
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(ctl, &c, sizeof(c), cudaMemcpyHostToDevice, w.st);
+  if (ce == cudaSuccess)
+    ce = tr_phase(hp, prm->precond, w.st, o, p, u, fel, f, gv, h, pf, part, w.d_e, d_e_pre, ctl, w.nblk);
+  if (ce == cudaSuccess) ce = cudaMemcpy(&c, ctl, sizeof(c), cudaMemcpyDeviceToHost);
   gfmd_solver *hh = hp;
-  int evals = 0, it = 0, status = GFMD_ENOTCONVERGED, rejects = 0;
-  double E = 0.0, Eprev = 0.0, fmax = 0.0, f2 = 0.0, gg = 0.0, delta = 0.0;
-  bool refining = false;
-  // With a refine handle, the first (bulk) phase ends when max|f| <= ftol, or
-  // when its energies can no longer rank a step: the model decrease below
-  // the FP32 noise of the energy (64 ulp of |E|), or 32 rejections in a row.
-  const double e_noise = hp->precision == GFMD_PREC_F32 ? 64.0 * 5.960464477539063e-8 : 0.0;
-  // h = P f, gg = f.h, g = f
-  auto precondition = [&]() -> cudaError_t {
-    if (prm->precond) {
-      RT(elastic(w, prm->precond, f, pf, false, nullptr));
-      evals++;
-      k_scale<<<w.nblk, kRedThreads, 0, w.st>>>(w.n, h, pf, -1.0);
-    } else {
-      RT(cudaMemcpyAsync(h, f, bytes, cudaMemcpyDeviceToDevice, w.st));
-    }
-    RT(cudaMemcpyAsync(g, f, bytes, cudaMemcpyDeviceToDevice, w.st));
-    k_dot<<<w.nblk, kRedThreads, 0, w.st>>>(w.n, g, h, w.part);
-    RT(fetch(w, 1, false));
-    gg = w.hres[0];
-    return cudaSuccess;
-  };
-  auto restart = [&]() -> cudaError_t {
-    RT(total_force(w, hh, o, u, fel, f, &E, &fmax, &f2));
-    evals++;
-    Eprev = E;
-    if (fmax <= prm->ftol || !std::isfinite(fmax)) return cudaSuccess;
-    RT(precondition());
-    delta = std::min(dmax, std::sqrt(gg));
-    return cudaSuccess;
-  };
-  ce = restart();
-  while (ce == cudaSuccess) {
-    if (!std::isfinite(fmax) || !std::isfinite(E)) { status = GFMD_ENONFINITE; break; }
-    if (fmax <= prm->ftol) {
-      if (prm->refine && !refining) {
-        refining = true;
-        hh = prm->refine;
-        if ((ce = restart()) != cudaSuccess) break;
-        continue;
-      }
-      status = GFMD_OK;
-      break;
-    }
-    if (it >= maxit) break;
-    if (!(gg > 0.0)) { status = GFMD_ENONFINITE; err = "the preconditioned gradient is not a descent direction"; break; }
-    const double sg = std::sqrt(gg), a = std::min(1.0, delta / sg);
-    if (prm->refine && !refining &&
-        ((a - 0.5 * a * a) * gg <= e_noise * std::fabs(E) || rejects >= 32)) {
-      refining = true;
-      hh = prm->refine;
-      rejects = 0;
-      if ((ce = restart()) != cudaSuccess) break;
-      continue;
-    }
-    k_axpby<<<w.nblk, kRedThreads, 0, w.st>>>(w.n, u, h, 1.0, a);
-    if ((ce = total_force(w, hh, o, u, fel, f, &E, &fmax, &f2)) != cudaSuccess) break;
-    evals++;
-    it++;
-    if (fmax <= prm->ftol) continue;  // converged at the new point
-    const double rho = (Eprev - E) / ((a - 0.5 * a * a) * gg);
-    if (!(rho >= rho_tol)) {
-      // declined: undo the step, keep the old gradient, shrink the radius
-      delta = 0.5 * a * sg;
-      k_axpby<<<w.nblk, kRedThreads, 0, w.st>>>(w.n, u, h, 1.0, -a);
-      if ((ce = cudaMemcpyAsync(f, g, bytes, cudaMemcpyDeviceToDevice, w.st)) != cudaSuccess) break;
-      E = Eprev;
-      rejects++;
-    } else {
-      rejects = 0;
-      const double fac = 2.0 * std::fabs(E - Eprev) / (std::min(0.5, 1.0 - delta / (2.0 * sg)) * sg);
-      delta = std::min(2.0 * delta, std::max(0.5 * delta, fac));
-      Eprev = E;
-      if ((ce = precondition()) != cudaSuccess) break;
-    }
+  if (ce == cudaSuccess && prm->refine && (c.done == 1 || c.done == 4)) {
+    // FP64 phase: restart with the refine handle
+    hh = prm->refine;
+    p.handover = 0;
+    p.e_noise = 0.0;
+    c.done = 0;
+    c.rejects = 0;
+    ce = cudaMemcpyAsync(ctl, &c, sizeof(c), cudaMemcpyHostToDevice, w.st);
+    if (ce == cudaSuccess)
+      ce = tr_phase(hh, prm->precond, w.st, o, p, u, fel, f, gv, h, pf, part, w.d_e, d_e_pre, ctl, w.nblk);
+    if (ce == cudaSuccess) ce = cudaMemcpy(&c, ctl, sizeof(c), cudaMemcpyDeviceToHost);
   }
-  if (ce == cudaSuccess && status != GFMD_ENONFINITE)
+  double E = 0.0, fmax = 0.0, f2 = 0.0;
+  if (ce == cudaSuccess && c.done != 3 && c.done != 5)
     ce = total_force(w, hh, o, u, fel, f, &E, &fmax, &f2);  // fresh forces at the end point
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(gs);
+  if (part) cudaFree(part);
+  if (d_e_pre) cudaFree(d_e_pre);
+  if (ctl) cudaFree(ctl);
+  if (ev) cudaEventDestroy(ev);
+  if (gs) cudaStreamDestroy(gs);
   if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return GFMD_ECUDA; }
+  int status = GFMD_ENOTCONVERGED;
+  if (c.done == 1) status = GFMD_OK;
+  else if (c.done == 3 || c.done == 5) status = GFMD_ENONFINITE;
+  if (c.done == 3 || c.done == 5) {
+    E = c.E;
+    fmax = c.fmax;
+    f2 = c.f2;
+  }
   if (rep) {
-    rep->iterations = it;
-    rep->force_evals = evals;
+    rep->iterations = c.it;
+    rep->force_evals = c.evals;
     rep->energy = E;
     rep->fmax = fmax;
     rep->fnorm = std::sqrt(f2);
   }
   if (status == GFMD_ENOTCONVERGED) err = "trust region reached the iteration cap before max|f| <= ftol";
-  if (status == GFMD_ENONFINITE && err.empty()) err = "non-finite force during the trust-region solve";
+  if (c.done == 5) err = "the preconditioned gradient is not a descent direction";
+  else if (status == GFMD_ENONFINITE) err = "non-finite force during the trust-region solve";
   return status;
 }
 
