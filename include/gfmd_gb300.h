@@ -102,10 +102,10 @@ int gfmd_force_f32(gfmd_handle_t h, const float *d_u, float *d_f, double *d_epot
  * Replaces: GFMDSolver::get_u0 (src/main/gfmd_solver.h:89-91). */
 int gfmd_get_u0(gfmd_handle_t h, double *u0);
 
-/* Launch plan of the fused path: rows per block of the row transforms
- * (chosen by the autotuner at gfmd_set_phi) and the Phi prefetch depth of
- * the column kernel (fixed); 0, 0 on the general path.  No counterpart in
- * the reference. */
+/* Launch plan of the fused path: rows per block of the shared-memory row
+ * transforms and the Phi prefetch depth of the column kernel (both chosen by
+ * the autotuner at gfmd_set_phi); 0, 0 on the general path.  No counterpart
+ * in the reference. */
 int gfmd_plan_info(gfmd_handle_t h, int *rows_per_block, int *phi_prefetch);
 
 /* Device bytes held by the handle (with the preconditioner gfmd_prec_gradient
@@ -140,8 +140,9 @@ int gfmd_kernel_plan(gfmd_handle_t h, int *row_warp_tma, int *col_cluster, int *
  * pairs that are exactly zero at every wavevector: 0 every pair; 1
  * layer-tridiagonal (3x3 blocks of layers two or more apart are zero); 2 as 1
  * with the blocks of all layers but the last diagonal (a slab with
- * nearest-neighbour interactions).  Used by the register-transform column
- * kernel at ndof 12; reals_per_wavevector = reals streamed per wavevector.
+ * nearest-neighbour interactions).  Used at ndof 12 by the FP32
+ * register-transform column kernel and by the general path's Phi application
+ * (both precisions); reals_per_wavevector = reals streamed per wavevector.
  * Forces are the same with every pattern (the skipped products are zero and
  * the kept ones are summed in the same order).  No counterpart in the
  * reference (introspection). */

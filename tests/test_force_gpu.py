@@ -321,3 +321,30 @@ def test_structured_table_is_bit_identical_to_dense(args, nx, ny, pattern, monke
         p.post_force(u, fp)
         pd.post_force(u, fpd)
         assert np.array_equal(fp, fpd)
+
+
+@pytest.mark.parametrize("prec,nx,ny", [("f64", 2048, 32), ("f64", 96, 80), ("f32", 96, 80)])
+def test_structured_table_on_the_general_path(prec, nx, ny, monkeypatch):
+    """The general path (FP64 grids whose column set exceeds shared memory,
+    and sizes that are not powers of two) applies the structured table with
+    the same sums in the same order: bit-identical to every-pair storage."""
+    g = gfmd_pkg()
+    args = "ft fcc100 1.0 4 pair-potential 1 1.0 height 64"
+    k = g.StiffnessKernel(args)
+    d = k.get_dimension()
+    half, linf = k.phi_table(nx, ny, "half")
+    u = np.random.default_rng(nx * ny).normal(0.0, 0.01, (d, nx * ny))
+    s = _solver(nx, ny, d, prec, half, "half", linf)
+    info = s.info()
+    assert not info["fused"] and info["phi_pattern"] == 2
+    assert info["phi_reals_per_wavevector"] == 12 + 2 * 30
+    monkeypatch.setenv("GFMD_PHI_DENSE", "1")
+    sd = _solver(nx, ny, d, prec, half, "half", linf)
+    monkeypatch.delenv("GFMD_PHI_DENSE")
+    f, fd = np.zeros_like(u), np.zeros_like(u)
+    e, ed = s.post_force(u, f), sd.post_force(u, fd)
+    assert np.array_equal(f, fd) and e == ed
+    f_ref, e_ref, _ = oracle_post_force(half_to_full(half, nx, ny), linf, u, nx, ny)
+    tol = F64_TOL if prec == "f64" else FP32_TOL
+    assert rel_l2(f, f_ref) <= tol
+    assert abs(e - e_ref) <= tol * abs(e_ref)

@@ -311,7 +311,14 @@ int set_error(int code, const std::string &msg) { return fail(code, msg); }
 size_t phi_index(const gfmd_solver *h, int ky, int pos, int e) {
   const Geom &g = h->g;
   size_t D2 = (size_t)g.npk;
-  if (!h->fast) return ((size_t)ky * D2 + e) * g.nxp + pos;  // [ky][e][nxp]
+  if (!h->fast) {  // [ky][e][nxp]
+    if (h->phi_pat != 0) {  // elements of the storage pattern only
+      if (h->phi_slot[e] < 0) return kPhiAbsent;
+      e = h->phi_slot[e];
+      D2 = (size_t)(g.ndof + 2 * pat_pairs(g.ndof, h->phi_pat));
+    }
+    return ((size_t)ky * D2 + e) * g.nxp + pos;
+  }
   const size_t blk = (size_t)ky * (g.nxp / 32) + pos / 32;
   if (h->col_cl > 0 && h->phi_v == 4) {  // [ky][x/32][e/4][32][4]
     if (h->phi_pat != 0) {  // elements of the storage pattern only
@@ -322,6 +329,12 @@ size_t phi_index(const gfmd_solver *h, int ky, int pos, int e) {
     return (blk * (D2 / 4) + e / 4) * 128 + (size_t)(pos % 32) * 4 + e % 4;
   }
   return (blk * D2 + e) * 32 + pos % 32;  // [ky][x/32][e][32]
+}
+
+int phi_reals(const gfmd_solver *h) {
+  const int D = h->g.ndof;
+  if (h->phi_pat == 0) return h->g.npk;
+  return h->fast ? pat_floats(D, h->phi_pat) : D + 2 * pat_pairs(D, h->phi_pat);
 }
 
 FftPlan make_plan(int n, std::vector<double> &tw) {
@@ -647,7 +660,8 @@ int gfmd_set_phi(gfmd_handle_t h, const double *phi, int layout, const double *l
   h->phi_pat = 0;
   h->phi_slot.clear();
   const char *dense_env = getenv("GFMD_PHI_DENSE");
-  if (h->col_r32 && !f64 && D == 12 && h->phi_v == 4 && !(dense_env && dense_env[0] == '1')) {
+  const bool pat_kernel = (h->col_r32 && !f64 && h->phi_v == 4) || !h->fast;  // kernels with pattern instances
+  if (pat_kernel && D == 12 && !(dense_env && dense_env[0] == '1')) {
     const size_t nsrc = layout == GFMD_PHI_FULL ? (size_t)g.nx * g.ny : (size_t)g.nx * g.nyc;
     std::mutex mu;
     std::vector<char> nz(D2, 0);
@@ -729,7 +743,7 @@ int gfmd_set_phi(gfmd_handle_t h, const double *phi, int layout, const double *l
   });
   if (!finite) return fail(GFMD_ENONFINITE, "gfmd_set_phi: table holds NaN or Inf");
   const void *hp = f64 ? (const void *)packd.data() : (const void *)packf.data();
-  const size_t per_q = h->phi_pat ? (size_t)gfmd::pat_floats(D, h->phi_pat) : (size_t)D2;
+  const size_t per_q = (size_t)gfmd::phi_reals(h);
   size_t bytes = nq * per_q * (f64 ? 8 : 4);
   CK(cudaMemcpy(h->d_phi, hp, bytes, cudaMemcpyHostToDevice), "gfmd_set_phi: upload");
   std::vector<double> lf(D / 3, 0.0);
@@ -1067,8 +1081,7 @@ int gfmd_kernel_plan(gfmd_handle_t h, int *row_warp_tma, int *col_cluster, int *
 int gfmd_phi_pattern(gfmd_handle_t h, int *pattern, int *reals_per_wavevector) {
   if (!h) return fail(GFMD_EINVAL, "gfmd_phi_pattern: NULL handle");
   if (pattern) *pattern = h->phi_pat;
-  if (reals_per_wavevector)
-    *reals_per_wavevector = h->phi_pat ? gfmd::pat_floats(h->g.ndof, h->phi_pat) : h->g.npk;
+  if (reals_per_wavevector) *reals_per_wavevector = gfmd::phi_reals(h);
   return GFMD_OK;
 }
 

@@ -225,6 +225,29 @@ template <typename T, int D> struct HermPairs {
   }
 };
 
+// The pairs of a table stored in pattern PAT (pat_keeps): the p-th kept pair
+// at elements D + 2p, D + 2p + 1, applied in row-major order like HermPairs.
+template <typename T, int D, int PAT> struct HermPairsPat {
+  template <int P>
+  static __device__ __forceinline__ void pair(const T *__restrict__ ph, size_t ps, const C<T> *uq,
+                                              C<T> *F) {
+    constexpr int I = pat_pair(D, PAT, P, 0), J = pat_pair(D, PAT, P, 1), E = D + 2 * P;
+    const T hr = ph[E * ps], hi = ph[(E + 1) * ps];
+    F[I].x += hr * uq[J].x - hi * uq[J].y;
+    F[I].y += hr * uq[J].y + hi * uq[J].x;
+    F[J].x += hr * uq[I].x + hi * uq[I].y;
+    F[J].y += hr * uq[I].y - hi * uq[I].x;
+  }
+  template <int... Ps>
+  static __device__ __forceinline__ void all(const T *__restrict__ ph, size_t ps, const C<T> *uq, C<T> *F,
+                                             std::integer_sequence<int, Ps...>) {
+    (pair<Ps>(ph, ps, uq, F), ...);
+  }
+  static __device__ __forceinline__ void run(const T *__restrict__ ph, size_t ps, const C<T> *uq, C<T> *F) {
+    all(ph, ps, uq, F, std::make_integer_sequence<int, pat_pairs(D, PAT)>{});
+  }
+};
+
 // One Stockham stage over `nb` transforms of length n stored with stride
 // bstride (complex elements), in -> out:
 //   out[(j/Ns)*Ns*R + j%Ns + r*Ns] = DFT_R( in[j + t*n/R] * w^(t*(j%Ns)) )[r].

@@ -195,6 +195,8 @@ int force_launches(const gfmd_solver *h);
 // Index (in reals) of packed element e of the wavevector at storage position
 // pos (digit-reversed kx on the fused path, kx otherwise) of row ky.
 size_t phi_index(const gfmd_solver *h, int ky, int pos, int e);
+// Reals per wavevector of h's packed table (every pair, or its storage pattern's).
+int phi_reals(const gfmd_solver *h);
 // Device bytes of the spectrum/Phi arrays and the number of energy partials.
 void force_layout(const Geom &g, int precision, size_t *w_bytes, size_t *phi_bytes, int *n_epart);
 }  // namespace gfmd

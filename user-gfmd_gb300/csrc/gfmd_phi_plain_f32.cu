@@ -12,8 +12,8 @@ namespace gfmd {
 
 namespace {
 
-template <typename T, int D> cudaError_t launch_phi(gfmd_solver *h, dim3 grid) {
-  k_phi_apply<T, D><<<grid, kPhiThreads, 0, h->stream>>>(reinterpret_cast<C<T> *>(h->d_W),
+template <typename T, int D, int PAT = 0> cudaError_t launch_phi(gfmd_solver *h, dim3 grid) {
+  k_phi_apply<T, D, PAT><<<grid, kPhiThreads, 0, h->stream>>>(reinterpret_cast<C<T> *>(h->d_W),
                                                          reinterpret_cast<const T *>(h->d_phi), h->g, h->d_linf,
                                                          h->d_epart, h->d_scal);
   return cudaGetLastError();
@@ -24,7 +24,10 @@ template <typename T> cudaError_t phi_t(gfmd_solver *h, dim3 grid) {
     case 3: return launch_phi<T, 3>(h, grid);
     case 6: return launch_phi<T, 6>(h, grid);
     case 9: return launch_phi<T, 9>(h, grid);
-    case 12: return launch_phi<T, 12>(h, grid);
+    case 12:  // layer-tridiagonal tables stream and multiply only their kept pairs
+      if (h->phi_pat == 2) return launch_phi<T, 12, 2>(h, grid);
+      if (h->phi_pat == 1) return launch_phi<T, 12, 1>(h, grid);
+      return launch_phi<T, 12>(h, grid);
     case 15: return launch_phi<T, 15>(h, grid);
     case 18: return launch_phi<T, 18>(h, grid);
     case 21: return launch_phi<T, 21>(h, grid);

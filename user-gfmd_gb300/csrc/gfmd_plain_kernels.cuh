@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(kThreads) k_col_fft(C<T> *__restrict__ W, Geom
 // the pair (Re H_ij, Im H_ij).  F_i = sum_j H_ij u_j with H_ji = conj H_ij.
 // e = w(ky) Re(conj(F).u) (weight 2 for ky with a mirror partner in the
 // stored half, else 1), accumulated in FP64.
-template <typename T, int D>
+template <typename T, int D, int PAT = 0>
 __global__ void __launch_bounds__(kPhiThreads) k_phi_apply(C<T> *__restrict__ W, const T *__restrict__ phi,
                                                            Geom g, const double *__restrict__ linf,
                                                            double *__restrict__ epart,
@@ -180,7 +180,9 @@ __global__ void __launch_bounds__(kPhiThreads) k_phi_apply(C<T> *__restrict__ W,
   if (x < g.nx) {
     const size_t cs = (size_t)g.nxp;
     C<T> *col = W + (size_t)ky * D * cs + x;
-    const T *ph = phi + (size_t)ky * g.npk * cs + x;
+    // reals per wavevector: every pair, or the kept pairs of the pattern
+    const size_t npk = PAT == 0 ? (size_t)g.npk : (size_t)(D + 2 * pat_pairs(D, PAT));
+    const T *ph = phi + (size_t)ky * npk * cs + x;
     C<T> uq[D], F[D];
 #pragma unroll
     for (int j = 0; j < D; j++) {
@@ -194,7 +196,8 @@ __global__ void __launch_bounds__(kPhiThreads) k_phi_apply(C<T> *__restrict__ W,
       F[i].y += h * uq[i].y;
     }
     // F_i += H_ij u_j ; F_j += conj(H_ij) u_i
-    HermPairs<T, D>::run(ph, cs, uq, F);
+    if constexpr (PAT == 0) HermPairs<T, D>::run(ph, cs, uq, F);
+    else HermPairsPat<T, D, PAT>::run(ph, cs, uq, F);
     const bool mirror_self = (ky == 0) || (g.ny_even && ky == g.ny / 2);
     const double w = mirror_self ? 1.0 : 2.0;
     T es = 0;
