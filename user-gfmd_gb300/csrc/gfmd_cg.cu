@@ -56,6 +56,7 @@
 #include "gfmd_internal.h"
 #include "gfmd_obstacle.cuh"
 #include "gfmd_reduce.cuh"
+#include "gfmd_vec.cuh"
 
 namespace gfmd {
 
@@ -499,34 +500,6 @@ __device__ __noinline__ WallDelta<Tv> wall_delta(const Obst &o, const Geom &gm, 
   for (int c = 0; c < 3; c++) r.g[c] = (Tv)((double)go.v[c] + a * (double)fk.v[c] + (w1.f[c] - w0.f[c]));
   return r;
 }
-
-// V consecutive sites per thread: V = 4 with 16-byte loads (two for FP64)
-// for grids with nx*ny divisible by 4 (all power-of-two grids), V = 1 else.
-// The streaming kernels are bound by the loads each thread keeps in flight.
-template <typename T, int V> struct VecN;
-template <typename T> struct VecN<T, 1> {
-  static __device__ __forceinline__ void ld(const T *p, T o[1]) { o[0] = *p; }
-  static __device__ __forceinline__ void st(T *p, const T o[1]) { *p = o[0]; }
-};
-template <> struct VecN<float, 4> {
-  static __device__ __forceinline__ void ld(const float *p, float o[4]) {
-    const float4 v = *reinterpret_cast<const float4 *>(p);
-    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
-  }
-  static __device__ __forceinline__ void st(float *p, const float o[4]) {
-    *reinterpret_cast<float4 *>(p) = make_float4(o[0], o[1], o[2], o[3]);
-  }
-};
-template <> struct VecN<double, 4> {
-  static __device__ __forceinline__ void ld(const double *p, double o[4]) {
-    const double2 a = *reinterpret_cast<const double2 *>(p), b = *reinterpret_cast<const double2 *>(p + 2);
-    o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
-  }
-  static __device__ __forceinline__ void st(double *p, const double o[4]) {
-    *reinterpret_cast<double2 *>(p) = make_double2(o[0], o[1]);
-    *reinterpret_cast<double2 *>(p + 2) = make_double2(o[2], o[3]);
-  }
-};
 
 // Dot products of the streaming kernels: the terms of one loop trip (at most
 // V x ndof) are summed in the vector type, each trip sum then enters the

@@ -5,7 +5,7 @@
 //              of step 1: v_h = v + dt/2 (f - gamma v); u += dt v_h
 //   WHILE(step < nsteps) {
 //     f_el = F_el(u)                 (the handle's force evaluation)
-//     k_second   f = f_el + F_w(u) + f_ext; v = (v_h + dt/2 f) / (1 + dt gamma/2);
+//     k_second   f = f_el + F_w(u) + f_ext (not stored); v = (v_h + dt/2 f) / (1 + dt gamma/2);
 //                E(step) in FP64 by the last block, which also advances the
 //                step and sets the loop condition; then, unless this was the
 //                last step, the first half of the next one in the same pass
@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <chrono>
+#include <cstdint>
 #include <cmath>
 #include <string>
 #include <vector>
@@ -25,6 +26,7 @@
 #include "gfmd_internal.h"
 #include "gfmd_obstacle.cuh"
 #include "gfmd_reduce.cuh"
+#include "gfmd_vec.cuh"
 
 namespace gfmd {
 
@@ -86,49 +88,79 @@ __device__ __forceinline__ bool atom_wall(const Obst &o, int ix, int iy, int l, 
 // energy of the state into energies[step] (advancing step first with kick).
 // Unless this was the last step, the first half of the next step follows in
 // the same pass (v_h = v + dt/2 (f - gamma v), u += dt v_h), so a step costs
-// one evaluation and one pass over the state.
-template <typename T>
+// one evaluation and one pass over the state: read f_el, v, u, write v, u
+// (the total force itself is not stored).  V consecutive sites per thread
+// (V = 4: 16-byte loads); OBST = false compiles the pass without the wall
+// code.  |v|^2 and |f|^2 are summed per loop trip in T, each trip sum then
+// entering the thread's Dot (FP64, or a compensated FP32 pair).
+template <typename T, int V, bool OBST>
 __global__ void __launch_bounds__(kT) k_second(Obst o, Geom gm, T *__restrict__ u, T *__restrict__ v,
-                                                const T *__restrict__ fel, T *__restrict__ f, T dt, T gamma,
-                                                int kick, const double *__restrict__ d_eel,
-                                                double *__restrict__ energies, double *__restrict__ part,
-                                                DynCtl *ctl, double *__restrict__ last,
+                                                const T *__restrict__ fel, T dt, T gamma, int kick,
+                                                const double *__restrict__ d_eel, double *__restrict__ energies,
+                                                double *__restrict__ part, DynCtl *ctl, double *__restrict__ last,
                                                 cudaGraphConditionalHandle hc, int use_hc) {
   const int N = gm.nx * gm.ny;
   const int nl = gm.ndof / 3;
   const T hdt = (T)0.5 * dt;
   const T den = (T)1 / ((T)1 + hdt * gamma);
-  const bool obst = o.kind != GFMD_OBST_NONE || o.fz_ext != 0.0;
   // read before the last block advances the step: is there a next step?
   const bool next = (ctl->step + (kick ? 1 : 0)) < ctl->nsteps;
   Dot<T> vv, ff;
   double ew = 0.0;
   float fm = 0.0f;
-  for (int s = blockIdx.x * kT + threadIdx.x; s < N; s += gridDim.x * kT) {
-    const int ix = s / gm.ny, iy = s - ix * gm.ny;
-    for (int l = 0; l < nl; l++) {
-      double fw[3] = {0.0, 0.0, 0.0};
-      const bool hit = obst && atom_wall<T>(o, ix, iy, l, s, N, u, fw, ew);
+  for (int s0 = V * (blockIdx.x * kT + threadIdx.x); s0 < N; s0 += V * gridDim.x * kT) {
+    int six[V], siy[V];
+    if constexpr (OBST) {
+      int ix = s0 / gm.ny, iy = s0 - ix * gm.ny;  // one division per trip
 #pragma unroll
-      for (int c = 0; c < 3; c++) {
-        const size_t idx = (size_t)(3 * l + c) * N + s;
-        T fv = fel[idx];
-        if (hit) fv = (T)((double)fv + fw[c]);
-        f[idx] = fv;
-        T vn = v[idx];
-        if (kick) vn = (vn + hdt * fv) * den;
-        vv.add(vn, vn);
-        ff.add(fv, fv);
-        fm = fmaxf(fm, fabsf((float)fv));
-        if (next) {
-          const T vh = vn + hdt * (fv - gamma * vn);
-          v[idx] = vh;
-          u[idx] = u[idx] + dt * vh;
-        } else if (kick) {
-          v[idx] = vn;
+      for (int j = 0; j < V; j++) {
+        six[j] = ix;
+        siy[j] = iy;
+        if (++iy == gm.ny) {
+          iy = 0;
+          ix++;
         }
       }
     }
+    T svv = (T)0, sff = (T)0;
+    for (int l = 0; l < nl; l++) {
+      double fw[V][3];
+      bool hit[V];
+      if constexpr (OBST) {
+#pragma unroll
+        for (int j = 0; j < V; j++) hit[j] = atom_wall<T>(o, six[j], siy[j], l, s0 + j, N, u, fw[j], ew);
+      }
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const size_t idx = (size_t)(3 * l + c) * N + s0;
+        T fv[V], vn[V], uu[V];
+        VecN<T, V>::ld(fel + idx, fv);
+        VecN<T, V>::ld(v + idx, vn);
+        if (next) VecN<T, V>::ld(u + idx, uu);
+#pragma unroll
+        for (int j = 0; j < V; j++) {
+          if constexpr (OBST) {
+            if (hit[j]) fv[j] = (T)((double)fv[j] + fw[j][c]);
+          }
+          if (kick) vn[j] = (vn[j] + hdt * fv[j]) * den;
+          svv = fma(vn[j], vn[j], svv);
+          sff = fma(fv[j], fv[j], sff);
+          fm = fmaxf(fm, fabsf((float)fv[j]));
+          if (next) {
+            vn[j] = vn[j] + hdt * (fv[j] - gamma * vn[j]);
+            uu[j] = uu[j] + dt * vn[j];
+          }
+        }
+        if (next) {
+          VecN<T, V>::st(v + idx, vn);
+          VecN<T, V>::st(u + idx, uu);
+        } else if (kick) {
+          VecN<T, V>::st(v + idx, vn);
+        }
+      }
+    }
+    vv.addsum(svv);
+    ff.addsum(sff);
   }
   const double acc[4] = {vv.get(), ew, ff.get(), (double)fm};
   __shared__ double res[4];
@@ -144,6 +176,25 @@ __global__ void __launch_bounds__(kT) k_second(Obst o, Geom gm, T *__restrict__ 
     const bool go_on = ctl->status == 0 && ctl->step < ctl->nsteps;
     if (use_hc) cudaGraphSetConditional(hc, go_on ? 1u : 0u);
   }
+}
+
+// One launch of the pass in the variant that fits the grid and the buffers.
+template <typename T>
+cudaError_t launch_second(int nblk, cudaStream_t st, const Obst &o, const Geom &gm, T *u, T *v, const T *fel, T dt,
+                          T gamma, int kick, const double *d_eel, double *en, double *part, DynCtl *ctl,
+                          double *last, cudaGraphConditionalHandle hc) {
+  const bool obst = o.kind != GFMD_OBST_NONE || o.fz_ext != 0.0;
+  auto al16 = [](const void *p) { return ((uintptr_t)p & 15) == 0; };
+  const bool v4 = ((size_t)gm.nx * gm.ny) % 4 == 0 && al16(u) && al16(v) && al16(fel);
+  if (v4 && obst)
+    k_second<T, 4, true><<<nblk, kT, 0, st>>>(o, gm, u, v, fel, dt, gamma, kick, d_eel, en, part, ctl, last, hc, 1);
+  else if (v4)
+    k_second<T, 4, false><<<nblk, kT, 0, st>>>(o, gm, u, v, fel, dt, gamma, kick, d_eel, en, part, ctl, last, hc, 1);
+  else if (obst)
+    k_second<T, 1, true><<<nblk, kT, 0, st>>>(o, gm, u, v, fel, dt, gamma, kick, d_eel, en, part, ctl, last, hc, 1);
+  else
+    k_second<T, 1, false><<<nblk, kT, 0, st>>>(o, gm, u, v, fel, dt, gamma, kick, d_eel, en, part, ctl, last, hc, 1);
+  return cudaGetLastError();
 }
 
 __global__ void k_cvt_f(size_t n, const double *__restrict__ a, float *__restrict__ b) {
@@ -197,7 +248,7 @@ cudaError_t run_t(gfmd_solver *h, const Obst &o0, double dt, double gamma, int n
   DT_CHECK(cudaEventCreateWithFlags(&b.ev, cudaEventDisableTiming));
   auto up = [](size_t x) { return (x + 255) / 256 * 256; };
   const bool map = o.kind == GFMD_OBST_MAP_EXP && f32;
-  const size_t sz[8] = {up(sizeof(T) * n), up(sizeof(T) * n), f32 ? up(sizeof(T) * n) : 0, f32 ? up(sizeof(T) * n) : 0,
+  const size_t sz[8] = {up(sizeof(T) * n), 0, f32 ? up(sizeof(T) * n) : 0, f32 ? up(sizeof(T) * n) : 0,
                         up(sizeof(double) * (nsteps + 1)), up(sizeof(double) * kQ * nblk), up(sizeof(double) * 4 + sizeof(DynCtl)),
                         map ? up(sizeof(float) * nsite) : 0};
   size_t off[8], tot = 0;
@@ -208,7 +259,6 @@ cudaError_t run_t(gfmd_solver *h, const Obst &o0, double dt, double gamma, int n
   DT_CHECK(cudaMalloc(&b.arena, tot));
   char *a = static_cast<char *>(b.arena);
   T *fel = reinterpret_cast<T *>(a + off[0]);
-  T *f = reinterpret_cast<T *>(a + off[1]);
   T *u = f32 ? reinterpret_cast<T *>(a + off[2]) : reinterpret_cast<T *>(d_u);
   T *v = f32 ? reinterpret_cast<T *>(a + off[3]) : reinterpret_cast<T *>(d_v);
   double *en = reinterpret_cast<double *>(a + off[4]);
@@ -237,10 +287,8 @@ cudaError_t run_t(gfmd_solver *h, const Obst &o0, double dt, double gamma, int n
   DT_CHECK(cudaGraphConditionalHandleCreate(&hc, b.graph, 0, cudaGraphCondAssignDefault));
   DT_CHECK(cudaStreamBeginCaptureToGraph(b.cs, b.graph, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
   cudaError_t e = eval_dyn(h, b.cs, u, fel, t, scal);
-  if (e == cudaSuccess) {
-    k_second<T><<<nblk, kT, 0, b.cs>>>(o, gm, u, v, fel, f, (T)dt, (T)gamma, 0, scal, en, part, ctl, scal + 1, hc, 1);
-    e = cudaGetLastError();
-  }
+  if (e == cudaSuccess)
+    e = launch_second<T>(nblk, b.cs, o, gm, u, v, fel, (T)dt, (T)gamma, 0, scal, en, part, ctl, scal + 1, hc);
   cudaGraph_t body = nullptr;
   if (e == cudaSuccess) {
     cudaStreamCaptureStatus cs;
@@ -267,10 +315,8 @@ cudaError_t run_t(gfmd_solver *h, const Obst &o0, double dt, double gamma, int n
   if (e != cudaSuccess) return e;
   DT_CHECK(cudaStreamBeginCaptureToGraph(b.cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
   e = eval_dyn(h, b.cs, u, fel, t, scal);
-  if (e == cudaSuccess) {
-    k_second<T><<<nblk, kT, 0, b.cs>>>(o, gm, u, v, fel, f, (T)dt, (T)gamma, 1, scal, en, part, ctl, scal + 1, hc, 1);
-    e = cudaGetLastError();
-  }
+  if (e == cudaSuccess)
+    e = launch_second<T>(nblk, b.cs, o, gm, u, v, fel, (T)dt, (T)gamma, 1, scal, en, part, ctl, scal + 1, hc);
   e2 = cudaStreamEndCapture(b.cs, &got);
   if (e == cudaSuccess) e = e2;
   if (e != cudaSuccess) return e;
