@@ -67,7 +67,6 @@ using red::kQ;
 using red::Dot;
 using red::reduce_last;
 constexpr int kLsMax = 8;   // Newton probes per line search
-constexpr size_t kBatchGroups = 8;  // graphs (and streams) a batched phase runs concurrently
 
 // Grids whose site count allows the 4-site vector kernels.
 inline bool nsite4(const Geom &g) { return ((size_t)g.nx * g.ny) % 4 == 0; }
@@ -1055,100 +1054,42 @@ struct GraphHolder {
 template <typename Tx, typename Tv>
 cudaError_t run_phase(std::vector<Item *> &its, bool refine, cudaStream_t ms, cudaEvent_t fork,
                       std::vector<cudaEvent_t> &join) {
+  GraphHolder gh;
   const double t0 = now_s();
   const bool direct = no_graphs();
-  // Items in groups, one graph and one stream per group: the conditional
-  // loops of the branches of one graph run one after another, while graphs
-  // on separate streams run concurrently.  Items go round-robin to
-  // kBatchGroups groups; a single group runs on ms.
-  const size_t n = its.size();
-  const size_t G = direct ? 1 : std::min<size_t>(n, kBatchGroups);
-  std::vector<std::vector<Item *>> grp(G);
-  std::vector<std::vector<cudaEvent_t>> gjoin(G);
-  for (size_t i = 0; i < n; i++) {
-    grp[i % G].push_back(its[i]);
-    gjoin[i % G].push_back(join[i]);
-  }
-  struct Groups {
-    std::vector<cudaStream_t> st;
-    std::vector<cudaEvent_t> fork, done;
-    ~Groups() {
-      for (cudaEvent_t e : fork) if (e) cudaEventDestroy(e);
-      for (cudaEvent_t e : done) if (e) cudaEventDestroy(e);
-      for (cudaStream_t x : st) if (x) cudaStreamDestroy(x);
-    }
-  } gs;
-  std::vector<cudaStream_t> gst(G, ms);
-  std::vector<cudaEvent_t> gfork(G, fork);
-  if (G > 1) {
-    gs.st.assign(G, nullptr);
-    gs.fork.assign(G, nullptr);
-    gs.done.assign(G + 1, nullptr);
-    for (size_t g = 0; g < G; g++) {
-      RT_CHECK(cudaStreamCreateWithFlags(&gs.st[g], cudaStreamNonBlocking));
-      RT_CHECK(cudaEventCreateWithFlags(&gs.fork[g], cudaEventDisableTiming));
-      RT_CHECK(cudaEventCreateWithFlags(&gs.done[g], cudaEventDisableTiming));
-      gst[g] = gs.st[g];
-      gfork[g] = gs.fork[g];
-    }
-    RT_CHECK(cudaEventCreateWithFlags(&gs.done[G], cudaEventDisableTiming));
-    RT_CHECK(cudaEventRecord(gs.done[G], ms));  // the groups start after ms's work
-    for (size_t g = 0; g < G; g++) RT_CHECK(cudaStreamWaitEvent(gst[g], gs.done[G], 0));
-  }
-  std::vector<GraphHolder> gh(G);
-  if (!direct)
-    for (size_t g = 0; g < G; g++)
-      RT_CHECK((build_phase<Tx, Tv>(grp[g], refine, gst[g], gfork[g], gjoin[g], &gh[g].g, &gh[g].x)));
+  if (!direct) RT_CHECK((build_phase<Tx, Tv>(its, refine, ms, fork, join, &gh.g, &gh.x)));
   const double t1 = now_s();
   int launches = 0;
   for (Item *it : its) it->it0 = it->b.hctl->it;
-  std::vector<char> live(G, 1);
   for (;;) {
     launches++;
     if (direct) RT_CHECK((run_launch_direct<Tx, Tv>(its, refine, ms)));
-    for (size_t g = 0; g < G; g++) {
-      if (!live[g]) continue;
-      if (!direct) RT_CHECK(cudaGraphLaunch(gh[g].x, gst[g]));
-      for (Item *it : grp[g])
-        RT_CHECK(cudaMemcpyAsync(it->b.hctl, it->b.ctl, sizeof(CgCtl), cudaMemcpyDeviceToHost, gst[g]));
-    }
-    for (size_t g = 0; g < G; g++)
-      if (live[g]) RT_CHECK(cudaStreamSynchronize(gst[g]));
+    else RT_CHECK(cudaGraphLaunch(gh.x, ms));
+    for (Item *it : its) RT_CHECK(cudaMemcpyAsync(it->b.hctl, it->b.ctl, sizeof(CgCtl), cudaMemcpyDeviceToHost, ms));
+    RT_CHECK(cudaStreamSynchronize(ms));
     bool all = true;
-    for (size_t g = 0; g < G; g++) {
-      if (!live[g]) continue;
-      bool any = false;
-      for (Item *it : grp[g]) {
-        CgCtl &c = *it->b.hctl;
-        if (c.parked) continue;
-        it->evals += 1 + (c.it - it->it0);
-        const bool ran = c.it != it->it0;
-        it->it0 = c.it;
-        if (c.done == 0) {
-          if (!ran) return cudaErrorUnknown;  // an armed loop always iterates
-          if (!(c.bulk && c.since >= c.recompute && !(c.fmax < 0.5 * c.fmax_restart))) {
-            all = false;
-            any = true;
-            continue;
-          }
-          c.done = 1;  // FP32 stagnation: the bulk phase is over for this item
+    for (Item *it : its) {
+      CgCtl &c = *it->b.hctl;
+      if (c.parked) continue;
+      it->evals += 1 + (c.it - it->it0);
+      const bool ran = c.it != it->it0;
+      it->it0 = c.it;
+      if (c.done == 0) {
+        if (!ran) return cudaErrorUnknown;  // an armed loop always iterates
+        if (!(c.bulk && c.since >= c.recompute && !(c.fmax < 0.5 * c.fmax_restart))) {
+          all = false;
+          continue;
         }
-        it->done = c.done;
-        c.parked = 1;
-        RT_CHECK(cudaMemcpyAsync(it->b.ctl, &c, sizeof(CgCtl), cudaMemcpyHostToDevice, gst[g]));
+        c.done = 1;  // FP32 stagnation: the bulk phase is over for this item
       }
-      live[g] = any ? 1 : 0;
+      it->done = c.done;
+      c.parked = 1;
+      RT_CHECK(cudaMemcpyAsync(it->b.ctl, &c, sizeof(CgCtl), cudaMemcpyHostToDevice, ms));
     }
     if (all) {
-      if (G > 1) {  // ms continues after every group
-        for (size_t g = 0; g < G; g++) {
-          RT_CHECK(cudaEventRecord(gs.done[g], gst[g]));
-          RT_CHECK(cudaStreamWaitEvent(ms, gs.done[g], 0));
-        }
-      }
       if (trace_on())
-        std::fprintf(stderr, "gfmd cg phase <%s,%s> items %zu in %zu graphs: build %.3f s, %d launches %.3f s\n",
-                     sizeof(Tx) == 8 ? "f64" : "f32", sizeof(Tv) == 8 ? "f64" : "f32", its.size(), G, t1 - t0,
+        std::fprintf(stderr, "gfmd cg phase <%s,%s> items %zu: graph build %.3f s, %d launches %.3f s\n",
+                     sizeof(Tx) == 8 ? "f64" : "f32", sizeof(Tv) == 8 ? "f64" : "f32", its.size(), t1 - t0,
                      launches, now_s() - t1);
       return cudaSuccess;
     }
