@@ -809,6 +809,14 @@ def run_gb300(args):
                 "algorithmic_bytes": bts, "peak_kind": peak_kind,
                 "phi_reals_per_wavevector": phi_reals,
                 "phi_pattern": info.get("phi_pattern", 0)}
+    # the three-launch structure's floor: the half spectrum W (complex, the
+    # handle's precision) makes four passes through HBM that the algorithmic
+    # count excludes, since the 2-D transform's transpose separates the row
+    # and column launches and W is larger than L2 at this size
+    w_bytes = (ny // 2 + 1) * d * ((nx + 31) // 32 * 32) * 2 * sz
+    floor = bts + 4 * w_bytes
+    roofline["structure_floor_bytes"] = floor
+    roofline["structure_floor_frac"] = floor / (ms * 1e-3) / 1e9 / peak
     if kernel_ms:
         roofline["kernel_ms"] = kernel_ms
 
