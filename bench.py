@@ -800,23 +800,28 @@ def run_gb300(args):
     peak, peak_kind = measured_peaks()
     sz = 4 if args.precision == "f32" else 8
     info = s.info()
-    phi_reals = info.get("phi_reals_per_wavevector") or d * d
-    bts = algorithmic_bytes(nx, ny, d, sz, phi_reals)
+    # canonical bytes of an evaluation (ndof^2 table reals per wavevector)
+    bts = algorithmic_bytes(nx, ny, d, sz)
     achieved = bts / (ms * 1e-3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": profile_traffic(),
                 "kernel": "one force evaluation (all launches of the evaluation)",
-                "algorithmic_bytes": bts, "peak_kind": peak_kind,
-                "phi_reals_per_wavevector": phi_reals,
-                "phi_pattern": info.get("phi_pattern", 0)}
-    # the three-launch structure's floor: the half spectrum W (complex, the
-    # handle's precision) makes four passes through HBM that the algorithmic
-    # count excludes, since the 2-D transform's transpose separates the row
-    # and column launches and W is larger than L2 at this size
+                "algorithmic_bytes": bts, "peak_kind": peak_kind}
+    # the bytes this evaluation needs with the table's storage pattern (the
+    # pairs that are zero at every wavevector are not stored), and the
+    # three-launch structure's floor: the half spectrum W (complex, the
+    # handle's precision) makes four passes through HBM that neither count
+    # includes, since the 2-D transform's transpose separates the row and
+    # column launches and W is larger than L2 at this size
+    phi_reals = info.get("phi_reals_per_wavevector") or d * d
+    needed = algorithmic_bytes(nx, ny, d, sz, phi_reals)
     w_bytes = (ny // 2 + 1) * d * ((nx + 31) // 32 * 32) * 2 * sz
-    floor = bts + 4 * w_bytes
-    roofline["structure_floor_bytes"] = floor
-    roofline["structure_floor_frac"] = floor / (ms * 1e-3) / 1e9 / peak
+    floor = needed + 4 * w_bytes
+    roofline["table_storage"] = {"pattern": info.get("phi_pattern", 0), "reals_per_wavevector": phi_reals,
+                                 "needed_bytes": needed,
+                                 "needed_frac": needed / (ms * 1e-3) / 1e9 / peak,
+                                 "structure_floor_bytes": floor,
+                                 "structure_floor_frac": floor / (ms * 1e-3) / 1e9 / peak}
     if kernel_ms:
         roofline["kernel_ms"] = kernel_ms
 
