@@ -203,6 +203,7 @@ cudaError_t setup_fp32_kernels(gfmd_solver *h) {
       if (e != cudaSuccess) return e;
       h->col_r32 = true;
       h->col_cl = cl;
+      h->col_minb = D == 12 ? 2 : 3;  // compiled residency of the default instance
       h->phi_v = (D * D) % 4 == 0 ? 4 : 1;
       h->bytes += (double)f.size() * sizeof(float);
     }
@@ -500,7 +501,8 @@ int gfmd_memory_usage(gfmd_handle_t h, double *bytes) {
 // of the largest that fits the shared-memory budget) and, for the
 // register-transform column kernel, the rounds of its Phi stream prefetched
 // into L2 ahead of use (1-3) and the resident blocks per SM it is compiled
-// for (2 or 3, for the 12-column kernel at nx = 2048).  With the table
+// for (2 or 3 for the 12-column kernel, 2-4 for the 3-column kernel, at
+// nx = 2048), plus the rows per block of the warp-row kernels.  With the table
 // uploaded, each candidate is timed (CUDA events, best of 3 runs of 4
 // evaluations after a warm-up, each evaluation after a write of 1.25x the L2
 // size) on scratch inputs and the fastest is kept; results are cached per grid,
@@ -570,6 +572,7 @@ cudaError_t autotune(gfmd_solver *h) {
   if (h->col_r32) {
     pfs = {1, 2, 3};
     if (h->g.ndof == 12 && h->g.nx == 2048) minbs = {2, 3};
+    if (h->g.ndof == 3 && h->g.nx == 2048) minbs = {2, 3, 4};
   }
   for (int rb : rbs)
     for (int pf : pfs)

@@ -18,7 +18,11 @@ cudaError_t enqueue_col_r32(gfmd_solver *h, float2 *W, double *d_epot) {
   if (D == 12 && CL == 2 && !n2k) return launch_col_r32<12, 2, 10, 3>(h, W, d_epot);
   if (D == 6 && CL == 2 && n2k) return launch_col_r32<6, 2, 11, 3>(h, W, d_epot);
   if (D == 6 && CL == 1 && !n2k) return launch_col_r32<6, 1, 10, 3>(h, W, d_epot);
-  if (D == 3 && CL == 1 && n2k) return launch_col_r32<3, 1, 11, 3>(h, W, d_epot);
+  if (D == 3 && CL == 1 && n2k) {  // 2048 / 1025 one-ky blocks: the residency sets the last wave
+    if (h->col_minb == 4) return launch_col_r32<3, 1, 11, 4>(h, W, d_epot);
+    if (h->col_minb == 2) return launch_col_r32<3, 1, 11, 2>(h, W, d_epot);
+    return launch_col_r32<3, 1, 11, 3>(h, W, d_epot);
+  }
   if (D == 3 && CL == 1 && !n2k) return launch_col_r32<3, 1, 10, 3>(h, W, d_epot);
   return cudaErrorInvalidValue;
 }

@@ -104,7 +104,7 @@ struct gfmd_solver {
                              // q = (nx/32) (kx mod 32) + kx/32; else digit-reversed kx
   void *d_twc = nullptr;     // float4 [k1][t] w_nx^(t k1) of that kernel
   int col_pf = 1;            // Phi rounds prefetched into L2 ahead (tuned)
-  int col_minb = 2;          // resident blocks per SM the kernel is compiled for (tuned: 2 or 3)
+  int col_minb = 2;          // resident blocks per SM the kernel is compiled for (tuned: 2-4)
   void *d_tw32 = nullptr;    // float4: [k1][l] w_1024^(l k1), then e^{-2 pi i k/2048}, k = 0..1024
   CUtensorMap tm_w[2];       // W as floats {2 nxp, ndof, nyc}, boxes {16, 1, 128} and {32, 1, 64}
   int row_rb = 8;            // rows per block of those kernels (8 or 16, tuned)
