@@ -146,18 +146,20 @@ def test_fp32_cg_without_refinement():
     assert rel_l2(u32.cpu().numpy(), u64.cpu().numpy()) <= 1e-3
 
 
-def test_damped_verlet_matches_oracle():
-    nx = ny = 16
+# 16 x 16: the 4-site pass; 15 x 14 (210 sites): the one-site pass; with and
+# without an obstacle (the pass compiled without the wall code)
+@pytest.mark.parametrize("nx,ny,wall", [(16, 16, True), (15, 14, True), (16, 16, False), (15, 14, False)])
+def test_damped_verlet_matches_oracle(nx, ny, wall):
     d, half, full, linf = tables(KERNEL_FCC2, nx, ny)
     el = oracle_elastic(full, linf, nx, ny)
     rng = np.random.default_rng(9)
     u0 = rng.normal(0, 0.05, (d, nx * ny))
     v0 = rng.normal(0, 0.01, (d, nx * ny))
     ob = osv.ObstacleSpec(osv.SPHERE_EXP, center=(8.0, 8.0, 6.2), radius=6.0, epsilon=0.05,
-                          sigma=0.5, cutoff=3.0, layer_offsets=[(0, 0, 0), (0.5, 0.5, -0.7071)])
+                          sigma=0.5, cutoff=3.0, layer_offsets=[(0, 0, 0), (0.5, 0.5, -0.7071)]) if wall else None
     u_ref, v_ref, e_ref = osv.verlet(el, ob, u0, v0, nx, ny, 0.01, 0.1, 100)
     s = _solver(nx, ny, d, half, linf)
-    o, _ = _gpu_obst(ob)
+    o = _gpu_obst(ob)[0] if wall else None
     u = torch.from_numpy(u0).cuda()
     v = torch.from_numpy(v0).cuda()
     e, rep = s.run_dynamics(u, v, 0.01, 0.1, 100, o)
