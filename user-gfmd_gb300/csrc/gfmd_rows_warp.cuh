@@ -25,6 +25,7 @@
 #define GFMD_GB300_ROWS_WARP_CUH
 
 #include <cuda.h>
+#include <cstdint>
 #include <cuda_runtime.h>
 
 #include "gfmd_fft.cuh"
@@ -180,8 +181,15 @@ __global__ void __launch_bounds__(32 * RB, RB == 8 ? 2 : 1)
   };
   if ((int)blockIdx.x < nsets) load_rows(blockIdx.x);
   int cc = 0;  // tiles pairs committed by this block so far (stage buffer parity)
+  const bool aligned = ((uintptr_t)u & 15) == 0;
   for (int set = blockIdx.x; set < nsets; set += gridDim.x) {
     const int dof = set / nxb, ix0 = (set % nxb) * kRB;
+    // the next set's row of this warp streams into L2 during the transform
+    // (its loads, issued after it, then hit L2)
+    if (lane == 0 && aligned && set + (int)gridDim.x < nsets) {
+      const int nset = set + gridDim.x, ndof = nset / nxb, nix0 = (nset % nxb) * kRB;
+      bulk_prefetch_l2(u + ((size_t)ndof * g.nx + nix0 + warp) * (size_t)(2 * kN), 2 * kN * sizeof(Tin));
+    }
     // ---- row transform (one warp per row) ----
     {
       float2 *row = xs + warp * kPitch;

@@ -92,6 +92,12 @@ __device__ __forceinline__ void prefetch_tmap(const CUtensorMap *map) {
   asm volatile("prefetch.tensormap [%0];\n" ::"l"(map) : "memory");
 }
 
+// Asynchronous prefetch of `bytes` (a multiple of 16) of global memory from
+// the 16-byte-aligned address g into L2.
+__device__ __forceinline__ void bulk_prefetch_l2(const void *g, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(g), "r"(bytes) : "memory");
+}
+
 }  // namespace gfmd
 
 #endif
