@@ -305,13 +305,6 @@ __global__ void __launch_bounds__(32 * RB, RB == 8 ? 2 : 1)
       __syncthreads();  // buffer p & 1 consumed
       if (threadIdx.x == 0 && p + 2 < npairs) issue(p + 2);
     }
-    // the next set's tiles beyond its first two pairs (the pairs whose TMA
-    // loads start during its pre-split) stream into L2 during the transform
-    if (set + (int)gridDim.x < nsets) {
-      const int nset = set + gridDim.x, ndof = nset / nxb, nix0 = (nset % nxb) * kRB;
-      for (int ky = 2 * kChunk + (int)threadIdx.x; ky <= kN - 2 * kChunk; ky += K::kThreads)
-        bulk_prefetch_l2(W + ((size_t)ky * g.ndof + ndof) * g.nxp + nix0, kRB * 8);
-    }
     // ---- row transform (one warp per row) ----
     float2 *row = xs + warp * kPitch;
     float2 x[32];
