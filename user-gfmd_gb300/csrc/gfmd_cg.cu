@@ -686,15 +686,24 @@ __global__ void __launch_bounds__(kT) k_pcg_init(size_t n, const Tv *__restrict_
 
 // After the update: beta = max(0, z.(g - g_old) / (g_old.z_old)) with the
 // descent check h'.g = z.g + beta h.g > 0 (min_cg_gfmd.cpp:172-196).
-template <typename Tv>
+template <typename Tv, int V = 4>
 __global__ void __launch_bounds__(kT) k_pcg_beta(size_t n, const Tv *__restrict__ g, const Tv *__restrict__ gp,
                                                   const Tv *__restrict__ mz, double *__restrict__ part,
                                                   CgCtl *ctl) {
-  Dot<Tv> zg, zgo;
-  for (size_t i = blockIdx.x * (size_t)kT + threadIdx.x; i < n; i += (size_t)gridDim.x * kT) {
-    const Tv z = -mz[i];
-    zg.add(z, g[i]);
-    zgo.add(z, gp[i]);
+  Dot<Tv> zg, zgo;  // trip sums of V terms, then compensated (as in k_update)
+  for (size_t i = V * (blockIdx.x * (size_t)kT + threadIdx.x); i < n; i += V * (size_t)gridDim.x * kT) {
+    Tv zv[V], gv[V], pv[V];
+    VecN<Tv, V>::ld(mz + i, zv);
+    VecN<Tv, V>::ld(g + i, gv);
+    VecN<Tv, V>::ld(gp + i, pv);
+    Tv s1 = (Tv)0, s2 = (Tv)0;
+#pragma unroll
+    for (int j = 0; j < V; j++) {
+      s1 = fma(-zv[j], gv[j], s1);
+      s2 = fma(-zv[j], pv[j], s2);
+    }
+    zg.addsum(s1);
+    zgo.addsum(s2);
   }
   const double acc[2] = {zg.get(), zgo.get()};
   __shared__ double res[2];
@@ -942,7 +951,8 @@ cudaError_t enqueue_iteration(Item &it, cudaStream_t st, cudaGraphConditionalHan
         it.o, gm, x, h, fKh, g, gp, b.active, b.part, b.ctl, hwh, use_hc);
   if (it.hpre) {
     RT_CHECK(eval_on(it.hpre, st, g, io_type<Tv>(), mz, io_type<Tv>(), b.d_e, false));
-    k_pcg_beta<Tv><<<b.nblk, kT, 0, st>>>(b.n, g, gp, mz, b.part, b.ctl);
+    if (v4) k_pcg_beta<Tv, 4><<<grid_for(k_pcg_beta<Tv, 4>, sms, b.n, 4 * kT), kT, 0, st>>>(b.n, g, gp, mz, b.part, b.ctl);
+    else k_pcg_beta<Tv, 1><<<grid_for(k_pcg_beta<Tv, 1>, sms, b.n, kT), kT, 0, st>>>(b.n, g, gp, mz, b.part, b.ctl);
   }
   if (v4) k_dir<Tv, 4><<<grid_for(k_dir<Tv, 4>, sms, b.n, 4 * kT), kT, 0, st>>>(b.n, h, g, mz, b.part, b.ctl);
   else k_dir<Tv, 1><<<grid_for(k_dir<Tv, 1>, sms, b.n, kT), kT, 0, st>>>(b.n, h, g, mz, b.part, b.ctl);
