@@ -348,3 +348,38 @@ def test_structured_table_on_the_general_path(prec, nx, ny, monkeypatch):
     tol = F64_TOL if prec == "f64" else FP32_TOL
     assert rel_l2(f, f_ref) <= tol
     assert abs(e - e_ref) <= tol * abs(e_ref)
+
+
+@pytest.mark.parametrize("pattern", [1, 2])
+@pytest.mark.parametrize("prec,nx,ny", [("f32", 1024, 32), ("f64", 96, 80)])
+def test_structured_synthetic_tables(pattern, prec, nx, ny, monkeypatch):
+    """Seeded Hermitian tables (the oracle's generator) with the blocks
+    outside a storage pattern set to zero: gfmd_set_phi detects the pattern
+    (1: layer-tridiagonal with dense 3x3 blocks, 2: also diagonal blocks above
+    the last layer), and the forces equal the every-pair storage bit for bit
+    and the oracle's to the precision's tolerance."""
+    from conftest import oracle
+
+    d, L = 12, 4
+    full = np.empty((nx * ny, d, d), np.complex128)
+    oracle().orc_synthetic_phi_full(nx, ny, d, 7 + pattern, 1e-3, full.ctypes.data, 0)
+    for i in range(d):
+        for j in range(d):
+            li, lj = i // 3, j // 3
+            keep = abs(li - lj) <= 1 and not (pattern == 2 and li == lj and li < L - 1 and i != j)
+            if not keep:
+                full[:, i, j] = 0.0
+    linf = np.zeros(L)
+    u = np.random.default_rng(nx + pattern).normal(0.0, 0.01, (d, nx * ny))
+    s = _solver(nx, ny, d, prec, full, "full", linf)
+    assert s.info()["phi_pattern"] == pattern
+    monkeypatch.setenv("GFMD_PHI_DENSE", "1")
+    sd = _solver(nx, ny, d, prec, full, "full", linf)
+    monkeypatch.delenv("GFMD_PHI_DENSE")
+    f, fd = np.zeros_like(u), np.zeros_like(u)
+    e, ed = s.post_force(u, f), sd.post_force(u, fd)
+    assert np.array_equal(f, fd) and e == ed
+    f_ref, e_ref, _ = oracle_post_force(full, linf, u, nx, ny)
+    tol = F64_TOL if prec == "f64" else FP32_TOL
+    assert rel_l2(f, f_ref) <= tol
+    assert abs(e - e_ref) <= tol * abs(e_ref)
