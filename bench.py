@@ -456,12 +456,18 @@ def warmstart_run(g, torch, dev, n_train=256, n_pairs=256, epochs=20, n_apply=10
     tl = 10 ** np.linspace(-4, -2, n_loads)
     ts = list(range(seed + 10_000, seed + 10_000 + n_loads))
 
+    handles = {}
+
     def items(guesses=None, shift=0.0):
-        """Solver handles, obstacles and start vectors, built outside the
-        timings (table packing and upload are one-time costs)."""
+        """Obstacles and start vectors, with one set of solver handles per
+        preconditioner shift shared by the loads (they are solved one after
+        another); all built outside the timings (table packing and upload
+        are one-time costs)."""
+        if shift not in handles:
+            handles[shift] = rc.solvers(g, n_apply, shift)
+        hs = handles[shift]
         out, zs = [], []
         for i, (p, sd) in enumerate(zip(tl, ts)):
-            hs = rc.solvers(g, n_apply, shift)
             z, ob = rc.problem(g, torch, n_apply, p, sd)
             u = torch.zeros(3, n_apply * n_apply, dtype=torch.float64, device=dev)
             if guesses is not None:
