@@ -1,6 +1,8 @@
 // Solver loops around the force evaluation, resident on the GPU:
-//   static  - FIRE (FixFIRE, src/cuda/fix_fire.cpp:117-297); conjugate
-//             gradients live in gfmd_cg.cu;
+//   static  - FIRE (FixFIRE, src/cuda/fix_fire.cpp:117-297) and the trust
+//             region (MinTRGFMD, src/extras/min_tr_gfmd.cpp:95-241), each a
+//             CUDA graph per phase with its scalar logic on the device;
+//             conjugate gradients live in gfmd_cg.cu;
 //   dynamic - damped velocity Verlet lives in gfmd_dynamics.cu.
 // Obstacles (gfmd_obstacle.cuh) act on every atom of the grid.
 //
