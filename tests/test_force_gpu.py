@@ -213,7 +213,7 @@ def test_autotuned_plan_is_valid_and_changes_no_result(monkeypatch):
 @pytest.mark.parametrize(
     "args,nx,ny,rows,cl",
     [
-        ("ft fcc100 1.0 4 pair-potential 1 1.0 height 64", 2048, 2048, True, 3),
+        ("ft fcc100 1.0 4 pair-potential 1 1.0 height 64", 2048, 2048, True, 6),
         ("ft fcc100 1.0 2 pair-potential 1 1.0 height 64", 512, 2048, True, 1),
         ("ft sc100 1 1.0 pair-potential 2 1.0 1.0 height 128", 256, 256, False, 1),
         ("ft fcc100 1.0 4 pair-potential 1 1.0 height 64", 4096, 64, False, 4),

@@ -11,10 +11,8 @@ namespace gfmd {
 cudaError_t enqueue_col_r32(gfmd_solver *h, float2 *W, double *d_epot) {
   const int D = h->g.ndof, CL = h->col_cl;
   const bool n2k = h->g.nx == 2048;
-  const bool m3 = h->col_minb == 3;
   if (D == 12 && h->phi_pat != 0) return enqueue_col_r32_pat(h, W, d_epot);
-  if (D == 12 && CL == 3 && n2k)
-    return m3 ? launch_col_r32<12, 3, 11, 3>(h, W, d_epot) : launch_col_r32<12, 3, 11, 2>(h, W, d_epot);
+  if (D == 12 && CL == 6 && n2k) return launch_col_r32<12, 6, 11, 4>(h, W, d_epot);
   if (D == 12 && CL == 2 && !n2k) return launch_col_r32<12, 2, 10, 3>(h, W, d_epot);
   if (D == 6 && CL == 2 && n2k) return launch_col_r32<6, 2, 11, 3>(h, W, d_epot);
   if (D == 6 && CL == 1 && !n2k) return launch_col_r32<6, 1, 10, 3>(h, W, d_epot);

@@ -11,13 +11,10 @@ namespace gfmd {
 cudaError_t enqueue_col_r32_pat(gfmd_solver *h, float2 *W, double *d_epot) {
   const int CL = h->col_cl;
   const bool n2k = h->g.nx == 2048;
-  const bool m3 = h->col_minb == 3;
   if (h->g.ndof != 12) return cudaErrorInvalidValue;
-  if (CL == 3 && n2k) {
-    if (h->phi_pat == 2)
-      return m3 ? launch_col_r32<12, 3, 11, 3, 2>(h, W, d_epot) : launch_col_r32<12, 3, 11, 2, 2>(h, W, d_epot);
-    if (h->phi_pat == 1)
-      return m3 ? launch_col_r32<12, 3, 11, 3, 1>(h, W, d_epot) : launch_col_r32<12, 3, 11, 2, 1>(h, W, d_epot);
+  if (CL == 6 && n2k) {
+    if (h->phi_pat == 2) return launch_col_r32<12, 6, 11, 4, 2>(h, W, d_epot);
+    if (h->phi_pat == 1) return launch_col_r32<12, 6, 11, 4, 1>(h, W, d_epot);
   }
   if (CL == 2 && !n2k) {
     if (h->phi_pat == 2) return launch_col_r32<12, 2, 10, 3, 2>(h, W, d_epot);
