@@ -146,6 +146,59 @@ def test_fp32_cg_without_refinement():
     assert rel_l2(u32.cpu().numpy(), u64.cpu().numpy()) <= 1e-3
 
 
+_LS_SCRIPT = r"""
+import sys, numpy as np, torch
+sys.path.insert(0, sys.argv[1])
+from solver_cases import KERNEL_SC, gpu_obstacle, sphere_spec, tables
+from conftest import gfmd_pkg
+n, R, pen = int(sys.argv[3]), float(sys.argv[4]), float(sys.argv[5])
+d, half, full, linf = tables(KERNEL_SC, n, n)
+s = gfmd_pkg().gfmd_solver_factory("static/gb300/f32")
+s.set_grid_size(n, n, d); s.set_phi(half, "half", linf)
+r = gfmd_pkg().gfmd_solver_factory("static/gb300")
+r.set_grid_size(n, n, d); r.set_phi(half, "half", linf)
+u = torch.zeros(d, n * n, dtype=torch.float64, device="cuda")
+rep = s.minimize(u, gpu_obstacle(sphere_spec(n, n, R=R, pen=pen, cutoff=4.0)), "cg", ftol=1e-8, refine=r)
+assert rep["fmax"] <= 1e-8
+np.save(sys.argv[2], u.cpu().numpy())
+"""
+
+
+def _ls_run(tmp_path, n, R, pen, cluster):
+    import os
+    import subprocess
+    import sys
+    script = tmp_path / "ls.py"
+    script.write_text(_LS_SCRIPT)
+    out = tmp_path / f"u{int(cluster)}.npy"
+    env = dict(os.environ, GFMD_LS_CLUSTER="1" if cluster else "0", GFMD_TRACE="1")
+    p = subprocess.run([sys.executable, str(script), os.path.dirname(__file__), str(out), str(n), str(R), str(pen)],
+                       env=env, timeout=300, capture_output=True, text=True)
+    assert p.returncode == 0, p.stderr[-3000:]
+    return np.load(out), p.stderr
+
+
+# The FP32 phase's line search in one thread-block cluster against the
+# grid-wide probes (GFMD_LS_CLUSTER=0), mixed solves refined to 1e-8: a small
+# contact is searched by the cluster kernel (same minimum); a contact whose
+# box is larger than the cluster takes goes to the probes inside the graph's
+# IF node (the same kernels as without the cluster kernel: identical result).
+# R = 400 on 256^2: the line-search set (gap below 10) spans a ~182^2 box,
+# above the cluster's 24 576 sites, while the wall's range (gap below 4)
+# stays clear of the periodic wrap of the sphere's nearest image.
+@pytest.mark.parametrize("n,R,pen,small", [(64, 8.0, 0.3, True), (256, 400.0, 0.3, False)],
+                         ids=["cluster", "probes"])
+def test_cluster_line_search_matches_probes(tmp_path, n, R, pen, small):
+    u1, err1 = _ls_run(tmp_path, n, R, pen, True)
+    u0, err0 = _ls_run(tmp_path, n, R, pen, False)
+    assert "cluster line search off" not in err1
+    assert "cluster line search" in err1 and "cluster line search" not in err0
+    if small:
+        assert rel_l2(u1, u0) <= 1e-6
+    else:
+        assert np.array_equal(u1, u0)
+
+
 # 16 x 16: the 4-site pass; 15 x 14 (210 sites): the one-site pass; with and
 # without an obstacle (the pass compiled without the wall code)
 @pytest.mark.parametrize("nx,ny,wall", [(16, 16, True), (15, 14, True), (16, 16, False), (15, 14, False)])

@@ -42,9 +42,11 @@
 // reason the FP32 phase evaluates sphere and map walls in FP32.  Per-block
 // partials are combined in FP64 in a fixed order by the last block, so
 // results are bit-reproducible.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <chrono>
 #include <cstdio>
@@ -478,6 +480,173 @@ __global__ void __launch_bounds__(kT) k_probe(const __grid_constant__ Obst o, Ge
   }
 }
 
+// ---- the whole line search in one thread-block cluster ---------------------
+// FP32 phase, a sphere wall on one atom layer, a set whose box holds at most
+// kLsCap sites.  The set's x and h stay in registers for the whole search:
+// a Newton step is a pass over registers, a compensated FP32 reduction per
+// block and two cluster barriers (block sums gathered in block 0's shared
+// memory, the next step published there).  One launch replaces k_lsinit
+// and up to kLsMax probes, each of which chains a grid-wide reduction
+// through global memory.  A larger box leaves the search to those kernels:
+// block 0 sets the conditional that runs them.
+constexpr int kLsCl = 8;                     // blocks of the cluster (portable size)
+constexpr int kLsT = 1024;                   // threads per block
+constexpr int kLsS = 3;                      // sites per thread
+constexpr int kLsCap = kLsCl * kLsT * kLsS;  // largest box taken (sites)
+
+__host__ __device__ inline int ls_box_sites(const CgCtl &c) {
+  const int w = c.by1 - c.by0 + 1, ht = c.bx1 - c.bx0 + 1;
+  return (w > 0 && ht > 0) ? w * ht : 0;
+}
+
+// Unnormalised FP32 pair hi + lo; the sum adds the rounding error of
+// hi_a + hi_b (TwoSum) to the low parts.
+struct F2 {
+  float hi, lo;
+};
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bb = __fsub_rn(s, a.hi);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+  return F2{s, __fadd_rn(__fadd_rn(a.lo, b.lo), e)};
+}
+__device__ __forceinline__ F2 f2_down(F2 v, int off) {
+  return F2{__shfl_down_sync(0xffffffffu, v.hi, off), __shfl_down_sync(0xffffffffu, v.lo, off)};
+}
+
+template <typename Tx, typename Tv>
+__global__ void __cluster_dims__(kLsCl, 1, 1) __launch_bounds__(kLsT, 1)
+    k_ls_cluster(const __grid_constant__ Obst o, Geom gm, const Tx *__restrict__ x, const Tv *__restrict__ h,
+                 const unsigned char *__restrict__ active, const double *__restrict__ eh, CgCtl *ctl,
+                 cudaGraphConditionalHandle hls, int use_hc) {
+  static_assert(sizeof(Tx) == 4 && sizeof(Tv) == 4, "the FP32 phase's line search");
+  static_assert(kLsT == 32 * 32, "one warp reduces the block's 32 warp sums");
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank();
+  const int nb = ls_box_sites(*ctl);
+  const bool big = nb > kLsCap;  // uniform over the cluster
+  if (rank == 0 && threadIdx.x == 0) set_loop(hls, use_hc, big ? 1u : 0u);
+  if (big) return;
+
+  __shared__ F2 ws[kLsT / 32][2];  // warp sums
+  __shared__ F2 bs[kLsCl][2];      // block sums (block 0)
+  __shared__ float pub_a;          // step published by block 0
+  __shared__ int pub_done;
+  __shared__ LineState L;          // block 0, thread 0
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int N = gm.nx * gm.ny;
+  const int w = ctl->by1 - ctl->by0 + 1, x0 = ctl->bx0, y0 = ctl->by0;
+  // this thread's sites of the set (box positions t, t + nthr, ...) as
+  // ix << 16 | iy (nx, ny <= 8192), -1 for none, with their x and h
+  int sp[kLsS];
+  float xc[kLsS][3], hc[kLsS][3];
+#pragma unroll
+  for (int k = 0; k < kLsS; k++) {
+    const int i = rank * kLsT + (int)threadIdx.x + k * kLsCl * kLsT;
+    sp[k] = -1;
+#pragma unroll
+    for (int c = 0; c < 3; c++) xc[k][c] = hc[k][c] = 0.0f;
+    if (i < nb) {
+      const int r = i / w;
+      const int ix = x0 + r, iy = y0 + (i - r * w);
+      const int s = ix * gm.ny + iy;
+      if (active[s]) {
+        sp[k] = ix << 16 | iy;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          xc[k][c] = (float)x[(size_t)c * N + s];
+          hc[k][c] = (float)h[(size_t)c * N + s];
+        }
+      }
+    }
+  }
+  cl.sync();  // every block has started before shared memory is written across the cluster
+  // F_w(x + a h).h and h^T H_w h over this thread's sites
+  auto pass = [&](float a, F2 &fh, F2 &cw) {
+    fh = F2{0.0f, 0.0f};
+    cw = F2{0.0f, 0.0f};
+#pragma unroll
+    for (int k = 0; k < kLsS; k++) {
+      if (sp[k] < 0) continue;
+      const SphereOff q = sphere_off(o, gm.nx, gm.ny, sp[k] >> 16, sp[k] & 0xffff, 0, xc[k][0] + a * hc[k][0],
+                                     xc[k][1] + a * hc[k][1], xc[k][2] + a * hc[k][2]);
+      float e, f[3], cv;
+      if (sphere_wall_f(o, q, hc[k], e, f, cv)) {
+        fh = f2_add(fh, F2{f[0] * hc[k][0] + f[1] * hc[k][1] + f[2] * hc[k][2], 0.0f});
+        cw = f2_add(cw, F2{cv, 0.0f});
+      }
+    }
+  };
+  // cluster sums of (fa, fb): valid in block 0, thread 0
+  F2 *bs0 = cl.map_shared_rank(&bs[0][0], 0);
+  auto cluster_sum = [&](F2 fa, F2 fb, double &sa, double &sb) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      fa = f2_add(fa, f2_down(fa, off));
+      fb = f2_add(fb, f2_down(fb, off));
+    }
+    if (lane == 0) {
+      ws[warp][0] = fa;
+      ws[warp][1] = fb;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      fa = ws[lane][0];
+      fb = ws[lane][1];
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        fa = f2_add(fa, f2_down(fa, off));
+        fb = f2_add(fb, f2_down(fb, off));
+      }
+      if (lane == 0) {
+        bs0[2 * rank] = fa;
+        bs0[2 * rank + 1] = fb;
+      }
+    }
+    cl.sync();
+    if (rank == 0 && warp == 0) {
+      fa = lane < kLsCl ? bs[lane][0] : F2{0.0f, 0.0f};
+      fb = lane < kLsCl ? bs[lane][1] : F2{0.0f, 0.0f};
+#pragma unroll
+      for (int off = kLsCl / 2; off > 0; off >>= 1) {
+        fa = f2_add(fa, f2_down(fa, off));
+        fb = f2_add(fb, f2_down(fb, off));
+      }
+      sa = (double)fa.hi + (double)fa.lo;
+      sb = (double)fb.hi + (double)fb.lo;
+    }
+  };
+  const float *pa = cl.map_shared_rank(&pub_a, 0);
+  const int *pd = cl.map_shared_rank(&pub_done, 0);
+  F2 fh, cw;
+  double s0 = 0.0, s1 = 0.0;
+  pass(0.0f, fh, cw);
+  cluster_sum(fh, cw, s0, s1);
+  if (rank == 0 && threadIdx.x == 0) {
+    ls_init(L, s0, s1, ctl->gh, 2.0 * (*eh), ctl->hmax, ctl->dmax, true);
+    pub_a = (float)L.a;
+    pub_done = L.done;
+  }
+  cl.sync();
+  float a = *pa;
+  int done = *pd;
+  while (!done) {  // uniform: every thread reads block 0's flag
+    pass(a, fh, cw);
+    cluster_sum(fh, cw, s0, s1);
+    if (rank == 0 && threadIdx.x == 0) {
+      ls_step(L, s0, s1);
+      pub_a = (float)L.a;
+      pub_done = L.done;
+    }
+    cl.sync();
+    a = *pa;
+    done = *pd;
+  }
+  cl.sync();  // block 0's shared memory outlives the other blocks' last reads
+  if (rank == 0 && threadIdx.x == 0) ls_store(ctl, L);
+}
+
 // ---- update after the line search ------------------------------------------
 // u += a h; g += a fKh + F_w(u_new) - F_w(u_old).  The elastic part of g is
 // updated through the linearity of F_el, so f_el itself is not stored, and
@@ -885,6 +1054,46 @@ template <typename Tx> Tx *phase_x(Item &it) {
   else return it.u;
 }
 
+// The cluster line search: on unless GFMD_LS_CLUSTER=0, the device cannot
+// place its cluster, or a graph holding it was refused (then off for the
+// process).
+std::atomic<int> g_ls_cluster{-1};
+bool ls_cluster_on() {
+  int v = g_ls_cluster.load();
+  if (v < 0) {
+    const char *env = std::getenv("GFMD_LS_CLUSTER");
+    v = (env && env[0] == '0') ? 0 : 1;
+    if (v) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(kLsCl);
+      cfg.blockDim = dim3(kLsT);
+      int ncl = 0;
+      if (cudaOccupancyMaxActiveClusters(&ncl, k_ls_cluster<float, float>, &cfg) != cudaSuccess || ncl < 1) {
+        (void)cudaGetLastError();
+        v = 0;
+      }
+    }
+    g_ls_cluster.store(v);
+  }
+  return v == 1;
+}
+
+// Items whose phase <Tx, Tv> runs the cluster line search: the FP32 phase
+// with a sphere wall on one atom layer.
+template <typename Tx, typename Tv, bool BIC> bool ls_cluster_item(const Item &it) {
+  return sizeof(Tx) == 4 && sizeof(Tv) == 4 && !BIC &&
+         (it.o.kind == GFMD_OBST_SPHERE_EXP || it.o.kind == GFMD_OBST_SPHERE_LJ) && it.o.nlayer == 1 &&
+         ls_cluster_on();
+}
+
+// Where the probes of a cluster item go in graph mode: an IF node on hls
+// added to the body graph being captured; the caller fills probe_body.
+struct LsGraph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphConditionalHandle hls = 0;
+  cudaGraph_t probe_body = nullptr;
+};
+
 // Adds a conditional node of the given type after the capture's current
 // dependencies on stream st; returns its body graph.
 cudaError_t add_cond(cudaStream_t st, cudaGraph_t top, cudaGraphConditionalHandle hc,
@@ -924,25 +1133,50 @@ cudaError_t enqueue_restart(Item &it, bool refine, cudaStream_t st, cudaGraphCon
   return cudaGetLastError();
 }
 
-// One CG iteration of one item on stream st.
+// Line search by the grid-wide kernels: k_lsinit and the probes.
+template <typename Tx, typename Tv, bool BIC = false> cudaError_t enqueue_probes(Item &it, cudaStream_t st) {
+  CgBufs &b = it.b;
+  const Geom &gm = it.hp->g;
+  Tx *x = phase_x<Tx>(it);
+  Tv *h = reinterpret_cast<Tv *>(b.h);
+  const bool obst = it.o.kind != GFMD_OBST_NONE;
+  k_lsinit<Tx, Tv, BIC><<<obst ? b.nblk : 1, kT, 0, st>>>(it.o, gm, x, h, b.active, b.d_e, b.part, b.ctl);
+  if (obst)
+    for (int p = 0; p < kLsMax; p++) k_probe<Tx, Tv, BIC><<<b.nblk, kT, 0, st>>>(it.o, gm, x, h, b.active, b.part, b.ctl);
+  return cudaGetLastError();
+}
+
+// One CG iteration of one item on stream st.  The line search of a cluster
+// item is k_ls_cluster, followed by the probes when its box is too large:
+// in graph mode (ls given) inside an IF node that k_ls_cluster sets; with
+// direct launches by the same rule, from the host's copy of the control
+// block (current: the host reads it back after every iteration).
 template <typename Tx, typename Tv, bool BIC = false>
-cudaError_t enqueue_iteration(Item &it, cudaStream_t st, cudaGraphConditionalHandle hwh, int use_hc) {
+cudaError_t enqueue_iteration(Item &it, cudaStream_t st, cudaGraphConditionalHandle hwh, int use_hc,
+                              LsGraph *ls = nullptr) {
   CgBufs &b = it.b;
   gfmd_solver *hd = it.hp;
   const Geom &gm = hd->g;
   Tx *x = phase_x<Tx>(it);
   Tv *g = reinterpret_cast<Tv *>(b.g), *h = reinterpret_cast<Tv *>(b.h), *fKh = reinterpret_cast<Tv *>(b.fKh);
   RT_CHECK(eval_on(hd, st, h, io_type<Tv>(), fKh, io_type<Tv>(), b.d_e, false));
+  bool probes = true;
+  if constexpr (sizeof(Tx) == 4 && sizeof(Tv) == 4 && !BIC) {
+    if (ls_cluster_item<Tx, Tv, BIC>(it)) {
+      k_ls_cluster<Tx, Tv><<<kLsCl, kLsT, 0, st>>>(it.o, gm, x, h, b.active, b.d_e, b.ctl, ls ? ls->hls : 0,
+                                                   ls ? 1 : 0);
+      RT_CHECK(cudaGetLastError());
+      if (ls) RT_CHECK(add_cond(st, ls->graph, ls->hls, cudaGraphCondTypeIf, &ls->probe_body));
+      probes = !ls && ls_box_sites(*b.hctl) > kLsCap;
+    }
+  }
+  if (probes) RT_CHECK((enqueue_probes<Tx, Tv, BIC>(it, st)));
   auto al16 = [](const void *p) { return p == nullptr || ((uintptr_t)p & 15) == 0; };
   Tv *gp = it.hpre ? reinterpret_cast<Tv *>(b.gp) : nullptr;
   Tv *mz = it.hpre ? reinterpret_cast<Tv *>(b.mz) : nullptr;
   const bool v4 = nsite4(gm) && al16(x) && al16(h) && al16(fKh) && al16(g) && al16(gp) && al16(mz);
   const size_t nsite = (size_t)gm.nx * gm.ny;
   const int sms = it.hp->sm_count;
-  const bool obst = it.o.kind != GFMD_OBST_NONE;
-  k_lsinit<Tx, Tv, BIC><<<obst ? b.nblk : 1, kT, 0, st>>>(it.o, gm, x, h, b.active, b.d_e, b.part, b.ctl);
-  if (obst)
-    for (int p = 0; p < kLsMax; p++) k_probe<Tx, Tv, BIC><<<b.nblk, kT, 0, st>>>(it.o, gm, x, h, b.active, b.part, b.ctl);
   if (v4)
     k_update<Tx, Tv, BIC, 4><<<grid_for(k_update<Tx, Tv, BIC, 4>, sms, nsite, 4 * kT), kT, 0, st>>>(
         it.o, gm, x, h, fKh, g, gp, b.active, b.part, b.ctl, hwh, use_hc);
@@ -1001,12 +1235,24 @@ cudaError_t build_phase(std::vector<Item *> &its, bool refine, cudaStream_t ms, 
     e2 = cudaStreamEndCapture(st, &got);
     if (e == cudaSuccess) e = e2;
     if (e != cudaSuccess) return e;
+    const bool bic = its[i]->o.kind == GFMD_OBST_MAP_BICUBIC;
+    LsGraph lsg;
+    lsg.graph = bwh[i];
+    const bool lsc = !bic && ls_cluster_item<Tx, Tv, false>(*its[i]);
+    if (lsc) RT_CHECK(cudaGraphConditionalHandleCreate(&lsg.hls, bwh[i], 0, cudaGraphCondAssignDefault));
     RT_CHECK(cudaStreamBeginCaptureToGraph(st, bwh[i], nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-    e = its[i]->o.kind == GFMD_OBST_MAP_BICUBIC ? enqueue_iteration<Tx, Tv, true>(*its[i], st, hwh[i], 1)
-                                                : enqueue_iteration<Tx, Tv>(*its[i], st, hwh[i], 1);
+    e = bic ? enqueue_iteration<Tx, Tv, true>(*its[i], st, hwh[i], 1)
+            : enqueue_iteration<Tx, Tv>(*its[i], st, hwh[i], 1, lsc ? &lsg : nullptr);
     e2 = cudaStreamEndCapture(st, &got);
     if (e == cudaSuccess) e = e2;
     if (e != cudaSuccess) return e;
+    if (lsg.probe_body) {  // the probes for a box the cluster kernel does not take
+      RT_CHECK(cudaStreamBeginCaptureToGraph(st, lsg.probe_body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+      e = enqueue_probes<Tx, Tv>(*its[i], st);
+      e2 = cudaStreamEndCapture(st, &got);
+      if (e == cudaSuccess) e = e2;
+      if (e != cudaSuccess) return e;
+    }
   }
   return cudaGraphInstantiate(exec_out, top, 0);
 }
@@ -1049,10 +1295,13 @@ cudaError_t run_launch_direct(std::vector<Item *> &its, bool refine, cudaStream_
 struct GraphHolder {
   cudaGraph_t g = nullptr;
   cudaGraphExec_t x = nullptr;
-  ~GraphHolder() {
+  void reset() {
     if (x) cudaGraphExecDestroy(x);
     if (g) cudaGraphDestroy(g);
+    x = nullptr;
+    g = nullptr;
   }
+  ~GraphHolder() { reset(); }
 };
 
 // Runs one phase of the batch until every item has converged, failed or hit
@@ -1067,7 +1316,21 @@ cudaError_t run_phase(std::vector<Item *> &its, bool refine, cudaStream_t ms, cu
   GraphHolder gh;
   const double t0 = now_s();
   const bool direct = no_graphs();
-  if (!direct) RT_CHECK((build_phase<Tx, Tv>(its, refine, ms, fork, join, &gh.g, &gh.x)));
+  bool lsc = false;
+  for (Item *it : its) lsc = lsc || ls_cluster_item<Tx, Tv, false>(*it);
+  if (!direct) {
+    cudaError_t eb = build_phase<Tx, Tv>(its, refine, ms, fork, join, &gh.g, &gh.x);
+    if (eb != cudaSuccess && lsc) {
+      // a graph with the cluster line search's nested IF node was refused:
+      // the probes alone, for the rest of the process
+      (void)cudaGetLastError();
+      gh.reset();
+      g_ls_cluster.store(0);
+      if (trace_on()) std::fprintf(stderr, "gfmd cg: cluster line search off (%s)\n", cudaGetErrorString(eb));
+      eb = build_phase<Tx, Tv>(its, refine, ms, fork, join, &gh.g, &gh.x);
+    }
+    RT_CHECK(eb);
+  }
   const double t1 = now_s();
   int launches = 0;
   for (Item *it : its) it->it0 = it->b.hctl->it;
@@ -1098,9 +1361,10 @@ cudaError_t run_phase(std::vector<Item *> &its, bool refine, cudaStream_t ms, cu
     }
     if (all) {
       if (trace_on())
-        std::fprintf(stderr, "gfmd cg phase <%s,%s> items %zu: graph build %.3f s, %d launches %.3f s\n",
+        std::fprintf(stderr, "gfmd cg phase <%s,%s> items %zu: graph build %.3f s, %d launches %.3f s%s\n",
                      sizeof(Tx) == 8 ? "f64" : "f32", sizeof(Tv) == 8 ? "f64" : "f32", its.size(), t1 - t0,
-                     launches, now_s() - t1);
+                     launches, now_s() - t1,
+                     lsc && g_ls_cluster.load() == 1 ? ", cluster line search" : "");
       return cudaSuccess;
     }
   }
