@@ -484,8 +484,10 @@ __global__ void __launch_bounds__(kT) k_probe(const __grid_constant__ Obst o, Ge
 // FP32 phase, a sphere wall on one atom layer, a set whose box holds at most
 // kLsCap sites.  The set's x and h stay in registers for the whole search:
 // a Newton step is a pass over registers, a compensated FP32 reduction per
-// block and two cluster barriers (block sums gathered in block 0's shared
-// memory, the next step published there).  One launch replaces k_lsinit
+// block and one cluster barrier (every block writes its sums into every
+// block's shared memory, double-buffered by step parity, and every block
+// reduces them in the same order and takes the same Newton step, so no step
+// is broadcast).  One launch replaces k_lsinit
 // and up to kLsMax probes, each of which chains a grid-wide reduction
 // through global memory.  A larger box leaves the search to those kernels:
 // block 0 sets the conditional that runs them.
@@ -529,11 +531,11 @@ __global__ void __cluster_dims__(kLsCl, 1, 1) __launch_bounds__(kLsT, 1)
   if (rank == 0 && threadIdx.x == 0) set_loop(hls, use_hc, big ? 1u : 0u);
   if (big) return;
 
-  __shared__ F2 ws[kLsT / 32][2];  // warp sums
-  __shared__ F2 bs[kLsCl][2];      // block sums (block 0)
-  __shared__ float pub_a;          // step published by block 0
+  __shared__ F2 ws[kLsT / 32][2];   // warp sums
+  __shared__ F2 bs[2][kLsCl][2];    // block sums of a step (by parity), from every block
+  __shared__ float pub_a;           // step and flag from this block's thread 0
   __shared__ int pub_done;
-  __shared__ LineState L;          // block 0, thread 0
+  __shared__ LineState L;           // thread 0; the same in every block
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int N = gm.nx * gm.ny;
   const int w = ctl->by1 - ctl->by0 + 1, x0 = ctl->bx0, y0 = ctl->by0;
@@ -578,9 +580,10 @@ __global__ void __cluster_dims__(kLsCl, 1, 1) __launch_bounds__(kLsT, 1)
       }
     }
   };
-  // cluster sums of (fa, fb): valid in block 0, thread 0
-  F2 *bs0 = cl.map_shared_rank(&bs[0][0], 0);
-  auto cluster_sum = [&](F2 fa, F2 fb, double &sa, double &sb) {
+  // cluster sums of (fa, fb) for the step of parity par, valid in thread 0
+  // of every block: each block reduces the kLsCl block sums in rank order,
+  // so every block holds the same values (and takes the same Newton step)
+  auto cluster_sum = [&](F2 fa, F2 fb, int par, double &sa, double &sb) {
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
       fa = f2_add(fa, f2_down(fa, off));
@@ -599,15 +602,18 @@ __global__ void __cluster_dims__(kLsCl, 1, 1) __launch_bounds__(kLsT, 1)
         fa = f2_add(fa, f2_down(fa, off));
         fb = f2_add(fb, f2_down(fb, off));
       }
-      if (lane == 0) {
-        bs0[2 * rank] = fa;
-        bs0[2 * rank + 1] = fb;
+      fa = F2{__shfl_sync(0xffffffffu, fa.hi, 0), __shfl_sync(0xffffffffu, fa.lo, 0)};
+      fb = F2{__shfl_sync(0xffffffffu, fb.hi, 0), __shfl_sync(0xffffffffu, fb.lo, 0)};
+      if (lane < kLsCl) {  // lane q delivers this block's sums to block q
+        F2 *dst = cl.map_shared_rank(&bs[par][rank][0], lane);
+        dst[0] = fa;
+        dst[1] = fb;
       }
     }
     cl.sync();
-    if (rank == 0 && warp == 0) {
-      fa = lane < kLsCl ? bs[lane][0] : F2{0.0f, 0.0f};
-      fb = lane < kLsCl ? bs[lane][1] : F2{0.0f, 0.0f};
+    if (warp == 0) {
+      fa = lane < kLsCl ? bs[par][lane][0] : F2{0.0f, 0.0f};
+      fb = lane < kLsCl ? bs[par][lane][1] : F2{0.0f, 0.0f};
 #pragma unroll
       for (int off = kLsCl / 2; off > 0; off >>= 1) {
         fa = f2_add(fa, f2_down(fa, off));
@@ -617,33 +623,34 @@ __global__ void __cluster_dims__(kLsCl, 1, 1) __launch_bounds__(kLsT, 1)
       sb = (double)fb.hi + (double)fb.lo;
     }
   };
-  const float *pa = cl.map_shared_rank(&pub_a, 0);
-  const int *pd = cl.map_shared_rank(&pub_done, 0);
   F2 fh, cw;
   double s0 = 0.0, s1 = 0.0;
+  int par = 0;
   pass(0.0f, fh, cw);
-  cluster_sum(fh, cw, s0, s1);
-  if (rank == 0 && threadIdx.x == 0) {
+  cluster_sum(fh, cw, par, s0, s1);
+  if (threadIdx.x == 0) {
     ls_init(L, s0, s1, ctl->gh, 2.0 * (*eh), ctl->hmax, ctl->dmax, true);
     pub_a = (float)L.a;
     pub_done = L.done;
   }
-  cl.sync();
-  float a = *pa;
-  int done = *pd;
-  while (!done) {  // uniform: every thread reads block 0's flag
+  __syncthreads();
+  float a = pub_a;
+  int done = pub_done;
+  while (!done) {  // uniform: every block takes the same steps
+    par ^= 1;
     pass(a, fh, cw);
-    cluster_sum(fh, cw, s0, s1);
-    if (rank == 0 && threadIdx.x == 0) {
+    cluster_sum(fh, cw, par, s0, s1);
+    if (threadIdx.x == 0) {
       ls_step(L, s0, s1);
       pub_a = (float)L.a;
       pub_done = L.done;
     }
-    cl.sync();
-    a = *pa;
-    done = *pd;
+    __syncthreads();
+    a = pub_a;
+    done = pub_done;
   }
-  cl.sync();  // block 0's shared memory outlives the other blocks' last reads
+  // no shared memory is written across the cluster after the last cluster
+  // barrier: the blocks may leave in any order
   if (rank == 0 && threadIdx.x == 0) ls_store(ctl, L);
 }
 
