@@ -11,6 +11,10 @@
 //                                  gamma-point term); F_el is linear, so
 //                                  F_el(u + a h) = F_el(u) + a fKh exactly,
 //                                  and its energy is h.K.h / 2
+//   k_ls_cluster                   FP32 phase with a sphere wall on one atom
+//                                  layer: the whole line search in one
+//                                  thread-block cluster; for a set too large
+//                                  for it, sets the IF node that runs:
 //   k_lsinit                       wall curvature and F_w.h along h at a = 0
 //                                  over the line-search set, first Newton step
 //   k_probe x kLsMax               Newton steps on the line derivative over the
@@ -26,7 +30,10 @@
 // launch of the graph runs at most `recompute` iterations.  Each launch
 // starts from a fresh evaluation of F_el(u) (the drift of the incremental
 // update is reset) and steepest descent.  Only k_update and k_dir stream the
-// vectors; the line-search kernels visit the box of the set.
+// vectors; the line-search kernels visit the box of the set.  A batch or
+// single solve that qualifies for k_ls_cluster nests the IF node in the
+// WHILE body; a runtime that refuses the nested node gets the graph
+// without it (probes only).
 //
 // Precision: the state is held in two types, Tx for u (the quantity that
 // accumulates) and Tv for g, h and fKh.  Plain FP64 runs
