@@ -236,6 +236,41 @@ def test_nve_energy_conservation_like_the_reference_test():
     assert np.abs(e - e.mean()).max() / abs(e.mean()) < 1e-4
 
 
+def test_restart_continuity_like_the_reference_test(tmp_path):
+    # tests/TEST_restart of the reference: NVE on `fcc100 1.0 1`, 10 x 10,
+    # random displacements of 0.1, dt = 0.01; the state is written to disk,
+    # the solver is rebuilt from its kernel arguments and the state read
+    # back, and the run goes on.  The energy is continuous across the
+    # restart (the reference's bound: 1e-6), and the continued run is the
+    # uninterrupted one.
+    nx = ny = 10
+
+    def fresh():
+        d, half, full, linf = tables("fcc100 1.0 1", nx, ny)
+        return d, _solver(nx, ny, d, half, linf)
+
+    d, s = fresh()
+    u0 = np.random.default_rng(12472634).uniform(-0.1, 0.1, (d, nx * ny))
+    u = torch.from_numpy(u0.copy()).cuda()
+    v = torch.zeros_like(u)
+    e1, _ = s.run_dynamics(u, v, 0.01, 0.0, 2000)
+    np.savez(tmp_path / "restart.npz", u=u.cpu().numpy(), v=v.cpu().numpy())
+    del s, u, v
+    d, s = fresh()
+    st = np.load(tmp_path / "restart.npz")
+    u2 = torch.from_numpy(st["u"]).cuda()
+    v2 = torch.from_numpy(st["v"]).cuda()
+    e2, _ = s.run_dynamics(u2, v2, 0.01, 0.0, 2000)
+    assert abs(e1[-1] - e2[0]) < 1e-6
+    d, s = fresh()
+    ua = torch.from_numpy(u0.copy()).cuda()
+    va = torch.zeros_like(ua)
+    ea, _ = s.run_dynamics(ua, va, 0.01, 0.0, 4000)
+    assert rel_l2(u2.cpu().numpy(), ua.cpu().numpy()) <= 1e-12
+    assert rel_l2(v2.cpu().numpy(), va.cpu().numpy()) <= 1e-12
+    assert np.abs(ea[2000:] - e2).max() <= 1e-12 * np.abs(ea).max()
+
+
 def test_solver_status_codes():
     g = gfmd_pkg()
     nx = ny = 16
