@@ -49,6 +49,49 @@ def test_argument_errors_return_status_without_gpu():
     assert L.gfmd_minimize(None, None, None, None, None) == 1
 
 
+# Every entry point that takes a handle, or sizes and pointers, rejects NULL
+# handles, NULL outputs and impossible sizes with GFMD_EINVAL and a message,
+# before any CUDA call (this host has no GPU): nothing aborts or exits.
+_BAD_CALLS = {
+    "gfmd_set_stream": (None, None),
+    "gfmd_post_force_host": (None, None, None, None),
+    "gfmd_force_f64": (None, None, None, None),
+    "gfmd_force_f32": (None, None, None, None),
+    "gfmd_get_u0": (None, None),
+    "gfmd_plan_info": (None, None, None),
+    "gfmd_memory_usage": (None, None),
+    "gfmd_solver_info": (None, None, None),
+    "gfmd_phi_pattern": (None, None, None),
+    "gfmd_make_preconditioner": (None, 0.0, None),
+    "gfmd_minimize_batch": (0, None, None),
+    "gfmd_run_dynamics": (None, None, 0.01, 0.0, 10, None, None, None, None),
+    "gfmd_obstacle_force": (0, 8, 3, None, None, None, None, None),
+    "gfmd_post_force_noalloc": (0, 8, 3, None, None, None, None, None, None),
+    "gfmd_kernel_create": (None, None),
+    "gfmd_kernel_destroy": (None,),
+    "gfmd_kernel_info": (None, None, None),
+    "gfmd_kernel_phi": (None, 8, 8, 0, None, None, 0),
+    "gfmd_atoms_to_grid": (-1, None, None, None, None, 8, 8, 3, 8.0, 8.0, 0, 0, None, None, None, None, None),
+    "gfmd_grid_to_atoms": (-1, None, None, 8, 8, 3, None, 0, None, None),
+    "gfmd_rough_surface": (0, 8, None, None, None),
+    "gfmd_ws_create": (0, 0, 0, 0, None),
+    "gfmd_ws_destroy": (None,),
+    "gfmd_ws_set_stream": (None, None),
+    "gfmd_ws_num_params": (None, None),
+    "gfmd_ws_get_params": (None, None, None),
+    "gfmd_ws_set_params": (None, None),
+    "gfmd_ws_forward": (None, 1, 8, 8, None, None),
+    "gfmd_ws_adam_step": (None, 1e-3, 0.9, 0.999, 1e-8),
+}
+
+
+@pytest.mark.parametrize("name", sorted(_BAD_CALLS))
+def test_every_entry_point_rejects_bad_arguments_without_gpu(name):
+    L = gfmd_pkg().lib()
+    assert getattr(L, name)(*_BAD_CALLS[name]) == 1  # GFMD_EINVAL
+    assert L.gfmd_last_error().startswith(name.encode() + b":")
+
+
 def test_solver_factory_names():
     g = gfmd_pkg()
     assert g.gfmd_solver_factory().get_name() == "static/gb300"
