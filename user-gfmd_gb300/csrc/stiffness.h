@@ -105,6 +105,8 @@ class StiffnessKernel {
   // The values given with the `linf` keyword.
   const std::vector<double> &linf_keyword() const { return linf_; }
   const std::string &name() const { return name_; }
+  // The crystal surface of an `ft` kernel (cell, basis, neighbour list).
+  const CrystalSurface &surface() const { return surf_; }
 
   // U0, U, V at one wavevector (each dim*dim, row-major).
   void dynamical_matrices(double qx, double qy, cplx *U0, cplx *U, cplx *V) const;
